@@ -1,0 +1,451 @@
+"""Benchmark of the GB300 HBT pair-binning engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload central|small] [--precision fp64|fp32w]
+
+Workload "central" (default): 1000 pi+ events, multiplicity Poisson(1500),
+emission source sigma_xy = 7 fm, tau0 = 12 fm/c, oversample factor 100
+(event_buffer_size = 150000 -> ~150k particles per group), 41^3 q grid on
+[-0.15, 0.15] GeV, 8 K_T bins on [0, 1] GeV x 8 K_phi bins, 10 rotated
+mixed-event partners per event, no pair cap (needed_number_of_pairs = 1e18).
+Synthetic, seeded data of those shapes (no public dataset exists).
+
+One step = one oversample group through the hot path: its same-event pairs
+i < j plus every event's mixed pairs against its 10 partners.  The unit of
+work is the reference's candidate pair (n(n-1)/2 same-event plus n1*n2
+mixed-event pairs).  `value` times the device-resident entry points with
+CUDA events on the engine's stream; `e2e` times the host-buffer C-ABI calls
+(pinned host arrays copied in, histograms copied back every step) with the
+host clock.  The L2 is flushed (256 MB write) between timed steps.
+
+--impl reference times the reference algorithm on the host cores (the CPU
+oracle, multi-threaded) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+# FP64 operations per pair and stage, counted from the reference's code
+# (src/HBT_correlation.cpp): add/mul + div + sqrt + cos, each counted once.
+STAGE_OPS_SAME = (11, 12, 5, 11, 15)
+STAGE_OPS_MIXED = (11, 12, 5, 11, 2)
+
+
+def workload_params(name: str) -> dict:
+    if name == "small":
+        return dict(qnpts=41, q_min=-0.15, q_max=0.15, n_KT=5, KT_min=0.0, KT_max=1.0,
+                    n_Kphi=8, azimuthal_flag=0, invariant_radius_flag=0,
+                    long_comoving_boost=1, needed_number_of_pairs=1e18)
+    return dict(qnpts=41, q_min=-0.15, q_max=0.15, n_KT=9, KT_min=0.0, KT_max=1.0, n_Kphi=8,
+                azimuthal_flag=1, invariant_radius_flag=0, long_comoving_boost=1,
+                needed_number_of_pairs=1e18)
+
+
+def make_workload(name: str, seed: int = 1, max_groups: int | None = None):
+    """Groups of (same-event SoA, [(list1 SoA4, list2 SoA4) per event])."""
+    from hadronic_afterburner_toolkit_gb300 import synth
+    if name == "small":
+        ev = synth.small_pions(seed=seed)
+        buf, nmix = 5000, 5
+    else:
+        ev = synth.central_pions(seed=seed)
+        buf, nmix = 150000, 10
+    rng = np.random.default_rng(seed + 1000)
+    groups = []
+    for (a, b) in synth.buffers(ev, buf):
+        if max_groups is not None and len(groups) >= max_groups:
+            break
+        g = synth.subset(ev, a, b)
+        cols = [np.ascontiguousarray(getattr(g, k)) for k in
+                ("px", "py", "pz", "E", "x", "y", "z", "t")]
+        nev = g.n_events
+        mixed = []
+        for e in range(nev):
+            lo, hi = g.offsets[e], g.offsets[e + 1]
+            l1 = [c[lo:hi].copy() for c in cols[:4]]
+            parts = []
+            for _ in range(nmix):
+                m = int(rng.integers(nev))
+                while m == e and nev > 1:
+                    m = int(rng.integers(nev))
+                phi = rng.uniform(0, 2 * np.pi)
+                c, s = np.cos(phi), np.sin(phi)
+                mlo, mhi = g.offsets[m], g.offsets[m + 1]
+                px, py = cols[0][mlo:mhi], cols[1][mlo:mhi]
+                parts.append((px * c - py * s, px * s + py * c, cols[2][mlo:mhi], cols[3][mlo:mhi]))
+            l2 = [np.ascontiguousarray(np.concatenate([p[f] for p in parts])) for f in range(4)]
+            mixed.append((l1, l2))
+        groups.append((cols, mixed))
+    return groups
+
+
+def group_pairs(group) -> int:
+    cols, mixed = group
+    n = cols[0].size
+    return n * (n - 1) // 2 + sum(l1[0].size * l2[0].size for l1, l2 in mixed)
+
+
+def survival_fractions(group, p, sample=400_000, seed=7):
+    """Stage survival fractions of the same-event chain on sampled pairs
+    (K_T pass, q_out pass, q_side pass, binned), FP64 numpy."""
+    cols = group[0]
+    n = cols[0].size
+    rng = np.random.default_rng(seed)
+    i = rng.integers(0, n, sample)
+    j = rng.integers(0, n, sample)
+    keep = i != j
+    i, j = i[keep], j[keep]
+    px, py, pz, E = cols[0], cols[1], cols[2], cols[3]
+    Kx = 0.5 * (px[i] + px[j]); Ky = 0.5 * (py[i] + py[j])
+    Kz = 0.5 * (pz[i] + pz[j]); KE = 0.5 * (E[i] + E[j])
+    Kp2 = Kx * Kx + Ky * Ky
+    kt = (Kp2 >= p["KT_min"] ** 2) & (Kp2 <= p["KT_max"] ** 2)
+    Kp = np.sqrt(Kp2)
+    qx = px[i] - px[j]; qy = py[i] - py[j]; qz = pz[i] - pz[j]; qE = E[i] - E[j]
+    dq = (p["q_max"] - p["q_min"]) / (p["qnpts"] - 1)
+    lo, hi = p["q_min"] - dq / 2 + 1e-8, p["q_max"] + dq / 2 - 1e-8
+    with np.errstate(all="ignore"):
+        qo = (qx * Kx + qy * Ky) / Kp
+        qs = (qy * Kx - qx * Ky) / Kp
+        Mt = np.sqrt(KE * KE - Kz * Kz)
+        ql = (KE / Mt) * (qz - (Kz / KE) * qE)
+    o = kt & (qo >= lo) & (qo <= hi)
+    s = o & (qs >= lo) & (qs <= hi)
+    b = s & (ql >= lo) & (ql <= hi)
+    m = float(i.size)
+    return (1.0, kt.sum() / m, o.sum() / m, s.sum() / m, b.sum() / m)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measure_fp64_peak() -> dict:
+    """Live FP64 / FP32 FMA issue rate on this GPU (hbt_probe)."""
+    import ctypes
+    from hadronic_afterburner_toolkit_gb300 import build
+    L = ctypes.CDLL(build.build_probe())
+    out = {}
+    for name, fn, iters in (("fp64", L.hbt_probe_fp64, 1 << 14), ("fp32", L.hbt_probe_fp32, 1 << 16)):
+        fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                       ctypes.POINTER(ctypes.c_double)]
+        ms, fl = ctypes.c_float(), ctypes.c_double()
+        best = 0.0
+        for _ in range(3):
+            if fn(152 * 16, iters, ctypes.byref(ms), ctypes.byref(fl)) != 0:
+                raise RuntimeError("probe failed")
+            best = max(best, fl.value / (ms.value * 1e-3))
+        out[name + "_tflops"] = best / 1e12
+    return out
+
+
+def cpu_baseline(group, p, nthreads=1, target_s=12.0) -> dict:
+    """Oracle (sequential restatement of the reference loops) on a bounded
+    sample: the first rows of the group's same-event list and the first
+    events' mixed lists."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    cols, mixed = group
+    orc = oracle_lib.Oracle(**{k: v for k, v in p.items()})
+    # calibrate on a small slice, then scale to ~target_s
+    n0 = min(3000, cols[0].size)
+    t0 = time.perf_counter()
+    orc.bin_same([c[:n0] for c in cols], nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    rate = (n0 * (n0 - 1) / 2) / max(dt, 1e-6)
+    n_same = int(min(cols[0].size, np.sqrt(2 * rate * target_s / 2)))
+    n_ev = 0
+    budget_mixed = rate * target_s / 2
+    acc = 0
+    for l1, l2 in mixed:
+        if acc >= budget_mixed:
+            break
+        acc += l1[0].size * l2[0].size
+        n_ev += 1
+    orc = oracle_lib.Oracle(**p)
+    t0 = time.perf_counter()
+    orc.bin_same([c[:n_same] for c in cols], nthreads=nthreads)
+    for l1, l2 in mixed[:n_ev]:
+        orc.bin_mixed(l1, l2, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    pairs = n_same * (n_same - 1) // 2 + sum(l1[0].size * l2[0].size for l1, l2 in mixed[:n_ev])
+    return {"value": pairs / dt, "unit": "pairs/s", "cores": nthreads, "kind": "port",
+            "sample": "same-event pairs of the first %d particles of one ~%dk-particle group + "
+                      "mixed pairs of its first %d events (%.3g pairs, %.1f s)"
+                      % (n_same, cols[0].size // 1000, n_ev, pairs, dt)}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    p = workload_params(args.workload)
+    groups = make_workload(args.workload, max_groups=1)
+    nthreads = os.cpu_count() or 1
+    steps = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(groups[0], p, nthreads=nthreads, target_s=4.0)
+        if k >= args.warmup:
+            steps.append(r)
+    v = statistics.median(s["value"] for s in steps)
+    line = {"impl": "reference", "metric": "candidate pairs binned per second (same + mixed event)",
+            "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "reference_arm": "CPU oracle port of the "
+                       "reference pair loops, all host threads"},
+            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": nthreads, "kind": "port",
+                             "sample": steps[-1]["sample"]},
+            "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="central", choices=["central", "small"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32w"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    from hadronic_afterburner_toolkit_gb300 import engine as E
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    p = workload_params(args.workload)
+    prec = E.PRECISION_FP64 if args.precision == "fp64" else E.PRECISION_FP32W
+    n_groups = args.warmup + args.steps
+    groups = make_workload(args.workload, seed=1 + rank, max_groups=n_groups)
+    dev = torch.device("cuda", local)
+
+    # device-resident inputs
+    dgroups = []
+    for cols, mixed in groups:
+        dc = [torch.from_numpy(c).to(dev) for c in cols]
+        dm = [([torch.from_numpy(x).to(dev) for x in l1], [torch.from_numpy(x).to(dev) for x in l2])
+              for l1, l2 in mixed]
+        dgroups.append((dc, dm))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    eng = E.Engine(device=local, precision=prec, **p)
+    eng.set_stream(stream.cuda_stream)
+
+    def step_device(k):
+        dc, dm = dgroups[k % len(dgroups)]
+        eng.bin_same(dc, device=True)
+        for l1, l2 in dm:
+            eng.bin_mixed(l1, l2, device=True)
+
+    for k in range(args.warmup):
+        step_device(k)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = eng.stats()["launches"]
+    ms_steps, ms_same, pairs = [], [], 0
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            g = args.warmup + k
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e2 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dc, dm = dgroups[g % len(dgroups)]
+            eng.bin_same(dc, device=True)
+            e1.record(stream)
+            for l1, l2 in dm:
+                eng.bin_mixed(l1, l2, device=True)
+            e2.record(stream)
+            e2.synchronize()
+            ms_steps.append(e0.elapsed_time(e2))
+            ms_same.append(e0.elapsed_time(e1))
+            pairs += group_pairs(groups[g % len(groups)])
+    torch.cuda.synchronize()
+    launches = eng.stats()["launches"] - launches0
+    t_ms = sum(ms_steps)
+    if world > 1:
+        t = torch.tensor([t_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(t.item())
+        pt = torch.tensor([float(pairs)], device=dev)
+        torch.distributed.all_reduce(pt)
+        pairs_all = float(pt.item())
+    else:
+        pairs_all = float(pairs)
+    value = pairs_all / (t_ms * 1e-3)
+
+    # roofline of the dominant (same-event) kernel against the live FP64 peak
+    peaks = measure_fp64_peak()
+    g0 = groups[args.warmup % len(groups)]
+    fr = survival_fractions(g0, p)
+    n = g0[0][0].size
+    P_same = n * (n - 1) / 2
+    ops = sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)) * P_same
+    t_same = statistics.median(ms_same) * 1e-3
+    achieved = ops / t_same / 1e12
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
+                "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"], "traffic": None,
+                "kernel": "k_same (same-event pair binning)",
+                "peak_source": "measured live: FP64 FMA probe (lib/libhbt_probe.so)",
+                "ops_per_pair": round(ops / P_same, 2),
+                "survival": [round(x, 4) for x in fr],
+                "same_event_ms_per_group": round(statistics.median(ms_same), 3),
+                "fp32_tflops_measured": peaks["fp32_tflops"]}
+
+    # end to end through the host-buffer C ABI (pinned host arrays)
+    e2e = None
+    if not args.no_e2e:
+        eng2 = E.Engine(device=local, precision=prec, **p)
+        pin = []
+        for cols, mixed in groups:
+            pc = [torch.from_numpy(c).pin_memory().numpy() for c in cols]
+            pm = [([torch.from_numpy(x).pin_memory().numpy() for x in l1],
+                   [torch.from_numpy(x).pin_memory().numpy() for x in l2]) for l1, l2 in mixed]
+            pin.append((pc, pm))
+        nb = eng2.L.hbt_n_bins(eng2.handle)
+        out = [torch.empty(nb, dtype=torch.float64).pin_memory().numpy() for _ in range(6)]
+        import ctypes
+
+        def step_host(k):
+            pc, pm = pin[k % len(pin)]
+            eng2.bin_same(pc)
+            for l1, l2 in pm:
+                eng2.bin_mixed(l1, l2)
+            eng2._check(eng2.L.hbt_read_hist(eng2.handle, *[o.ctypes.data_as(E._PD) for o in out]))
+
+        for k in range(args.warmup):
+            step_host(k)
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        e2e_pairs = 0
+        for k in range(args.steps):
+            g = args.warmup + k
+            step_host(g)
+            pc, pm = pin[g % len(pin)]
+            h2d += sum(c.nbytes for c in pc) + sum(x.nbytes for l1, l2 in pm for x in l1 + l2)
+            d2h += 6 * nb * 8
+            e2e_pairs += group_pairs(groups[g % len(groups)])
+        t_e2e = time.perf_counter() - t0
+        e2e = {"value": e2e_pairs / t_e2e, "unit": "pairs/s",
+               "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps}
+        eng2.close()
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        cpu = cpu_baseline(groups[0], p, nthreads=1)
+
+    if rank == 0:
+        st = eng.stats()
+        line = {"metric": "candidate pairs binned per second (same + mixed event)",
+                "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else "f64 bins / f32 weights",
+                "data": "synthetic",
+                "config": {"workload": args.workload, "events": 1000 if args.workload == "central" else 100,
+                           "oversample": 100 if args.workload == "central" else 10,
+                           "particles_per_group": int(np.mean([g[0][0].size for g in groups])),
+                           "mixed_partners": 10 if args.workload == "central" else 5,
+                           "qnpts": p["qnpts"], "n_KT_bins": p["n_KT"] - 1,
+                           "n_Kphi": p["n_Kphi"] if p["azimuthal_flag"] else 1,
+                           "precision": args.precision, "l2": "flushed (256 MB write) between steps",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "pairs_per_step": pairs_all / args.steps / max(world, 1),
+                "binned_same_fraction": round(fr[4], 4),
+                "gpu_launches": launches,
+                "clocks": clk.summary(),
+                "roofline": roofline,
+                "e2e": e2e,
+                "cpu_baseline": cpu,
+                "stats": st}
+        print(json.dumps(line))
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

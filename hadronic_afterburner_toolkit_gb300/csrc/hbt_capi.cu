@@ -1,0 +1,619 @@
+// C ABI of the HBT pair-binning engine (include/hbt_gpu.h).
+//
+// Owns the device histograms of one analysis, stages host particle lists
+// into HBM, chooses per launch between the fast path (no pair cap can bind)
+// and ordered cap admission, and decides the few K_phi bins that lie on a
+// bin edge with the C library's atan2 (as the reference does,
+// src/HBT_correlation.cpp:408-416).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/hbt_gpu.h"
+#include "hbt_engine.cuh"
+
+using hbt::u64;
+
+namespace {
+
+const double kHbarC = 0.197327053;  // GeV fm (src/parameters.h:4)
+const unsigned kDeferCap = 1u << 16;
+const u64 kInf = ~0ull;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct hbt_ctx {
+    hbt_params prm;
+    int device = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    cudaEvent_t staged = nullptr;
+    hbt::Device d;
+    u64 cap = 0, cap_qinv = 0;
+    int n_stream = 0;  // 3-D slots + q_inv K_T bins
+    // histograms
+    DevBuf sums, cnt, den, qi_sums, qi_cnt, qi_den, stats, defer, n_defer;
+    // ordered admission scratch
+    DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
+    // input staging
+    DevBuf in;
+    // upper bounds of the four counter families (num 3-D, den 3-D, num
+    // q_inv, den q_inv): max counter <= bound
+    u64 ub[4] = {0, 0, 0, 0};
+    hbt_stats st;
+    std::string err;
+};
+
+namespace {
+
+hbt_status fail(hbt_ctx *c, hbt_status s, const std::string &msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+#define CU(call)                                                                     \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess)                                                       \
+            return fail(c, HBT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define TRY(expr)                          \
+    do {                                   \
+        hbt_status s_ = (expr);            \
+        if (s_ != HBT_OK) return s_;       \
+    } while (0)
+
+hbt_status dalloc(hbt_ctx *c, DevBuf &b, size_t bytes) {
+    if (b.bytes >= bytes && b.p) return HBT_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (bytes == 0) return HBT_OK;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) return fail(c, HBT_ERR_NOMEM, "cudaMalloc failed");
+    b.bytes = bytes;
+    return HBT_OK;
+}
+
+template <class T>
+T *ptr(DevBuf &b) {
+    return static_cast<T *>(b.p);
+}
+
+void refresh_device(hbt_ctx *c) {
+    c->d.h.sums = ptr<hbt::Sums>(c->sums);
+    c->d.h.cnt = ptr<u64>(c->cnt);
+    c->d.h.den = ptr<u64>(c->den);
+    c->d.h.qi_sums = ptr<hbt::QiSums>(c->qi_sums);
+    c->d.h.qi_cnt = ptr<u64>(c->qi_cnt);
+    c->d.h.qi_den = ptr<u64>(c->qi_den);
+    c->d.stats = ptr<u64>(c->stats);
+    c->d.defer = ptr<hbt::Deferral>(c->defer);
+    c->d.n_defer = ptr<unsigned>(c->n_defer);
+    c->d.defer_cap = kDeferCap;
+    c->d.caps.rowcnt = ptr<unsigned>(c->rowcnt);
+    c->d.caps.row_cut = ptr<long long>(c->row_cut);
+    c->d.caps.quota = ptr<unsigned long long>(c->quota);
+    c->d.caps.resolved = ptr<hbt::Resolved>(c->resolved);
+}
+
+// Reference K_phi decision on the host (src/HBT_correlation.cpp:408-416).
+int host_kphi(const hbt::Grid &g, double Kx, double Ky, double psi_ref) {
+    const double phi = atan2(Ky, Kx);
+    double d = phi - psi_ref;
+    while (d < 0.) d += 2. * M_PI;
+    while (d > 2. * M_PI) d -= 2. * M_PI;
+    const int ip = static_cast<int>(d / g.dKphi);
+    if (ip < 0 || ip >= g.n_Kphi) return -1;
+    return ip;
+}
+
+// True when c + P - 1 <= limit (all of P more admissions pass `<= limit`).
+bool fits_le(u64 c, u64 P, u64 limit) {
+    if (P == 0) return true;
+    if (c > limit) return false;
+    return P - 1 <= limit - c;
+}
+
+hbt_status read_defer_count(hbt_ctx *c, unsigned *n) {
+    CU(cudaMemcpyAsync(n, c->n_defer.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return HBT_OK;
+}
+
+// Bins the fast-mode deferrals collected so far (each record carries its
+// kind and the psi_ref of its launch, so they can wait until the
+// histograms or counters are read).
+hbt_status drain_deferrals(hbt_ctx *c) {
+    if (!c->prm.azimuthal_flag) return HBT_OK;
+    unsigned n = 0;
+    TRY(read_defer_count(c, &n));
+    if (n == 0) return HBT_OK;
+    if (n > kDeferCap) return fail(c, HBT_ERR_DEVICE, "K_phi deferral buffer overflow");
+    std::vector<hbt::Deferral> rec(n);
+    CU(cudaMemcpyAsync(rec.data(), c->defer.p, n * sizeof(hbt::Deferral),
+                       cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    std::vector<int> iphi(n);
+    for (unsigned k = 0; k < n; k++)
+        iphi[k] = host_kphi(c->d.g, rec[k].Kx, rec[k].Ky, rec[k].psi);
+    TRY(dalloc(c, c->apply_iphi, n * sizeof(int)));
+    CU(cudaMemcpyAsync(c->apply_iphi.p, iphi.data(), n * sizeof(int), cudaMemcpyHostToDevice,
+                       c->stream));
+    CU(hbt::launch_apply(c->d, ptr<hbt::Deferral>(c->defer), ptr<int>(c->apply_iphi), (int)n,
+                         c->stream));
+    CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    c->st.deferred_kphi += n;
+    c->st.launches++;
+    return HBT_OK;
+}
+
+// Exact counters: [num slots][den slots][num q_inv][den q_inv].
+hbt_status read_counters(hbt_ctx *c, std::vector<u64> &out) {
+    const int ns = c->d.g.n_slots, nk = c->d.g.n_KT;
+    const size_t n = 2 * ns + 2 * nk;
+    TRY(dalloc(c, c->counters, n * sizeof(u64)));
+    CU(hbt::launch_counters(c->d, ptr<unsigned long long>(c->counters), c->stream));
+    out.assign(n, 0);
+    CU(cudaMemcpyAsync(out.data(), c->counters.p, n * sizeof(u64), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    c->st.launches++;
+    // tighten the upper bounds
+    for (int f = 0; f < 4; f++) c->ub[f] = 0;
+    for (int s = 0; s < ns; s++) {
+        c->ub[0] = std::max(c->ub[0], out[s]);
+        c->ub[1] = std::max(c->ub[1], out[ns + s]);
+    }
+    for (int k = 0; k < nk; k++) {
+        c->ub[2] = std::max(c->ub[2], out[2 * ns + k]);
+        c->ub[3] = std::max(c->ub[3], out[2 * ns + nk + k]);
+    }
+    return HBT_OK;
+}
+
+// Can any cap reject one of P more pairs of this kind?  `mixed` selects the
+// denominator families.
+bool caps_may_bind(const hbt_ctx *c, int mixed, u64 P) {
+    const u64 ub3 = c->ub[mixed ? 1 : 0], ubq = c->ub[mixed ? 3 : 2];
+    if (!fits_le(ub3, P, c->cap)) return true;
+    if (c->prm.invariant_radius_flag == 1) {
+        if (c->cap_qinv == 0) return true;
+        if (!fits_le(ubq, P, c->cap_qinv - 1)) return true;
+    }
+    return false;
+}
+
+// Ordered admission for one launch (same-event: mixed = 0).
+hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
+                          const double *const *a, const double *const *b) {
+    TRY(drain_deferrals(c));
+    std::vector<u64> ctr;
+    TRY(read_counters(c, ctr));
+    const int ns = c->d.g.n_slots, nk = c->d.g.n_KT, nst = c->n_stream;
+    std::vector<u64> rem(nst, kInf);
+    for (int s = 0; s < ns; s++) {
+        const u64 v = ctr[(mixed ? ns : 0) + s];
+        if (v > c->cap)
+            rem[s] = 0;
+        else
+            rem[s] = (c->cap - v == kInf) ? kInf : c->cap - v + 1;
+    }
+    for (int k = 0; k < nk; k++) {
+        const u64 v = ctr[2 * ns + (mixed ? nk : 0) + k];
+        rem[ns + k] = (c->prm.invariant_radius_flag == 1) ? (v < c->cap_qinv ? c->cap_qinv - v : 0)
+                                                          : kInf;
+    }
+    TRY(dalloc(c, c->rowcnt, (size_t)nst * rows * sizeof(unsigned)));
+    TRY(dalloc(c, c->row_cut, nst * sizeof(long long)));
+    TRY(dalloc(c, c->quota, nst * sizeof(u64)));
+    TRY(dalloc(c, c->remaining, nst * sizeof(u64)));
+    refresh_device(c);
+    c->d.caps.n_resolved = 0;
+    CU(cudaMemsetAsync(c->rowcnt.p, 0, (size_t)nst * rows * sizeof(unsigned), c->stream));
+    CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
+    // pass A: survivors per (stream bin, row)
+    if (mixed)
+        CU(hbt::launch_mixed(c->d, hbt::MODE_COUNT, rows, a, cols, b, c->stream));
+    else
+        CU(hbt::launch_same(c->d, hbt::MODE_COUNT, rows, a, c->stream));
+    c->st.launches++;
+    // deferred K_phi bins: decided here, added to the row counts, and looked
+    // up by the admission passes
+    if (c->prm.azimuthal_flag) {
+        unsigned n = 0;
+        TRY(read_defer_count(c, &n));
+        if (n > kDeferCap) return fail(c, HBT_ERR_DEVICE, "K_phi deferral buffer overflow");
+        if (n > 0) {
+            std::vector<hbt::Deferral> rec(n);
+            CU(cudaMemcpyAsync(rec.data(), c->defer.p, n * sizeof(hbt::Deferral),
+                               cudaMemcpyDeviceToHost, c->stream));
+            CU(cudaStreamSynchronize(c->stream));
+            std::vector<hbt::Resolved> res(n);
+            for (unsigned k = 0; k < n; k++) {
+                res[k].key = rec[k].i * cols + rec[k].j;
+                res[k].iphi = host_kphi(c->d.g, rec[k].Kx, rec[k].Ky, rec[k].psi);
+                res[k].iK = rec[k].iK;
+            }
+            std::sort(res.begin(), res.end(),
+                      [](const hbt::Resolved &x, const hbt::Resolved &y) { return x.key < y.key; });
+            TRY(dalloc(c, c->resolved, n * sizeof(hbt::Resolved)));
+            refresh_device(c);
+            CU(cudaMemcpyAsync(c->resolved.p, res.data(), n * sizeof(hbt::Resolved),
+                               cudaMemcpyHostToDevice, c->stream));
+            c->d.caps.n_resolved = (int)n;
+            CU(hbt::launch_defer_count(c->d, rows, cols, (int)n, c->stream));
+            c->st.deferred_kphi += n;
+            c->st.launches++;
+        }
+        CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
+    }
+    CU(cudaMemcpyAsync(c->remaining.p, rem.data(), nst * sizeof(u64), cudaMemcpyHostToDevice,
+                       c->stream));
+    CU(hbt::launch_cut(c->d, rows, nst, ptr<unsigned long long>(c->remaining), c->stream));
+    // pass B: rows before each cut, then the cut rows in pair order
+    if (mixed) {
+        CU(hbt::launch_mixed(c->d, hbt::MODE_ORDER, rows, a, cols, b, c->stream));
+        CU(hbt::launch_mixed_straddle(c->d, rows, a, cols, b, nst, c->stream));
+    } else {
+        CU(hbt::launch_same(c->d, hbt::MODE_ORDER, rows, a, c->stream));
+        CU(hbt::launch_same_straddle(c->d, rows, a, nst, c->stream));
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    c->st.launches += 4;
+    c->st.ordered_passes++;
+    c->d.caps.n_resolved = 0;
+    return HBT_OK;
+}
+
+hbt_status bin_same_device(hbt_ctx *c, long long n, const double *const *c8) {
+    if (n < 2) return HBT_OK;
+    const u64 P = (u64)n * (u64)(n - 1) / 2;
+    c->st.pairs_same += P;
+    bool may_bind = caps_may_bind(c, 0, P);
+    if (may_bind) {
+        TRY(drain_deferrals(c));
+        std::vector<u64> ctr;
+        TRY(read_counters(c, ctr));
+        may_bind = caps_may_bind(c, 0, P);
+    }
+    if (may_bind) {
+        TRY(ordered_launch(c, 0, n, n, c8, nullptr));
+        std::vector<u64> ctr;
+        TRY(read_counters(c, ctr));
+    } else {
+        CU(hbt::launch_same(c->d, hbt::MODE_FAST, n, c8, c->stream));
+        c->st.launches++;
+        c->ub[0] += P;
+        if (c->prm.invariant_radius_flag == 1) c->ub[2] += P;
+    }
+    return HBT_OK;
+}
+
+hbt_status bin_mixed_device(hbt_ctx *c, long long n1, const double *const *l1, long long n2,
+                            const double *const *l2) {
+    if (n1 < 1 || n2 < 1) return HBT_OK;
+    const u64 P = (u64)n1 * (u64)n2;
+    c->st.pairs_mixed += P;
+    bool may_bind = caps_may_bind(c, 1, P);
+    if (may_bind) {
+        TRY(drain_deferrals(c));
+        std::vector<u64> ctr;
+        TRY(read_counters(c, ctr));
+        may_bind = caps_may_bind(c, 1, P);
+    }
+    if (may_bind) {
+        TRY(ordered_launch(c, 1, n1, n2, l1, l2));
+        std::vector<u64> ctr;
+        TRY(read_counters(c, ctr));
+    } else {
+        CU(hbt::launch_mixed(c->d, hbt::MODE_FAST, n1, l1, n2, l2, c->stream));
+        c->st.launches++;
+        c->ub[1] += P;
+        if (c->prm.invariant_radius_flag == 1) c->ub[3] += P;
+    }
+    return HBT_OK;
+}
+
+// Copies host columns into the staging buffer; returns device pointers.
+hbt_status stage(hbt_ctx *c, const double *const *src, const long long *len, int ncols,
+                 const double **dst) {
+    size_t total = 0;
+    for (int f = 0; f < ncols; f++) total += (size_t)((len[f] + 31) / 32 * 32);
+    TRY(dalloc(c, c->in, total * sizeof(double)));
+    double *base = ptr<double>(c->in);
+    size_t off = 0;
+    for (int f = 0; f < ncols; f++) {
+        dst[f] = base + off;
+        if (len[f] > 0) {
+            if (!src[f]) return fail(c, HBT_ERR_INVALID, "null particle array");
+            CU(cudaMemcpyAsync(base + off, src[f], len[f] * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+        }
+        off += (size_t)((len[f] + 31) / 32 * 32);
+    }
+    // the caller's arrays may be reused once the copies are done
+    CU(cudaEventRecord(c->staged, c->stream));
+    CU(cudaEventSynchronize(c->staged));
+    return HBT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
+    hbt_ctx *c = nullptr;
+    if (!p || !out) return HBT_ERR_INVALID;
+    *out = nullptr;
+    if (p->qnpts < 2 || p->n_KT < 2 || p->n_Kphi < 1 || p->qnpts > 1024)
+        return HBT_ERR_INVALID;
+    if (p->precision != HBT_PRECISION_FP64 && p->precision != HBT_PRECISION_FP32W)
+        return HBT_ERR_INVALID;
+    c = new hbt_ctx();
+    c->prm = *p;
+    c->device = device;
+    CU(cudaSetDevice(device));
+    CU(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking));
+    c->stream = c->own;
+    CU(cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming));
+
+    // constants with the reference's expressions (src/HBT_correlation.cpp:25-61)
+    hbt::Grid &g = c->d.g;
+    g.qnpts = p->qnpts;
+    g.n_KT = p->n_KT;
+    g.n_Kphi = p->n_Kphi;
+    g.azimuthal = p->azimuthal_flag == 1;
+    g.qinv = p->invariant_radius_flag == 1;
+    g.boost = p->long_comoving_boost == 1;
+    g.n_slots = g.azimuthal ? p->n_KT * p->n_Kphi : p->n_KT;
+    g.q3 = (long long)p->qnpts * p->qnpts * p->qnpts;
+    g.delta_q = (p->q_max - p->q_min) / (p->qnpts - 1);
+    g.q_lo = p->q_min - g.delta_q / 2. + 1e-8;
+    g.q_hi = p->q_max + g.delta_q / 2. - 1e-8;
+    g.q_base = p->q_min - g.delta_q / 2.;
+    g.KT_min = p->KT_min;
+    g.dKT = (p->KT_max - p->KT_min) / (p->n_KT - 1);
+    g.KT_min_sq = p->KT_min * p->KT_min;
+    g.KT_max_sq = p->KT_max * p->KT_max;
+    g.dKphi = 2 * M_PI / p->n_Kphi;
+    g.two_pi = 2. * M_PI;
+    g.psi_ref = 0.0;
+    g.kphi_tol = p->kphi_defer_tol > 0 ? p->kphi_defer_tol : 1e-13;
+    g.hbarC_inv = 1. / kHbarC;
+    c->cap = static_cast<u64>(p->needed_number_of_pairs);
+    c->cap_qinv = 50 * c->cap;
+    c->n_stream = g.n_slots + g.n_KT;
+
+    const size_t nb = (size_t)g.n_slots * g.q3, nq = (size_t)g.n_KT * g.qnpts;
+    hbt_status s = HBT_OK;
+    if ((s = dalloc(c, c->sums, nb * sizeof(hbt::Sums))) != HBT_OK ||
+        (s = dalloc(c, c->cnt, nb * sizeof(u64))) != HBT_OK ||
+        (s = dalloc(c, c->den, nb * sizeof(u64))) != HBT_OK ||
+        (s = dalloc(c, c->qi_sums, nq * sizeof(hbt::QiSums))) != HBT_OK ||
+        (s = dalloc(c, c->qi_cnt, nq * sizeof(u64))) != HBT_OK ||
+        (s = dalloc(c, c->qi_den, nq * sizeof(u64))) != HBT_OK ||
+        (s = dalloc(c, c->stats, hbt::STAT_N * sizeof(u64))) != HBT_OK ||
+        (s = dalloc(c, c->defer, kDeferCap * sizeof(hbt::Deferral))) != HBT_OK ||
+        (s = dalloc(c, c->n_defer, sizeof(unsigned))) != HBT_OK) {
+        hbt_destroy(c);
+        return s;
+    }
+    refresh_device(c);
+    s = hbt_reset(c);
+    if (s != HBT_OK) {
+        hbt_destroy(c);
+        return s;
+    }
+    *out = c;
+    return HBT_OK;
+}
+
+void hbt_destroy(hbt_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
+                      &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
+                      &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
+                      &c->apply_iphi, &c->in};
+    for (DevBuf *b : bufs)
+        if (b->p) cudaFree(b->p);
+    if (c->staged) cudaEventDestroy(c->staged);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+}
+
+const char *hbt_last_error(const hbt_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+hbt_status hbt_set_stream(hbt_ctx *c, void *s) {
+    if (!c) return HBT_ERR_INVALID;
+    c->stream = s ? static_cast<cudaStream_t>(s) : c->own;
+    return HBT_OK;
+}
+
+hbt_status hbt_set_psi_ref(hbt_ctx *c, double psi) {
+    if (!c) return HBT_ERR_INVALID;
+    c->d.g.psi_ref = psi;
+    return HBT_OK;
+}
+
+hbt_status hbt_reset(hbt_ctx *c) {
+    if (!c) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    CU(cudaMemsetAsync(c->sums.p, 0, c->sums.bytes, c->stream));
+    CU(cudaMemsetAsync(c->cnt.p, 0, c->cnt.bytes, c->stream));
+    CU(cudaMemsetAsync(c->den.p, 0, c->den.bytes, c->stream));
+    CU(cudaMemsetAsync(c->qi_sums.p, 0, c->qi_sums.bytes, c->stream));
+    CU(cudaMemsetAsync(c->qi_cnt.p, 0, c->qi_cnt.bytes, c->stream));
+    CU(cudaMemsetAsync(c->qi_den.p, 0, c->qi_den.bytes, c->stream));
+    CU(cudaMemsetAsync(c->stats.p, 0, c->stats.bytes, c->stream));
+    CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    for (int f = 0; f < 4; f++) c->ub[f] = 0;
+    memset(&c->st, 0, sizeof(c->st));
+    return HBT_OK;
+}
+
+hbt_status hbt_bin_same_dev(hbt_ctx *c, int64_t n, const hbt_soa8 *l) {
+    if (!c || !l || n < 0) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    const double *c8[8] = {l->px, l->py, l->pz, l->E, l->x, l->y, l->z, l->t};
+    return bin_same_device(c, n, c8);
+}
+
+hbt_status hbt_bin_mixed_dev(hbt_ctx *c, int64_t n1, const hbt_soa4 *a, int64_t n2,
+                             const hbt_soa4 *b) {
+    if (!c || !a || !b || n1 < 0 || n2 < 0) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    const double *l1[4] = {a->px, a->py, a->pz, a->E};
+    const double *l2[4] = {b->px, b->py, b->pz, b->E};
+    return bin_mixed_device(c, n1, l1, n2, l2);
+}
+
+hbt_status hbt_bin_same(hbt_ctx *c, int64_t n, const hbt_soa8 *l) {
+    if (!c || !l || n < 0) return HBT_ERR_INVALID;
+    if (n < 2) {
+        if (n >= 0) c->st.pairs_same += 0;
+        return HBT_OK;
+    }
+    CU(cudaSetDevice(c->device));
+    const double *src[8] = {l->px, l->py, l->pz, l->E, l->x, l->y, l->z, l->t};
+    const long long len[8] = {n, n, n, n, n, n, n, n};
+    const double *dv[8];
+    TRY(stage(c, src, len, 8, dv));
+    return bin_same_device(c, n, dv);
+}
+
+hbt_status hbt_bin_mixed(hbt_ctx *c, int64_t n1, const hbt_soa4 *a, int64_t n2,
+                         const hbt_soa4 *b) {
+    if (!c || !a || !b || n1 < 0 || n2 < 0) return HBT_ERR_INVALID;
+    if (n1 == 0 || n2 == 0) return HBT_OK;
+    CU(cudaSetDevice(c->device));
+    const double *src[8] = {a->px, a->py, a->pz, a->E, b->px, b->py, b->pz, b->E};
+    const long long len[8] = {n1, n1, n1, n1, n2, n2, n2, n2};
+    const double *dv[8];
+    TRY(stage(c, src, len, 8, dv));
+    return bin_mixed_device(c, n1, dv, n2, dv + 4);
+}
+
+hbt_status hbt_sync(hbt_ctx *c, uint64_t timeout_us) {
+    if (!c) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    if (timeout_us == 0) {
+        CU(cudaStreamSynchronize(c->stream));
+    } else {
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            const cudaError_t e = cudaStreamQuery(c->stream);
+            if (e == cudaSuccess) break;
+            if (e != cudaErrorNotReady)
+                return fail(c, HBT_ERR_CUDA, std::string("cudaStreamQuery: ") + cudaGetErrorString(e));
+            const auto us = std::chrono::duration_cast<std::chrono::microseconds>(
+                                std::chrono::steady_clock::now() - t0)
+                                .count();
+            if ((uint64_t)us >= timeout_us)
+                return fail(c, HBT_ERR_TIMEOUT, "hbt_sync: work still running");
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+    u64 stats[hbt::STAT_N];
+    CU(cudaMemcpy(stats, c->stats.p, sizeof(stats), cudaMemcpyDeviceToHost));
+    if (stats[hbt::STAT_ERROR] != 0)
+        return fail(c, HBT_ERR_DEVICE, "a kernel raised its error flag");
+    return HBT_OK;
+}
+
+int64_t hbt_n_bins(const hbt_ctx *c) { return c ? (int64_t)c->d.g.n_slots * c->d.g.q3 : 0; }
+
+hbt_status hbt_read_hist(hbt_ctx *c, double *num_count, double *q_out_sum, double *q_side_sum,
+                         double *q_long_sum, double *num, double *den) {
+    if (!c) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    TRY(drain_deferrals(c));
+    TRY(hbt_sync(c, 0));
+    const size_t nb = (size_t)hbt_n_bins(c);
+    if (q_out_sum || q_side_sum || q_long_sum || num) {
+        std::vector<hbt::Sums> s(nb);
+        CU(cudaMemcpy(s.data(), c->sums.p, nb * sizeof(hbt::Sums), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < nb; k++) {
+            if (q_out_sum) q_out_sum[k] = s[k].qo;
+            if (q_side_sum) q_side_sum[k] = s[k].qs;
+            if (q_long_sum) q_long_sum[k] = s[k].ql;
+            if (num) num[k] = s[k].w;
+        }
+    }
+    std::vector<u64> v(nb);
+    if (num_count) {
+        CU(cudaMemcpy(v.data(), c->cnt.p, nb * sizeof(u64), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < nb; k++) num_count[k] = (double)v[k];
+    }
+    if (den) {
+        CU(cudaMemcpy(v.data(), c->den.p, nb * sizeof(u64), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < nb; k++) den[k] = (double)v[k];
+    }
+    return HBT_OK;
+}
+
+hbt_status hbt_read_qinv(hbt_ctx *c, double *qinv_sum, double *num, double *num_count,
+                         double *den) {
+    if (!c) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    TRY(hbt_sync(c, 0));
+    const size_t nq = (size_t)c->d.g.n_KT * c->d.g.qnpts;
+    std::vector<hbt::QiSums> s(nq);
+    CU(cudaMemcpy(s.data(), c->qi_sums.p, nq * sizeof(hbt::QiSums), cudaMemcpyDeviceToHost));
+    std::vector<u64> a(nq), b(nq);
+    CU(cudaMemcpy(a.data(), c->qi_cnt.p, nq * sizeof(u64), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(b.data(), c->qi_den.p, nq * sizeof(u64), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < nq; k++) {
+        if (qinv_sum) qinv_sum[k] = s[k].q;
+        if (num) num[k] = s[k].w;
+        if (num_count) num_count[k] = (double)a[k];
+        if (den) den[k] = (double)b[k];
+    }
+    return HBT_OK;
+}
+
+hbt_status hbt_read_counters(hbt_ctx *c, uint64_t *num, uint64_t *den, uint64_t *num_qinv,
+                             uint64_t *den_qinv) {
+    if (!c) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    TRY(drain_deferrals(c));
+    std::vector<u64> ctr;
+    TRY(read_counters(c, ctr));
+    const int ns = c->d.g.n_slots, nk = c->d.g.n_KT;
+    for (int s = 0; s < ns; s++) {
+        if (num) num[s] = ctr[s];
+        if (den) den[s] = ctr[ns + s];
+    }
+    for (int k = 0; k < nk; k++) {
+        if (num_qinv) num_qinv[k] = ctr[2 * ns + k];
+        if (den_qinv) den_qinv[k] = ctr[2 * ns + nk + k];
+    }
+    return HBT_OK;
+}
+
+hbt_status hbt_get_stats(hbt_ctx *c, hbt_stats *out) {
+    if (!c || !out) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    TRY(hbt_sync(c, 0));
+    u64 stats[hbt::STAT_N];
+    CU(cudaMemcpy(stats, c->stats.p, sizeof(stats), cudaMemcpyDeviceToHost));
+    *out = c->st;
+    out->anomalies = stats[hbt::STAT_ANOMALY];
+    return HBT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+// Shared definitions of the HBT pair-binning engine (device kernels and the
+// C ABI layer).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hbt {
+
+typedef unsigned long long u64;
+
+// Histogram geometry and the constants the reference derives in its
+// constructor (src/HBT_correlation.cpp:25-61, :253, :289-290, :342-345),
+// computed once on the host with the reference's expressions.
+struct Grid {
+    int qnpts, n_KT, n_Kphi, n_slots;
+    int azimuthal, qinv, boost;
+    long long q3;
+    double q_lo, q_hi, q_base, delta_q;
+    double KT_min, dKT, KT_min_sq, KT_max_sq;
+    double dKphi, two_pi, psi_ref, kphi_tol;
+    double hbarC_inv;
+};
+
+// Per-bin numerator sums, one 32-byte L2 sector per bin.
+struct __align__(32) Sums {
+    double qo, qs, ql, w;
+};
+struct __align__(16) QiSums {
+    double q, w;
+};
+
+// Device histogram storage.
+//  sums  [n_slots*q3] {q_out, q_side, q_long, cos(q.dx)} - one 32-byte sector
+//  cnt   [n_slots*q3] numerator pair count
+//  den   [n_slots*q3] denominator pair count
+//  qi_*  [n_KT*qnpts] q_inv histograms
+struct Hist {
+    Sums *sums;  // 32-byte aligned {q_out, q_side, q_long, cos}
+    u64 *cnt;
+    u64 *den;
+    QiSums *qi_sums;  // {q_inv, cos(q.dx)}
+    u64 *qi_cnt;
+    u64 *qi_den;
+};
+
+// Pair whose K_phi bin sits within kphi_tol of a bin edge: its azimuthal
+// bin is decided on the host with the C library's atan2.  The record holds
+// everything needed to bin the pair afterwards.
+struct Deferral {
+    long long i, j;          // row (list-1 / i) and column (list-2 / j) index
+    double Kx, Ky;           // 0.5*(px_i + px_j), 0.5*(py_i + py_j), exact FP64
+    double psi;              // psi_ref in force for the launch
+    double qo, qs, ql, cosw; // LCMS components and cos(q.dx) (same-event)
+    int iK, bin;             // K_T bin and 3-D bin within the slot
+    int mixed, pad;          // 1: denominator pair
+};
+
+// Resolved deferral, sorted by key = i * cols + j.
+struct Resolved {
+    long long key;
+    int iphi;  // -1: out of range (skip)
+    int iK;
+};
+
+enum StatIdx {
+    STAT_ANOMALY = 0,   // NaN LCMS component or K_T index out of range
+    STAT_DEFER = 1,     // deferrals raised
+    STAT_ERROR = 2,     // error flags (deferral overflow, missing lookup)
+    STAT_N = 4
+};
+
+// Ordered cap admission (order-dependent needed_number_of_pairs caps).
+// Stream bins: 3-D slots [0, n_slots) then q_inv K_T bins
+// [n_slots, n_slots + n_KT).
+struct Caps {
+    unsigned *rowcnt;          // [n_stream][rows] survivors per row (count pass)
+    long long *row_cut;        // [n_stream] rows < cut admitted, == cut straddles
+    unsigned long long *quota; // [n_stream] admissions left in the straddle row
+    const Resolved *resolved;  // deferred pairs resolved on the host
+    int n_resolved;
+};
+
+struct Device {
+    Grid g;
+    Hist h;
+    u64 *stats;
+    Deferral *defer;
+    unsigned *n_defer;
+    unsigned defer_cap;
+    Caps caps;
+};
+
+enum Mode { MODE_FAST = 0, MODE_COUNT = 1, MODE_ORDER = 2 };
+
+// Launchers (hbt_kernels.cu).
+cudaError_t launch_same(const Device &d, int mode, long long n, const double *const *c8,
+                        cudaStream_t st);
+cudaError_t launch_mixed(const Device &d, int mode, long long n1, const double *const *l1,
+                         long long n2, const double *const *l2, cudaStream_t st);
+cudaError_t launch_same_straddle(const Device &d, long long n, const double *const *c8,
+                                 int n_stream, cudaStream_t st);
+cudaError_t launch_mixed_straddle(const Device &d, long long n1, const double *const *l1,
+                                  long long n2, const double *const *l2, int n_stream,
+                                  cudaStream_t st);
+cudaError_t launch_cut(const Device &d, long long rows, int n_stream,
+                       const unsigned long long *remaining, cudaStream_t st);
+// Bins n deferred records with their host-resolved K_phi bins (iphi[k]).
+cudaError_t launch_apply(const Device &d, const Deferral *rec, const int *iphi, int n,
+                         cudaStream_t st);
+cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, int n_res,
+                               cudaStream_t st);
+cudaError_t launch_counters(const Device &d, unsigned long long *out, cudaStream_t st);
+
+}  // namespace hbt

@@ -1,0 +1,607 @@
+// HBT pair-binning kernels for sm_103a (plain FP64 form).
+//
+// Every bin-deciding expression follows the reference's operand order
+// (src/HBT_correlation.cpp:311-458 same-event, :574-687 mixed-event) and the
+// translation unit is compiled with --fmad=false, so each FP64 add, multiply,
+// divide and square root is the same IEEE-rounded operation the reference's
+// CPU build performs.  Pair counts and bin indices are therefore bit-exact;
+// only the order of the FP64 sums differs.
+//
+// Launch shapes
+//  same-event : one CTA per (i-tile <= j-tile) pair of 128-particle tiles;
+//               the j-tile is staged in shared memory, each thread owns one i.
+//  mixed-event: one CTA per (list-1 tile, list-2 tile).
+// Admission modes for the order-dependent pair caps (needed_number_of_pairs):
+//  FAST  - no cap can bind in this launch: bin every survivor.
+//  COUNT - count survivors per (stream bin, row) for the ordered pass.
+//  ORDER - admit rows before each stream bin's cut row; the cut row itself
+//          is admitted in pair order by the straddle kernel.
+#include "hbt_engine.cuh"
+
+namespace hbt {
+namespace {
+
+constexpr int TILE = 128;
+
+struct Cols8 {
+    const double *p[8];  // px py pz E x y z t
+};
+struct Cols4 {
+    const double *p[4];  // px py pz E
+};
+
+// Result of one pair's decision chain.
+struct Chain {
+    int iK;       // K_T bin, -1: K_T cut failed (or anomaly)
+    int qi_k;     // q_inv bin, -1: no q_inv event
+    int ev3;      // 0: no 3-D event, 1: event in `slot`, 2: K_phi deferred
+    int slot;     // 3-D slot
+    int bin;      // (iqout*qnpts + iqside)*qnpts + iqlong
+    int anomaly;  // NaN LCMS component / K_T index out of range
+    double qinv, qo, qs, ql, phase, Kx, Ky;
+};
+
+// K_phi bin of the pair (src/HBT_correlation.cpp:408-423): -1 out of
+// range, -2 within kphi_tol of an edge or of the 0 / 2 pi wrap (the host
+// decides those with the C library's atan2).
+__device__ __forceinline__ int kphi_bin(const Grid &g, double Kx, double Ky) {
+    const double phi = atan2(Ky, Kx);
+    double d = phi - g.psi_ref;
+    if (fabs(d) <= g.kphi_tol || fabs(d - g.two_pi) <= g.kphi_tol) return -2;
+    while (d < 0.) d += g.two_pi;
+    while (d > g.two_pi) d -= g.two_pi;
+    if (d <= g.kphi_tol || g.two_pi - d <= g.kphi_tol) return -2;
+    const double r = d / g.dKphi;
+    const double nearest = rint(r);
+    if (fabs(r - nearest) * g.dKphi <= g.kphi_tol) return -2;
+    const int ip = static_cast<int>(r);
+    if (ip < 0 || ip >= g.n_Kphi) return -1;
+    return ip;
+}
+
+// The reference's per-pair chain.  MIXED selects the mixed-event variant
+// (inclusive upper window bounds, q_inv index check, no space-time phase).
+template <bool MIXED>
+__device__ __forceinline__ Chain pair_chain(const Grid &g, double apx, double apy,
+                                            double apz, double aE, double bpx,
+                                            double bpy, double bpz, double bE,
+                                            const double *ax, const double *bx) {
+    Chain c;
+    c.iK = -1;
+    c.qi_k = -1;
+    c.ev3 = 0;
+    c.anomaly = 0;
+    const double K_z = 0.5 * (apz + bpz);
+    const double K_E = 0.5 * (aE + bE);
+    const double K_x = 0.5 * (apx + bpx);
+    const double K_y = 0.5 * (apy + bpy);
+    const double Kp2 = K_x * K_x + K_y * K_y;
+    if (Kp2 < g.KT_min_sq || Kp2 > g.KT_max_sq) return c;
+    const double Kp = sqrt(Kp2);
+    const int iK = static_cast<int>((Kp - g.KT_min) / g.dKT);
+    if (iK < 0 || iK >= g.n_KT) {
+        c.anomaly = 1;
+        return c;
+    }
+    c.iK = iK;
+    const double q_x = apx - bpx;
+    const double q_y = apy - bpy;
+    const double q_z = apz - bpz;
+    const double q_E = aE - bE;
+    if (!MIXED) {
+        // x, y, z, t differences for the phase (q.dx)/hbarC
+        const double dt = ax[3] - bx[3];
+        const double dx = ax[0] - bx[0];
+        const double dy = ax[1] - bx[1];
+        const double dz = ax[2] - bx[2];
+        c.phase = g.hbarC_inv * (q_E * dt - q_x * dx - q_y * dy - q_z * dz);
+    }
+    if (g.qinv) {
+        const double qinv = sqrt(-(q_E * q_E - q_x * q_x - q_y * q_y - q_z * q_z));
+        if (qinv > g.q_lo && qinv < g.q_hi) {
+            const int k = static_cast<int>((qinv - g.q_base) / g.delta_q);
+            if (k < g.qnpts) {
+                c.qi_k = k;
+                c.qinv = qinv;
+            } else if (!MIXED) {
+                // the reference indexes past its array here (no check on the
+                // numerator side); never reached for a window inside the grid
+                c.anomaly = 1;
+            }
+        }
+    }
+    const double cphi = K_x / Kp;
+    const double sphi = K_y / Kp;
+    const double qo = q_x * cphi + q_y * sphi;
+    if (qo != qo) {
+        c.anomaly = 1;
+        return c;
+    }
+    if (qo < g.q_lo || (MIXED ? qo >= g.q_hi : qo > g.q_hi)) return c;
+    const int io = static_cast<int>((qo - g.q_base) / g.delta_q);
+    if (io >= g.qnpts) return c;
+    const double qs = q_y * cphi - q_x * sphi;
+    if (qs != qs) {
+        c.anomaly = 1;
+        return c;
+    }
+    if (qs < g.q_lo || (MIXED ? qs >= g.q_hi : qs > g.q_hi)) return c;
+    const int is = static_cast<int>((qs - g.q_base) / g.delta_q);
+    if (is >= g.qnpts) return c;
+    double ql = q_z;
+    if (g.boost) {
+        const double Mt = sqrt(K_E * K_E - K_z * K_z);
+        const double gamma = K_E / Mt;
+        const double beta = K_z / K_E;
+        ql = gamma * (q_z - beta * q_E);
+    }
+    if (ql != ql) {
+        c.anomaly = 1;
+        return c;
+    }
+    if (ql < g.q_lo || (MIXED ? ql >= g.q_hi : ql > g.q_hi)) return c;
+    const int il = static_cast<int>((ql - g.q_base) / g.delta_q);
+    if (il >= g.qnpts) return c;
+    c.bin = (io * g.qnpts + is) * g.qnpts + il;
+    c.qo = qo;
+    c.qs = qs;
+    c.ql = ql;
+    c.Kx = K_x;
+    c.Ky = K_y;
+    if (g.azimuthal) {
+        const int ip = kphi_bin(g, K_x, K_y);
+        if (ip == -1) return c;
+        if (ip == -2) {
+            c.ev3 = 2;
+            return c;
+        }
+        c.slot = iK * g.n_Kphi + ip;
+    } else {
+        c.slot = iK;
+    }
+    c.ev3 = 1;
+    return c;
+}
+
+// Histogram updates ---------------------------------------------------------
+
+__device__ __forceinline__ void bin_num3(const Device &d, int slot, int bin,
+                                         const Chain &c) {
+    const long long at = (long long)slot * d.g.q3 + bin;
+    Sums *s = d.h.sums + at;
+    atomicAdd(&s->qo, c.qo);
+    atomicAdd(&s->qs, c.qs);
+    atomicAdd(&s->ql, c.ql);
+    atomicAdd(&s->w, cos(c.phase));
+    atomicAdd(d.h.cnt + at, 1ull);
+}
+
+__device__ __forceinline__ void bin_den3(const Device &d, int slot, int bin) {
+    atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
+}
+
+__device__ __forceinline__ void bin_num_qinv(const Device &d, const Chain &c) {
+    const int at = c.iK * d.g.qnpts + c.qi_k;
+    atomicAdd(&d.h.qi_sums[at].q, c.qinv);
+    atomicAdd(&d.h.qi_sums[at].w, cos(c.phase));
+    atomicAdd(d.h.qi_cnt + at, 1ull);
+}
+
+__device__ __forceinline__ void bin_den_qinv(const Device &d, const Chain &c) {
+    atomicAdd(d.h.qi_den + c.iK * d.g.qnpts + c.qi_k, 1ull);
+}
+
+template <bool MIXED>
+__device__ __forceinline__ void push_deferral(const Device &d, long long i, long long j,
+                                              const Chain &c) {
+    const unsigned k = atomicAdd(d.n_defer, 1u);
+    atomicAdd(d.stats + STAT_DEFER, 1ull);
+    if (k < d.defer_cap) {
+        Deferral r;
+        r.i = i;
+        r.j = j;
+        r.Kx = c.Kx;
+        r.Ky = c.Ky;
+        r.psi = d.g.psi_ref;
+        r.mixed = MIXED ? 1 : 0;
+        r.pad = 0;
+        r.qo = c.qo;
+        r.qs = c.qs;
+        r.ql = c.ql;
+        r.cosw = MIXED ? 0.0 : cos(c.phase);
+        r.iK = c.iK;
+        r.bin = c.bin;
+        d.defer[k] = r;
+    } else {
+        atomicAdd(d.stats + STAT_ERROR, 1ull);
+    }
+}
+
+// Slot of a deferred pair from the host-resolved table (-1: skip).
+__device__ __forceinline__ int resolved_slot(const Device &d, long long key, int iK) {
+    int lo = 0, hi = d.caps.n_resolved - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const long long k = d.caps.resolved[mid].key;
+        if (k == key) {
+            const int ip = d.caps.resolved[mid].iphi;
+            return ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
+        }
+        if (k < key)
+            lo = mid + 1;
+        else
+            hi = mid - 1;
+    }
+    atomicAdd(d.stats + STAT_ERROR, 1ull);
+    return -1;
+}
+
+// Consumes one pair's chain according to the admission mode.
+template <bool MIXED, int MODE>
+__device__ __forceinline__ void consume(const Device &d, long long i, long long j,
+                                        long long cols, long long rows, const Chain &c) {
+    if (c.anomaly) atomicAdd(d.stats + STAT_ANOMALY, 1ull);
+    if (c.iK < 0) return;
+    const int ns = d.g.n_slots;
+    if (c.qi_k >= 0) {
+        const int b = ns + c.iK;
+        if (MODE == MODE_FAST) {
+            if (MIXED)
+                bin_den_qinv(d, c);
+            else
+                bin_num_qinv(d, c);
+        } else if (MODE == MODE_COUNT) {
+            atomicAdd(d.caps.rowcnt + (long long)b * rows + i, 1u);
+        } else if (i < d.caps.row_cut[b]) {
+            if (MIXED)
+                bin_den_qinv(d, c);
+            else
+                bin_num_qinv(d, c);
+        }
+    }
+    if (c.ev3 == 0) return;
+    int slot = c.slot;
+    if (c.ev3 == 2) {
+        if (MODE != MODE_ORDER) {
+            push_deferral<MIXED>(d, i, j, c);
+            return;
+        }
+        slot = resolved_slot(d, i * cols + j, c.iK);
+        if (slot < 0) return;
+    }
+    if (MODE == MODE_FAST) {
+        if (MIXED)
+            bin_den3(d, slot, c.bin);
+        else
+            bin_num3(d, slot, c.bin, c);
+    } else if (MODE == MODE_COUNT) {
+        atomicAdd(d.caps.rowcnt + (long long)slot * rows + i, 1u);
+    } else if (i < d.caps.row_cut[slot]) {
+        if (MIXED)
+            bin_den3(d, slot, c.bin);
+        else
+            bin_num3(d, slot, c.bin, c);
+    }
+}
+
+__device__ __forceinline__ void tri_tile(long long k, long long &ti, long long &tj) {
+    long long b = (long long)((sqrt(8.0 * (double)k + 1.0) - 1.0) * 0.5);
+    while (b * (b + 1) / 2 > k) b--;
+    while ((b + 1) * (b + 2) / 2 <= k) b++;
+    tj = b;
+    ti = k - b * (b + 1) / 2;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TILE) k_same(Device d, long long n, Cols8 c) {
+    __shared__ double sj[8][TILE];
+    long long ti, tj;
+    tri_tile(blockIdx.x, ti, tj);
+    const int tid = threadIdx.x;
+    const long long j0 = tj * TILE;
+    for (int f = 0; f < 8; f++) sj[f][tid] = (j0 + tid < n) ? c.p[f][j0 + tid] : 0.0;
+    __syncthreads();
+    const long long i = ti * TILE + tid;
+    if (i >= n) return;
+    const double apx = c.p[0][i], apy = c.p[1][i], apz = c.p[2][i], aE = c.p[3][i];
+    const double ax[4] = {c.p[4][i], c.p[5][i], c.p[6][i], c.p[7][i]};
+    const int jend = (int)min((long long)TILE, n - j0);
+    for (int jj = 0; jj < jend; jj++) {
+        const long long j = j0 + jj;
+        if (j <= i) continue;
+        const double bx[4] = {sj[4][jj], sj[5][jj], sj[6][jj], sj[7][jj]};
+        const Chain ch = pair_chain<false>(d.g, apx, apy, apz, aE, sj[0][jj], sj[1][jj],
+                                           sj[2][jj], sj[3][jj], ax, bx);
+        consume<false, MODE>(d, i, j, n, n, ch);
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TILE) k_mixed(Device d, long long n1, Cols4 l1,
+                                                long long n2, Cols4 l2, long long tiles1) {
+    __shared__ double sj[4][TILE];
+    const long long ti = blockIdx.x % tiles1;
+    const long long tj = blockIdx.x / tiles1;
+    const int tid = threadIdx.x;
+    const long long j0 = tj * TILE;
+    for (int f = 0; f < 4; f++) sj[f][tid] = (j0 + tid < n2) ? l2.p[f][j0 + tid] : 0.0;
+    __syncthreads();
+    const long long i = ti * TILE + tid;
+    if (i >= n1) return;
+    const double apx = l1.p[0][i], apy = l1.p[1][i], apz = l1.p[2][i], aE = l1.p[3][i];
+    const int jend = (int)min((long long)TILE, n2 - j0);
+    for (int jj = 0; jj < jend; jj++) {
+        const Chain ch = pair_chain<true>(d.g, apx, apy, apz, aE, sj[0][jj], sj[1][jj],
+                                          sj[2][jj], sj[3][jj], nullptr, nullptr);
+        consume<true, MODE>(d, i, j0 + jj, n2, n1, ch);
+    }
+}
+
+// Ordered admission of one stream bin's cut row: the first `quota`
+// survivors in pair order (one warp per stream bin).
+template <bool MIXED>
+__global__ void k_straddle(Device d, long long rows, long long cols, Cols8 a8, Cols4 b4) {
+    const int b = blockIdx.x;
+    const long long r = d.caps.row_cut[b];
+    if (r >= rows) return;
+    const unsigned long long quota = d.caps.quota[b];
+    const int lane = threadIdx.x;
+    const int ns = d.g.n_slots;
+    unsigned long long admitted = 0;
+    const double apx = a8.p[0][r], apy = a8.p[1][r], apz = a8.p[2][r], aE = a8.p[3][r];
+    double ax[4] = {0, 0, 0, 0};
+    if (!MIXED) {
+        ax[0] = a8.p[4][r];
+        ax[1] = a8.p[5][r];
+        ax[2] = a8.p[6][r];
+        ax[3] = a8.p[7][r];
+    }
+    const long long jstart = MIXED ? 0 : r + 1;
+    for (long long j0 = jstart; j0 < cols && admitted < quota; j0 += 32) {
+        const long long j = j0 + lane;
+        Chain c;
+        c.iK = -1;
+        bool has = false;
+        int slot = -1;
+        if (j < cols) {
+            double bx[4] = {0, 0, 0, 0};
+            if (!MIXED) {
+                bx[0] = a8.p[4][j];
+                bx[1] = a8.p[5][j];
+                bx[2] = a8.p[6][j];
+                bx[3] = a8.p[7][j];
+            }
+            const double *src0 = MIXED ? b4.p[0] : a8.p[0];
+            const double *src1 = MIXED ? b4.p[1] : a8.p[1];
+            const double *src2 = MIXED ? b4.p[2] : a8.p[2];
+            const double *src3 = MIXED ? b4.p[3] : a8.p[3];
+            c = pair_chain<MIXED>(d.g, apx, apy, apz, aE, src0[j], src1[j], src2[j], src3[j],
+                                  ax, bx);
+            if (c.iK >= 0) {
+                if (b >= ns) {
+                    has = c.qi_k >= 0 && ns + c.iK == b;
+                } else if (c.ev3 == 1) {
+                    slot = c.slot;
+                    has = slot == b;
+                } else if (c.ev3 == 2) {
+                    slot = resolved_slot(d, r * cols + j, c.iK);
+                    has = slot == b;
+                }
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, has);
+        const unsigned long long rank =
+            admitted + __popc(m & ((1u << lane) - 1u));
+        if (has && rank < quota) {
+            if (b >= ns) {
+                if (MIXED)
+                    bin_den_qinv(d, c);
+                else
+                    bin_num_qinv(d, c);
+            } else {
+                if (MIXED)
+                    bin_den3(d, slot, c.bin);
+                else
+                    bin_num3(d, slot, c.bin, c);
+            }
+        }
+        admitted += __popc(m);
+    }
+}
+
+// Per stream bin: first row at which the running survivor count exceeds
+// remaining[b]; everything before it is admitted, `quota` more inside it.
+__global__ void __launch_bounds__(1024) k_cut(Device d, long long rows,
+                                              const unsigned long long *remaining) {
+    const int b = blockIdx.x;
+    const unsigned long long rem = remaining[b];
+    const unsigned *rc = d.caps.rowcnt + (long long)b * rows;
+    __shared__ unsigned long long warp_tot[32];
+    __shared__ long long found;
+    __shared__ unsigned long long found_quota;
+    if (threadIdx.x == 0) found = rows;
+    unsigned long long running = 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (long long base = 0; base < rows; base += 1024) {
+        const long long r = base + threadIdx.x;
+        const unsigned long long v = r < rows ? rc[r] : 0;
+        unsigned long long incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_tot[w] = incl;
+        __syncthreads();
+        unsigned long long before = 0;
+        for (int k = 0; k < w; k++) before += warp_tot[k];
+        incl += before;
+        unsigned long long chunk = 0;
+        for (int k = 0; k < 32; k++) chunk += warp_tot[k];
+        const unsigned long long excl = running + incl - v;
+        if (r < rows && running + incl > rem && excl <= rem) {
+            // exactly one row satisfies this: the first that crosses rem
+            found = r;
+            found_quota = rem - excl;
+        }
+        __syncthreads();
+        if (found < rows) break;
+        running += chunk;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        d.caps.row_cut[b] = found;
+        d.caps.quota[b] = found < rows ? found_quota : 0ull;
+    }
+}
+
+// Bins deferred records with their host-resolved K_phi bins (fast mode).
+__global__ void k_apply(Device d, const Deferral *rec, const int *iphi, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int ip = iphi[k];
+    if (ip < 0) return;
+    const Deferral r = rec[k];
+    const long long at = (long long)(r.iK * d.g.n_Kphi + ip) * d.g.q3 + r.bin;
+    if (r.mixed) {
+        atomicAdd(d.h.den + at, 1ull);
+    } else {
+        Sums *s = d.h.sums + at;
+        atomicAdd(&s->qo, r.qo);
+        atomicAdd(&s->qs, r.qs);
+        atomicAdd(&s->ql, r.ql);
+        atomicAdd(&s->w, r.cosw);
+        atomicAdd(d.h.cnt + at, 1ull);
+    }
+}
+
+// Adds host-resolved deferred pairs to the per-row survivor counts.
+__global__ void k_defer_count(Device d, long long rows, long long cols, int n_res) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_res) return;
+    const Resolved rv = d.caps.resolved[k];
+    if (rv.iphi < 0) return;
+    const long long i = rv.key / cols;
+    const int slot = rv.iK * d.g.n_Kphi + rv.iphi;
+    atomicAdd(d.caps.rowcnt + (long long)slot * rows + i, 1u);
+}
+
+// Pair counters = sums of the count histograms (each counter is
+// incremented exactly when a pair is binned).  out: [num slots][den
+// slots][num q_inv][den q_inv].
+__global__ void __launch_bounds__(256) k_counters(Device d, unsigned long long *out) {
+    const int ns = d.g.n_slots, nk = d.g.n_KT;
+    const int b = blockIdx.x;
+    const u64 *src;
+    long long len;
+    if (b < ns) {
+        src = d.h.cnt + (long long)b * d.g.q3;
+        len = d.g.q3;
+    } else if (b < 2 * ns) {
+        src = d.h.den + (long long)(b - ns) * d.g.q3;
+        len = d.g.q3;
+    } else if (b < 2 * ns + nk) {
+        src = d.h.qi_cnt + (long long)(b - 2 * ns) * d.g.qnpts;
+        len = d.g.qnpts;
+    } else {
+        src = d.h.qi_den + (long long)(b - 2 * ns - nk) * d.g.qnpts;
+        len = d.g.qnpts;
+    }
+    unsigned long long s = 0;
+    for (long long k = threadIdx.x; k < len; k += blockDim.x) s += src[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    __shared__ unsigned long long ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int k = 0; k < 8; k++) t += ws[k];
+        out[b] = t;
+    }
+}
+
+Cols8 cols8(const double *const *c) {
+    Cols8 r;
+    for (int f = 0; f < 8; f++) r.p[f] = c ? c[f] : nullptr;
+    return r;
+}
+Cols4 cols4(const double *const *c) {
+    Cols4 r;
+    for (int f = 0; f < 4; f++) r.p[f] = c ? c[f] : nullptr;
+    return r;
+}
+
+}  // namespace
+
+cudaError_t launch_same(const Device &d, int mode, long long n, const double *const *c8,
+                        cudaStream_t st) {
+    if (n < 2) return cudaSuccess;
+    const long long nt = (n + TILE - 1) / TILE;
+    const long long blocks = nt * (nt + 1) / 2;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const Cols8 c = cols8(c8);
+    if (mode == MODE_FAST)
+        k_same<MODE_FAST><<<(unsigned)blocks, TILE, 0, st>>>(d, n, c);
+    else if (mode == MODE_COUNT)
+        k_same<MODE_COUNT><<<(unsigned)blocks, TILE, 0, st>>>(d, n, c);
+    else
+        k_same<MODE_ORDER><<<(unsigned)blocks, TILE, 0, st>>>(d, n, c);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mixed(const Device &d, int mode, long long n1, const double *const *l1,
+                         long long n2, const double *const *l2, cudaStream_t st) {
+    if (n1 < 1 || n2 < 1) return cudaSuccess;
+    const long long t1 = (n1 + TILE - 1) / TILE, t2 = (n2 + TILE - 1) / TILE;
+    const long long blocks = t1 * t2;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const Cols4 a = cols4(l1), b = cols4(l2);
+    if (mode == MODE_FAST)
+        k_mixed<MODE_FAST><<<(unsigned)blocks, TILE, 0, st>>>(d, n1, a, n2, b, t1);
+    else if (mode == MODE_COUNT)
+        k_mixed<MODE_COUNT><<<(unsigned)blocks, TILE, 0, st>>>(d, n1, a, n2, b, t1);
+    else
+        k_mixed<MODE_ORDER><<<(unsigned)blocks, TILE, 0, st>>>(d, n1, a, n2, b, t1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_same_straddle(const Device &d, long long n, const double *const *c8,
+                                 int n_stream, cudaStream_t st) {
+    k_straddle<false><<<n_stream, 32, 0, st>>>(d, n, n, cols8(c8), cols4(nullptr));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_straddle(const Device &d, long long n1, const double *const *l1,
+                                  long long n2, const double *const *l2, int n_stream,
+                                  cudaStream_t st) {
+    Cols8 a;
+    for (int f = 0; f < 8; f++) a.p[f] = f < 4 ? l1[f] : nullptr;
+    k_straddle<true><<<n_stream, 32, 0, st>>>(d, n1, n2, a, cols4(l2));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cut(const Device &d, long long rows, int n_stream,
+                       const unsigned long long *remaining, cudaStream_t st) {
+    k_cut<<<n_stream, 1024, 0, st>>>(d, rows, remaining);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply(const Device &d, const Deferral *rec, const int *iphi, int n,
+                         cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_apply<<<(n + 127) / 128, 128, 0, st>>>(d, rec, iphi, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, int n_res,
+                               cudaStream_t st) {
+    if (n_res <= 0) return cudaSuccess;
+    k_defer_count<<<(n_res + 127) / 128, 128, 0, st>>>(d, rows, cols, n_res);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_counters(const Device &d, unsigned long long *out, cudaStream_t st) {
+    k_counters<<<2 * d.g.n_slots + 2 * d.g.n_KT, 256, 0, st>>>(d, out);
+    return cudaGetLastError();
+}
+
+}  // namespace hbt

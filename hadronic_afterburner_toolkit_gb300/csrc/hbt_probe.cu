@@ -1,0 +1,62 @@
+// Pipe-throughput probes used by the benchmark to measure, on the GPU it runs
+// on, the peak issue rate of the arithmetic the HBT kernels are bound by
+// (FP64 and FP32 fused multiply-add).  Each thread runs 8 independent FMA
+// chains in registers and writes one value, so the memory traffic is one
+// store per thread.
+#include <cuda_runtime.h>
+
+namespace {
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma(T *out, int iters, T a, T b) {
+    T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    T x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int k = 0; k < iters; k++) {
+        x0 = x0 * a + b;
+        x1 = x1 * a + b;
+        x2 = x2 * a + b;
+        x3 = x3 * a + b;
+        x4 = x4 * a + b;
+        x5 = x5 * a + b;
+        x6 = x6 * a + b;
+        x7 = x7 * a + b;
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <typename T>
+int run(int blocks, int iters, float *ms, double *flops) {
+    T *out = nullptr;
+    if (cudaMalloc(&out, (size_t)blocks * 256 * sizeof(T)) != cudaSuccess) return 1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fma<T><<<blocks, 256>>>(out, iters / 8 + 1, (T)0.999, (T)0.001);  // warm-up
+    cudaEventRecord(e0);
+    k_fma<T><<<blocks, 256>>>(out, iters, (T)0.999, (T)0.001);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    *flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const cudaError_t err = cudaGetLastError();
+    cudaFree(out);
+    return err == cudaSuccess ? 0 : 2;
+}
+
+}  // namespace
+
+extern "C" {
+
+// FP64 FMA throughput: returns 0 and the elapsed ms and flop count.
+int hbt_probe_fp64(int blocks, int iters, float *ms, double *flops) {
+    return run<double>(blocks, iters, ms, flops);
+}
+
+// FP32 FMA throughput.
+int hbt_probe_fp32(int blocks, int iters, float *ms, double *flops) {
+    return run<float>(blocks, iters, ms, flops);
+}
+
+}  // extern "C"

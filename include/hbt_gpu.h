@@ -1,0 +1,162 @@
+/*
+ * hbt_gpu.h - C ABI of the GB300 HBT pair-binning engine (libhbt_gpu.so).
+ *
+ * The engine owns the device-resident correlation histograms of one HBT
+ * analysis and bins particle pairs into them with sm_103a CUDA kernels.  It
+ * replaces the pair loops and the histogram storage of the reference's
+ * HBT_correlation class (src/HBT_correlation.{h,cpp} of
+ * chunshen1987/hadronic_afterburner_toolkit); the host side (parameter
+ * reading, event buffering, rapidity gather, random partner selection and
+ * rotation, output files) stays in C++ above this boundary.
+ *
+ * Conventions
+ *  - Plain C types only.  Every entry point returns an hbt_status
+ *    (HBT_OK == 0); hbt_last_error() describes the last failure.  Nothing
+ *    calls exit() or throws across the boundary.
+ *  - Host arrays passed in are read during the call only.  Device arrays
+ *    (the *_dev entry points) must stay valid until the work is complete
+ *    (hbt_sync).
+ *  - Work is ordered on the context's CUDA stream.  A context is used by
+ *    one host thread at a time.
+ *  - Bin indices and pair counts are bit-exact against the reference's CPU
+ *    path; the cos(q.dx) numerator and mean-q sums are FP64 sums whose
+ *    order differs (relative difference of order 1e-15 per bin).
+ */
+#ifndef HBT_GPU_H
+#define HBT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hbt_status {
+    HBT_OK = 0,
+    HBT_ERR_INVALID = 1,  /* bad argument or parameter */
+    HBT_ERR_CUDA = 2,     /* a CUDA call failed */
+    HBT_ERR_NOMEM = 3,    /* device or host allocation failed */
+    HBT_ERR_TIMEOUT = 4,  /* hbt_sync budget ran out */
+    HBT_ERR_DEVICE = 5,   /* a kernel raised its error flag */
+    HBT_ERR_STATE = 6     /* call not valid in the context's current state */
+} hbt_status;
+
+/* Numerics of the weights and q sums. */
+typedef enum hbt_precision {
+    HBT_PRECISION_FP64 = 0, /* plain form: everything in FP64 */
+    HBT_PRECISION_FP32W = 1 /* cos(q.dx) weight and q sums in FP32 partials,
+                               merged into FP64 bins with Kahan compensation;
+                               bins and counts stay exact */
+} hbt_precision;
+
+/* The HBT keys of parameters.dat that shape the histograms
+ * (HBT_correlation::HBT_correlation, src/HBT_correlation.cpp:16-143). */
+typedef struct hbt_params {
+    int32_t qnpts;                  /* "qnpts" */
+    double q_min, q_max;            /* "q_min", "q_max" [GeV] */
+    int32_t n_KT;                   /* "n_KT": number of K_T edges */
+    double KT_min, KT_max;          /* "KT_min", "KT_max" [GeV] */
+    int32_t n_Kphi;                 /* "n_Kphi" */
+    int32_t azimuthal_flag;         /* "azimuthal_flag" */
+    int32_t invariant_radius_flag;  /* "invariant_radius_flag" */
+    int32_t long_comoving_boost;    /* "long_comoving_boost" */
+    double needed_number_of_pairs;  /* "needed_number_of_pairs" (pair cap) */
+    int32_t precision;              /* hbt_precision */
+    /* Half-width (rad) of the zone around a K_phi bin edge inside which a
+     * pair's azimuthal bin is decided on the host with the C library's
+     * atan2 instead of the device's; 0 selects the default (1e-13). */
+    double kphi_defer_tol;
+} hbt_params;
+
+typedef struct hbt_ctx hbt_ctx;
+
+/* Structure-of-arrays particle lists, FP64. */
+typedef struct hbt_soa8 {
+    const double *px, *py, *pz, *E, *x, *y, *z, *t;
+} hbt_soa8;
+typedef struct hbt_soa4 {
+    const double *px, *py, *pz, *E;
+} hbt_soa4;
+
+/* Totals kept by the engine. */
+typedef struct hbt_stats {
+    uint64_t pairs_same;      /* candidate same-event pairs, n(n-1)/2 summed */
+    uint64_t pairs_mixed;     /* candidate mixed-event pairs, n1*n2 summed */
+    uint64_t launches;        /* kernel launches issued */
+    uint64_t ordered_passes;  /* launches that needed ordered cap admission */
+    uint64_t deferred_kphi;   /* pairs whose K_phi bin was decided on the host */
+    uint64_t anomalies;       /* pairs skipped: NaN LCMS component (K_perp == 0)
+                                 or a K_T index outside [0, n_KT) */
+} hbt_stats;
+
+/* Creates a context on `device` and allocates the zeroed histograms
+ * (replaces the histogram allocation of HBT_correlation::HBT_correlation,
+ * src/HBT_correlation.cpp:16-143). */
+hbt_status hbt_create(const hbt_params *params, int device, hbt_ctx **out);
+void hbt_destroy(hbt_ctx *ctx);
+const char *hbt_last_error(const hbt_ctx *ctx);
+
+/* Uses a caller-owned cudaStream_t (NULL: the context's own stream). */
+hbt_status hbt_set_stream(hbt_ctx *ctx, void *cuda_stream);
+
+/* Event-plane reference angle for the K_phi bins of the next launches
+ * (the psi_ref member set by calculate_flow_event_plane_angle,
+ * src/HBT_correlation.cpp:233-249). */
+hbt_status hbt_set_psi_ref(hbt_ctx *ctx, double psi_ref);
+
+/* Zeroes histograms, pair counters and statistics. */
+hbt_status hbt_reset(hbt_ctx *ctx);
+
+/* Same-event pairs i < j of one gathered buffer, host arrays
+ * (replaces the pair loop of HBT_correlation::combine_and_bin_particle_pairs,
+ * src/HBT_correlation.cpp:282-461). */
+hbt_status hbt_bin_same(hbt_ctx *ctx, int64_t n, const hbt_soa8 *list);
+
+/* Mixed-event pairs list1 x list2 (list2 = the rotated partners), host
+ * arrays (replaces the pair loop of
+ * HBT_correlation::combine_and_bin_particle_pairs_mixed_events,
+ * src/HBT_correlation.cpp:554-689). */
+hbt_status hbt_bin_mixed(hbt_ctx *ctx, int64_t n1, const hbt_soa4 *list1,
+                         int64_t n2, const hbt_soa4 *list2);
+
+/* As above with device-resident arrays (inputs already in HBM). */
+hbt_status hbt_bin_same_dev(hbt_ctx *ctx, int64_t n, const hbt_soa8 *list);
+hbt_status hbt_bin_mixed_dev(hbt_ctx *ctx, int64_t n1, const hbt_soa4 *list1,
+                             int64_t n2, const hbt_soa4 *list2);
+
+/* Waits for the context's stream, polling up to timeout_us microseconds
+ * (0: wait without limit).  Returns HBT_ERR_TIMEOUT if work is still
+ * running, HBT_ERR_DEVICE if a kernel raised its error flag. */
+hbt_status hbt_sync(hbt_ctx *ctx, uint64_t timeout_us);
+
+/* Number of 3-D bins: n_slots * qnpts^3 with n_slots = n_KT, or
+ * n_KT * n_Kphi when azimuthal_flag == 1.  Bin order [slot][iqout][iqside]
+ * [iqlong], slot = iKT (* n_Kphi + iKphi). */
+int64_t hbt_n_bins(const hbt_ctx *ctx);
+
+/* Copies the histograms to host arrays of hbt_n_bins() doubles (any may be
+ * NULL): numerator pair count, q_out / q_side / q_long sums, cos(q.dx)
+ * numerator, denominator pair count.  These are the arrays the reference's
+ * writer reads (correl_3d_num_count, q_out_mean, q_side_mean, q_long_mean,
+ * correl_3d_num, correl_3d_denorm and their K_phi twins,
+ * src/HBT_correlation.h:55-61). */
+hbt_status hbt_read_hist(hbt_ctx *ctx, double *num_count, double *q_out_sum,
+                         double *q_side_sum, double *q_long_sum, double *num,
+                         double *den);
+
+/* q_inv histograms, n_KT * qnpts doubles each (q_inv_mean,
+ * correl_1d_inv_num, correl_1d_inv_num_count, correl_1d_inv_denorm). */
+hbt_status hbt_read_qinv(hbt_ctx *ctx, double *qinv_sum, double *num,
+                         double *num_count, double *den);
+
+/* Pair counters (number_of_pairs_{numerator,denormenator}_KTdiff or
+ * _KTKphidiff: n_slots entries; _qinv_: n_KT entries). */
+hbt_status hbt_read_counters(hbt_ctx *ctx, uint64_t *num, uint64_t *den,
+                             uint64_t *num_qinv, uint64_t *den_qinv);
+
+hbt_status hbt_get_stats(hbt_ctx *ctx, hbt_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HBT_GPU_H */

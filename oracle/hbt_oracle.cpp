@@ -94,6 +94,10 @@ struct orc_ctx {
     std::vector<double> KT_array, Kphi_array, q_grid;
     double psi_ref = 0.0;
     Hist h;
+    // per-thread partial histograms of the multi-threaded loops, merged into
+    // h before anything reads h; pend_* bound the pairs they hold
+    std::vector<Hist> part;
+    unsigned long long pend_num = 0, pend_den = 0;
     unsigned long long pairs_same = 0, pairs_mixed = 0;
     std::mt19937 gen;
     std::uniform_real_distribution<double> u01{0.0, 1.0};
@@ -101,6 +105,20 @@ struct orc_ctx {
 };
 
 namespace {
+
+void flush_parts(const orc_ctx *cc) {
+    orc_ctx *c = const_cast<orc_ctx *>(cc);
+    for (auto &x : c->part) c->h.add(x);
+    c->part.clear();
+    c->pend_num = c->pend_den = 0;
+}
+
+void ensure_parts(orc_ctx *c, int nthreads) {
+    if ((int)c->part.size() == nthreads) return;
+    flush_parts(c);
+    c->part.resize(nthreads);
+    for (auto &x : c->part) x.init(c->n_slots * c->q3, c->n_slots, c->p.n_KT, c->p.qnpts);
+}
 
 inline int slot_of(const orc_ctx &c, int iK, int iphi) {
     return c.p.azimuthal_flag ? iK * c.p.n_Kphi + iphi : iK;
@@ -390,12 +408,14 @@ double orc_event_plane_angle(int64_t n, const double *px, const double *py,
 }
 
 void orc_bin_same(orc_ctx *c, int64_t n, const double *const *cols8) {
+    flush_parts(c);
     c->pairs_same += (unsigned long long)(n * (n - 1) / 2);
     same_rows(*c, c->h, n, cols8, 0, 1, true);
 }
 
 void orc_bin_mixed(orc_ctx *c, int64_t n1, const double *const *l1, int64_t n2,
                    const double *const *l2) {
+    flush_parts(c);
     c->pairs_mixed += (unsigned long long)(n1 * n2);
     mixed_rows(*c, c->h, n1, l1, n2, l2, 0, 1, true);
 }
@@ -403,38 +423,38 @@ void orc_bin_mixed(orc_ctx *c, int64_t n1, const double *const *l1, int64_t n2,
 void orc_bin_same_mt(orc_ctx *c, int64_t n, const double *const *cols8,
                      int32_t nthreads) {
     const unsigned long long pairs = (unsigned long long)(n * (n - 1) / 2);
-    if (nthreads <= 1 || !caps_cannot_bind(*c, c->h.c_num, c->h.c_num_qi, pairs)) {
+    if (nthreads <= 1 ||
+        !caps_cannot_bind(*c, c->h.c_num, c->h.c_num_qi, pairs + c->pend_num)) {
+        flush_parts(c);
         orc_bin_same(c, n, cols8);
         return;
     }
+    ensure_parts(c, nthreads);
     c->pairs_same += pairs;
-    std::vector<Hist> part(nthreads);
+    c->pend_num += pairs;
     std::vector<std::thread> th;
-    for (int t = 0; t < nthreads; t++) {
-        part[t].init(c->n_slots * c->q3, c->n_slots, c->p.n_KT, c->p.qnpts);
-        th.emplace_back([&, t] { same_rows(*c, part[t], n, cols8, t, nthreads, false); });
-    }
+    for (int t = 0; t < nthreads; t++)
+        th.emplace_back([&, t] { same_rows(*c, c->part[t], n, cols8, t, nthreads, false); });
     for (auto &x : th) x.join();
-    for (auto &x : part) c->h.add(x);
 }
 
 void orc_bin_mixed_mt(orc_ctx *c, int64_t n1, const double *const *l1, int64_t n2,
                       const double *const *l2, int32_t nthreads) {
     const unsigned long long pairs = (unsigned long long)(n1 * n2);
-    if (nthreads <= 1 || !caps_cannot_bind(*c, c->h.c_den, c->h.c_den_qi, pairs)) {
+    if (nthreads <= 1 ||
+        !caps_cannot_bind(*c, c->h.c_den, c->h.c_den_qi, pairs + c->pend_den)) {
+        flush_parts(c);
         orc_bin_mixed(c, n1, l1, n2, l2);
         return;
     }
+    ensure_parts(c, nthreads);
     c->pairs_mixed += pairs;
-    std::vector<Hist> part(nthreads);
+    c->pend_den += pairs;
     std::vector<std::thread> th;
-    for (int t = 0; t < nthreads; t++) {
-        part[t].init(c->n_slots * c->q3, c->n_slots, c->p.n_KT, c->p.qnpts);
+    for (int t = 0; t < nthreads; t++)
         th.emplace_back(
-            [&, t] { mixed_rows(*c, part[t], n1, l1, n2, l2, t, nthreads, false); });
-    }
+            [&, t] { mixed_rows(*c, c->part[t], n1, l1, n2, l2, t, nthreads, false); });
     for (auto &x : th) x.join();
-    for (auto &x : part) c->h.add(x);
 }
 
 void orc_process_buffer(orc_ctx *c, int32_t nev, const int64_t *off,
@@ -495,6 +515,7 @@ int64_t orc_n_bins(const orc_ctx *c) { return c->n_slots * c->q3; }
 
 void orc_get_hist(const orc_ctx *c, double *num_count, double *q_out_sum,
                   double *q_side_sum, double *q_long_sum, double *num, double *den) {
+    flush_parts(c);
     const size_t n = c->h.cnt.size() * sizeof(double);
     if (num_count) memcpy(num_count, c->h.cnt.data(), n);
     if (q_out_sum) memcpy(q_out_sum, c->h.qo.data(), n);
@@ -506,6 +527,7 @@ void orc_get_hist(const orc_ctx *c, double *num_count, double *q_out_sum,
 
 void orc_get_qinv(const orc_ctx *c, double *qinv_sum, double *num, double *num_count,
                   double *den) {
+    flush_parts(c);
     const size_t n = c->h.qi_sum.size() * sizeof(double);
     if (qinv_sum) memcpy(qinv_sum, c->h.qi_sum.data(), n);
     if (num) memcpy(num, c->h.qi_num.data(), n);
@@ -515,6 +537,7 @@ void orc_get_qinv(const orc_ctx *c, double *qinv_sum, double *num, double *num_c
 
 void orc_get_counters(const orc_ctx *c, uint64_t *num, uint64_t *den,
                       uint64_t *num_qinv, uint64_t *den_qinv) {
+    flush_parts(c);
     for (int s = 0; s < c->n_slots; s++) {
         if (num) num[s] = c->h.c_num[s];
         if (den) den[s] = c->h.c_den[s];
@@ -525,7 +548,10 @@ void orc_get_counters(const orc_ctx *c, uint64_t *num, uint64_t *den,
     }
 }
 
-uint64_t orc_anomalies(const orc_ctx *c) { return c->h.anomalies; }
+uint64_t orc_anomalies(const orc_ctx *c) {
+    flush_parts(c);
+    return c->h.anomalies;
+}
 uint64_t orc_pairs_same(const orc_ctx *c) { return c->pairs_same; }
 uint64_t orc_pairs_mixed(const orc_ctx *c) { return c->pairs_mixed; }
 
@@ -562,6 +588,7 @@ void write_3d(const orc_ctx &c, FILE *f, int slot, double ratio, bool eco) {
 }  // namespace
 
 int orc_write(const orc_ctx *c, const char *path, int32_t eco_output) {
+    flush_parts(c);
     const bool eco = eco_output == 1;
     if (c->p.invariant_radius_flag == 1) {
         for (int iK = 0; iK < c->p.n_KT - 1; iK++) {

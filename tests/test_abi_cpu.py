@@ -1,0 +1,59 @@
+"""The C ABI library builds for sm_103a, loads without a GPU and exports
+every entry point include/hbt_gpu.h declares (no compute calls here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from hadronic_afterburner_toolkit_gb300 import build, engine
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                      "include", "hbt_gpu.h")
+
+
+def _declared_functions(path):
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(hbt_[a-z_0-9]+)\s*\(", text)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build_gpu()
+    return ctypes.CDLL(engine.LIB_PATH)
+
+
+def test_header_declares_the_engine_api():
+    names = _declared_functions(HEADER)
+    assert "hbt_create" in names and "hbt_bin_same" in names and "hbt_bin_mixed" in names
+    # the Python mirror binds exactly what the header declares
+    assert sorted(engine.exported_symbols()) == names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in _declared_functions(HEADER):
+        assert hasattr(lib, name), name
+
+
+def test_binding_loads_without_gpu(lib):
+    L = engine.load()
+    assert L.hbt_n_bins(None) == 0
+    assert L.hbt_last_error(None) == b"null context"
+
+
+def test_invalid_parameters_rejected_before_any_device_call(lib):
+    L = engine.load()
+    p = engine.HbtParams(qnpts=1, q_min=-0.1, q_max=0.1, n_KT=5, KT_min=0, KT_max=1,
+                         n_Kphi=4, needed_number_of_pairs=1e18)
+    h = ctypes.c_void_p()
+    assert L.hbt_create(ctypes.byref(p), 0, ctypes.byref(h)) == 1  # HBT_ERR_INVALID
+    p.qnpts = 11
+    p.precision = 7
+    assert L.hbt_create(ctypes.byref(p), 0, ctypes.byref(h)) == 1
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(engine.HbtError):
+        engine.load(str(tmp_path / "libhbt_gpu.so"))

@@ -1,0 +1,250 @@
+"""GPU parity of the C-ABI engine against the CPU oracle (FP64 form).
+
+Counts, denominators and pair counters must be identical to the oracle's;
+the FP64 sums agree to the tolerance stated in tests/parity.py.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib
+import parity
+
+pytestmark = pytest.mark.gpu
+
+BASIC = dict(qnpts=9, q_min=-0.15, q_max=0.15, n_KT=5, KT_min=0.0, KT_max=1.0, n_Kphi=4,
+             azimuthal_flag=0, invariant_radius_flag=0, long_comoving_boost=1,
+             needed_number_of_pairs=1e18)
+FULL = dict(BASIC, invariant_radius_flag=1, azimuthal_flag=1, n_Kphi=4, q_min=0.0, q_max=0.2,
+            qnpts=11)
+CUTS = dict(BASIC, KT_min=0.15, KT_max=0.55, long_comoving_boost=0, q_min=-0.1, q_max=0.2,
+            qnpts=7, n_KT=4)
+PARAMS = {"basic": BASIC, "full": FULL, "cuts": CUTS}
+
+
+def _engine(**kw):
+    from hadronic_afterburner_toolkit_gb300 import engine
+    return engine.Engine(**kw)
+
+
+def _oracle(**kw):
+    kw = dict(kw)
+    kw.pop("kphi_defer_tol", None)
+    return oracle_lib.Oracle(**kw)
+
+
+def _qscale(p):
+    return max(abs(p["q_min"]), abs(p["q_max"])) + (p["q_max"] - p["q_min"]) / (p["qnpts"] - 1)
+
+
+@pytest.mark.parametrize("name", sorted(PARAMS))
+def test_same_event_matches_oracle(name):
+    p = PARAMS[name]
+    ev = parity.lists(seed=101)
+    eng, orc = _engine(**p), _oracle(**p)
+    eng.set_psi_ref(0.37)
+    orc.set_psi_ref(0.37)
+    c = parity.cols8(ev)
+    eng.bin_same(c)
+    orc.bin_same(c)
+    h = orc.hist()
+    assert h["count"].sum() > 100
+    parity.compare(eng.hist(), h, _qscale(p))
+
+
+@pytest.mark.parametrize("name", sorted(PARAMS))
+def test_mixed_event_matches_oracle(name):
+    p = PARAMS[name]
+    ev = parity.lists(seed=202)
+    eng, orc = _engine(**p), _oracle(**p)
+    eng.set_psi_ref(-1.1)
+    orc.set_psi_ref(-1.1)
+    m = ev.multiplicities()
+    o = ev.offsets
+    for e in range(3):
+        l1 = parity.rotated4(ev, 0.0, o[e], o[e + 1])
+        l2 = [np.concatenate(x) for x in zip(*[parity.rotated4(ev, 0.3 + k, o[k], o[k + 1])
+                                              for k in range(ev.n_events) if k != e])]
+        eng.bin_mixed(l1, l2)
+        orc.bin_mixed(l1, l2)
+    h = orc.hist()
+    assert h["den"].sum() > 100
+    parity.compare(eng.hist(), h, _qscale(p))
+    assert m.sum() > 0
+
+
+def test_several_buffers_accumulate():
+    p = dict(BASIC, invariant_radius_flag=1, q_min=0.0, q_max=0.2)
+    eng, orc = _engine(**p), _oracle(**p)
+    for seed in (1, 2, 3):
+        ev = parity.lists(seed=seed, n_events=4)
+        c = parity.cols8(ev)
+        eng.bin_same(c)
+        orc.bin_same(c)
+        l1 = parity.rotated4(ev, 0.0, 0, ev.offsets[1])
+        l2 = parity.rotated4(ev, 1.0, ev.offsets[1], None)
+        eng.bin_mixed(l1, l2)
+        orc.bin_mixed(l1, l2)
+    parity.compare(eng.hist(), orc.hist(), _qscale(p))
+
+
+@pytest.mark.parametrize("az", [0, 1])
+def test_binding_caps_admit_pairs_in_reference_order(az):
+    """needed_number_of_pairs binds inside launches: ordered admission."""
+    p = dict(BASIC, invariant_radius_flag=1, azimuthal_flag=az, n_Kphi=3,
+             needed_number_of_pairs=37)
+    eng, orc = _engine(**p), _oracle(**p)
+    eng.set_psi_ref(0.2)
+    orc.set_psi_ref(0.2)
+    for seed in (11, 12):
+        ev = parity.lists(seed=seed, n_events=5)
+        c = parity.cols8(ev)
+        eng.bin_same(c)
+        orc.bin_same(c)
+        o = ev.offsets
+        for e in range(ev.n_events):
+            l1 = parity.rotated4(ev, 0.0, o[e], o[e + 1])
+            l2 = parity.rotated4(ev, 0.7 * e, o[(e + 1) % ev.n_events],
+                                 o[(e + 1) % ev.n_events + 1])
+            eng.bin_mixed(l1, l2)
+            orc.bin_mixed(l1, l2)
+    h = orc.hist()
+    assert (h["ctr_num"] == 38).any() and (h["ctr_den"] == 38).any()
+    parity.compare(eng.hist(), h, _qscale(p))
+    assert eng.stats()["ordered_passes"] > 0
+
+
+def test_kphi_edge_pairs_decided_on_host():
+    """A wide deferral zone sends many pairs through the host atan2 path;
+    bins must still equal the oracle's exactly."""
+    p = dict(FULL, kphi_defer_tol=0.05)
+    eng, orc = _engine(**p), _oracle(**p)
+    eng.set_psi_ref(0.11)
+    orc.set_psi_ref(0.11)
+    ev = parity.lists(seed=303)
+    c = parity.cols8(ev)
+    eng.bin_same(c)
+    orc.bin_same(c)
+    l1 = parity.rotated4(ev, 0.0, 0, ev.offsets[2])
+    l2 = parity.rotated4(ev, 2.0, ev.offsets[2], None)
+    eng.bin_mixed(l1, l2)
+    orc.bin_mixed(l1, l2)
+    h = eng.hist()
+    assert eng.stats()["deferred_kphi"] > 100
+    parity.compare(h, orc.hist(), _qscale(p))
+
+
+def test_kphi_deferrals_with_binding_caps():
+    p = dict(FULL, kphi_defer_tol=0.05, needed_number_of_pairs=15, n_Kphi=3)
+    eng, orc = _engine(**p), _oracle(**p)
+    eng.set_psi_ref(-0.4)
+    orc.set_psi_ref(-0.4)
+    ev = parity.lists(seed=404)
+    c = parity.cols8(ev)
+    eng.bin_same(c)
+    orc.bin_same(c)
+    l1 = parity.rotated4(ev, 0.0, 0, ev.offsets[2])
+    l2 = parity.rotated4(ev, 2.0, ev.offsets[2], None)
+    eng.bin_mixed(l1, l2)
+    orc.bin_mixed(l1, l2)
+    parity.compare(eng.hist(), orc.hist(), _qscale(p))
+
+
+def _edge_pairs(p, seed=7, per_edge=25):
+    """Pairs whose q_out / q_side / q_long sit within a few ulps of every bin
+    edge and window bound (K along +x so q_out = q_x, q_side = q_y)."""
+    rng = np.random.default_rng(seed)
+    dq = (p["q_max"] - p["q_min"]) / (p["qnpts"] - 1)
+    base = p["q_min"] - dq / 2.0
+    edges = [base + k * dq for k in range(p["qnpts"] + 1)]
+    edges += [p["q_min"] - dq / 2.0 + 1e-8, p["q_max"] + dq / 2.0 - 1e-8]
+    rows = []
+    for e in edges:
+        for m in range(-per_edge, per_edge + 1):
+            val = e + m * 2.0 ** -55
+            px2 = rng.uniform(0.3, 0.6)
+            py = 0.0  # K_y = 0 exactly, so cos(phi_K) = 1 and sin(phi_K) = 0
+            pz2 = rng.uniform(-0.3, 0.3)
+            which = m % 3
+            qx = val if which == 0 else rng.uniform(-0.05, 0.05)
+            qy = val if which == 1 else rng.uniform(-0.05, 0.05)
+            qz = val if which == 2 else rng.uniform(-0.05, 0.05)
+            p1 = (px2 + qx, py + qy / 2.0, pz2 + qz)
+            p2 = (px2, py - qy / 2.0, pz2)
+            for (x, y, z) in (p1, p2):
+                E = np.sqrt(x * x + y * y + z * z + 0.13957 ** 2)
+                rows.append((x, y, z, E))
+    a = np.array(rows)
+    n = a.shape[0]
+    zeros = rng.normal(0, 1, size=(n, 4))
+    return [a[:, 0].copy(), a[:, 1].copy(), a[:, 2].copy(), a[:, 3].copy(),
+            zeros[:, 0].copy(), zeros[:, 1].copy(), zeros[:, 2].copy(), zeros[:, 3].copy()]
+
+
+@pytest.mark.parametrize("boost", [0, 1])
+def test_bin_edge_pairs_bit_exact(boost):
+    p = dict(BASIC, long_comoving_boost=boost, KT_min=0.3, KT_max=0.6, qnpts=7)
+    c = _edge_pairs(p)
+    eng, orc = _engine(**p), _oracle(**p)
+    eng.bin_same(c)
+    orc.bin_same(c)
+    eng.bin_mixed(c[:4], c[:4])
+    orc.bin_mixed(c[:4], c[:4])
+    h = orc.hist()
+    assert h["count"].sum() > 1000
+    parity.compare(eng.hist(), h, _qscale(p))
+
+
+def test_empty_and_single_particle_lists():
+    p = dict(BASIC, invariant_radius_flag=1)
+    eng, orc = _engine(**p), _oracle(**p)
+    ev = parity.lists(seed=5)
+    for n in (0, 1):
+        c = [x[:n] for x in parity.cols8(ev)]
+        eng.bin_same(c)
+        orc.bin_same(c)
+        eng.bin_mixed(c[:4], parity.cols8(ev)[:4])
+        orc.bin_mixed(c[:4], parity.cols8(ev)[:4])
+    h = eng.hist()
+    assert h["count"].sum() == 0
+    parity.compare(h, orc.hist(), _qscale(p))
+    assert h["pairs_mixed"] == 1 * ev.n_particles
+
+
+def test_counts_repeatable_across_runs():
+    ev = parity.lists(seed=9, n_events=8)
+    c = parity.cols8(ev)
+    hs = []
+    for _ in range(3):
+        eng = _engine(**BASIC)
+        eng.bin_same(c)
+        hs.append(eng.hist())
+    for h in hs[1:]:
+        assert np.array_equal(h["count"], hs[0]["count"])
+        assert np.allclose(h["num"], hs[0]["num"], rtol=0, atol=1e-9)
+
+
+def test_device_resident_entry_points():
+    torch = pytest.importorskip("torch")
+    ev = parity.lists(seed=77)
+    c = parity.cols8(ev)
+    eng_h, eng_d = _engine(**FULL), _engine(**FULL)
+    for e in (eng_h, eng_d):
+        e.set_psi_ref(0.5)
+    eng_h.bin_same(c)
+    dc = [torch.from_numpy(x).cuda() for x in c]
+    eng_d.bin_same(dc, device=True)
+    eng_h.bin_mixed(c[:4], c[:4])
+    eng_d.bin_mixed(dc[:4], dc[:4], device=True)
+    a, b = eng_h.hist(), eng_d.hist()
+    for k in ("count", "den", "qinv_count", "qinv_den"):
+        assert np.array_equal(a[k], b[k])
+
+
+def test_sync_with_timeout_and_stats():
+    eng = _engine(**BASIC)
+    ev = parity.lists(seed=3)
+    eng.bin_same(parity.cols8(ev))
+    eng.sync(timeout_us=10_000_000)
+    st = eng.stats()
+    assert st["pairs_same"] == ev.n_particles * (ev.n_particles - 1) // 2
+    assert st["launches"] >= 1
