@@ -273,8 +273,11 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="central", choices=["central", "small"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32w"])
+    ap.add_argument("--kernel", default="screened", choices=["screened", "reference-chain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the one-step measurement of the plain reference-chain kernel")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -308,7 +311,8 @@ def main() -> None:
         dgroups.append((dc, dm))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(device=dev)
-    eng = E.Engine(device=local, precision=prec, **p)
+    kern = E.KERNEL_SCREENED if args.kernel == "screened" else E.KERNEL_REFERENCE_CHAIN
+    eng = E.Engine(device=local, precision=prec, kernel=kern, **p)
     eng.set_stream(stream.cuda_stream)
 
     def step_device(k):
@@ -356,6 +360,30 @@ def main() -> None:
     else:
         pairs_all = float(pairs)
     value = pairs_all / (t_ms * 1e-3)
+
+    # the plain form (FP64 reference chain on every pair), one step, same GPU
+    plain = None
+    if not args.no_plain and kern == E.KERNEL_SCREENED:
+        engp = E.Engine(device=local, precision=E.PRECISION_FP64,
+                        kernel=E.KERNEL_REFERENCE_CHAIN, **p)
+        engp.set_stream(stream.cuda_stream)
+        g = args.warmup % len(dgroups)
+        dc, dm = dgroups[g]
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        engp.bin_same(dc, device=True)
+        for l1, l2 in dm:
+            engp.bin_mixed(l1, l2, device=True)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        plain = {"kernel": "reference-chain (FP64 reference order on every pair)",
+                 "value": group_pairs(groups[g]) / (ms * 1e-3), "ms_per_step": ms,
+                 "steps": 1}
+        engp.close()
 
     # roofline of the dominant (same-event) kernel against the live FP64 peak
     peaks = measure_fp64_peak()
@@ -431,13 +459,16 @@ def main() -> None:
                            "mixed_partners": 10 if args.workload == "central" else 5,
                            "qnpts": p["qnpts"], "n_KT_bins": p["n_KT"] - 1,
                            "n_Kphi": p["n_Kphi"] if p["azimuthal_flag"] else 1,
-                           "precision": args.precision, "l2": "flushed (256 MB write) between steps",
+                           "precision": args.precision, "kernel": args.kernel,
+                           "l2": "flushed (256 MB write) between steps",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "pairs_per_step": pairs_all / args.steps / max(world, 1),
                 "binned_same_fraction": round(fr[4], 4),
                 "gpu_launches": launches,
                 "clocks": clk.summary(),
                 "roofline": roofline,
+                "plain_kernel": plain,
+                "speedup_vs_plain": (value / plain["value"]) if plain else None,
                 "e2e": e2e,
                 "cpu_baseline": cpu,
                 "stats": st}

@@ -37,6 +37,7 @@ NVCC_COMMON = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
 GPU_UNITS = {
     "hbt_kernels.cu": ["--fmad=false"],
     "hbt_capi.cu": ["--fmad=false"],
+    "hbt_fast.cu": ["--fmad=false"],
 }
 
 

@@ -277,6 +277,39 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
     return HBT_OK;
 }
 
+// FP32 copies of the screen constants with their rounding slack.
+void fill_screen(hbt_ctx *c) {
+    const hbt::Grid &g = c->d.g;
+    hbt::Screen &s = c->d.s;
+    auto f = [](double v) { return static_cast<float>(v); };
+    auto slack = [](double v, float v32) { return std::fabs(v - static_cast<double>(v32)); };
+    const double lo4 = 4.0 * g.KT_min_sq, hi4 = 4.0 * g.KT_max_sq;
+    s.kt_lo4 = f(lo4);
+    s.kt_hi4 = f(hi4);
+    s.kt_slack = f(std::max(slack(lo4, s.kt_lo4), slack(hi4, s.kt_hi4)) + 1e-7 * hi4);
+    s.lo = f(g.q_lo);
+    s.hi = f(g.q_hi);
+    s.win_slack = f(std::max(slack(g.q_lo, s.lo), slack(g.q_hi, s.hi)) + 1e-12);
+    s.base = f(g.q_base);
+    s.inv_dq = f(1.0 / g.delta_q);
+    s.t_slack = f(slack(g.q_base, s.base) / g.delta_q + 4.0 * 5.96e-8 * g.qnpts + 1e-9);
+    s.KT_min = f(g.KT_min);
+    s.inv_dKT = f(1.0 / g.dKT);
+    s.kt_t_slack = f(slack(g.KT_min, s.KT_min) / g.dKT + 4.0 * 5.96e-8 * g.n_KT + 1e-9);
+    s.psi = f(g.psi_ref);
+    s.psi_slack = f(slack(g.psi_ref, s.psi));
+    s.two_pi = f(g.two_pi);
+    s.inv_dKphi = f(1.0 / g.dKphi);
+    s.qnpts = g.qnpts;
+    s.n_KT = g.n_KT;
+    s.n_Kphi = g.n_Kphi;
+}
+
+bool screened_ok(const hbt_ctx *c) {
+    return c->prm.kernel == HBT_KERNEL_SCREENED && !c->d.g.qinv && c->d.g.n_KT <= 255 &&
+           c->d.g.qnpts <= 1024;
+}
+
 hbt_status bin_same_device(hbt_ctx *c, long long n, const double *const *c8) {
     if (n < 2) return HBT_OK;
     const u64 P = (u64)n * (u64)(n - 1) / 2;
@@ -293,7 +326,10 @@ hbt_status bin_same_device(hbt_ctx *c, long long n, const double *const *c8) {
         std::vector<u64> ctr;
         TRY(read_counters(c, ctr));
     } else {
-        CU(hbt::launch_same(c->d, hbt::MODE_FAST, n, c8, c->stream));
+        if (screened_ok(c))
+            CU(hbt::launch_same_fast(c->d, n, c8, c->stream));
+        else
+            CU(hbt::launch_same(c->d, hbt::MODE_FAST, n, c8, c->stream));
         c->st.launches++;
         c->ub[0] += P;
         if (c->prm.invariant_radius_flag == 1) c->ub[2] += P;
@@ -318,7 +354,10 @@ hbt_status bin_mixed_device(hbt_ctx *c, long long n1, const double *const *l1, l
         std::vector<u64> ctr;
         TRY(read_counters(c, ctr));
     } else {
-        CU(hbt::launch_mixed(c->d, hbt::MODE_FAST, n1, l1, n2, l2, c->stream));
+        if (screened_ok(c))
+            CU(hbt::launch_mixed_fast(c->d, n1, l1, n2, l2, c->stream));
+        else
+            CU(hbt::launch_mixed(c->d, hbt::MODE_FAST, n1, l1, n2, l2, c->stream));
         c->st.launches++;
         c->ub[1] += P;
         if (c->prm.invariant_radius_flag == 1) c->ub[3] += P;
@@ -392,6 +431,11 @@ hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
     g.psi_ref = 0.0;
     g.kphi_tol = p->kphi_defer_tol > 0 ? p->kphi_defer_tol : 1e-13;
     g.hbarC_inv = 1. / kHbarC;
+    if (p->kernel != HBT_KERNEL_SCREENED && p->kernel != HBT_KERNEL_REFERENCE_CHAIN) {
+        hbt_destroy(c);
+        return HBT_ERR_INVALID;
+    }
+    fill_screen(c);
     c->cap = static_cast<u64>(p->needed_number_of_pairs);
     c->cap_qinv = 50 * c->cap;
     c->n_stream = g.n_slots + g.n_KT;
@@ -446,6 +490,7 @@ hbt_status hbt_set_stream(hbt_ctx *c, void *s) {
 hbt_status hbt_set_psi_ref(hbt_ctx *c, double psi) {
     if (!c) return HBT_ERR_INVALID;
     c->d.g.psi_ref = psi;
+    fill_screen(c);
     return HBT_OK;
 }
 

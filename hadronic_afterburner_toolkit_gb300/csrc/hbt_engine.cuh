@@ -81,8 +81,20 @@ struct Caps {
     int n_resolved;
 };
 
+// FP32 copies of the constants used by the FP32 pair screen (hbt_fast.cu),
+// each with the bound on its rounding (slack) relative to the FP64 value.
+struct Screen {
+    float kt_lo4, kt_hi4, kt_slack;  // 4 KT_min^2, 4 KT_max^2 (0: no lower cut)
+    float lo, hi, win_slack;         // q window bounds
+    float base, inv_dq, t_slack;     // bin origin, 1/delta_q, slack in bin units
+    float KT_min, inv_dKT, kt_t_slack;
+    float psi, psi_slack, two_pi, inv_dKphi;
+    int qnpts, n_KT, n_Kphi;
+};
+
 struct Device {
     Grid g;
+    Screen s;
     Hist h;
     u64 *stats;
     Deferral *defer;
@@ -111,5 +123,13 @@ cudaError_t launch_apply(const Device &d, const Deferral *rec, const int *iphi, 
 cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, int n_res,
                                cudaStream_t st);
 cudaError_t launch_counters(const Device &d, unsigned long long *out, cudaStream_t st);
+
+// Screened fast-mode kernels (hbt_fast.cu): same results as MODE_FAST of the
+// reference-chain kernels; require invariant_radius_flag == 0, n_KT <= 255
+// and qnpts <= 1024.
+cudaError_t launch_same_fast(const Device &d, long long n, const double *const *c8,
+                             cudaStream_t st);
+cudaError_t launch_mixed_fast(const Device &d, long long n1, const double *const *l1,
+                              long long n2, const double *const *l2, cudaStream_t st);
 
 }  // namespace hbt

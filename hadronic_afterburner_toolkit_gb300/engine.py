@@ -21,6 +21,8 @@ STATUS = {0: "HBT_OK", 1: "HBT_ERR_INVALID", 2: "HBT_ERR_CUDA", 3: "HBT_ERR_NOME
           4: "HBT_ERR_TIMEOUT", 5: "HBT_ERR_DEVICE", 6: "HBT_ERR_STATE"}
 PRECISION_FP64 = 0
 PRECISION_FP32W = 1
+KERNEL_SCREENED = 0
+KERNEL_REFERENCE_CHAIN = 1
 
 _D = ctypes.c_double
 _I32 = ctypes.c_int32
@@ -37,7 +39,7 @@ class HbtParams(ctypes.Structure):
         ("n_Kphi", _I32), ("azimuthal_flag", _I32),
         ("invariant_radius_flag", _I32), ("long_comoving_boost", _I32),
         ("needed_number_of_pairs", _D), ("precision", _I32),
-        ("kphi_defer_tol", _D),
+        ("kphi_defer_tol", _D), ("kernel", _I32),
     ]
 
 
@@ -123,14 +125,15 @@ class Engine:
     def __init__(self, *, qnpts=41, q_min=-0.15, q_max=0.15, n_KT=5, KT_min=0.0,
                  KT_max=1.0, n_Kphi=8, azimuthal_flag=0, invariant_radius_flag=0,
                  long_comoving_boost=1, needed_number_of_pairs=1e18,
-                 precision=PRECISION_FP64, kphi_defer_tol=0.0, device=0):
+                 precision=PRECISION_FP64, kphi_defer_tol=0.0, kernel=0, device=0):
         self.L = load()
         self.params = dict(qnpts=qnpts, q_min=q_min, q_max=q_max, n_KT=n_KT, KT_min=KT_min,
                            KT_max=KT_max, n_Kphi=n_Kphi, azimuthal_flag=azimuthal_flag,
                            invariant_radius_flag=invariant_radius_flag,
                            long_comoving_boost=long_comoving_boost,
                            needed_number_of_pairs=needed_number_of_pairs,
-                           precision=precision, kphi_defer_tol=kphi_defer_tol)
+                           precision=precision, kphi_defer_tol=kphi_defer_tol,
+                           kernel=kernel)
         p = HbtParams(**self.params)
         h = ctypes.c_void_p()
         self._check(self.L.hbt_create(ctypes.byref(p), device, ctypes.byref(h)), None)

@@ -1,0 +1,352 @@
+#include "HBT_correlation.h"
+
+#include <cmath>
+#include <cstdio>
+#include <iostream>
+#include <sstream>
+#include <stdexcept>
+
+namespace {
+
+std::string fmt_edge(double v) {
+    std::ostringstream s;
+    s << v;  // default ostream formatting, as in the reference's file names
+    return s.str();
+}
+
+}  // namespace
+
+struct HBT_correlation::HostHist {
+    std::vector<double> cnt, qo, qs, ql, num, den, qi_sum, qi_num, qi_cnt, qi_den;
+    std::vector<uint64_t> c_num, c_den, c_num_qi, c_den_qi;
+};
+
+HBT_correlation::HBT_correlation(ParameterReader &paraRdr, std::string path,
+                                 std::shared_ptr<RandomUtil::Random> ran_gen)
+    : paraRdr_(paraRdr), path_(path), ran_gen_ptr_(ran_gen), ctx_(nullptr) {
+    // keys and derived constants of src/HBT_correlation.cpp:22-61
+    long_comoving_boost = paraRdr_.getVal("long_comoving_boost") == 1;
+    qnpts = static_cast<int>(paraRdr_.getVal("qnpts"));
+    q_min = paraRdr_.getVal("q_min");
+    q_max = paraRdr_.getVal("q_max");
+    delta_q = (q_max - q_min) / (qnpts - 1);
+    for (int i = 0; i < qnpts; i++) {
+        q_out.push_back(q_min + i * delta_q);
+        q_side.push_back(q_min + i * delta_q);
+        q_long.push_back(q_min + i * delta_q);
+    }
+    needed_number_of_pairs_ = paraRdr_.getVal("needed_number_of_pairs");
+    azimuthal_flag_ = static_cast<int>(paraRdr_.getVal("azimuthal_flag"));
+    invariant_radius_flag_ = static_cast<int>(paraRdr_.getVal("invariant_radius_flag"));
+    n_KT = static_cast<int>(paraRdr_.getVal("n_KT"));
+    n_Kphi = static_cast<int>(paraRdr_.getVal("n_Kphi"));
+    KT_min = paraRdr_.getVal("KT_min");
+    KT_max = paraRdr_.getVal("KT_max");
+    Krap_min_ = paraRdr_.getVal("HBTrap_min");
+    Krap_max_ = paraRdr_.getVal("HBTrap_max");
+    dKT = (KT_max - KT_min) / (n_KT - 1);
+    dKphi = 2 * M_PI / n_Kphi;
+    for (int i = 0; i < n_KT; i++) KT_array_.push_back(KT_min + i * dKT);
+    for (int i = 0; i < n_Kphi; i++) Kphi_array_.push_back(i * dKphi);
+    psi_ref = 0.;
+    number_of_mixed_events_ = 0;
+    number_of_oversample_events_ = 0;
+    fixed_mixed_partners_ = paraRdr_.exist("hbt_mixed_partners")
+                                ? static_cast<int>(paraRdr_.getVal("hbt_mixed_partners"))
+                                : 0;
+    echo_level_ = paraRdr_.exist("echo_level") ? static_cast<int>(paraRdr_.getVal("echo_level")) : 0;
+
+    hbt_params p;
+    p.qnpts = qnpts;
+    p.q_min = q_min;
+    p.q_max = q_max;
+    p.n_KT = n_KT;
+    p.KT_min = KT_min;
+    p.KT_max = KT_max;
+    p.n_Kphi = n_Kphi;
+    p.azimuthal_flag = azimuthal_flag_;
+    p.invariant_radius_flag = invariant_radius_flag_;
+    p.long_comoving_boost = long_comoving_boost ? 1 : 0;
+    p.needed_number_of_pairs = needed_number_of_pairs_;
+    p.precision = paraRdr_.exist("hbt_precision")
+                      ? static_cast<int>(paraRdr_.getVal("hbt_precision"))
+                      : HBT_PRECISION_FP64;
+    p.kphi_defer_tol = 0.0;
+    p.kernel = paraRdr_.exist("hbt_kernel") ? static_cast<int>(paraRdr_.getVal("hbt_kernel"))
+                                            : HBT_KERNEL_SCREENED;
+    const int device =
+        paraRdr_.exist("hbt_device") ? static_cast<int>(paraRdr_.getVal("hbt_device")) : 0;
+    const hbt_status s = hbt_create(&p, device, &ctx_);
+    if (s != HBT_OK)
+        throw std::runtime_error("HBT_correlation: hbt_create failed (status " +
+                                 std::to_string(static_cast<int>(s)) + ")");
+}
+
+HBT_correlation::~HBT_correlation() { hbt_destroy(ctx_); }
+
+void HBT_correlation::check(hbt_status s, const char *what) {
+    if (s != HBT_OK)
+        throw std::runtime_error(std::string("HBT_correlation: ") + what + ": " +
+                                 hbt_last_error(ctx_));
+}
+
+hbt_stats HBT_correlation::engine_stats() {
+    hbt_stats st;
+    check(hbt_get_stats(ctx_, &st), "hbt_get_stats");
+    return st;
+}
+
+// src/HBT_correlation.cpp:177-218
+void HBT_correlation::calculate_HBT_correlation_function(
+    std::shared_ptr<particleSamples> particle_list_in) {
+    set_particle_list(particle_list_in);
+    fetched_.reset();
+    const int nev = particle_list->get_number_of_events();
+    if (azimuthal_flag_ == 1) calculate_flow_event_plane_angle(2);
+    check(hbt_set_psi_ref(ctx_, psi_ref), "hbt_set_psi_ref");
+
+    number_of_oversample_events_ = nev;
+    std::vector<int> event_list(nev);
+    for (int k = 0; k < nev; k++) event_list[k] = k;
+    combine_and_bin_particle_pairs(event_list);
+
+    const int mixed_nev = particle_list->get_number_of_mixed_events();
+    number_of_mixed_events_ =
+        fixed_mixed_partners_ > 0 ? fixed_mixed_partners_ : mixed_nev / 2 + 1;
+    if (nev > 0 && mixed_nev == 0)
+        throw std::runtime_error("HBT_correlation: the mixed-event pool of this buffer is empty");
+    for (int iev = 0; iev < nev; iev++) {
+        std::vector<int> partners(number_of_mixed_events_, 0);
+        for (int k = 0; k < number_of_mixed_events_; k++) {
+            int id = ran_gen_ptr_->rand_int_uniform() % mixed_nev;
+            while (iev == id && mixed_nev != 1) id = ran_gen_ptr_->rand_int_uniform() % mixed_nev;
+            partners[k] = id;
+        }
+        combine_and_bin_particle_pairs_mixed_events(iev, partners);
+    }
+}
+
+// src/HBT_correlation.cpp:233-249
+void HBT_correlation::calculate_flow_event_plane_angle(int n_order) {
+    const int nev = particle_list->get_number_of_events();
+    double vn_real = 0.0, vn_imag = 0.0;
+    for (int iev = 0; iev < nev; iev++)
+        for (const particle_info &p : particle_list->event(iev)) {
+            const double phi = atan2(p.py, p.px);
+            vn_real += cos(n_order * phi);
+            vn_imag += sin(n_order * phi);
+        }
+    psi_ref = atan2(vn_imag, vn_real) / n_order;
+}
+
+// Gather of src/HBT_correlation.cpp:254-285, pair loop on the GPU.
+void HBT_correlation::combine_and_bin_particle_pairs(std::vector<int> event_list) {
+    const double ycut_max = tanh(Krap_max_);
+    const double ycut_min = tanh(Krap_min_);
+    for (auto &v : s8_) v.clear();
+    for (int j = 0; j < number_of_oversample_events_; j++)
+        for (const particle_info &p : particle_list->event(event_list[j])) {
+            const double ratio = p.pz / p.E;
+            if (ratio > ycut_min && ratio < ycut_max) {
+                s8_[0].push_back(p.px);
+                s8_[1].push_back(p.py);
+                s8_[2].push_back(p.pz);
+                s8_[3].push_back(p.E);
+                s8_[4].push_back(p.x);
+                s8_[5].push_back(p.y);
+                s8_[6].push_back(p.z);
+                s8_[7].push_back(p.t);
+            }
+        }
+    const long long n = static_cast<long long>(s8_[0].size());
+    if (echo_level_ > 5)
+        std::cout << "[Info] number of pairs: " << (unsigned long long)(n * (n - 1) / 2)
+                  << std::endl;
+    const hbt_soa8 soa = {s8_[0].data(), s8_[1].data(), s8_[2].data(), s8_[3].data(),
+                          s8_[4].data(), s8_[5].data(), s8_[6].data(), s8_[7].data()};
+    check(hbt_bin_same(ctx_, n, &soa), "hbt_bin_same");
+}
+
+// Gather and random rotation of src/HBT_correlation.cpp:466-552, pair loop
+// on the GPU.
+void HBT_correlation::combine_and_bin_particle_pairs_mixed_events(
+    int event_id1, std::vector<int> mixed_event_list) {
+    const double ycut_max = tanh(Krap_max_);
+    const double ycut_min = tanh(Krap_min_);
+    for (auto &v : l1_) v.clear();
+    for (auto &v : l2_) v.clear();
+    for (const particle_info &p : particle_list->event(event_id1)) {
+        const double ratio = p.pz / p.E;
+        if (ratio > ycut_min && ratio < ycut_max) {
+            l1_[0].push_back(p.px);
+            l1_[1].push_back(p.py);
+            l1_[2].push_back(p.pz);
+            l1_[3].push_back(p.E);
+        }
+    }
+    for (int iev = 0; iev < number_of_mixed_events_; iev++) {
+        const double random_rotation = ran_gen_ptr_->rand_uniform() * 2 * M_PI;
+        const double cos_phi = cos(random_rotation);
+        const double sin_phi = sin(random_rotation);
+        for (const particle_info &p : particle_list->mixed_event(mixed_event_list[iev])) {
+            const double ratio = p.pz / p.E;
+            if (ratio > ycut_min && ratio < ycut_max) {
+                l2_[0].push_back(p.px * cos_phi - p.py * sin_phi);
+                l2_[1].push_back(p.px * sin_phi + p.py * cos_phi);
+                l2_[2].push_back(p.pz);
+                l2_[3].push_back(p.E);
+            }
+        }
+    }
+    const long long n1 = static_cast<long long>(l1_[0].size());
+    const long long n2 = static_cast<long long>(l2_[0].size());
+    if (echo_level_ > 5)
+        std::cout << "[Info] number of mixed pairs: " << (unsigned long long)(n1 * n2)
+                  << std::endl;
+    const hbt_soa4 a = {l1_[0].data(), l1_[1].data(), l1_[2].data(), l1_[3].data()};
+    const hbt_soa4 b = {l2_[0].data(), l2_[1].data(), l2_[2].data(), l2_[3].data()};
+    check(hbt_bin_mixed(ctx_, n1, &a, n2, &b), "hbt_bin_mixed");
+}
+
+const HBT_correlation::HostHist &HBT_correlation::fetch() {
+    if (fetched_) return *fetched_;
+    std::unique_ptr<HostHist> h(new HostHist());
+    const size_t nb = static_cast<size_t>(hbt_n_bins(ctx_));
+    const size_t nq = static_cast<size_t>(n_KT) * qnpts;
+    const size_t ns = static_cast<size_t>(azimuthal_flag_ == 1 ? n_KT * n_Kphi : n_KT);
+    for (auto *v : {&h->cnt, &h->qo, &h->qs, &h->ql, &h->num, &h->den}) v->assign(nb, 0.0);
+    for (auto *v : {&h->qi_sum, &h->qi_num, &h->qi_cnt, &h->qi_den}) v->assign(nq, 0.0);
+    h->c_num.assign(ns, 0);
+    h->c_den.assign(ns, 0);
+    h->c_num_qi.assign(n_KT, 0);
+    h->c_den_qi.assign(n_KT, 0);
+    check(hbt_read_hist(ctx_, h->cnt.data(), h->qo.data(), h->qs.data(), h->ql.data(),
+                        h->num.data(), h->den.data()),
+          "hbt_read_hist");
+    check(hbt_read_qinv(ctx_, h->qi_sum.data(), h->qi_num.data(), h->qi_cnt.data(),
+                        h->qi_den.data()),
+          "hbt_read_qinv");
+    check(hbt_read_counters(ctx_, h->c_num.data(), h->c_den.data(), h->c_num_qi.data(),
+                            h->c_den_qi.data()),
+          "hbt_read_counters");
+    fetched_ = std::move(h);
+    return *fetched_;
+}
+
+namespace {
+
+hbt_params params_of(int qnpts, double q_min, double q_max, int n_KT, double KT_min,
+                     double KT_max, int n_Kphi, int az, int qinv) {
+    hbt_params p = {};
+    p.qnpts = qnpts;
+    p.q_min = q_min;
+    p.q_max = q_max;
+    p.n_KT = n_KT;
+    p.KT_min = KT_min;
+    p.KT_max = KT_max;
+    p.n_Kphi = n_Kphi;
+    p.azimuthal_flag = az;
+    p.invariant_radius_flag = qinv;
+    return p;
+}
+
+}  // namespace
+
+void HBT_correlation::output_HBTcorrelation() {
+    const HostHist &h = fetch();
+    const hbt_params p = params_of(qnpts, q_min, q_max, n_KT, KT_min, KT_max, n_Kphi,
+                                   azimuthal_flag_, invariant_radius_flag_);
+    const hbt_host_hist_view v = {h.cnt.data(),    h.qo.data(),     h.qs.data(),
+                                  h.ql.data(),     h.num.data(),    h.den.data(),
+                                  h.qi_sum.data(), h.qi_num.data(), h.qi_cnt.data(),
+                                  h.qi_den.data(), h.c_num.data(),  h.c_den.data(),
+                                  h.c_num_qi.data(), h.c_den_qi.data()};
+    const int eco = static_cast<int>(paraRdr_.getVal("ecoOutput", 0));
+    if (hbt_write_outputs(p, path_, eco, v) != 0)
+        throw std::runtime_error("HBT_correlation: cannot write output files under " + path_);
+}
+
+void HBT_correlation::output_correlation_function_inv() {
+    if (invariant_radius_flag_ == 1) output_HBTcorrelation();
+}
+void HBT_correlation::output_correlation_function() { output_HBTcorrelation(); }
+void HBT_correlation::output_correlation_function_Kphi_differential() { output_HBTcorrelation(); }
+
+// ------------------------------------------------------------------ writer
+
+namespace {
+
+void row5(FILE *f, bool eco, double a, double b, double c, double num, double den) {
+    // std::scientific, setprecision(8), setw(18) on the first field only
+    if (eco)
+        fprintf(f, "%18.8e    %.8e\n", num, den);
+    else
+        fprintf(f, "%18.8e    %.8e    %.8e    %.8e    %.8e\n", a, b, c, num, den);
+}
+
+}  // namespace
+
+int hbt_write_outputs(const hbt_params &p, const std::string &path, int eco_output,
+                      const hbt_host_hist_view &h) {
+    const bool eco = eco_output == 1;
+    const int n = p.qnpts;
+    const double delta_q = (p.q_max - p.q_min) / (n - 1);
+    const double dKT = (p.KT_max - p.KT_min) / (p.n_KT - 1);
+    const double dKphi = 2 * M_PI / p.n_Kphi;
+    std::vector<double> grid(n), KT(p.n_KT), Kphi(p.n_Kphi);
+    for (int i = 0; i < n; i++) grid[i] = p.q_min + i * delta_q;
+    for (int i = 0; i < p.n_KT; i++) KT[i] = p.KT_min + i * dKT;
+    for (int i = 0; i < p.n_Kphi; i++) Kphi[i] = i * dKphi;
+    const long long q3 = (long long)n * n * n;
+
+    // q_inv files (src/HBT_correlation.cpp:694-724)
+    if (p.invariant_radius_flag == 1) {
+        for (int iK = 0; iK < p.n_KT - 1; iK++) {
+            const double ratio = static_cast<double>(h.ctr_num_qinv[iK]) /
+                                 static_cast<double>(h.ctr_den_qinv[iK]);
+            const std::string fn = path + "/HBT_correlation_function_inv_KT_" + fmt_edge(KT[iK]) +
+                                   "_" + fmt_edge(KT[iK + 1]) + ".dat";
+            FILE *f = fopen(fn.c_str(), "w");
+            if (!f) return -1;
+            for (int k = 0; k < n; k++) {
+                const long long at = (long long)iK * n + k;
+                const double qmean = h.qinv_sum[at] / h.qinv_count[at];
+                const double den = h.qinv_den[at] * ratio;
+                if (eco)
+                    fprintf(f, "%18.8e    %.8e\n", h.qinv_num[at], den);
+                else
+                    fprintf(f, "%18.8e    %.8e    %.8e\n", qmean, h.qinv_num[at], den);
+            }
+            fclose(f);
+        }
+    }
+    // 3-D files (src/HBT_correlation.cpp:726-855)
+    const int nphi = p.azimuthal_flag == 1 ? p.n_Kphi : 1;
+    for (int iK = 0; iK < p.n_KT - 1; iK++)
+        for (int ip = 0; ip < nphi; ip++) {
+            const int s = p.azimuthal_flag == 1 ? iK * p.n_Kphi + ip : iK;
+            const double ratio =
+                static_cast<double>(h.ctr_num[s]) / static_cast<double>(h.ctr_den[s]);
+            std::string fn = path + "/HBT_correlation_function_KT_" + fmt_edge(KT[iK]) + "_" +
+                             fmt_edge(KT[iK + 1]);
+            if (p.azimuthal_flag == 1) fn += "_Kphi_" + fmt_edge(Kphi[ip]);
+            fn += ".dat";
+            FILE *f = fopen(fn.c_str(), "w");
+            if (!f) return -1;
+            for (int il = 0; il < n; il++)
+                for (int io = 0; io < n; io++)
+                    for (int is = 0; is < n; is++) {
+                        const long long at = s * q3 + ((long long)io * n + is) * n + il;
+                        const int npart_num = static_cast<int>(h.num_count[at]);
+                        const int npart_den = static_cast<int>(h.den[at]);
+                        if (npart_num < 2 || npart_den < 2)
+                            row5(f, eco, grid[io], grid[is], grid[il], 0.0,
+                                 static_cast<double>(npart_den));
+                        else
+                            row5(f, eco, h.q_out_sum[at] / npart_num, h.q_side_sum[at] / npart_num,
+                                 h.q_long_sum[at] / npart_num, h.num[at], ratio * h.den[at]);
+                    }
+            fclose(f);
+        }
+    return 0;
+}

@@ -1,0 +1,93 @@
+// Event buffers of the particle-of-interest for the HBT analysis.
+//
+// Source-compatible subset of the reference's particleSamples
+// (src/particleSamples.{h,cpp}) for the HBT path:
+//  - read_in_mode 10 (iSS gzip text, results/particle_samples.gz) and
+//    read_in_mode 0 (OSCAR text, results/OSCAR.DAT), plus the
+//    *_mixed_event files when read_in_real_mixed_events = 1;
+//  - buffering: whole events are read until the particle count reaches
+//    event_buffer_size (particleSamples.cpp:1256-1283, :689-712);
+//  - rapidity_shift boost of E and pz (:442-468);
+//  - particle_monval filter (:1329-1346): a Monte-Carlo number, or the
+//    class codes 9999 / +-9998 / +-9997 / +-9996 (charged, charge sign,
+//    baryon sign, strangeness sign) looked up in EOS/pdg.dat.
+// Other reader modes (UrQMD, JAM, SMASH, iSS binary) and resonance decays
+// are not part of this build; asking for them throws.
+#pragma once
+
+#include <cstdio>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ParameterReader.h"
+#include "Random.h"
+#include "particle_info.h"
+
+namespace hbt {
+class LineSource;
+}
+
+class particleSamples {
+  public:
+    particleSamples(ParameterReader &paraRdr, std::string path,
+                    std::shared_ptr<RandomUtil::Random> ran_gen);
+    ~particleSamples();
+
+    void read_in_particle_samples_and_filter();
+    void read_in_particle_samples_mixed_event_and_filter();
+    int read_in_particle_samples();
+    int read_in_particle_samples_mixed_event();
+
+    bool end_of_file() const;
+    bool end_of_file_mixed_event() const;
+    int get_event_buffer_size() const { return event_buffer_size_; }
+
+    int get_number_of_events() const { return static_cast<int>(list_->size()); }
+    int get_number_of_mixed_events() const { return static_cast<int>(mixed_list_->size()); }
+    int get_number_of_particles(int event_id) const {
+        return static_cast<int>((*list_)[event_id].size());
+    }
+    int get_number_of_particles_mixed_event(int event_id) const {
+        return static_cast<int>((*mixed_list_)[event_id].size());
+    }
+    particle_info get_particle(int event_id, int part_id) const {
+        return (*list_)[event_id][part_id];
+    }
+    particle_info get_particle_from_mixed_event(int event_id, int part_id) const {
+        return (*mixed_list_)[event_id][part_id];
+    }
+    // Direct, copy-free access used by the HBT gather.
+    const std::vector<particle_info> &event(int event_id) const { return (*list_)[event_id]; }
+    const std::vector<particle_info> &mixed_event(int event_id) const {
+        return (*mixed_list_)[event_id];
+    }
+
+  private:
+    typedef std::vector<std::vector<particle_info>> EventList;
+
+    const ParameterReader paraRdr_;
+    const std::string path_;
+    int echo_level_;
+    int event_buffer_size_;
+    int read_in_mode_;
+    double rap_shift_;
+    bool read_mixed_events_;
+    int particle_monval_;
+
+    std::unique_ptr<hbt::LineSource> in_, in_mixed_;
+    EventList full_, full_mixed_, filtered_, filtered_mixed_;
+    EventList *list_, *mixed_list_;
+
+    // Monte-Carlo number -> (charge, baryon, strange) from EOS/pdg.dat,
+    // loaded on first use by a class code.
+    std::map<int, int> charge_, baryon_, strange_;
+    bool pdg_loaded_ = false;
+
+    int read_buffer(hbt::LineSource &src, EventList &out);
+    void boost(EventList &evs) const;
+    void filter(const EventList &full, EventList &out);
+    bool pick(int monval);
+    void load_pdg();
+};

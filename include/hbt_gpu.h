@@ -66,7 +66,17 @@ typedef struct hbt_params {
      * pair's azimuthal bin is decided on the host with the C library's
      * atan2 instead of the device's; 0 selects the default (1e-13). */
     double kphi_defer_tol;
+    int32_t kernel; /* hbt_kernel */
 } hbt_params;
+
+/* Kernel family for pairs no cap can reject.  Both give the same bins and
+ * counts; HBT_KERNEL_REFERENCE_CHAIN evaluates the reference's FP64 chain
+ * for every pair and is kept as the plain baseline the screened form is
+ * measured against. */
+typedef enum hbt_kernel {
+    HBT_KERNEL_SCREENED = 0,       /* FP32 screen + FP64 for binned pairs */
+    HBT_KERNEL_REFERENCE_CHAIN = 1 /* FP64 reference chain on every pair */
+} hbt_kernel;
 
 typedef struct hbt_ctx hbt_ctx;
 

@@ -1,0 +1,53 @@
+/*
+ * hbt_host.h - C ABI of the drop-in host side (libhbt_host.so).
+ *
+ * The C++ classes ParameterReader, RandomUtil::Random, particleSamples,
+ * HBT_correlation and Analysis under hadronic_afterburner_toolkit_gb300/host
+ * are source-compatible with the reference's (src/*.h of
+ * chunshen1987/hadronic_afterburner_toolkit); C++ callers use them directly.
+ * These entry points serve callers through an FFI.
+ */
+#ifndef HBT_HOST_H
+#define HBT_HOST_H
+
+#include <stdint.h>
+
+#include "hbt_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The reference executable's HBT run (src/main.cpp:21-46 with
+ * Analysis::PerformAnalysis, src/Analysis.cpp:54-112): reads `param_file`
+ * plus key=value strings argv[1..argc-1], reads the samples under
+ * `results_path` and writes the HBT_correlation_function_*.dat files there.
+ * Returns 0, 255 for a parameter error, 1 for any other error (message on
+ * stderr). */
+int hbt_host_run(int argc, char **argv, const char *param_file, const char *results_path);
+
+/* Writes the reference's output files from histogram arrays laid out as
+ * hbt_read_hist / hbt_read_qinv / hbt_read_counters return them
+ * (HBT_correlation::output_HBTcorrelation, src/HBT_correlation.cpp:220-228,
+ * :694-855).  The q_inv arrays are read only when invariant_radius_flag is
+ * 1.  Returns 0, or -1 if a file cannot be opened. */
+int hbt_host_write(const hbt_params *params, const char *path, int32_t eco_output,
+                   const double *num_count, const double *q_out_sum, const double *q_side_sum,
+                   const double *q_long_sum, const double *num, const double *den,
+                   const double *qinv_sum, const double *qinv_num, const double *qinv_count,
+                   const double *qinv_den, const uint64_t *ctr_num, const uint64_t *ctr_den,
+                   const uint64_t *ctr_num_qinv, const uint64_t *ctr_den_qinv);
+
+/* Reads the samples of a parameter file's HBT setup buffer by buffer with
+ * the reference's reader rules (particleSamples, src/particleSamples.cpp),
+ * without binning anything: for each buffer, the event count and particle
+ * count of the species of interest, same-event list then mixed-event pool.
+ * Fills up to `cap` buffers; returns the number of buffers, or -1 on error. */
+int hbt_host_scan_buffers(const char *param_file, const char *results_path, int32_t cap,
+                          int32_t *nev, int64_t *n_particles, int32_t *mixed_nev,
+                          int64_t *n_mixed_particles);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HBT_HOST_H */

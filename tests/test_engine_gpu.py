@@ -248,3 +248,92 @@ def test_sync_with_timeout_and_stats():
     st = eng.stats()
     assert st["pairs_same"] == ev.n_particles * (ev.n_particles - 1) // 2
     assert st["launches"] >= 1
+
+
+# ------------------------------------------------------------------ screen
+# The default (screened) kernels decide most bins in FP32 with an error
+# bound; these cases put many pairs where that bound matters.
+
+def _hard_lists(seed, n=900):
+    """Momenta up to several GeV (larger FP32 rounding) and a tight source."""
+    from hadronic_afterburner_toolkit_gb300 import synth
+    return synth.generate(3, n / 3.0, seed=seed, T=1.2, sigma_xy=1.0, tau_mean=1.0)
+
+
+@pytest.mark.parametrize("az,boost", [(0, 1), (1, 1), (1, 0), (0, 0)])
+def test_screened_and_reference_chain_kernels_agree(az, boost):
+    p = dict(BASIC, azimuthal_flag=az, long_comoving_boost=boost, n_Kphi=8, qnpts=15,
+             n_KT=9, KT_max=2.0)
+    ev = _hard_lists(31 + az + 2 * boost)
+    c = parity.cols8(ev)
+    hs = []
+    for kernel in (0, 1):
+        eng = _engine(kernel=kernel, **p)
+        eng.set_psi_ref(0.9)
+        eng.bin_same(c)
+        eng.bin_mixed(c[:4], [x[::-1].copy() for x in c[:4]])
+        hs.append(eng.hist())
+    orc = _oracle(**p)
+    orc.set_psi_ref(0.9)
+    orc.bin_same(c)
+    orc.bin_mixed(c[:4], [x[::-1].copy() for x in c[:4]])
+    h = orc.hist()
+    assert h["count"].sum() > 500
+    for eh in hs:
+        parity.compare(eh, h, _qscale(p))
+
+
+def test_screen_pairs_with_vanishing_pair_momentum():
+    """p_T(2) ~ -p_T(1): K_perp near 0 makes the FP32 bounds unusable; such
+    pairs must take the FP64 path (and K_perp == 0 exactly is an anomaly)."""
+    rng = np.random.default_rng(5)
+    n = 400
+    px = rng.uniform(-0.3, 0.3, n)
+    py = rng.uniform(-0.3, 0.3, n)
+    eps = rng.choice([0.0, 1e-9, 1e-7, 1e-5, 1e-3], size=n)
+    px2 = -px + eps
+    py2 = -py - eps
+    pz = rng.uniform(-0.2, 0.2, 2 * n)
+    pxs = np.concatenate([px, px2])
+    pys = np.concatenate([py, py2])
+    E = np.sqrt(pxs ** 2 + pys ** 2 + pz ** 2 + 0.13957 ** 2)
+    pos = rng.normal(0, 1, size=(4, 2 * n))
+    c = [pxs, pys, pz, E, pos[0], pos[1], pos[2], pos[3]]
+    p = dict(BASIC, q_min=-1.0, q_max=1.0, qnpts=11)
+    eng, orc = _engine(**p), _oracle(**p)
+    eng.bin_same(c)
+    orc.bin_same(c)
+    eng.bin_mixed(c[:4], [x[:n] for x in c[:4]])
+    orc.bin_mixed(c[:4], [x[:n] for x in c[:4]])
+    h = orc.hist()
+    parity.compare(eng.hist(), h, 1.0)
+
+
+def test_screen_kphi_edges():
+    """K directions placed within float rounding of K_phi bin edges."""
+    rng = np.random.default_rng(8)
+    psi = 0.4
+    n_kphi = 8
+    rows = []
+    for m in range(n_kphi):
+        edge = psi + m * 2 * np.pi / n_kphi
+        for k in range(-6, 7):
+            ang = edge + k * 3e-8
+            kt = rng.uniform(0.1, 0.6)
+            q = rng.uniform(-0.05, 0.05, 3)
+            K = np.array([kt * np.cos(ang), kt * np.sin(ang), rng.uniform(-0.2, 0.2)])
+            for s in (+1, -1):
+                v = K + s * q / 2
+                rows.append((v[0], v[1], v[2], np.sqrt(v @ v + 0.13957 ** 2)))
+    a = np.array(rows)
+    pos = rng.normal(0, 1, size=(4, a.shape[0]))
+    c = [a[:, 0].copy(), a[:, 1].copy(), a[:, 2].copy(), a[:, 3].copy()] + [x.copy() for x in pos]
+    p = dict(BASIC, azimuthal_flag=1, n_Kphi=n_kphi, qnpts=11)
+    eng, orc = _engine(**p), _oracle(**p)
+    for x in (eng, orc):
+        x.set_psi_ref(psi)
+        x.bin_same(c)
+        x.bin_mixed(c[:4], c[:4])
+    h = orc.hist()
+    assert h["count"].sum() > 50
+    parity.compare(eng.hist(), h, _qscale(p))
