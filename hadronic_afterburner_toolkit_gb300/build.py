@@ -38,6 +38,7 @@ GPU_UNITS = {
     "hbt_kernels.cu": ["--fmad=false"],
     "hbt_capi.cu": ["--fmad=false"],
     "hbt_fast.cu": ["--fmad=false"],
+    "hbt_noalloc.cu": ["--fmad=false"],
 }
 
 

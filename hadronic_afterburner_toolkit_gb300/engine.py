@@ -76,6 +76,11 @@ _SIGNATURES = {
     "hbt_read_qinv": (_I32, [ctypes.c_void_p] + [_PD] * 4),
     "hbt_read_counters": (_I32, [ctypes.c_void_p] + [_PU64] * 4),
     "hbt_get_stats": (_I32, [ctypes.c_void_p, ctypes.POINTER(HbtStats)]),
+    "hbt_bin_mixed_rotated_noalloc": (_I32, [ctypes.POINTER(HbtParams), _I64,
+                                             ctypes.POINTER(HbtSoa4), _I64,
+                                             ctypes.POINTER(HbtSoa4), _D, _D,
+                                             ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_char_p, ctypes.c_size_t]),
 }
 
 _lib = None

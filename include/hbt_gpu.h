@@ -25,6 +25,7 @@
 #ifndef HBT_GPU_H
 #define HBT_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -165,6 +166,30 @@ hbt_status hbt_read_counters(hbt_ctx *ctx, uint64_t *num, uint64_t *den,
                              uint64_t *num_qinv, uint64_t *den_qinv);
 
 hbt_status hbt_get_stats(hbt_ctx *ctx, hbt_stats *out);
+
+/* Largest partner pool hbt_bin_mixed_rotated_noalloc accepts (particles). */
+#define HBT_NOALLOC_MAX_POOL 65536
+
+/* No counterpart in the reference.  Mixed-event binning for callers that
+ * cannot allocate device memory (a host framework that owns the device
+ * memory through its own pool, or a loop that cannot afford an
+ * allocation's implicit synchronisation).  Everything is caller-owned and
+ * device-resident: list1 (n1 particles), the partner pool before rotation
+ * (n2 <= HBT_NOALLOC_MAX_POOL particles) and the denominator histogram
+ * `den` (hbt_n_bins() u64 counts for these params, not cleared: counts are
+ * added).  The pool is rotated by (cos_phi, sin_phi) as the reference
+ * rotates a mixed event and binned against list1 on `stream`; the rotated
+ * copy lives in a fixed 2 MB __device__ scratch array that every GPU loading
+ * the library holds until exit.  Requires azimuthal_flag == 0 and
+ * invariant_radius_flag == 0; applies no needed_number_of_pairs cap.  Calls
+ * share the scratch and race if they overlap on the GPU.  The first call on
+ * a device looks up the scratch address and should come before any stream
+ * capture.  On error a message is written to errbuf (may be NULL). */
+hbt_status hbt_bin_mixed_rotated_noalloc(const hbt_params *params, int64_t n1,
+                                         const hbt_soa4 *list1, int64_t n2,
+                                         const hbt_soa4 *pool, double cos_phi,
+                                         double sin_phi, uint64_t *den, void *stream,
+                                         char *errbuf, size_t errlen);
 
 #ifdef __cplusplus
 }
