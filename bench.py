@@ -361,29 +361,42 @@ def main() -> None:
         pairs_all = float(pairs)
     value = pairs_all / (t_ms * 1e-3)
 
-    # the plain form (FP64 reference chain on every pair), one step, same GPU
+    def time_variant(kernel, precision, nsteps, label):
+        """Same workload, another kernel family / precision, same GPU."""
+        engv = E.Engine(device=local, precision=precision, kernel=kernel, **p)
+        engv.set_stream(stream.cuda_stream)
+        ms_tot, prs = 0.0, 0
+        for k in range(nsteps + 1):  # the first step warms up
+            g = (args.warmup + k) % len(dgroups)
+            dc, dm = dgroups[g]
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            engv.bin_same(dc, device=True)
+            for l1, l2 in dm:
+                engv.bin_mixed(l1, l2, device=True)
+            e1.record(stream)
+            e1.synchronize()
+            if k > 0:
+                ms_tot += e0.elapsed_time(e1)
+                prs += group_pairs(groups[g])
+        engv.close()
+        return {"kernel": label, "value": prs / (ms_tot * 1e-3),
+                "ms_per_step": ms_tot / nsteps, "steps": nsteps}
+
+    # the plain form (FP64 reference chain on every pair) and the other
+    # precision, on the same GPU
     plain = None
+    variants = {}
     if not args.no_plain and kern == E.KERNEL_SCREENED:
-        engp = E.Engine(device=local, precision=E.PRECISION_FP64,
-                        kernel=E.KERNEL_REFERENCE_CHAIN, **p)
-        engp.set_stream(stream.cuda_stream)
-        g = args.warmup % len(dgroups)
-        dc, dm = dgroups[g]
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        engp.bin_same(dc, device=True)
-        for l1, l2 in dm:
-            engp.bin_mixed(l1, l2, device=True)
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        plain = {"kernel": "reference-chain (FP64 reference order on every pair)",
-                 "value": group_pairs(groups[g]) / (ms * 1e-3), "ms_per_step": ms,
-                 "steps": 1}
-        engp.close()
+        plain = time_variant(E.KERNEL_REFERENCE_CHAIN, E.PRECISION_FP64, 1,
+                             "reference-chain (FP64 reference order on every pair)")
+        other = E.PRECISION_FP32W if prec == E.PRECISION_FP64 else E.PRECISION_FP64
+        variants["screened-fp32w" if other == E.PRECISION_FP32W else "screened-fp64"] = \
+            time_variant(E.KERNEL_SCREENED, other, 2,
+                         "screened, %s" % ("FP32 weights" if other else "FP64"))
 
     # roofline of the dominant (same-event) kernel against the live FP64 peak
     peaks = measure_fp64_peak()
@@ -469,6 +482,8 @@ def main() -> None:
                 "roofline": roofline,
                 "plain_kernel": plain,
                 "speedup_vs_plain": (value / plain["value"]) if plain else None,
+                "variants": {k: dict(v, speedup_vs_plain=(v["value"] / plain["value"])
+                                     if plain else None) for k, v in variants.items()},
                 "e2e": e2e,
                 "cpu_baseline": cpu,
                 "stats": st}

@@ -42,6 +42,8 @@ struct hbt_ctx {
     int n_stream = 0;  // 3-D slots + q_inv K_T bins
     // histograms
     DevBuf sums, cnt, den, qi_sums, qi_cnt, qi_den, stats, defer, n_defer;
+    // FP32-weight form: partial sums and Kahan compensation
+    DevBuf part, comp;
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging
@@ -105,6 +107,8 @@ void refresh_device(hbt_ctx *c) {
     c->d.caps.row_cut = ptr<long long>(c->row_cut);
     c->d.caps.quota = ptr<unsigned long long>(c->quota);
     c->d.caps.resolved = ptr<hbt::Resolved>(c->resolved);
+    c->d.part = ptr<float4>(c->part);
+    c->d.comp = ptr<hbt::Sums>(c->comp);
 }
 
 // Reference K_phi decision on the host (src/HBT_correlation.cpp:408-416).
@@ -439,6 +443,10 @@ hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
     c->cap = static_cast<u64>(p->needed_number_of_pairs);
     c->cap_qinv = 50 * c->cap;
     c->n_stream = g.n_slots + g.n_KT;
+    c->d.precision = p->precision;
+    // merge the FP32 partials every 16384 same-event CTAs (~2.7e8 pairs)
+    c->d.merge_chunk_blocks = 16384;
+    c->d.block_offset = 0;
 
     const size_t nb = (size_t)g.n_slots * g.q3, nq = (size_t)g.n_KT * g.qnpts;
     hbt_status s = HBT_OK;
@@ -450,7 +458,10 @@ hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
         (s = dalloc(c, c->qi_den, nq * sizeof(u64))) != HBT_OK ||
         (s = dalloc(c, c->stats, hbt::STAT_N * sizeof(u64))) != HBT_OK ||
         (s = dalloc(c, c->defer, kDeferCap * sizeof(hbt::Deferral))) != HBT_OK ||
-        (s = dalloc(c, c->n_defer, sizeof(unsigned))) != HBT_OK) {
+        (s = dalloc(c, c->n_defer, sizeof(unsigned))) != HBT_OK ||
+        (p->precision == HBT_PRECISION_FP32W &&
+         ((s = dalloc(c, c->part, nb * sizeof(float4))) != HBT_OK ||
+          (s = dalloc(c, c->comp, nb * sizeof(hbt::Sums))) != HBT_OK))) {
         hbt_destroy(c);
         return s;
     }
@@ -471,7 +482,7 @@ void hbt_destroy(hbt_ctx *c) {
     DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
-                      &c->apply_iphi, &c->in};
+                      &c->apply_iphi, &c->in, &c->part, &c->comp};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->staged) cudaEventDestroy(c->staged);
@@ -504,6 +515,8 @@ hbt_status hbt_reset(hbt_ctx *c) {
     CU(cudaMemsetAsync(c->qi_cnt.p, 0, c->qi_cnt.bytes, c->stream));
     CU(cudaMemsetAsync(c->qi_den.p, 0, c->qi_den.bytes, c->stream));
     CU(cudaMemsetAsync(c->stats.p, 0, c->stats.bytes, c->stream));
+    if (c->part.p) CU(cudaMemsetAsync(c->part.p, 0, c->part.bytes, c->stream));
+    if (c->comp.p) CU(cudaMemsetAsync(c->comp.p, 0, c->comp.bytes, c->stream));
     CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
     CU(cudaStreamSynchronize(c->stream));
     for (int f = 0; f < 4; f++) c->ub[f] = 0;

@@ -101,6 +101,13 @@ struct Device {
     unsigned *n_defer;
     unsigned defer_cap;
     Caps caps;
+    // FP32-weight form: FP32 partial sums per bin {q_out, q_side, q_long,
+    // cos}, merged into h.sums with the Kahan compensation terms `comp`
+    int precision;                 // hbt_precision
+    float4 *part;
+    Sums *comp;
+    long long merge_chunk_blocks;  // same-event CTAs between two merges
+    long long block_offset;        // first triangular tile pair of a launch chunk
 };
 
 enum Mode { MODE_FAST = 0, MODE_COUNT = 1, MODE_ORDER = 2 };
