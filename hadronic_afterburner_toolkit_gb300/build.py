@@ -39,6 +39,7 @@ GPU_UNITS = {
     "hbt_capi.cu": ["--fmad=false"],
     "hbt_fast.cu": ["--fmad=false"],
     "hbt_noalloc.cu": ["--fmad=false"],
+    "hbt_batch.cu": ["--fmad=false"],
 }
 
 

@@ -1,0 +1,75 @@
+// Device tables of the batched, culled, persistent pair binning
+// (hbt_batch.cu), filled by the C ABI layer (hbt_capi.cu).
+#pragma once
+
+#include "hbt_engine.cuh"
+
+namespace hbt {
+
+// One particle list of a batch, as the caller passed it.
+struct BatchList {
+    const double *src[8];  // caller columns px py pz E (x y z t for same-event)
+    long long n;           // particles
+    long long off;         // first row in the sorted table
+    long long tiles;       // ceil(n / 128)
+    long long tile_off;    // first box of this list
+    int ncols;             // 8 (same-event) or 4 (mixed-event)
+    int pad;
+};
+
+// One job: same-event pairs of list la (kind 0) or la x lb (kind 1).
+struct BatchJob {
+    int kind, la, lb, pad;
+    long long pair_off;  // first candidate tile pair of this job
+    long long n_pairs;   // candidate tile pairs
+};
+
+// Momentum-space box of a 128-particle tile.
+struct Box {
+    double x0, x1, y0, y1;  // p_x, p_y ranges
+    double Y0, Y1;          // rapidity range
+    double m0;              // smallest m_T = sqrt(E^2 - p_z^2)
+    double z0, z1;          // p_z range
+};
+
+struct Item {
+    unsigned job, ti, tj;
+};
+
+struct BatchDev {
+    const BatchList *lists;
+    const BatchJob *jobs;
+    const long long *list_off;  // [n_lists] first particle of each list
+    const long long *tile_off;  // [n_lists] first tile of each list
+    const long long *pair_off;  // [n_jobs] first tile pair of each job
+    int n_lists, n_jobs;
+    long long total;        // particles in the batch
+    long long total_tiles;  // tiles in the batch
+    long long total_pairs;  // candidate tile pairs
+    long long cap;          // row capacity of the sorted table
+    double *table;          // [8][cap] sorted particle table
+    unsigned long long *keys_in, *keys_out;
+    unsigned *vals_in, *vals_out;
+    void *sort_temp;
+    size_t sort_temp_bytes;
+    Box *boxes;
+    Item *items;
+    unsigned item_cap;
+    unsigned *n_items;    // culled queue length
+    unsigned *item_next;  // persistent-kernel cursor
+    // cell sizes of the sort key and the cull thresholds
+    double p_extent, inv_cell_pt, y_extent, inv_cell_y;
+    double qt2_max;  // 2 Q^2 (1 + 1e-6): largest q_x^2 + q_y^2 that can bin
+    double ql_max;   // Q (1 + 1e-6): largest |q_long| that can bin
+    int boost;
+};
+
+int persistent_blocks_per_sm();
+size_t batch_sort_temp_bytes(long long cap);
+// Sort, box, cull and bin one batch.  items_upper bounds the culled queue
+// (its capacity); chunk > 0 splits the FP32-weight form into chunks of that
+// many items with a merge of the FP32 partials after each.
+cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned items_upper,
+                      unsigned chunk, cudaStream_t st);
+
+}  // namespace hbt

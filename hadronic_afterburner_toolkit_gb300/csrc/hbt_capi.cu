@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/hbt_gpu.h"
+#include "hbt_batch.cuh"
 #include "hbt_engine.cuh"
 
 using hbt::u64;
@@ -44,6 +45,10 @@ struct hbt_ctx {
     DevBuf sums, cnt, den, qi_sums, qi_cnt, qi_den, stats, defer, n_defer;
     // FP32-weight form: partial sums and Kahan compensation
     DevBuf part, comp;
+    // batched path: tables, sorted particle table, sort scratch, boxes, queue
+    DevBuf b_lists, b_jobs, b_offs, b_table, b_keys, b_vals, b_sort_temp, b_boxes, b_items,
+        b_counters;
+    int persistent_grid = 152 * 4;
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging
@@ -310,8 +315,122 @@ void fill_screen(hbt_ctx *c) {
 }
 
 bool screened_ok(const hbt_ctx *c) {
-    return c->prm.kernel == HBT_KERNEL_SCREENED && !c->d.g.qinv && c->d.g.n_KT <= 255 &&
-           c->d.g.qnpts <= 1024;
+    return (c->prm.kernel == HBT_KERNEL_SCREENED || c->prm.kernel == HBT_KERNEL_SCREENED_GRID) &&
+           !c->d.g.qinv && c->d.g.n_KT <= 255 && c->d.g.qnpts <= 1024;
+}
+
+bool batched_ok(const hbt_ctx *c) {
+    return screened_ok(c) && c->prm.kernel == HBT_KERNEL_SCREENED;
+}
+
+// One job of a fast batch (device columns).
+struct FastJob {
+    int kind;
+    long long na, nb;
+    const double *a[8];
+    const double *b[4];
+};
+
+// Sort, cull and bin fast jobs in one persistent launch (hbt_batch.cu).
+hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
+    std::vector<hbt::BatchList> lists;
+    std::vector<hbt::BatchJob> bj;
+    std::vector<long long> list_off, tile_off, pair_off;
+    long long total = 0, tiles = 0, pairs = 0;
+    auto add_list = [&](const double *const *src, int ncols, long long n) {
+        hbt::BatchList l = {};
+        for (int f = 0; f < 8; f++) l.src[f] = f < ncols ? src[f] : nullptr;
+        l.n = n;
+        l.off = total;
+        l.tiles = (n + 127) / 128;
+        l.tile_off = tiles;
+        l.ncols = ncols;
+        list_off.push_back(total);
+        tile_off.push_back(tiles);
+        total += n;
+        tiles += l.tiles;
+        lists.push_back(l);
+        return (int)lists.size() - 1;
+    };
+    for (const FastJob &j : jobs) {
+        hbt::BatchJob b = {};
+        b.kind = j.kind;
+        if (j.kind == 0) {
+            if (j.na < 2) continue;
+            b.la = b.lb = add_list(j.a, 8, j.na);
+            const long long t = lists[b.la].tiles;
+            b.n_pairs = t * (t + 1) / 2;
+        } else {
+            if (j.na < 1 || j.nb < 1) continue;
+            b.la = add_list(j.a, 4, j.na);
+            b.lb = add_list(j.b, 4, j.nb);
+            b.n_pairs = lists[b.la].tiles * lists[b.lb].tiles;
+        }
+        b.pair_off = pairs;
+        pair_off.push_back(pairs);
+        pairs += b.n_pairs;
+        bj.push_back(b);
+    }
+    if (bj.empty()) return HBT_OK;
+    if (pairs > 0xffffffffLL) return fail(c, HBT_ERR_INVALID, "batch too large (tile pairs)");
+    // device tables and scratch, grown as needed
+    const size_t sort_bytes = hbt::batch_sort_temp_bytes(total);
+    TRY(dalloc(c, c->b_lists, lists.size() * sizeof(hbt::BatchList)));
+    TRY(dalloc(c, c->b_jobs, bj.size() * sizeof(hbt::BatchJob)));
+    TRY(dalloc(c, c->b_offs, (2 * lists.size() + bj.size()) * sizeof(long long)));
+    TRY(dalloc(c, c->b_table, (size_t)8 * total * sizeof(double)));
+    TRY(dalloc(c, c->b_keys, (size_t)2 * total * sizeof(unsigned long long)));
+    TRY(dalloc(c, c->b_vals, (size_t)2 * total * sizeof(unsigned)));
+    TRY(dalloc(c, c->b_sort_temp, sort_bytes));
+    TRY(dalloc(c, c->b_boxes, (size_t)tiles * sizeof(hbt::Box)));
+    TRY(dalloc(c, c->b_items, (size_t)pairs * sizeof(hbt::Item)));
+    TRY(dalloc(c, c->b_counters, 2 * sizeof(unsigned)));
+    std::vector<long long> offs(list_off);
+    offs.insert(offs.end(), tile_off.begin(), tile_off.end());
+    offs.insert(offs.end(), pair_off.begin(), pair_off.end());
+    CU(cudaMemcpyAsync(c->b_lists.p, lists.data(), lists.size() * sizeof(hbt::BatchList),
+                       cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->b_jobs.p, bj.data(), bj.size() * sizeof(hbt::BatchJob),
+                       cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->b_offs.p, offs.data(), offs.size() * sizeof(long long),
+                       cudaMemcpyHostToDevice, c->stream));
+    hbt::BatchDev b = {};
+    const long long *o = ptr<long long>(c->b_offs);
+    b.lists = ptr<hbt::BatchList>(c->b_lists);
+    b.jobs = ptr<hbt::BatchJob>(c->b_jobs);
+    b.list_off = o;
+    b.tile_off = o + lists.size();
+    b.pair_off = o + 2 * lists.size();
+    b.n_lists = (int)lists.size();
+    b.n_jobs = (int)bj.size();
+    b.total = total;
+    b.total_tiles = tiles;
+    b.total_pairs = pairs;
+    b.cap = total;
+    b.table = ptr<double>(c->b_table);
+    b.keys_in = ptr<unsigned long long>(c->b_keys);
+    b.keys_out = b.keys_in + total;
+    b.vals_in = ptr<unsigned>(c->b_vals);
+    b.vals_out = b.vals_in + total;
+    b.sort_temp = c->b_sort_temp.p;
+    b.sort_temp_bytes = c->b_sort_temp.bytes;
+    b.boxes = ptr<hbt::Box>(c->b_boxes);
+    b.items = ptr<hbt::Item>(c->b_items);
+    b.item_cap = (unsigned)pairs;
+    b.n_items = ptr<unsigned>(c->b_counters);
+    b.item_next = b.n_items + 1;
+    b.p_extent = 1024 * 0.02 / 2;
+    b.inv_cell_pt = 1.0 / 0.02;
+    b.y_extent = 1024 * 0.05 / 2;
+    b.inv_cell_y = 1.0 / 0.05;
+    const double Q = std::max(std::fabs(c->d.g.q_lo), std::fabs(c->d.g.q_hi));
+    b.qt2_max = 2.0 * Q * Q * (1.0 + 1e-6) + 1e-300;
+    b.ql_max = Q * (1.0 + 1e-6) + 1e-300;
+    b.boost = c->d.g.boost;
+    CU(hbt::run_batch(c->d, b, c->persistent_grid, (unsigned)pairs,
+                      (unsigned)c->d.merge_chunk_blocks, c->stream));
+    c->st.launches += 6;
+    return HBT_OK;
 }
 
 hbt_status bin_same_device(hbt_ctx *c, long long n, const double *const *c8) {
@@ -330,10 +449,17 @@ hbt_status bin_same_device(hbt_ctx *c, long long n, const double *const *c8) {
         std::vector<u64> ctr;
         TRY(read_counters(c, ctr));
     } else {
-        if (screened_ok(c))
+        if (batched_ok(c)) {
+            FastJob j = {};
+            j.kind = 0;
+            j.na = n;
+            for (int f = 0; f < 8; f++) j.a[f] = c8[f];
+            TRY(run_fast_jobs(c, std::vector<FastJob>{j}));
+        } else if (screened_ok(c)) {
             CU(hbt::launch_same_fast(c->d, n, c8, c->stream));
-        else
+        } else {
             CU(hbt::launch_same(c->d, hbt::MODE_FAST, n, c8, c->stream));
+        }
         c->st.launches++;
         c->ub[0] += P;
         if (c->prm.invariant_radius_flag == 1) c->ub[2] += P;
@@ -358,10 +484,21 @@ hbt_status bin_mixed_device(hbt_ctx *c, long long n1, const double *const *l1, l
         std::vector<u64> ctr;
         TRY(read_counters(c, ctr));
     } else {
-        if (screened_ok(c))
+        if (batched_ok(c)) {
+            FastJob j = {};
+            j.kind = 1;
+            j.na = n1;
+            j.nb = n2;
+            for (int f = 0; f < 4; f++) {
+                j.a[f] = l1[f];
+                j.b[f] = l2[f];
+            }
+            TRY(run_fast_jobs(c, std::vector<FastJob>{j}));
+        } else if (screened_ok(c)) {
             CU(hbt::launch_mixed_fast(c->d, n1, l1, n2, l2, c->stream));
-        else
+        } else {
             CU(hbt::launch_mixed(c->d, hbt::MODE_FAST, n1, l1, n2, l2, c->stream));
+        }
         c->st.launches++;
         c->ub[1] += P;
         if (c->prm.invariant_radius_flag == 1) c->ub[3] += P;
@@ -435,7 +572,8 @@ hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
     g.psi_ref = 0.0;
     g.kphi_tol = p->kphi_defer_tol > 0 ? p->kphi_defer_tol : 1e-13;
     g.hbarC_inv = 1. / kHbarC;
-    if (p->kernel != HBT_KERNEL_SCREENED && p->kernel != HBT_KERNEL_REFERENCE_CHAIN) {
+    if (p->kernel != HBT_KERNEL_SCREENED && p->kernel != HBT_KERNEL_REFERENCE_CHAIN &&
+        p->kernel != HBT_KERNEL_SCREENED_GRID) {
         hbt_destroy(c);
         return HBT_ERR_INVALID;
     }
@@ -447,6 +585,11 @@ hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
     // merge the FP32 partials every 16384 same-event CTAs (~2.7e8 pairs)
     c->d.merge_chunk_blocks = 16384;
     c->d.block_offset = 0;
+    {
+        int sms = 0;
+        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        c->persistent_grid = sms * hbt::persistent_blocks_per_sm();
+    }
 
     const size_t nb = (size_t)g.n_slots * g.q3, nq = (size_t)g.n_KT * g.qnpts;
     hbt_status s = HBT_OK;
@@ -482,7 +625,9 @@ void hbt_destroy(hbt_ctx *c) {
     DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
-                      &c->apply_iphi, &c->in, &c->part, &c->comp};
+                      &c->apply_iphi, &c->in, &c->part, &c->comp, &c->b_lists,
+                      &c->b_jobs, &c->b_offs, &c->b_table, &c->b_keys, &c->b_vals,
+                      &c->b_sort_temp, &c->b_boxes, &c->b_items, &c->b_counters};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->staged) cudaEventDestroy(c->staged);
@@ -564,6 +709,98 @@ hbt_status hbt_bin_mixed(hbt_ctx *c, int64_t n1, const hbt_soa4 *a, int64_t n2,
     const double *dv[8];
     TRY(stage(c, src, len, 8, dv));
     return bin_mixed_device(c, n1, dv, n2, dv + 4);
+}
+
+hbt_status hbt_bin_batch_dev(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs) {
+    if (!c || n_jobs < 0 || (n_jobs > 0 && !jobs)) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    u64 P_same = 0, P_mixed = 0;
+    for (int k = 0; k < n_jobs; k++) {
+        const hbt_job &j = jobs[k];
+        if (j.kind != 0 && j.kind != 1) return fail(c, HBT_ERR_INVALID, "job kind must be 0 or 1");
+        if (j.na < 0 || j.nb < 0) return fail(c, HBT_ERR_INVALID, "negative list size");
+        if (j.kind == 0 && j.na >= 2) P_same += (u64)j.na * (u64)(j.na - 1) / 2;
+        if (j.kind == 1) P_mixed += (u64)j.na * (u64)j.nb;
+    }
+    bool sequential = !batched_ok(c) || caps_may_bind(c, 0, P_same) || caps_may_bind(c, 1, P_mixed);
+    if (sequential && batched_ok(c)) {
+        TRY(drain_deferrals(c));
+        std::vector<u64> ctr;
+        TRY(read_counters(c, ctr));
+        sequential = caps_may_bind(c, 0, P_same) || caps_may_bind(c, 1, P_mixed);
+    }
+    if (sequential) {
+        // one job at a time keeps the reference's order for the caps
+        for (int k = 0; k < n_jobs; k++) {
+            const hbt_job &j = jobs[k];
+            if (j.kind == 0) {
+                TRY(hbt_bin_same_dev(c, j.na, &j.a));
+            } else {
+                const hbt_soa4 a = {j.a.px, j.a.py, j.a.pz, j.a.E};
+                const hbt_soa4 b = {j.b.px, j.b.py, j.b.pz, j.b.E};
+                TRY(hbt_bin_mixed_dev(c, j.na, &a, j.nb, &b));
+            }
+        }
+        return HBT_OK;
+    }
+    std::vector<FastJob> fj;
+    for (int k = 0; k < n_jobs; k++) {
+        const hbt_job &j = jobs[k];
+        FastJob f = {};
+        f.kind = j.kind;
+        f.na = j.na;
+        f.nb = j.nb;
+        const double *a[8] = {j.a.px, j.a.py, j.a.pz, j.a.E, j.a.x, j.a.y, j.a.z, j.a.t};
+        for (int q = 0; q < 8; q++) f.a[q] = a[q];
+        const double *b[4] = {j.b.px, j.b.py, j.b.pz, j.b.E};
+        for (int q = 0; q < 4; q++) f.b[q] = b[q];
+        fj.push_back(f);
+    }
+    c->st.pairs_same += P_same;
+    c->st.pairs_mixed += P_mixed;
+    TRY(run_fast_jobs(c, fj));
+    c->ub[0] += P_same;
+    c->ub[1] += P_mixed;
+    return HBT_OK;
+}
+
+hbt_status hbt_bin_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs) {
+    if (!c || n_jobs < 0 || (n_jobs > 0 && !jobs)) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    // stage every host column of the batch into one device buffer
+    std::vector<const double *> src;
+    std::vector<long long> len;
+    for (int k = 0; k < n_jobs; k++) {
+        const hbt_job &j = jobs[k];
+        const double *a[8] = {j.a.px, j.a.py, j.a.pz, j.a.E, j.a.x, j.a.y, j.a.z, j.a.t};
+        const int na = j.kind == 0 ? 8 : 4;
+        for (int q = 0; q < na; q++) {
+            src.push_back(a[q]);
+            len.push_back(j.na);
+        }
+        if (j.kind == 1) {
+            const double *b[4] = {j.b.px, j.b.py, j.b.pz, j.b.E};
+            for (int q = 0; q < 4; q++) {
+                src.push_back(b[q]);
+                len.push_back(j.nb);
+            }
+        }
+    }
+    std::vector<const double *> dv(src.size());
+    TRY(stage(c, src.data(), len.data(), (int)src.size(), dv.data()));
+    std::vector<hbt_job> dj(jobs, jobs + n_jobs);
+    size_t at = 0;
+    for (int k = 0; k < n_jobs; k++) {
+        hbt_job &j = dj[k];
+        const double **a[8] = {&j.a.px, &j.a.py, &j.a.pz, &j.a.E, &j.a.x, &j.a.y, &j.a.z, &j.a.t};
+        const int na = j.kind == 0 ? 8 : 4;
+        for (int q = 0; q < na; q++) *a[q] = dv[at++];
+        if (j.kind == 1) {
+            const double **b[4] = {&j.b.px, &j.b.py, &j.b.pz, &j.b.E};
+            for (int q = 0; q < 4; q++) *b[q] = dv[at++];
+        }
+    }
+    return hbt_bin_batch_dev(c, n_jobs, dj.data());
 }
 
 hbt_status hbt_sync(hbt_ctx *c, uint64_t timeout_us) {

@@ -131,6 +131,9 @@ cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, 
                                cudaStream_t st);
 cudaError_t launch_counters(const Device &d, unsigned long long *out, cudaStream_t st);
 
+// Merge of the FP32-weight partial sums into the FP64 bins (hbt_fast.cu).
+cudaError_t launch_merge(const Device &d, cudaStream_t st);
+
 // Screened fast-mode kernels (hbt_fast.cu): same results as MODE_FAST of the
 // reference-chain kernels; require invariant_radius_flag == 0, n_KT <= 255
 // and qnpts <= 1024.

@@ -1,0 +1,410 @@
+// Screened pair binning of one tile pair (device code shared by the grid
+// kernels of hbt_fast.cu and the persistent batch kernel of hbt_batch.cu).
+//
+// GB300 runs FP64 at 1/58 of its FP32 rate, so every pair is first screened
+// in FP32 and only the pairs that are binned pay for more work:
+//
+//  A. Window screen (every pair).  From FP32 copies of the momenta it forms
+//     K_perp^2, q_out, q_side, q_long and a rigorous bound on how far each
+//     lies from the value the reference computes in FP64 (error analysis
+//     below).  A pair is rejected when a window check fails by more than its
+//     bound; otherwise it is queued.
+//  B. Per-warp compaction.  Queued pairs are processed 32 at a time with all
+//     lanes active: the bin indices are decided in FP32 when every
+//     truncation is farther from its edge than its bound (they are then the
+//     reference's indices exactly), K_phi likewise with atan2f; any pair
+//     with an undecided window, index or angle runs the reference-order FP64
+//     chain of hbt_chain.cuh instead.
+//  C. Histogram update.  Mixed pairs add 1 to their denominator bin.
+//     Same-event pairs add q_out, q_side, q_long and cos(q.dx / hbarC):
+//       FP64 form  - FP64 values from algebraically identical expressions
+//                    (q_out = (q_x S_x + q_y S_y) / |S|, ...) and CUDA cos;
+//       FP32W form - the FP32 screen values, and cos of the phase computed
+//                    and range-reduced in FP64, evaluated in FP32 by a Taylor
+//                    polynomial; added with one float4 vector atomic into
+//                    FP32 partial bins that hbt_capi.cu merges into the FP64
+//                    bins with Kahan compensation.
+//
+// Error analysis (u = 2^-24).  Inputs are FP64 values v rounded once to
+// FP32: |v32 - v| <= u|v|.  For s = a +- b in FP32, |s - S| <= 2.01 u A with
+// A = |a| + |b| and S the exact sum of the FP64 inputs.  Products, sums, the
+// reciprocal square root (rsqrtf: at most 2 ulp) and the approximate
+// divisions used only inside the bounds (__fdividef: at most 2 ulp, the
+// bounds carry a 1e-4 relative margin for it) propagate this as coded in
+// screen_windows() and decide_bins(); every bound is then doubled and widened
+// by the rounding of the FP32 copies of the constants, which also covers the
+// FP64 reference's own rounding (2^-29 times smaller).
+#pragma once
+
+#include "hbt_chain.cuh"
+
+namespace hbt {
+namespace tile {
+
+using namespace chain;
+
+constexpr float U = 5.9604645e-8f;  // 2^-24
+constexpr int FT = 128;             // tile edge (particles) for both lists
+constexpr int QCAP = 64;            // per-warp compaction queue
+
+// FP32 screen quantities of one pair and their error bounds.
+struct Q {
+    float sx, sy, Ax, Ay, k2, ek2;
+    float qo, eqo, qs, eqs, ql, eql;
+};
+
+// 0: certainly outside [lo, hi], 1: certainly inside, 2: undecided.
+__device__ __forceinline__ int window_class(const Screen &S, float v, float err) {
+    const float e = 2.0f * err + S.win_slack;
+    if (v + e < S.lo || v - e > S.hi) return 0;
+    if (v - e > S.lo && v + e < S.hi) return 1;
+    return 2;
+}
+
+// Stage A: window checks.  Returns 0 (reject), 1 (all windows certainly
+// passed), 2 (undecided).
+template <bool BOOST>
+__device__ __forceinline__ int screen_windows(const Screen &S, float4 a, float4 b, Q &q) {
+    q.sx = a.x + b.x;
+    q.sy = a.y + b.y;
+    const float dx = a.x - b.x, dy = a.y - b.y;
+    q.Ax = fabsf(a.x) + fabsf(b.x);
+    q.Ay = fabsf(a.y) + fabsf(b.y);
+    q.k2 = __fmaf_rn(q.sx, q.sx, q.sy * q.sy);
+    const float AA = __fmaf_rn(q.Ax, q.Ax, q.Ay * q.Ay);
+    // |k2 - (S_x^2 + S_y^2)|
+    q.ek2 = 6.1f * U * __fmaf_rn(q.Ax, fabsf(q.sx), q.Ay * fabsf(q.sy)) + 3.1f * U * q.k2 +
+            1e-13f * AA;
+    // K_T window (reference rejects Kp2 < KT_min^2 or Kp2 > KT_max^2)
+    const float ekt = 2.0f * q.ek2 + S.kt_slack;
+    if ((S.kt_lo4 > 0.0f && q.k2 + ekt < S.kt_lo4) || q.k2 - ekt > S.kt_hi4) return 0;
+    int cls = ((S.kt_lo4 == 0.0f || q.k2 - ekt > S.kt_lo4) && q.k2 + ekt < S.kt_hi4) ? 1 : 2;
+    const float rel_k2 = __fdividef(q.ek2, q.k2) * 1.0001f;
+    if (!(q.k2 > 0.0f) || !(rel_k2 <= 0.05f)) return 2;  // |S| too small for the bounds
+    const float inv = rsqrtf(q.k2);
+    const float rel_inv = 0.53f * rel_k2 + 4.5f * U;
+    const float eN = 9.0f * U * AA;
+    const float no = __fmaf_rn(dx, q.sx, dy * q.sy);
+    const float ns = __fmaf_rn(dy, q.sx, -(dx * q.sy));
+    q.qo = no * inv;
+    q.eqo = __fmaf_rn(fabsf(no), rel_inv, eN) * inv + U * fabsf(q.qo);
+    q.qs = ns * inv;
+    q.eqs = __fmaf_rn(fabsf(ns), rel_inv, eN) * inv + U * fabsf(q.qs);
+    const float dz = a.z - b.z;
+    const float Az = fabsf(a.z) + fabsf(b.z);
+    if (BOOST) {
+        const float sE = a.w + b.w, sz = a.z + b.z, dE = a.w - b.w;
+        const float AE = fabsf(a.w) + fabsf(b.w);
+        const float m = sE - sz, p = sE + sz;
+        const float e0 = 2.01f * U * (AE + Az);
+        const float rel_m2 =
+            (__fdividef(e0 + U * fabsf(m), m) + __fdividef(e0 + U * fabsf(p), p)) * 1.0001f +
+            1.01f * U;
+        if (!(m > 0.0f) || !(p > 0.0f) || !(rel_m2 <= 0.05f)) return 2;
+        const float rl = rsqrtf(m * p);
+        const float rel_rl = 0.53f * rel_m2 + 4.5f * U;
+        const float nl = __fmaf_rn(sE, dz, -(sz * dE));
+        q.ql = nl * rl;
+        q.eql = __fmaf_rn(fabsf(nl), rel_rl, 17.0f * U * AE * Az) * rl + U * fabsf(q.ql);
+    } else {
+        q.ql = dz;
+        q.eql = 2.1f * U * Az;
+    }
+    const int wo = window_class(S, q.qo, q.eqo), ws = window_class(S, q.qs, q.eqs),
+              wl = window_class(S, q.ql, q.eql);
+    if (wo == 0 || ws == 0 || wl == 0) return 0;
+    if (wo == 2 || ws == 2 || wl == 2) return 2;
+    return cls;
+}
+
+// floor((v - base) / delta_q) when certain, else -1.
+__device__ __forceinline__ int q_index(const Screen &S, float v, float err) {
+    const float t = (v - S.base) * S.inv_dq;
+    const float et = (2.0f * err + S.win_slack) * S.inv_dq + 4.0f * U * fabsf(t) +
+                     2.0f * U * (fabsf(v) + fabsf(S.base)) * S.inv_dq + S.t_slack;
+    const float k = floorf(t);
+    const float fr = t - k;
+    if (!(fr > et) || !(fr < 1.0f - et) || k < 0.0f || k >= (float)S.qnpts) return -1;
+    return (int)k;
+}
+
+// Stage B: K_T and q bin indices of a pair whose windows all passed.
+// Returns false when any index is undecided.
+__device__ __forceinline__ bool decide_bins(const Screen &S, const Q &q, int &iK, int &bin) {
+    const float inv = rsqrtf(q.k2);
+    const float kp = 0.5f * q.k2 * inv;  // |S|/2 = K_perp
+    const float ekp = 0.5f * q.ek2 * inv * 1.1f + 8.0f * U * kp;
+    const float t = (kp - S.KT_min) * S.inv_dKT;
+    const float et = 2.0f * ekp * S.inv_dKT + 4.0f * U * (fabsf(t) + S.KT_min * S.inv_dKT) +
+                     S.kt_t_slack;
+    const float k = floorf(t);
+    const float fr = t - k;
+    if (!(fr > et) || !(fr < 1.0f - et) || k < 0.0f || k >= (float)S.n_KT) return false;
+    iK = (int)k;
+    const int io = q_index(S, q.qo, q.eqo), is = q_index(S, q.qs, q.eqs),
+              il = q_index(S, q.ql, q.eql);
+    if (io < 0 || is < 0 || il < 0) return false;
+    bin = (io * S.qnpts + is) * S.qnpts + il;
+    return true;
+}
+
+// K_phi bin from the FP32 screen values: >= 0 certain, -2 undecided.
+__device__ __forceinline__ int kphi_screen(const Screen &S, const Q &q) {
+    const float phi = atan2f(q.sy, q.sx);
+    // angle error from the inputs, atan2f (3 ulp), psi_ref rounding, wrap
+    const float e = 2.02f * U * __fdividef(__fmaf_rn(q.Ax, fabsf(q.sy), q.Ay * fabsf(q.sx)), q.k2) +
+                    1.0e-6f + S.psi_slack;
+    float d = phi - S.psi;
+    if (d < 0.0f) d += S.two_pi;
+    const float ed = 2.0f * e + 1.0e-6f;
+    if (!(d > ed) || !(d < S.two_pi - ed)) return -2;
+    const float r = d * S.inv_dKphi;
+    const float er = ed * S.inv_dKphi + 4.0f * U * r;
+    const float k = floorf(r);
+    const float fr = r - k;
+    if (!(fr > er) || !(fr < 1.0f - er) || k < 0.0f || k >= (float)S.n_Kphi) return -2;
+    return (int)k;
+}
+
+// FP64 summed values of an accepted same-event pair (algebraically the
+// reference's q_out, q_side, q_long and cos(q.dx / hbarC)).
+template <bool BOOST>
+__device__ __forceinline__ void values64(const Grid &g, const double *a, const double *b,
+                                         double &qo, double &qs, double &ql, double &w) {
+    const double sx = a[0] + b[0], sy = a[1] + b[1];
+    const double dx = a[0] - b[0], dy = a[1] - b[1];
+    const double dz = a[2] - b[2], dE = a[3] - b[3];
+    const double inv = rsqrt(__fma_rn(sx, sx, sy * sy));
+    qo = __fma_rn(dx, sx, dy * sy) * inv;
+    qs = __fma_rn(dy, sx, -(dx * sy)) * inv;
+    if (BOOST) {
+        const double sE = a[3] + b[3], sz = a[2] + b[2];
+        ql = __fma_rn(sE, dz, -(sz * dE)) * rsqrt((sE - sz) * (sE + sz));
+    } else {
+        ql = dz;
+    }
+    const double ph = dE * (a[7] - b[7]) - dx * (a[4] - b[4]) - dy * (a[5] - b[5]) -
+                      dz * (a[6] - b[6]);
+    w = cos(g.hbarC_inv * ph);
+}
+
+// Summed values of the FP32-weight form.  The momentum sums and differences
+// are taken in FP64 (no cancellation), then q_out, q_side, q_long follow in
+// FP32 (relative error a few 1e-7).  cos: the phase is computed and reduced
+// to [-pi, pi] in FP64 (Cody-Waite with a two-part 2 pi), then to
+// [-pi/4, pi/4] by quadrant in FP32, where Taylor polynomials of cos (to
+// x^8) and sin (to x^9) are accurate to 3e-8 and 2e-9: error < 2e-7.
+template <bool BOOST>
+__device__ __forceinline__ float4 values32(const Grid &g, const double *a, const double *b) {
+    const double dx = a[0] - b[0], dy = a[1] - b[1];
+    const double dz = a[2] - b[2], dE = a[3] - b[3];
+    const float fsx = (float)(a[0] + b[0]), fsy = (float)(a[1] + b[1]);
+    const float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+    const float inv = rsqrtf(__fmaf_rn(fsx, fsx, fsy * fsy));
+    float4 v;
+    v.x = __fmaf_rn(fdx, fsx, fdy * fsy) * inv;
+    v.y = __fmaf_rn(fdy, fsx, -(fdx * fsy)) * inv;
+    if (BOOST) {
+        const float sE = (float)(a[3] + b[3]), sz = (float)(a[2] + b[2]), fdE = (float)dE;
+        v.z = __fmaf_rn(sE, fdz, -(sz * fdE)) * rsqrtf((sE - sz) * (sE + sz));
+    } else {
+        v.z = fdz;
+    }
+    const double ph = g.hbarC_inv * (dE * (a[7] - b[7]) - dx * (a[4] - b[4]) -
+                                     dy * (a[5] - b[5]) - dz * (a[6] - b[6]));
+    const double k = rint(ph * 0.15915494309189535);  // 1 / (2 pi)
+    double r = __fma_rn(-k, 6.283185307179586, ph);   // 2 pi, leading double
+    r = __fma_rn(-k, 2.4492935982947064e-16, r);      // 2 pi - leading double
+    const float rf = (float)r;
+    const float j = rintf(rf * 0.63661977f);           // 2 / pi
+    float x = __fmaf_rn(-j, 1.5707963f, rf);           // pi/2 = 1.5707963 + 4.37114e-8
+    x = __fmaf_rn(-j, -4.37113883e-8f, x);
+    const float x2 = x * x;
+    const float c = __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, 2.48015873e-5f,
+                                                                      -1.38888889e-3f),
+                                                          4.16666667e-2f),
+                                            -0.5f),
+                              1.0f);
+    const float s = x * __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, 2.75573192e-6f,
+                                                                          -1.98412698e-4f),
+                                                              8.33333333e-3f),
+                                                -1.66666667e-1f),
+                                  1.0f);
+    const int quad = ((int)j) & 3;  // cos(x + j pi/2)
+    v.w = quad == 0 ? c : quad == 1 ? -s : quad == 2 ? -c : s;
+    return v;
+}
+
+// Shared memory of one tile pair.
+struct TileSmem {
+    double si[8][FT];  // FP64 i-tile (same-event)
+    double sj[8][FT];  // FP64 j-tile (same-event)
+    float4 fi[FT];     // FP32 momenta of the i-tile
+    float4 fj[FT];     // FP32 momenta of the j-tile
+    unsigned queue[FT / 32][QCAP];
+};
+
+// Appends this lane's pair to the warp queue when `take`, and runs
+// `process` on 32 queued pairs whenever 32 are waiting.
+template <class F>
+__device__ __forceinline__ void enqueue(unsigned *q, int &count, bool take, unsigned entry,
+                                        int lane, F &process) {
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    if (take) q[count + __popc(m & ((1u << lane) - 1u))] = entry;
+    count += __popc(m);
+    __syncwarp();
+    if (count >= 32) {
+        process(q[lane]);
+        __syncwarp();
+        if (lane < count - 32) q[lane] = q[32 + lane];
+        __syncwarp();
+        count -= 32;
+    }
+}
+
+// Same-event pairs i < j of the tiles starting at i0 and j0 (i0 <= j0) of
+// one list of n particles with columns c = px py pz E x y z t.  Called by
+// all FT threads of the CTA; the caller syncs before reusing `sm`.
+template <bool AZ, bool BOOST, int PREC>
+__device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
+                                               const double *const *c, long long n,
+                                               long long i0, long long j0) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (int f = 0; f < 8; f++) {
+        sm.si[f][tid] = (i0 + tid < n) ? c[f][i0 + tid] : 0.0;
+        sm.sj[f][tid] = (j0 + tid < n) ? c[f][j0 + tid] : 0.0;
+    }
+    __syncthreads();
+    sm.fi[tid] = make_float4((float)sm.si[0][tid], (float)sm.si[1][tid], (float)sm.si[2][tid],
+                             (float)sm.si[3][tid]);
+    sm.fj[tid] = make_float4((float)sm.sj[0][tid], (float)sm.sj[1][tid], (float)sm.sj[2][tid],
+                             (float)sm.sj[3][tid]);
+    __syncthreads();
+    const Screen &S = d.s;
+    const int il = w * 32 + lane;
+    const long long i = i0 + il;
+    const float4 a = sm.fi[il];
+    const int jend = (int)min((long long)FT, n - j0);
+    unsigned *q = sm.queue[w];
+    int count = 0;
+
+    // stages B and C for one queued pair (all lanes of the warp in step)
+    auto process = [&](unsigned e) {
+        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        Q s;
+        const int wcls = screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+        int iK = 0, bin = 0, slot = -1;
+        if (wcls == 1 && decide_bins(S, s, iK, bin)) {
+            slot = iK;
+            if (AZ) {
+                const int ip = kphi_screen(S, s);
+                slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
+            }
+        }
+        double A[8], B[8];
+#pragma unroll
+        for (int f = 0; f < 8; f++) {
+            A[f] = sm.si[f][qi];
+            B[f] = sm.sj[f][qj];
+        }
+        if (slot < 0) {
+            // undecided somewhere: the reference chain decides (and may hand
+            // a K_phi edge to the host)
+            const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2],
+                                                 B[3], A + 4, B + 4);
+            if (PREC == 0 || full.ev3 != 1) {
+                consume<false, MODE_FAST>(d, i0 + qi, j0 + qj, n, n, full);
+            } else {
+                const long long at = (long long)full.slot * d.g.q3 + full.bin;
+                atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
+                atomicAdd(d.h.cnt + at, 1ull);
+            }
+            return;
+        }
+        const long long at = (long long)slot * d.g.q3 + bin;
+        if (PREC == 0) {
+            double vo, vs, vl, vw;
+            values64<BOOST>(d.g, A, B, vo, vs, vl, vw);
+            Sums *h = d.h.sums + at;
+            atomicAdd(&h->qo, vo);
+            atomicAdd(&h->qs, vs);
+            atomicAdd(&h->ql, vl);
+            atomicAdd(&h->w, vw);
+        } else {
+            atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
+        }
+        atomicAdd(d.h.cnt + at, 1ull);
+    };
+
+    for (int jj = 0; jj < jend; jj++) {
+        const long long j = j0 + jj;
+        int cls = 0;
+        if (i < n && j > i) {
+            Q s;
+            cls = screen_windows<BOOST>(S, a, sm.fj[jj], s);
+        }
+        enqueue(q, count, cls != 0, (unsigned)il | ((unsigned)jj << 8), lane, process);
+    }
+    if (lane < count) process(q[lane]);
+}
+
+// Mixed-event pairs of the list-1 tile at i0 (n1 particles, columns l1 =
+// px py pz E) and the list-2 tile at j0 (n2 particles, columns l2).
+template <bool AZ, bool BOOST>
+__device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
+                                                const double *const *l1, long long n1,
+                                                const double *const *l2, long long n2,
+                                                long long i0, long long j0) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    sm.fi[tid] = (i0 + tid < n1) ? make_float4((float)l1[0][i0 + tid], (float)l1[1][i0 + tid],
+                                               (float)l1[2][i0 + tid], (float)l1[3][i0 + tid])
+                                 : make_float4(0.f, 0.f, 0.f, 1.f);
+    sm.fj[tid] = (j0 + tid < n2) ? make_float4((float)l2[0][j0 + tid], (float)l2[1][j0 + tid],
+                                               (float)l2[2][j0 + tid], (float)l2[3][j0 + tid])
+                                 : make_float4(0.f, 0.f, 0.f, 1.f);
+    __syncthreads();
+    const Screen &S = d.s;
+    const int il = w * 32 + lane;
+    const bool active = i0 + il < n1;
+    const float4 a = sm.fi[il];
+    const int jend = (int)min((long long)FT, n2 - j0);
+    unsigned *q = sm.queue[w];
+    int count = 0;
+
+    auto process = [&](unsigned e) {
+        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        Q s;
+        const int wcls = screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+        int iK = 0, bin = 0, slot = -1;
+        if (wcls == 1 && decide_bins(S, s, iK, bin)) {
+            slot = iK;
+            if (AZ) {
+                const int ip = kphi_screen(S, s);
+                slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
+            }
+        }
+        if (slot >= 0) {
+            atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
+        } else {
+            const long long i = i0 + qi, j = j0 + qj;
+            const Chain ch = pair_chain<true>(d.g, l1[0][i], l1[1][i], l1[2][i], l1[3][i],
+                                              l2[0][j], l2[1][j], l2[2][j], l2[3][j], nullptr,
+                                              nullptr);
+            consume<true, MODE_FAST>(d, i, j, n2, n1, ch);
+        }
+    };
+
+    for (int jj = 0; jj < jend; jj++) {
+        int cls = 0;
+        if (active) {
+            Q s;
+            cls = screen_windows<BOOST>(S, a, sm.fj[jj], s);
+        }
+        enqueue(q, count, cls != 0, (unsigned)il | ((unsigned)jj << 8), lane, process);
+    }
+    if (lane < count) process(q[lane]);
+}
+
+}  // namespace tile
+}  // namespace hbt

@@ -23,6 +23,7 @@ PRECISION_FP64 = 0
 PRECISION_FP32W = 1
 KERNEL_SCREENED = 0
 KERNEL_REFERENCE_CHAIN = 1
+KERNEL_SCREENED_GRID = 2
 
 _D = ctypes.c_double
 _I32 = ctypes.c_int32
@@ -51,6 +52,10 @@ class HbtSoa4(ctypes.Structure):
     _fields_ = [(k, ctypes.c_void_p) for k in ("px", "py", "pz", "E")]
 
 
+class HbtJob(ctypes.Structure):
+    _fields_ = [("kind", _I32), ("na", _I64), ("nb", _I64), ("a", HbtSoa8), ("b", HbtSoa8)]
+
+
 class HbtStats(ctypes.Structure):
     _fields_ = [(k, _U64) for k in ("pairs_same", "pairs_mixed", "launches",
                                     "ordered_passes", "deferred_kphi", "anomalies")]
@@ -70,6 +75,8 @@ _SIGNATURES = {
     "hbt_bin_same_dev": (_I32, [ctypes.c_void_p, _I64, ctypes.POINTER(HbtSoa8)]),
     "hbt_bin_mixed_dev": (_I32, [ctypes.c_void_p, _I64, ctypes.POINTER(HbtSoa4), _I64,
                                  ctypes.POINTER(HbtSoa4)]),
+    "hbt_bin_batch": (_I32, [ctypes.c_void_p, _I32, ctypes.POINTER(HbtJob)]),
+    "hbt_bin_batch_dev": (_I32, [ctypes.c_void_p, _I32, ctypes.POINTER(HbtJob)]),
     "hbt_sync": (_I32, [ctypes.c_void_p, _U64]),
     "hbt_n_bins": (_I64, [ctypes.c_void_p]),
     "hbt_read_hist": (_I32, [ctypes.c_void_p] + [_PD] * 6),
@@ -205,6 +212,31 @@ class Engine:
         b = HbtSoa4(*[_ptr(c) for c in l2[:4]])
         fn = self.L.hbt_bin_mixed_dev if device else self.L.hbt_bin_mixed
         self._check(fn(self._h, n1, ctypes.byref(a), n2, ctypes.byref(b)))
+
+    def bin_batch(self, jobs: Sequence, device: bool = False):
+        """Many jobs in one persistent launch.  Each job is ("same", cols8)
+        or ("mixed", cols4_list1, cols4_list2)."""
+        arr = (HbtJob * max(len(jobs), 1))()
+        keep = []
+        for k, job in enumerate(jobs):
+            if job[0] == "same":
+                cols = job[1] if device else [_arr(c) for c in job[1]]
+                keep.append(cols)
+                arr[k].kind = 0
+                arr[k].na = int(cols[0].shape[0])
+                arr[k].nb = 0
+                arr[k].a = HbtSoa8(*[_ptr(c) for c in cols])
+            else:
+                a = job[1] if device else [_arr(c) for c in job[1]]
+                b = job[2] if device else [_arr(c) for c in job[2]]
+                keep.append((a, b))
+                arr[k].kind = 1
+                arr[k].na = int(a[0].shape[0])
+                arr[k].nb = int(b[0].shape[0])
+                arr[k].a = HbtSoa8(*([_ptr(c) for c in a[:4]] + [0, 0, 0, 0]))
+                arr[k].b = HbtSoa8(*([_ptr(c) for c in b[:4]] + [0, 0, 0, 0]))
+        fn = self.L.hbt_bin_batch_dev if device else self.L.hbt_bin_batch
+        self._check(fn(self._h, len(jobs), arr))
 
     # ------------------------------------------------------------ results
     def hist(self) -> dict:

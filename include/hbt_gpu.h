@@ -75,8 +75,12 @@ typedef struct hbt_params {
  * for every pair and is kept as the plain baseline the screened form is
  * measured against. */
 typedef enum hbt_kernel {
-    HBT_KERNEL_SCREENED = 0,       /* FP32 screen + FP64 for binned pairs */
-    HBT_KERNEL_REFERENCE_CHAIN = 1 /* FP64 reference chain on every pair */
+    HBT_KERNEL_SCREENED = 0,       /* lists sorted in momentum space, tile pairs
+                                      that cannot bin culled, persistent kernel
+                                      with FP32 screen + FP64 for binned pairs */
+    HBT_KERNEL_REFERENCE_CHAIN = 1, /* FP64 reference chain on every pair */
+    HBT_KERNEL_SCREENED_GRID = 2   /* FP32 screen, one CTA per tile pair, no
+                                      sorting or culling */
 } hbt_kernel;
 
 typedef struct hbt_ctx hbt_ctx;
@@ -134,6 +138,24 @@ hbt_status hbt_bin_mixed(hbt_ctx *ctx, int64_t n1, const hbt_soa4 *list1,
 hbt_status hbt_bin_same_dev(hbt_ctx *ctx, int64_t n, const hbt_soa8 *list);
 hbt_status hbt_bin_mixed_dev(hbt_ctx *ctx, int64_t n1, const hbt_soa4 *list1,
                              int64_t n2, const hbt_soa4 *list2);
+
+/* One job of a batch: the same-event pairs of list a (kind 0, eight
+ * columns), or the mixed-event pairs a x b (kind 1, columns px py pz E). */
+typedef struct hbt_job {
+    int32_t kind;
+    int64_t na, nb;
+    hbt_soa8 a, b;
+} hbt_job;
+
+/* Bins a batch of jobs in one persistent launch from a work queue of
+ * (job, i-tile, j-tile) items - the pair loops of many
+ * combine_and_bin_particle_pairs / _mixed_events calls at once
+ * (src/HBT_correlation.cpp:282-461, :554-689).  The result equals calling
+ * hbt_bin_same / hbt_bin_mixed for each job in order; when a pair cap could
+ * bind, the jobs are run one by one to keep the reference's admission
+ * order.  hbt_bin_batch takes host arrays, hbt_bin_batch_dev device arrays. */
+hbt_status hbt_bin_batch(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs);
+hbt_status hbt_bin_batch_dev(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs);
 
 /* Waits for the context's stream, polling up to timeout_us microseconds
  * (0: wait without limit).  Returns HBT_ERR_TIMEOUT if work is still
