@@ -86,6 +86,7 @@ __global__ void k_gather(BatchDev b) {
         const BatchList &l = b.lists[L];
         const long long k = (long long)b.vals_out[s] - l.off;
         for (int f = 0; f < l.ncols; f++) b.table[(long long)f * b.cap + s] = l.src[f][k];
+        b.orig[s] = (unsigned)k;  // position in the caller's list (pair orientation)
     }
 }
 
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(FT) k_persistent(Device d, BatchDev b, unsigne
             const double *c[8];
 #pragma unroll
             for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
-            same_tile_pair<AZ, BOOST, PREC>(d, sm, c, la.n, (long long)it.ti * FT,
+            same_tile_pair<AZ, BOOST, PREC>(d, sm, c, b.orig + la.off, la.n, (long long)it.ti * FT,
                                             (long long)it.tj * FT);
         } else {
             const BatchList &lb = b.lists[job.lb];

@@ -48,6 +48,7 @@ struct BatchDev {
     long long total_pairs;  // candidate tile pairs
     long long cap;          // row capacity of the sorted table
     double *table;          // [8][cap] sorted particle table
+    unsigned *orig;         // [cap] each row's position in the caller's list
     unsigned long long *keys_in, *keys_out;
     unsigned *vals_in, *vals_out;
     void *sort_temp;

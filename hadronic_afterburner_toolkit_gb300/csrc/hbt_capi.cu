@@ -380,7 +380,7 @@ hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
     TRY(dalloc(c, c->b_offs, (2 * lists.size() + bj.size()) * sizeof(long long)));
     TRY(dalloc(c, c->b_table, (size_t)8 * total * sizeof(double)));
     TRY(dalloc(c, c->b_keys, (size_t)2 * total * sizeof(unsigned long long)));
-    TRY(dalloc(c, c->b_vals, (size_t)2 * total * sizeof(unsigned)));
+    TRY(dalloc(c, c->b_vals, (size_t)3 * total * sizeof(unsigned)));
     TRY(dalloc(c, c->b_sort_temp, sort_bytes));
     TRY(dalloc(c, c->b_boxes, (size_t)tiles * sizeof(hbt::Box)));
     TRY(dalloc(c, c->b_items, (size_t)pairs * sizeof(hbt::Item)));
@@ -412,6 +412,7 @@ hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
     b.keys_out = b.keys_in + total;
     b.vals_in = ptr<unsigned>(c->b_vals);
     b.vals_out = b.vals_in + total;
+    b.orig = b.vals_in + 2 * total;
     b.sort_temp = c->b_sort_temp.p;
     b.sort_temp_bytes = c->b_sort_temp.bytes;
     b.boxes = ptr<hbt::Box>(c->b_boxes);

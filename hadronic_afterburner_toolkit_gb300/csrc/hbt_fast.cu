@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(FT) k_same_screened(Device d, long long n, Col
     __shared__ TileSmem sm;
     long long ti, tj;
     tri_tile((long long)blockIdx.x + d.block_offset, ti, tj);
-    same_tile_pair<AZ, BOOST, PREC>(d, sm, c.p, n, ti * FT, tj * FT);
+    same_tile_pair<AZ, BOOST, PREC>(d, sm, c.p, nullptr, n, ti * FT, tj * FT);
 }
 
 template <bool AZ, bool BOOST>

@@ -242,6 +242,7 @@ struct TileSmem {
     float4 fi[FT];     // FP32 momenta of the i-tile
     float4 fj[FT];     // FP32 momenta of the j-tile
     unsigned queue[FT / 32][QCAP];
+    unsigned oi[FT], oj[FT];  // original list positions (pair orientation)
 };
 
 // Appends this lane's pair to the warp queue when `take`, and runs
@@ -263,18 +264,24 @@ __device__ __forceinline__ void enqueue(unsigned *q, int &count, bool take, unsi
     }
 }
 
-// Same-event pairs i < j of the tiles starting at i0 and j0 (i0 <= j0) of
-// one list of n particles with columns c = px py pz E x y z t.  Called by
-// all FT threads of the CTA; the caller syncs before reusing `sm`.
+// Same-event pairs of the tiles starting at i0 and j0 (i0 <= j0) of one list
+// of n particles with columns c = px py pz E x y z t.  Every unordered pair
+// is visited once (position j > i); it is oriented as the reference orients
+// it, q = p_first - p_second with `first` the particle earlier in the
+// caller's list: orig[k] is that original index of row k, or nullptr when
+// the rows are in the caller's order.  Called by all FT threads of the CTA;
+// the caller syncs before reusing `sm`.
 template <bool AZ, bool BOOST, int PREC>
 __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
-                                               const double *const *c, long long n,
-                                               long long i0, long long j0) {
+                                               const double *const *c, const unsigned *orig,
+                                               long long n, long long i0, long long j0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     for (int f = 0; f < 8; f++) {
         sm.si[f][tid] = (i0 + tid < n) ? c[f][i0 + tid] : 0.0;
         sm.sj[f][tid] = (j0 + tid < n) ? c[f][j0 + tid] : 0.0;
     }
+    sm.oi[tid] = orig ? (i0 + tid < n ? orig[i0 + tid] : 0u) : (unsigned)(i0 + tid);
+    sm.oj[tid] = orig ? (j0 + tid < n ? orig[j0 + tid] : 0u) : (unsigned)(j0 + tid);
     __syncthreads();
     sm.fi[tid] = make_float4((float)sm.si[0][tid], (float)sm.si[1][tid], (float)sm.si[2][tid],
                              (float)sm.si[3][tid]);
@@ -285,6 +292,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
     const int il = w * 32 + lane;
     const long long i = i0 + il;
     const float4 a = sm.fi[il];
+    const unsigned oa = sm.oi[il];
     const int jend = (int)min((long long)FT, n - j0);
     unsigned *q = sm.queue[w];
     int count = 0;
@@ -292,8 +300,10 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
     // stages B and C for one queued pair (all lanes of the warp in step)
     auto process = [&](unsigned e) {
         const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        const bool swap = (e >> 16) & 1u;
         Q s;
-        const int wcls = screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+        const int wcls = swap ? screen_windows<BOOST>(S, sm.fj[qj], sm.fi[qi], s)
+                              : screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
         int iK = 0, bin = 0, slot = -1;
         if (wcls == 1 && decide_bins(S, s, iK, bin)) {
             slot = iK;
@@ -302,11 +312,12 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
                 slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
             }
         }
-        double A[8], B[8];
+        double A[8], B[8];  // first and second particle of the pair
 #pragma unroll
         for (int f = 0; f < 8; f++) {
-            A[f] = sm.si[f][qi];
-            B[f] = sm.sj[f][qj];
+            const double u = sm.si[f][qi], v = sm.sj[f][qj];
+            A[f] = swap ? v : u;
+            B[f] = swap ? u : v;
         }
         if (slot < 0) {
             // undecided somewhere: the reference chain decides (and may hand
@@ -340,11 +351,14 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
     for (int jj = 0; jj < jend; jj++) {
         const long long j = j0 + jj;
         int cls = 0;
+        const bool swap = oa > sm.oj[jj];
         if (i < n && j > i) {
             Q s;
-            cls = screen_windows<BOOST>(S, a, sm.fj[jj], s);
+            cls = swap ? screen_windows<BOOST>(S, sm.fj[jj], a, s)
+                       : screen_windows<BOOST>(S, a, sm.fj[jj], s);
         }
-        enqueue(q, count, cls != 0, (unsigned)il | ((unsigned)jj << 8), lane, process);
+        enqueue(q, count, cls != 0,
+                (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16), lane, process);
     }
     if (lane < count) process(q[lane]);
 }
