@@ -59,6 +59,10 @@ def make_workload(name: str, seed: int = 1, max_groups: int | None = None):
     if name == "small":
         ev = synth.small_pions(seed=seed)
         buf, nmix = 5000, 5
+    elif name == "medium":
+        # the central workload's events and grid, 30x oversampling (profiling)
+        ev = synth.central_pions(n_events=300, seed=seed)
+        buf, nmix = 45000, 10
     else:
         ev = synth.central_pions(seed=seed)
         buf, nmix = 150000, 10
@@ -271,7 +275,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="central", choices=["central", "small"])
+    ap.add_argument("--workload", default="central", choices=["central", "medium", "small"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32w"])
     ap.add_argument("--kernel", default="screened", choices=["screened", "reference-chain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -315,19 +319,27 @@ def main() -> None:
     eng = E.Engine(device=local, precision=prec, kernel=kern, **p)
     eng.set_stream(stream.cuda_stream)
 
-    def step_device(k):
-        dc, dm = dgroups[k % len(dgroups)]
-        eng.bin_same(dc, device=True)
-        for l1, l2 in dm:
-            eng.bin_mixed(l1, l2, device=True)
+    batched = kern == E.KERNEL_SCREENED
+
+    def run_group(engine, grp, batch, device=True):
+        """One oversample group: its same-event pairs and every event's
+        mixed pairs, as one batch (persistent launch) or call by call."""
+        dc, dm = grp
+        if batch:
+            engine.bin_batch([("same", dc)] + [("mixed", l1, l2) for l1, l2 in dm],
+                             device=device)
+        else:
+            engine.bin_same(dc, device=device)
+            for l1, l2 in dm:
+                engine.bin_mixed(l1, l2, device=device)
 
     for k in range(args.warmup):
-        step_device(k)
+        run_group(eng, dgroups[k % len(dgroups)], batched)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     launches0 = eng.stats()["launches"]
-    ms_steps, ms_same, pairs = [], [], 0
+    ms_steps, pairs = [], 0
     with ClockSampler(local) as clk:
         for k in range(args.steps):
             g = args.warmup + k
@@ -335,17 +347,11 @@ def main() -> None:
                 flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
-            e2 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            dc, dm = dgroups[g % len(dgroups)]
-            eng.bin_same(dc, device=True)
+            run_group(eng, dgroups[g % len(dgroups)], batched)
             e1.record(stream)
-            for l1, l2 in dm:
-                eng.bin_mixed(l1, l2, device=True)
-            e2.record(stream)
-            e2.synchronize()
-            ms_steps.append(e0.elapsed_time(e2))
-            ms_same.append(e0.elapsed_time(e1))
+            e1.synchronize()
+            ms_steps.append(e0.elapsed_time(e1))
             pairs += group_pairs(groups[g % len(groups)])
     torch.cuda.synchronize()
     launches = eng.stats()["launches"] - launches0
@@ -361,22 +367,19 @@ def main() -> None:
         pairs_all = float(pairs)
     value = pairs_all / (t_ms * 1e-3)
 
-    def time_variant(kernel, precision, nsteps, label):
+    def time_variant(kernel, precision, nsteps, label, batch):
         """Same workload, another kernel family / precision, same GPU."""
         engv = E.Engine(device=local, precision=precision, kernel=kernel, **p)
         engv.set_stream(stream.cuda_stream)
         ms_tot, prs = 0.0, 0
         for k in range(nsteps + 1):  # the first step warms up
             g = (args.warmup + k) % len(dgroups)
-            dc, dm = dgroups[g]
             with torch.cuda.stream(stream):
                 flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            engv.bin_same(dc, device=True)
-            for l1, l2 in dm:
-                engv.bin_mixed(l1, l2, device=True)
+            run_group(engv, dgroups[g], batch)
             e1.record(stream)
             e1.synchronize()
             if k > 0:
@@ -386,40 +389,46 @@ def main() -> None:
         return {"kernel": label, "value": prs / (ms_tot * 1e-3),
                 "ms_per_step": ms_tot / nsteps, "steps": nsteps}
 
-    # the plain form (FP64 reference chain on every pair) and the other
-    # precision, on the same GPU
+    # the plain form (FP64 reference chain on every pair, one call per list)
+    # and the other forms, on the same GPU
     plain = None
     variants = {}
     if not args.no_plain and kern == E.KERNEL_SCREENED:
         plain = time_variant(E.KERNEL_REFERENCE_CHAIN, E.PRECISION_FP64, 1,
-                             "reference-chain (FP64 reference order on every pair)")
+                             "reference-chain (FP64 reference order on every pair)", False)
         other = E.PRECISION_FP32W if prec == E.PRECISION_FP64 else E.PRECISION_FP64
-        variants["screened-fp32w" if other == E.PRECISION_FP32W else "screened-fp64"] = \
+        variants["batched-fp32w" if other == E.PRECISION_FP32W else "batched-fp64"] = \
             time_variant(E.KERNEL_SCREENED, other, 2,
-                         "screened, %s" % ("FP32 weights" if other else "FP64"))
+                         "batched persistent, %s" % ("FP32 weights" if other else "FP64"), True)
+        variants["grid-" + args.precision] = time_variant(
+            E.KERNEL_SCREENED_GRID, prec, 1,
+            "screened, one launch per list, no sorting or culling", False)
 
-    # roofline of the dominant (same-event) kernel against the live FP64 peak
+    # roofline of the step's pair binning against the live FP64 peak
     peaks = measure_fp64_peak()
     g0 = groups[args.warmup % len(groups)]
     fr = survival_fractions(g0, p)
     n = g0[0][0].size
     P_same = n * (n - 1) / 2
-    ops = sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)) * P_same
-    t_same = statistics.median(ms_same) * 1e-3
-    achieved = ops / t_same / 1e12
+    P_mixed = sum(l1[0].size * l2[0].size for l1, l2 in g0[1])
+    ops = (sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)) * P_same +
+           sum(o * f for o, f in zip(STAGE_OPS_MIXED, fr)) * P_mixed)
+    t_step = statistics.median(ms_steps) * 1e-3
+    achieved = ops / t_step / 1e12
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
                 "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"], "traffic": None,
-                "kernel": "k_same (same-event pair binning)",
+                "kernel": "k_persistent (batched screened pair binning)" if batched
+                          else "pair-binning kernels",
                 "peak_source": "measured live: FP64 FMA probe (lib/libhbt_probe.so)",
-                "ops_per_pair": round(ops / P_same, 2),
+                "ops_per_pair_same": round(sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)), 2),
+                "ops_per_pair_mixed": round(sum(o * f for o, f in zip(STAGE_OPS_MIXED, fr)), 2),
                 "survival": [round(x, 4) for x in fr],
-                "same_event_ms_per_group": round(statistics.median(ms_same), 3),
                 "fp32_tflops_measured": peaks["fp32_tflops"]}
 
     # end to end through the host-buffer C ABI (pinned host arrays)
     e2e = None
     if not args.no_e2e:
-        eng2 = E.Engine(device=local, precision=prec, **p)
+        eng2 = E.Engine(device=local, precision=prec, kernel=kern, **p)
         pin = []
         for cols, mixed in groups:
             pc = [torch.from_numpy(c).pin_memory().numpy() for c in cols]
@@ -431,10 +440,7 @@ def main() -> None:
         import ctypes
 
         def step_host(k):
-            pc, pm = pin[k % len(pin)]
-            eng2.bin_same(pc)
-            for l1, l2 in pm:
-                eng2.bin_mixed(l1, l2)
+            run_group(eng2, pin[k % len(pin)], batched, device=False)
             eng2._check(eng2.L.hbt_read_hist(eng2.handle, *[o.ctypes.data_as(E._PD) for o in out]))
 
         for k in range(args.warmup):
