@@ -19,10 +19,11 @@
 //     which grows with m_T1, m_T2 and |y1 - y2|, so its smallest value over
 //     two tiles bounds |q_long| from below; without the boost q_long = q_z.
 //     Each bound carries a 1e-6 relative margin for rounding;
-//  4. k_persistent: one CTA per SM slot pulls (job, i-tile, j-tile) items
-//     from the culled queue and runs the screened tile-pair bodies of
-//     hbt_tile.cuh.  The FP32-weight form runs the queue in chunks and
-//     merges the FP32 partials between them.
+//  4. k_persistent_same / k_persistent_mixed: persistent CTAs (5 per SM)
+//     pull (job, i-tile, j-tile) items from the culled same-event and
+//     mixed-event queues and run the screened tile-pair bodies of
+//     hbt_tile.cuh.  The FP32-weight form runs the same-event queue in
+//     chunks and merges the FP32 partials between them.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "hbt_batch.cuh"
@@ -156,6 +157,8 @@ __device__ __forceinline__ bool boxes_may_pair(const BatchDev &b, const Box &a, 
     return true;
 }
 
+// Culled queues: same-event items at items[0, same_cap), mixed-event items
+// at items[same_cap, same_cap + mixed_cap); n_items[0] / n_items[1] count them.
 __global__ void k_cull(BatchDev b) {
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < b.total_pairs;
          p += (long long)gridDim.x * blockDim.x) {
@@ -173,52 +176,77 @@ __global__ void k_cull(BatchDev b) {
         const Box &A = b.boxes[b.lists[job.la].tile_off + ti];
         const Box &B = b.boxes[b.lists[job.lb].tile_off + tj];
         if (boxes_may_pair(b, A, B)) {
-            const unsigned slot = atomicAdd(b.n_items, 1u);
-            if (slot < b.item_cap) b.items[slot] = Item{(unsigned)J, (unsigned)ti, (unsigned)tj};
+            const Item it = Item{(unsigned)J, (unsigned)ti, (unsigned)tj};
+            if (job.kind == 0) {
+                const unsigned slot = atomicAdd(b.n_items, 1u);
+                if (slot < b.same_cap) b.items[slot] = it;
+            } else {
+                const unsigned slot = atomicAdd(b.n_items + 1, 1u);
+                if (slot < b.mixed_cap) b.items[b.same_cap + slot] = it;
+            }
         }
     }
 }
 
+// Same-event items [base, min(end, queued)) pulled by persistent CTAs.
 template <bool AZ, bool BOOST, int PREC>
-__global__ void __launch_bounds__(FT) k_persistent(Device d, BatchDev b, unsigned base,
-                                                   unsigned end) {
+__global__ void __launch_bounds__(FT, 5) k_persistent_same(Device d, BatchDev b, unsigned base,
+                                                           unsigned end) {
     __shared__ TileSmem sm;
     __shared__ unsigned item;
-    const unsigned n_items = min(*b.n_items, b.item_cap);
-    const unsigned stop = min(end, n_items);
+    const unsigned stop = min(end, min(b.n_items[0], b.same_cap));
     for (;;) {
         if (threadIdx.x == 0) item = base + atomicAdd(b.item_next, 1u);
         __syncthreads();
         const unsigned k = item;
         if (k >= stop) break;
         const Item it = b.items[k];
+        const BatchList &la = b.lists[b.jobs[it.job].la];
+        const double *c[8];
+#pragma unroll
+        for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
+        same_tile_pair<AZ, BOOST, PREC>(d, sm, c, b.orig + la.off, la.n, (long long)it.ti * FT,
+                                        (long long)it.tj * FT);
+        __syncthreads();
+    }
+}
+
+// Mixed-event items, all in one launch.
+template <bool AZ, bool BOOST>
+__global__ void __launch_bounds__(FT, 5) k_persistent_mixed(Device d, BatchDev b) {
+    __shared__ TileSmem sm;
+    __shared__ unsigned item;
+    const unsigned stop = min(b.n_items[1], b.mixed_cap);
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(b.item_next + 1, 1u);
+        __syncthreads();
+        const unsigned k = item;
+        if (k >= stop) break;
+        const Item it = b.items[b.same_cap + k];
         const BatchJob &job = b.jobs[it.job];
-        const BatchList &la = b.lists[job.la];
-        if (job.kind == 0) {
-            const double *c[8];
+        const BatchList &la = b.lists[job.la], &lb = b.lists[job.lb];
+        const double *c1[4], *c2[4];
 #pragma unroll
-            for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
-            same_tile_pair<AZ, BOOST, PREC>(d, sm, c, b.orig + la.off, la.n, (long long)it.ti * FT,
-                                            (long long)it.tj * FT);
-        } else {
-            const BatchList &lb = b.lists[job.lb];
-            const double *c1[4], *c2[4];
-#pragma unroll
-            for (int f = 0; f < 4; f++) {
-                c1[f] = b.table + (long long)f * b.cap + la.off;
-                c2[f] = b.table + (long long)f * b.cap + lb.off;
-            }
-            mixed_tile_pair<AZ, BOOST>(d, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
-                                       (long long)it.tj * FT);
+        for (int f = 0; f < 4; f++) {
+            c1[f] = b.table + (long long)f * b.cap + la.off;
+            c2[f] = b.table + (long long)f * b.cap + lb.off;
         }
+        mixed_tile_pair<AZ, BOOST>(d, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
+                                   (long long)it.tj * FT);
         __syncthreads();
     }
 }
 
 template <bool AZ, bool BOOST, int PREC>
-cudaError_t persistent_launch(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+cudaError_t launch_same_items(const Device &d, const BatchDev &b, unsigned base, unsigned end,
                               int grid, cudaStream_t st) {
-    k_persistent<AZ, BOOST, PREC><<<grid, FT, 0, st>>>(d, b, base, end);
+    k_persistent_same<AZ, BOOST, PREC><<<grid, FT, 0, st>>>(d, b, base, end);
+    return cudaGetLastError();
+}
+
+template <bool AZ, bool BOOST>
+cudaError_t launch_mixed_items(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
+    k_persistent_mixed<AZ, BOOST><<<grid, FT, 0, st>>>(d, b);
     return cudaGetLastError();
 }
 
@@ -226,8 +254,8 @@ cudaError_t persistent_launch(const Device &d, const BatchDev &b, unsigned base,
 
 int persistent_blocks_per_sm() {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_persistent<true, true, 0>, FT, 0) !=
-        cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_persistent_same<true, true, 0>, FT,
+                                                      0) != cudaSuccess)
         return 4;
     return nb > 0 ? nb : 1;
 }
@@ -240,8 +268,8 @@ size_t batch_sort_temp_bytes(long long cap) {
     return bytes;
 }
 
-cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned items_upper,
-                      unsigned chunk, cudaStream_t st) {
+cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
+                      cudaStream_t st) {
     cudaError_t e;
     const int gs = 152 * 8;
     if (b.total > 0) {
@@ -258,19 +286,23 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned ite
         k_boxes<<<(unsigned)((b.total_tiles * 32 + 255) / 256), 256, 0, st>>>(b);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    if ((e = cudaMemsetAsync(b.n_items, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(b.n_items, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(b.item_next, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
     if (b.total_pairs > 0) {
         k_cull<<<gs, 256, 0, st>>>(b);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     const bool az = d.g.azimuthal, boost = d.g.boost;
     const int prec = d.precision;
-    if (chunk == 0 || prec == 0) chunk = items_upper;
-    for (unsigned base = 0; base < items_upper; base += chunk) {
-        const unsigned end = (unsigned)min((unsigned long long)base + chunk,
-                                           (unsigned long long)items_upper);
-        if ((e = cudaMemsetAsync(b.item_next, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
-#define HBT_P(AZ_, BO_, PR_) e = persistent_launch<AZ_, BO_, PR_>(d, b, base, end, grid, st)
+    // same-event items (chunked for the FP32-weight form)
+    const unsigned upper = b.same_cap;
+    if (chunk == 0 || prec == 0) chunk = upper;
+    for (unsigned base = 0; base < upper; base += chunk) {
+        const unsigned end =
+            (unsigned)min((unsigned long long)base + chunk, (unsigned long long)upper);
+        if (base > 0 && (e = cudaMemsetAsync(b.item_next, 0, sizeof(unsigned), st)) != cudaSuccess)
+            return e;
+#define HBT_P(AZ_, BO_, PR_) e = launch_same_items<AZ_, BO_, PR_>(d, b, base, end, grid, st)
         if (prec == 0) {
             if (az && boost) HBT_P(true, true, 0);
             else if (az) HBT_P(true, false, 0);
@@ -287,6 +319,14 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned ite
         if (prec) {
             if ((e = launch_merge(d, st)) != cudaSuccess) return e;
         }
+    }
+    // mixed-event items
+    if (b.mixed_cap > 0) {
+        if (az && boost) e = launch_mixed_items<true, true>(d, b, grid, st);
+        else if (az) e = launch_mixed_items<true, false>(d, b, grid, st);
+        else if (boost) e = launch_mixed_items<false, true>(d, b, grid, st);
+        else e = launch_mixed_items<false, false>(d, b, grid, st);
+        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }

@@ -54,10 +54,11 @@ struct BatchDev {
     void *sort_temp;
     size_t sort_temp_bytes;
     Box *boxes;
-    Item *items;
-    unsigned item_cap;
-    unsigned *n_items;    // culled queue length
-    unsigned *item_next;  // persistent-kernel cursor
+    Item *items;          // same-event queue, then the mixed-event queue
+    unsigned same_cap;    // candidate same-event tile pairs
+    unsigned mixed_cap;   // candidate mixed-event tile pairs
+    unsigned *n_items;    // [2] culled queue lengths (same, mixed)
+    unsigned *item_next;  // [2] persistent-kernel cursors
     // cell sizes of the sort key and the cull thresholds
     double p_extent, inv_cell_pt, y_extent, inv_cell_y;
     double qt2_max;  // 2 Q^2 (1 + 1e-6): largest q_x^2 + q_y^2 that can bin
@@ -67,10 +68,10 @@ struct BatchDev {
 
 int persistent_blocks_per_sm();
 size_t batch_sort_temp_bytes(long long cap);
-// Sort, box, cull and bin one batch.  items_upper bounds the culled queue
-// (its capacity); chunk > 0 splits the FP32-weight form into chunks of that
-// many items with a merge of the FP32 partials after each.
-cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned items_upper,
-                      unsigned chunk, cudaStream_t st);
+// Sort, box, cull and bin one batch.  chunk > 0 splits the FP32-weight
+// form's same-event queue into chunks of that many items with a merge of
+// the FP32 partials after each.
+cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
+                      cudaStream_t st);
 
 }  // namespace hbt

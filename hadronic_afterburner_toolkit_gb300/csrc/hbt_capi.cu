@@ -336,7 +336,7 @@ hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
     std::vector<hbt::BatchList> lists;
     std::vector<hbt::BatchJob> bj;
     std::vector<long long> list_off, tile_off, pair_off;
-    long long total = 0, tiles = 0, pairs = 0;
+    long long total = 0, tiles = 0, pairs = 0, same_pairs = 0, mixed_pairs = 0;
     auto add_list = [&](const double *const *src, int ncols, long long n) {
         hbt::BatchList l = {};
         for (int f = 0; f < 8; f++) l.src[f] = f < ncols ? src[f] : nullptr;
@@ -369,6 +369,7 @@ hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
         b.pair_off = pairs;
         pair_off.push_back(pairs);
         pairs += b.n_pairs;
+        (b.kind == 0 ? same_pairs : mixed_pairs) += b.n_pairs;
         bj.push_back(b);
     }
     if (bj.empty()) return HBT_OK;
@@ -384,7 +385,7 @@ hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
     TRY(dalloc(c, c->b_sort_temp, sort_bytes));
     TRY(dalloc(c, c->b_boxes, (size_t)tiles * sizeof(hbt::Box)));
     TRY(dalloc(c, c->b_items, (size_t)pairs * sizeof(hbt::Item)));
-    TRY(dalloc(c, c->b_counters, 2 * sizeof(unsigned)));
+    TRY(dalloc(c, c->b_counters, 4 * sizeof(unsigned)));
     std::vector<long long> offs(list_off);
     offs.insert(offs.end(), tile_off.begin(), tile_off.end());
     offs.insert(offs.end(), pair_off.begin(), pair_off.end());
@@ -417,9 +418,10 @@ hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
     b.sort_temp_bytes = c->b_sort_temp.bytes;
     b.boxes = ptr<hbt::Box>(c->b_boxes);
     b.items = ptr<hbt::Item>(c->b_items);
-    b.item_cap = (unsigned)pairs;
+    b.same_cap = (unsigned)same_pairs;
+    b.mixed_cap = (unsigned)mixed_pairs;
     b.n_items = ptr<unsigned>(c->b_counters);
-    b.item_next = b.n_items + 1;
+    b.item_next = b.n_items + 2;
     b.p_extent = 1024 * 0.02 / 2;
     b.inv_cell_pt = 1.0 / 0.02;
     b.y_extent = 1024 * 0.05 / 2;
@@ -428,8 +430,8 @@ hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
     b.qt2_max = 2.0 * Q * Q * (1.0 + 1e-6) + 1e-300;
     b.ql_max = Q * (1.0 + 1e-6) + 1e-300;
     b.boost = c->d.g.boost;
-    CU(hbt::run_batch(c->d, b, c->persistent_grid, (unsigned)pairs,
-                      (unsigned)c->d.merge_chunk_blocks, c->stream));
+    CU(hbt::run_batch(c->d, b, c->persistent_grid, (unsigned)c->d.merge_chunk_blocks,
+                      c->stream));
     c->st.launches += 6;
     return HBT_OK;
 }
