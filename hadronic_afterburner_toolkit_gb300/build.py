@@ -40,6 +40,7 @@ GPU_UNITS = {
     "hbt_fast.cu": ["--fmad=false"],
     "hbt_noalloc.cu": ["--fmad=false"],
     "hbt_batch.cu": ["--fmad=false"],
+    "hbt_runner.cu": [],
 }
 
 

@@ -137,7 +137,7 @@ __global__ void k_boxes(BatchDev b) {
 }
 
 // Can a pair with one particle in box a and one in box b pass the windows?
-__device__ __forceinline__ bool boxes_may_pair(const BatchDev &b, const Box &a, const Box &c) {
+__device__ __forceinline__ bool boxes_may_pair(const BatchJob &b, const Box &a, const Box &c) {
     const double gx = fmax(0.0, fmax(a.x0 - c.x1, c.x0 - a.x1));
     const double gy = fmax(0.0, fmax(a.y0 - c.y1, c.y0 - a.y1));
     if (gx * gx + gy * gy > b.qt2_max) return false;
@@ -175,7 +175,7 @@ __global__ void k_cull(BatchDev b) {
         }
         const Box &A = b.boxes[b.lists[job.la].tile_off + ti];
         const Box &B = b.boxes[b.lists[job.lb].tile_off + tj];
-        if (boxes_may_pair(b, A, B)) {
+        if (boxes_may_pair(job, A, B)) {
             const Item it = Item{(unsigned)J, (unsigned)ti, (unsigned)tj};
             if (job.kind == 0) {
                 const unsigned slot = atomicAdd(b.n_items, 1u);
@@ -188,11 +188,25 @@ __global__ void k_cull(BatchDev b) {
     }
 }
 
+// Engine descriptor of an item: the launch's own, or (serving many
+// analyses) the job's entry of b.devs copied into shared memory.
+__device__ __forceinline__ const Device &item_device(const Device &d, const BatchDev &b,
+                                                    const BatchJob &job, Device &dsm) {
+    if (!b.devs) return d;
+    const int *src = reinterpret_cast<const int *>(b.devs + job.dev);
+    int *dst = reinterpret_cast<int *>(&dsm);
+    for (int k = threadIdx.x; k < (int)(sizeof(Device) / sizeof(int)); k += blockDim.x)
+        dst[k] = src[k];
+    __syncthreads();
+    return dsm;
+}
+
 // Same-event items [base, min(end, queued)) pulled by persistent CTAs.
 template <bool AZ, bool BOOST, int PREC>
 __global__ void __launch_bounds__(FT, 5) k_persistent_same(Device d, BatchDev b, unsigned base,
                                                            unsigned end) {
     __shared__ TileSmem sm;
+    __shared__ Device dsm;
     __shared__ unsigned item;
     const unsigned stop = min(end, min(b.n_items[0], b.same_cap));
     for (;;) {
@@ -201,11 +215,13 @@ __global__ void __launch_bounds__(FT, 5) k_persistent_same(Device d, BatchDev b,
         const unsigned k = item;
         if (k >= stop) break;
         const Item it = b.items[k];
-        const BatchList &la = b.lists[b.jobs[it.job].la];
+        const BatchJob &job = b.jobs[it.job];
+        const Device &dd = item_device(d, b, job, dsm);
+        const BatchList &la = b.lists[job.la];
         const double *c[8];
 #pragma unroll
         for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
-        same_tile_pair<AZ, BOOST, PREC>(d, sm, c, b.orig + la.off, la.n, (long long)it.ti * FT,
+        same_tile_pair<AZ, BOOST, PREC>(dd, sm, c, b.orig + la.off, la.n, (long long)it.ti * FT,
                                         (long long)it.tj * FT);
         __syncthreads();
     }
@@ -215,6 +231,7 @@ __global__ void __launch_bounds__(FT, 5) k_persistent_same(Device d, BatchDev b,
 template <bool AZ, bool BOOST>
 __global__ void __launch_bounds__(FT, 5) k_persistent_mixed(Device d, BatchDev b) {
     __shared__ TileSmem sm;
+    __shared__ Device dsm;
     __shared__ unsigned item;
     const unsigned stop = min(b.n_items[1], b.mixed_cap);
     for (;;) {
@@ -224,6 +241,7 @@ __global__ void __launch_bounds__(FT, 5) k_persistent_mixed(Device d, BatchDev b
         if (k >= stop) break;
         const Item it = b.items[b.same_cap + k];
         const BatchJob &job = b.jobs[it.job];
+        const Device &dd = item_device(d, b, job, dsm);
         const BatchList &la = b.lists[job.la], &lb = b.lists[job.lb];
         const double *c1[4], *c2[4];
 #pragma unroll
@@ -231,7 +249,7 @@ __global__ void __launch_bounds__(FT, 5) k_persistent_mixed(Device d, BatchDev b
             c1[f] = b.table + (long long)f * b.cap + la.off;
             c2[f] = b.table + (long long)f * b.cap + lb.off;
         }
-        mixed_tile_pair<AZ, BOOST>(d, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
+        mixed_tile_pair<AZ, BOOST>(dd, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
                                    (long long)it.tj * FT);
         __syncthreads();
     }
@@ -316,7 +334,7 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
         }
 #undef HBT_P
         if (e != cudaSuccess) return e;
-        if (prec) {
+        if (prec && !b.devs) {
             if ((e = launch_merge(d, st)) != cudaSuccess) return e;
         }
     }

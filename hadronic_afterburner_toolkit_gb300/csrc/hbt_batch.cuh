@@ -19,9 +19,16 @@ struct BatchList {
 
 // One job: same-event pairs of list la (kind 0) or la x lb (kind 1).
 struct BatchJob {
-    int kind, la, lb, pad;
+    int kind, la, lb;
+    int dev;             // engine descriptor (BatchDev::devs) when serving many analyses
     long long pair_off;  // first candidate tile pair of this job
     long long n_pairs;   // candidate tile pairs
+    // cull thresholds of the job's analysis, Q = max(|lo|, |hi|) of its q
+    // window: 2 Q^2 (1 + 1e-6) bounds q_x^2 + q_y^2 and Q (1 + 1e-6) bounds
+    // |q_long| of any pair that can be binned
+    double qt2_max;
+    double ql_max;
+    int boost, pad;
 };
 
 // Momentum-space box of a 128-particle tile.
@@ -59,11 +66,13 @@ struct BatchDev {
     unsigned mixed_cap;   // candidate mixed-event tile pairs
     unsigned *n_items;    // [2] culled queue lengths (same, mixed)
     unsigned *item_next;  // [2] persistent-kernel cursors
-    // cell sizes of the sort key and the cull thresholds
+    // cell sizes of the sort key
     double p_extent, inv_cell_pt, y_extent, inv_cell_y;
-    double qt2_max;  // 2 Q^2 (1 + 1e-6): largest q_x^2 + q_y^2 that can bin
-    double ql_max;   // Q (1 + 1e-6): largest |q_long| that can bin
-    int boost;
+    // Several analyses in one launch (the serving loop): each job's engine
+    // descriptor (grid, screen constants, histograms) is devs[job.dev];
+    // nullptr: every job belongs to the launch's own descriptor.
+    const Device *devs;
+    int n_devs;
 };
 
 int persistent_blocks_per_sm();

@@ -17,6 +17,8 @@
 #include "../../include/hbt_gpu.h"
 #include "hbt_batch.cuh"
 #include "hbt_engine.cuh"
+#include "hbt_internal.h"
+#include "hbt_runner.h"
 
 using hbt::u64;
 
@@ -46,8 +48,7 @@ struct hbt_ctx {
     // FP32-weight form: partial sums and Kahan compensation
     DevBuf part, comp;
     // batched path: tables, sorted particle table, sort scratch, boxes, queue
-    DevBuf b_lists, b_jobs, b_offs, b_table, b_keys, b_vals, b_sort_temp, b_boxes, b_items,
-        b_counters;
+    hbt::BatchRunner runner;
     int persistent_grid = 152 * 4;
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
@@ -323,115 +324,20 @@ bool batched_ok(const hbt_ctx *c) {
     return screened_ok(c) && c->prm.kernel == HBT_KERNEL_SCREENED;
 }
 
-// One job of a fast batch (device columns).
-struct FastJob {
-    int kind;
-    long long na, nb;
-    const double *a[8];
-    const double *b[4];
-};
+using hbt::FastJob;
 
-// Sort, cull and bin fast jobs in one persistent launch (hbt_batch.cu).
-hbt_status run_fast_jobs(hbt_ctx *c, const std::vector<FastJob> &jobs) {
-    std::vector<hbt::BatchList> lists;
-    std::vector<hbt::BatchJob> bj;
-    std::vector<long long> list_off, tile_off, pair_off;
-    long long total = 0, tiles = 0, pairs = 0, same_pairs = 0, mixed_pairs = 0;
-    auto add_list = [&](const double *const *src, int ncols, long long n) {
-        hbt::BatchList l = {};
-        for (int f = 0; f < 8; f++) l.src[f] = f < ncols ? src[f] : nullptr;
-        l.n = n;
-        l.off = total;
-        l.tiles = (n + 127) / 128;
-        l.tile_off = tiles;
-        l.ncols = ncols;
-        list_off.push_back(total);
-        tile_off.push_back(tiles);
-        total += n;
-        tiles += l.tiles;
-        lists.push_back(l);
-        return (int)lists.size() - 1;
-    };
-    for (const FastJob &j : jobs) {
-        hbt::BatchJob b = {};
-        b.kind = j.kind;
-        if (j.kind == 0) {
-            if (j.na < 2) continue;
-            b.la = b.lb = add_list(j.a, 8, j.na);
-            const long long t = lists[b.la].tiles;
-            b.n_pairs = t * (t + 1) / 2;
-        } else {
-            if (j.na < 1 || j.nb < 1) continue;
-            b.la = add_list(j.a, 4, j.na);
-            b.lb = add_list(j.b, 4, j.nb);
-            b.n_pairs = lists[b.la].tiles * lists[b.lb].tiles;
-        }
-        b.pair_off = pairs;
-        pair_off.push_back(pairs);
-        pairs += b.n_pairs;
-        (b.kind == 0 ? same_pairs : mixed_pairs) += b.n_pairs;
-        bj.push_back(b);
-    }
-    if (bj.empty()) return HBT_OK;
-    if (pairs > 0xffffffffLL) return fail(c, HBT_ERR_INVALID, "batch too large (tile pairs)");
-    // device tables and scratch, grown as needed
-    const size_t sort_bytes = hbt::batch_sort_temp_bytes(total);
-    TRY(dalloc(c, c->b_lists, lists.size() * sizeof(hbt::BatchList)));
-    TRY(dalloc(c, c->b_jobs, bj.size() * sizeof(hbt::BatchJob)));
-    TRY(dalloc(c, c->b_offs, (2 * lists.size() + bj.size()) * sizeof(long long)));
-    TRY(dalloc(c, c->b_table, (size_t)8 * total * sizeof(double)));
-    TRY(dalloc(c, c->b_keys, (size_t)2 * total * sizeof(unsigned long long)));
-    TRY(dalloc(c, c->b_vals, (size_t)3 * total * sizeof(unsigned)));
-    TRY(dalloc(c, c->b_sort_temp, sort_bytes));
-    TRY(dalloc(c, c->b_boxes, (size_t)tiles * sizeof(hbt::Box)));
-    TRY(dalloc(c, c->b_items, (size_t)pairs * sizeof(hbt::Item)));
-    TRY(dalloc(c, c->b_counters, 4 * sizeof(unsigned)));
-    std::vector<long long> offs(list_off);
-    offs.insert(offs.end(), tile_off.begin(), tile_off.end());
-    offs.insert(offs.end(), pair_off.begin(), pair_off.end());
-    CU(cudaMemcpyAsync(c->b_lists.p, lists.data(), lists.size() * sizeof(hbt::BatchList),
-                       cudaMemcpyHostToDevice, c->stream));
-    CU(cudaMemcpyAsync(c->b_jobs.p, bj.data(), bj.size() * sizeof(hbt::BatchJob),
-                       cudaMemcpyHostToDevice, c->stream));
-    CU(cudaMemcpyAsync(c->b_offs.p, offs.data(), offs.size() * sizeof(long long),
-                       cudaMemcpyHostToDevice, c->stream));
-    hbt::BatchDev b = {};
-    const long long *o = ptr<long long>(c->b_offs);
-    b.lists = ptr<hbt::BatchList>(c->b_lists);
-    b.jobs = ptr<hbt::BatchJob>(c->b_jobs);
-    b.list_off = o;
-    b.tile_off = o + lists.size();
-    b.pair_off = o + 2 * lists.size();
-    b.n_lists = (int)lists.size();
-    b.n_jobs = (int)bj.size();
-    b.total = total;
-    b.total_tiles = tiles;
-    b.total_pairs = pairs;
-    b.cap = total;
-    b.table = ptr<double>(c->b_table);
-    b.keys_in = ptr<unsigned long long>(c->b_keys);
-    b.keys_out = b.keys_in + total;
-    b.vals_in = ptr<unsigned>(c->b_vals);
-    b.vals_out = b.vals_in + total;
-    b.orig = b.vals_in + 2 * total;
-    b.sort_temp = c->b_sort_temp.p;
-    b.sort_temp_bytes = c->b_sort_temp.bytes;
-    b.boxes = ptr<hbt::Box>(c->b_boxes);
-    b.items = ptr<hbt::Item>(c->b_items);
-    b.same_cap = (unsigned)same_pairs;
-    b.mixed_cap = (unsigned)mixed_pairs;
-    b.n_items = ptr<unsigned>(c->b_counters);
-    b.item_next = b.n_items + 2;
-    b.p_extent = 1024 * 0.02 / 2;
-    b.inv_cell_pt = 1.0 / 0.02;
-    b.y_extent = 1024 * 0.05 / 2;
-    b.inv_cell_y = 1.0 / 0.05;
+// Sort, cull and bin fast jobs of this analysis in one persistent launch.
+hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs) {
     const double Q = std::max(std::fabs(c->d.g.q_lo), std::fabs(c->d.g.q_hi));
-    b.qt2_max = 2.0 * Q * Q * (1.0 + 1e-6) + 1e-300;
-    b.ql_max = Q * (1.0 + 1e-6) + 1e-300;
-    b.boost = c->d.g.boost;
-    CU(hbt::run_batch(c->d, b, c->persistent_grid, (unsigned)c->d.merge_chunk_blocks,
-                      c->stream));
+    for (FastJob &j : jobs) {
+        j.dev = 0;
+        j.q_window = Q;
+        j.boost = c->d.g.boost;
+    }
+    std::string err;
+    if (!c->runner.run(jobs, c->d, nullptr, 0, c->persistent_grid,
+                       (unsigned)c->d.merge_chunk_blocks, c->stream, err))
+        return fail(c, HBT_ERR_CUDA, err);
     c->st.launches += 6;
     return HBT_OK;
 }
@@ -628,9 +534,7 @@ void hbt_destroy(hbt_ctx *c) {
     DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
-                      &c->apply_iphi, &c->in, &c->part, &c->comp, &c->b_lists,
-                      &c->b_jobs, &c->b_offs, &c->b_table, &c->b_keys, &c->b_vals,
-                      &c->b_sort_temp, &c->b_boxes, &c->b_items, &c->b_counters};
+                      &c->apply_iphi, &c->in, &c->part, &c->comp};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->staged) cudaEventDestroy(c->staged);
@@ -915,3 +819,33 @@ hbt_status hbt_get_stats(hbt_ctx *c, hbt_stats *out) {
 }
 
 }  // extern "C"
+
+// Library-internal accessors (hbt_internal.h) for the serving loop.
+namespace hbt {
+
+const Device &ctx_device(const hbt_ctx *c) { return c->d; }
+
+int ctx_persistent_grid(const hbt_ctx *c) { return c->persistent_grid; }
+
+void ctx_add_pairs(hbt_ctx *c, u64 same, u64 mixed) {
+    c->st.pairs_same += same;
+    c->st.pairs_mixed += mixed;
+    c->ub[0] += same;
+    c->ub[1] += mixed;
+}
+
+cudaError_t ctx_merge(hbt_ctx *c, cudaStream_t st) {
+    if (c->d.precision != HBT_PRECISION_FP32W) return cudaSuccess;
+    return launch_merge(c->d, st);
+}
+
+size_t ctx_device_bytes(const hbt_params &p) {
+    const size_t slots = (size_t)p.n_KT * (p.azimuthal_flag == 1 ? p.n_Kphi : 1);
+    const size_t nb = slots * p.qnpts * p.qnpts * p.qnpts, nq = (size_t)p.n_KT * p.qnpts;
+    size_t bytes = nb * (sizeof(Sums) + 2 * sizeof(u64)) + nq * (sizeof(QiSums) + 2 * sizeof(u64)) +
+                   kDeferCap * sizeof(Deferral) + 4096;
+    if (p.precision == HBT_PRECISION_FP32W) bytes += nb * (sizeof(float4) + sizeof(Sums));
+    return bytes;
+}
+
+}  // namespace hbt

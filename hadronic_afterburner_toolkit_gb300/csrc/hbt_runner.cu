@@ -1,0 +1,149 @@
+// BatchRunner: device tables and scratch of the batched pair binning.
+#include "hbt_runner.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace hbt {
+
+BatchRunner::~BatchRunner() {
+    Buf *all[] = {&lists_, &jobs_, &offs_, &table_, &keys_, &vals_, &sort_temp_, &boxes_,
+                  &items_, &counters_};
+    for (Buf *b : all)
+        if (b->p) cudaFree(b->p);
+}
+
+bool BatchRunner::grow(Buf &b, size_t bytes, std::string &err) {
+    if (b.p && b.bytes >= bytes) return true;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (bytes == 0) return true;
+    // a little headroom so slowly growing batches do not reallocate each time
+    const size_t want = bytes + bytes / 8;
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+        err = "cudaMalloc of batch scratch failed";
+        b.p = nullptr;
+        return false;
+    }
+    b.bytes = want;
+    return true;
+}
+
+bool BatchRunner::run(const std::vector<FastJob> &jobs, const Device &d, const Device *devs,
+                      int n_devs, int grid, unsigned chunk, cudaStream_t st, std::string &err) {
+    std::vector<BatchList> lists;
+    std::vector<BatchJob> bj;
+    std::vector<long long> list_off, tile_off, pair_off;
+    long long total = 0, tiles = 0, pairs = 0, same_pairs = 0, mixed_pairs = 0;
+    auto add_list = [&](const double *const *src, int ncols, long long n) {
+        BatchList l = {};
+        for (int f = 0; f < 8; f++) l.src[f] = f < ncols ? src[f] : nullptr;
+        l.n = n;
+        l.off = total;
+        l.tiles = (n + 127) / 128;
+        l.tile_off = tiles;
+        l.ncols = ncols;
+        list_off.push_back(total);
+        tile_off.push_back(tiles);
+        total += n;
+        tiles += l.tiles;
+        lists.push_back(l);
+        return (int)lists.size() - 1;
+    };
+    for (const FastJob &j : jobs) {
+        BatchJob b = {};
+        b.kind = j.kind;
+        if (j.kind == 0) {
+            if (j.na < 2) continue;
+            b.la = b.lb = add_list(j.a, 8, j.na);
+            const long long t = lists[b.la].tiles;
+            b.n_pairs = t * (t + 1) / 2;
+            same_pairs += b.n_pairs;
+        } else {
+            if (j.na < 1 || j.nb < 1) continue;
+            b.la = add_list(j.a, 4, j.na);
+            b.lb = add_list(j.b, 4, j.nb);
+            b.n_pairs = lists[b.la].tiles * lists[b.lb].tiles;
+            mixed_pairs += b.n_pairs;
+        }
+        b.pair_off = pairs;
+        b.dev = j.dev;
+        b.qt2_max = 2.0 * j.q_window * j.q_window * (1.0 + 1e-6) + 1e-300;
+        b.ql_max = j.q_window * (1.0 + 1e-6) + 1e-300;
+        b.boost = j.boost;
+        pair_off.push_back(pairs);
+        pairs += b.n_pairs;
+        bj.push_back(b);
+    }
+    last_pairs_ = pairs;
+    if (bj.empty()) return true;
+    if (same_pairs > 0xffffffffLL || mixed_pairs > 0xffffffffLL || total > 0x7fffffffLL) {
+        err = "batch too large (tile pairs or particles)";
+        return false;
+    }
+    const size_t sort_bytes = batch_sort_temp_bytes(total);
+    if (!grow(lists_, lists.size() * sizeof(BatchList), err) ||
+        !grow(jobs_, bj.size() * sizeof(BatchJob), err) ||
+        !grow(offs_, (2 * lists.size() + bj.size()) * sizeof(long long), err) ||
+        !grow(table_, (size_t)8 * total * sizeof(double), err) ||
+        !grow(keys_, (size_t)2 * total * sizeof(unsigned long long), err) ||
+        !grow(vals_, (size_t)3 * total * sizeof(unsigned), err) ||
+        !grow(sort_temp_, sort_bytes, err) || !grow(boxes_, (size_t)tiles * sizeof(Box), err) ||
+        !grow(items_, (size_t)pairs * sizeof(Item), err) ||
+        !grow(counters_, 4 * sizeof(unsigned), err))
+        return false;
+    std::vector<long long> offs(list_off);
+    offs.insert(offs.end(), tile_off.begin(), tile_off.end());
+    offs.insert(offs.end(), pair_off.begin(), pair_off.end());
+    if (cudaMemcpyAsync(lists_.p, lists.data(), lists.size() * sizeof(BatchList),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(jobs_.p, bj.data(), bj.size() * sizeof(BatchJob), cudaMemcpyHostToDevice,
+                        st) != cudaSuccess ||
+        cudaMemcpyAsync(offs_.p, offs.data(), offs.size() * sizeof(long long),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        err = "uploading the batch tables failed";
+        return false;
+    }
+    BatchDev b = {};
+    const long long *o = static_cast<const long long *>(offs_.p);
+    b.lists = static_cast<const BatchList *>(lists_.p);
+    b.jobs = static_cast<const BatchJob *>(jobs_.p);
+    b.list_off = o;
+    b.tile_off = o + lists.size();
+    b.pair_off = o + 2 * lists.size();
+    b.n_lists = (int)lists.size();
+    b.n_jobs = (int)bj.size();
+    b.total = total;
+    b.total_tiles = tiles;
+    b.total_pairs = pairs;
+    b.cap = total;
+    b.table = static_cast<double *>(table_.p);
+    b.keys_in = static_cast<unsigned long long *>(keys_.p);
+    b.keys_out = b.keys_in + total;
+    b.vals_in = static_cast<unsigned *>(vals_.p);
+    b.vals_out = b.vals_in + total;
+    b.orig = b.vals_in + 2 * total;
+    b.sort_temp = sort_temp_.p;
+    b.sort_temp_bytes = sort_temp_.bytes;
+    b.boxes = static_cast<Box *>(boxes_.p);
+    b.items = static_cast<Item *>(items_.p);
+    b.same_cap = (unsigned)same_pairs;
+    b.mixed_cap = (unsigned)mixed_pairs;
+    b.n_items = static_cast<unsigned *>(counters_.p);
+    b.item_next = b.n_items + 2;
+    b.p_extent = 1024 * 0.02 / 2;
+    b.inv_cell_pt = 1.0 / 0.02;
+    b.y_extent = 1024 * 0.05 / 2;
+    b.inv_cell_y = 1.0 / 0.05;
+    b.devs = devs;
+    b.n_devs = n_devs;
+    const cudaError_t e = run_batch(d, b, grid, chunk, st);
+    if (e != cudaSuccess) {
+        err = std::string("batch launch failed: ") + cudaGetErrorString(e);
+        return false;
+    }
+    return true;
+}
+
+}  // namespace hbt
