@@ -41,6 +41,7 @@ GPU_UNITS = {
     "hbt_noalloc.cu": ["--fmad=false"],
     "hbt_batch.cu": ["--fmad=false"],
     "hbt_runner.cu": [],
+    "hbt_server.cu": ["--fmad=false"],
 }
 
 

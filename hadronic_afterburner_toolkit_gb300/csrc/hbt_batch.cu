@@ -287,7 +287,7 @@ size_t batch_sort_temp_bytes(long long cap) {
 }
 
 cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
-                      cudaStream_t st) {
+                      const Device *host_devs, int n_host_devs, cudaStream_t st) {
     cudaError_t e;
     const int gs = 152 * 8;
     if (b.total > 0) {
@@ -336,6 +336,9 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
         if (e != cudaSuccess) return e;
         if (prec && !b.devs) {
             if ((e = launch_merge(d, st)) != cudaSuccess) return e;
+        } else if (prec) {
+            for (int k = 0; k < n_host_devs; k++)
+                if ((e = launch_merge(host_devs[k], st)) != cudaSuccess) return e;
         }
     }
     // mixed-event items

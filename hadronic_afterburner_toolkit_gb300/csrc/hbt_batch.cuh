@@ -79,8 +79,9 @@ int persistent_blocks_per_sm();
 size_t batch_sort_temp_bytes(long long cap);
 // Sort, box, cull and bin one batch.  chunk > 0 splits the FP32-weight
 // form's same-event queue into chunks of that many items with a merge of
-// the FP32 partials after each.
+// the FP32 partials after each: of `d` for a one-analysis batch, of every
+// host_devs[k] (the host copies of b.devs) for a batch of many analyses.
 cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
-                      cudaStream_t st);
+                      const Device *host_devs, int n_host_devs, cudaStream_t st);
 
 }  // namespace hbt

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -40,6 +41,9 @@ struct hbt_ctx {
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
     cudaEvent_t staged = nullptr;
+    // stream-ordered allocation from this pool on `own` (serving loop
+    // contexts); nullptr: cudaMalloc / cudaFree
+    cudaMemPool_t pool = nullptr;
     hbt::Device d;
     u64 cap = 0, cap_qinv = 0;
     int n_stream = 0;  // 3-D slots + q_inv K_T bins
@@ -81,14 +85,27 @@ hbt_status fail(hbt_ctx *c, hbt_status s, const std::string &msg) {
         if (s_ != HBT_OK) return s_;       \
     } while (0)
 
-hbt_status dalloc(hbt_ctx *c, DevBuf &b, size_t bytes) {
-    if (b.bytes >= bytes && b.p) return HBT_OK;
-    if (b.p) cudaFree(b.p);
+void dfree(hbt_ctx *c, DevBuf &b) {
+    if (b.p) {
+        if (c->pool)
+            cudaFreeAsync(b.p, c->own);
+        else
+            cudaFree(b.p);
+    }
     b.p = nullptr;
     b.bytes = 0;
+}
+
+hbt_status dalloc(hbt_ctx *c, DevBuf &b, size_t bytes) {
+    if (b.bytes >= bytes && b.p) return HBT_OK;
+    dfree(c, b);
     if (bytes == 0) return HBT_OK;
-    cudaError_t e = cudaMalloc(&b.p, bytes);
-    if (e != cudaSuccess) return fail(c, HBT_ERR_NOMEM, "cudaMalloc failed");
+    cudaError_t e = c->pool ? cudaMallocFromPoolAsync(&b.p, bytes, c->pool, c->own)
+                            : cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return fail(c, HBT_ERR_NOMEM, "device allocation failed");
+    }
     b.bytes = bytes;
     return HBT_OK;
 }
@@ -335,8 +352,8 @@ hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs) {
         j.boost = c->d.g.boost;
     }
     std::string err;
-    if (!c->runner.run(jobs, c->d, nullptr, 0, c->persistent_grid,
-                       (unsigned)c->d.merge_chunk_blocks, c->stream, err))
+    if (!c->runner.run(jobs, c->d, c->persistent_grid, (unsigned)c->d.merge_chunk_blocks,
+                       c->stream, err))
         return fail(c, HBT_ERR_CUDA, err);
     c->st.launches += 6;
     return HBT_OK;
@@ -440,21 +457,43 @@ hbt_status stage(hbt_ctx *c, const double *const *src, const long long *len, int
 
 }  // namespace
 
+namespace hbt {
+
+bool params_valid(const hbt_params &p) {
+    if (p.qnpts < 2 || p.n_KT < 2 || p.n_Kphi < 1 || p.qnpts > 1024) return false;
+    if (p.precision != HBT_PRECISION_FP64 && p.precision != HBT_PRECISION_FP32W) return false;
+    if (p.kernel != HBT_KERNEL_SCREENED && p.kernel != HBT_KERNEL_REFERENCE_CHAIN &&
+        p.kernel != HBT_KERNEL_SCREENED_GRID)
+        return false;
+    return true;
+}
+
+}  // namespace hbt
+
 extern "C" {
 
 hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
+    return hbt::ctx_create(p, device, nullptr, out);
+}
+
+}  // extern "C"
+
+namespace hbt {
+
+hbt_status ctx_create(const hbt_params *p, int device, cudaMemPool_t pool, hbt_ctx **out) {
     hbt_ctx *c = nullptr;
     if (!p || !out) return HBT_ERR_INVALID;
     *out = nullptr;
-    if (p->qnpts < 2 || p->n_KT < 2 || p->n_Kphi < 1 || p->qnpts > 1024)
-        return HBT_ERR_INVALID;
-    if (p->precision != HBT_PRECISION_FP64 && p->precision != HBT_PRECISION_FP32W)
-        return HBT_ERR_INVALID;
+    if (!hbt::params_valid(*p)) return HBT_ERR_INVALID;
     c = new hbt_ctx();
     c->prm = *p;
     c->device = device;
-    CU(cudaSetDevice(device));
-    CU(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking));
+    c->pool = pool;
+    // a failure below leaves c to hbt_destroy
+    std::unique_ptr<hbt_ctx, void (*)(hbt_ctx *)> guard(c, hbt_destroy);
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess)
+        return HBT_ERR_CUDA;
     c->stream = c->own;
     CU(cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming));
 
@@ -481,11 +520,6 @@ hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
     g.psi_ref = 0.0;
     g.kphi_tol = p->kphi_defer_tol > 0 ? p->kphi_defer_tol : 1e-13;
     g.hbarC_inv = 1. / kHbarC;
-    if (p->kernel != HBT_KERNEL_SCREENED && p->kernel != HBT_KERNEL_REFERENCE_CHAIN &&
-        p->kernel != HBT_KERNEL_SCREENED_GRID) {
-        hbt_destroy(c);
-        return HBT_ERR_INVALID;
-    }
     fill_screen(c);
     c->cap = static_cast<u64>(p->needed_number_of_pairs);
     c->cap_qinv = 50 * c->cap;
@@ -513,19 +547,17 @@ hbt_status hbt_create(const hbt_params *p, int device, hbt_ctx **out) {
         (s = dalloc(c, c->n_defer, sizeof(unsigned))) != HBT_OK ||
         (p->precision == HBT_PRECISION_FP32W &&
          ((s = dalloc(c, c->part, nb * sizeof(float4))) != HBT_OK ||
-          (s = dalloc(c, c->comp, nb * sizeof(hbt::Sums))) != HBT_OK))) {
-        hbt_destroy(c);
+          (s = dalloc(c, c->comp, nb * sizeof(hbt::Sums))) != HBT_OK)))
         return s;
-    }
     refresh_device(c);
-    s = hbt_reset(c);
-    if (s != HBT_OK) {
-        hbt_destroy(c);
-        return s;
-    }
-    *out = c;
+    if ((s = hbt_reset(c)) != HBT_OK) return s;
+    *out = guard.release();
     return HBT_OK;
 }
+
+}  // namespace hbt
+
+extern "C" {
 
 void hbt_destroy(hbt_ctx *c) {
     if (!c) return;
@@ -535,8 +567,7 @@ void hbt_destroy(hbt_ctx *c) {
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
                       &c->apply_iphi, &c->in, &c->part, &c->comp};
-    for (DevBuf *b : bufs)
-        if (b->p) cudaFree(b->p);
+    for (DevBuf *b : bufs) dfree(c, *b);
     if (c->staged) cudaEventDestroy(c->staged);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
@@ -827,6 +858,8 @@ const Device &ctx_device(const hbt_ctx *c) { return c->d; }
 
 int ctx_persistent_grid(const hbt_ctx *c) { return c->persistent_grid; }
 
+cudaStream_t ctx_stream(const hbt_ctx *c) { return c->own; }
+
 void ctx_add_pairs(hbt_ctx *c, u64 same, u64 mixed) {
     c->st.pairs_same += same;
     c->st.pairs_mixed += mixed;
@@ -847,5 +880,9 @@ size_t ctx_device_bytes(const hbt_params &p) {
     if (p.precision == HBT_PRECISION_FP32W) bytes += nb * (sizeof(float4) + sizeof(Sums));
     return bytes;
 }
+
+bool ctx_batchable(const hbt_ctx *c) { return batched_ok(c); }
+
+bool ctx_caps_may_bind(const hbt_ctx *c, int mixed, u64 P) { return caps_may_bind(c, mixed, P); }
 
 }  // namespace hbt

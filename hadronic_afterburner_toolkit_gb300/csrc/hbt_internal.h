@@ -8,6 +8,15 @@
 
 namespace hbt {
 
+// hbt_create's parameter checks.
+bool params_valid(const hbt_params &p);
+// hbt_create with the context's device memory taken, stream-ordered on its
+// own stream, from `pool` (nullptr: cudaMalloc), so that creating and
+// destroying contexts does not synchronise the device.
+hbt_status ctx_create(const hbt_params *p, int device, cudaMemPool_t pool, hbt_ctx **out);
+// The context's own stream.
+cudaStream_t ctx_stream(const hbt_ctx *c);
+
 // The context's engine descriptor (grid, screen constants, histograms).
 const Device &ctx_device(const hbt_ctx *c);
 // Persistent-kernel grid for the context's device.
@@ -19,5 +28,11 @@ void ctx_add_pairs(hbt_ctx *c, u64 same, u64 mixed);
 cudaError_t ctx_merge(hbt_ctx *c, cudaStream_t st);
 // Device bytes hbt_create allocates for these parameters.
 size_t ctx_device_bytes(const hbt_params &p);
+// True when the context's fast pairs can go to the batched persistent
+// kernels (screened kernel family, no q_inv histograms).
+bool ctx_batchable(const hbt_ctx *c);
+// True when a needed_number_of_pairs cap could reject one of P more pairs
+// (mixed = 0: numerator families, 1: denominator families).
+bool ctx_caps_may_bind(const hbt_ctx *c, int mixed, u64 P);
 
 }  // namespace hbt

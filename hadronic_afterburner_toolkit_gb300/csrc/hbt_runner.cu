@@ -8,7 +8,7 @@ namespace hbt {
 
 BatchRunner::~BatchRunner() {
     Buf *all[] = {&lists_, &jobs_, &offs_, &table_, &keys_, &vals_, &sort_temp_, &boxes_,
-                  &items_, &counters_};
+                  &items_, &counters_, &devs_};
     for (Buf *b : all)
         if (b->p) cudaFree(b->p);
 }
@@ -30,8 +30,41 @@ bool BatchRunner::grow(Buf &b, size_t bytes, std::string &err) {
     return true;
 }
 
-bool BatchRunner::run(const std::vector<FastJob> &jobs, const Device &d, const Device *devs,
-                      int n_devs, int grid, unsigned chunk, cudaStream_t st, std::string &err) {
+bool BatchRunner::run(const std::vector<FastJob> &jobs, const Device &d, int grid,
+                      unsigned chunk, cudaStream_t st, std::string &err) {
+    return run_impl(jobs, d, nullptr, nullptr, 0, grid, chunk, st, err);
+}
+
+bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<Device> &devs,
+                            int grid, unsigned chunk, cudaStream_t st, std::string &err) {
+    if (devs.empty()) {
+        err = "no analyses in the batch";
+        return false;
+    }
+    for (const FastJob &j : jobs)
+        if (j.dev < 0 || j.dev >= (int)devs.size()) {
+            err = "job refers to a missing analysis";
+            return false;
+        }
+    for (const Device &x : devs)
+        if (x.g.azimuthal != devs[0].g.azimuthal || x.g.boost != devs[0].g.boost ||
+            x.precision != devs[0].precision) {
+            err = "analyses of one batch must share azimuthal_flag, boost and precision";
+            return false;
+        }
+    if (!grow(devs_, devs.size() * sizeof(Device), err)) return false;
+    if (cudaMemcpyAsync(devs_.p, devs.data(), devs.size() * sizeof(Device),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        err = "uploading the analysis descriptors failed";
+        return false;
+    }
+    return run_impl(jobs, devs[0], static_cast<const Device *>(devs_.p), devs.data(),
+                    (int)devs.size(), grid, chunk, st, err);
+}
+
+bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
+                           const Device *devs_dev, const Device *devs_host, int n_devs, int grid,
+                           unsigned chunk, cudaStream_t st, std::string &err) {
     std::vector<BatchList> lists;
     std::vector<BatchJob> bj;
     std::vector<long long> list_off, tile_off, pair_off;
@@ -136,9 +169,9 @@ bool BatchRunner::run(const std::vector<FastJob> &jobs, const Device &d, const D
     b.inv_cell_pt = 1.0 / 0.02;
     b.y_extent = 1024 * 0.05 / 2;
     b.inv_cell_y = 1.0 / 0.05;
-    b.devs = devs;
+    b.devs = devs_dev;
     b.n_devs = n_devs;
-    const cudaError_t e = run_batch(d, b, grid, chunk, st);
+    const cudaError_t e = run_batch(d, b, grid, chunk, devs_host, n_devs, st);
     if (e != cudaSuccess) {
         err = std::string("batch launch failed: ") + cudaGetErrorString(e);
         return false;

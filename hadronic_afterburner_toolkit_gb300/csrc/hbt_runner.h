@@ -31,13 +31,19 @@ class BatchRunner {
     BatchRunner(const BatchRunner &) = delete;
     BatchRunner &operator=(const BatchRunner &) = delete;
 
-    // Runs the jobs: with devs == nullptr every job uses `d` (one analysis;
-    // the FP32-weight partials are merged here); otherwise job.dev indexes
-    // the device array devs of n_devs descriptors and the caller merges.
-    // Returns false and sets `err` on failure.  Allocates scratch on first
-    // use and when a batch outgrows it.
-    bool run(const std::vector<FastJob> &jobs, const Device &d, const Device *devs, int n_devs,
-             int grid, unsigned chunk, cudaStream_t st, std::string &err);
+    // Runs the jobs of one analysis: every job bins into `d`.  Returns
+    // false and sets `err` on failure.  Allocates scratch on first use and
+    // when a batch outgrows it.
+    bool run(const std::vector<FastJob> &jobs, const Device &d, int grid, unsigned chunk,
+             cudaStream_t st, std::string &err);
+
+    // Runs jobs of several analyses in one launch: job.dev indexes `devs`,
+    // whose entries must share azimuthal_flag, long_comoving_boost and
+    // precision (they select the kernel).  The FP32-weight partials of
+    // every analysis are merged after each chunk of `chunk` same-event
+    // items and at the end.
+    bool run_multi(const std::vector<FastJob> &jobs, const std::vector<Device> &devs, int grid,
+                   unsigned chunk, cudaStream_t st, std::string &err);
 
     // Candidate and kept tile pairs of the last batch (kept read lazily).
     long long last_tile_pairs() const { return last_pairs_; }
@@ -48,7 +54,10 @@ class BatchRunner {
         size_t bytes = 0;
     };
     bool grow(Buf &b, size_t bytes, std::string &err);
-    Buf lists_, jobs_, offs_, table_, keys_, vals_, sort_temp_, boxes_, items_, counters_;
+    bool run_impl(const std::vector<FastJob> &jobs, const Device &d, const Device *devs_dev,
+                  const Device *devs_host, int n_devs, int grid, unsigned chunk, cudaStream_t st,
+                  std::string &err);
+    Buf lists_, jobs_, offs_, table_, keys_, vals_, sort_temp_, boxes_, items_, counters_, devs_;
     long long last_pairs_ = 0;
 };
 

@@ -8,8 +8,9 @@ import pytest
 
 from hadronic_afterburner_toolkit_gb300 import build, engine
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
-                      "include", "hbt_gpu.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+HEADER = os.path.join(INCLUDE, "hbt_gpu.h")
+SERVER_HEADER = os.path.join(INCLUDE, "hbt_server.h")
 
 
 def _declared_functions(path):
@@ -33,8 +34,29 @@ def test_header_declares_the_engine_api():
 
 
 def test_library_exports_every_declared_symbol(lib):
-    for name in _declared_functions(HEADER):
+    for name in _declared_functions(HEADER) + _declared_functions(SERVER_HEADER):
         assert hasattr(lib, name), name
+
+
+def test_server_header_matches_its_binding(lib):
+    from hadronic_afterburner_toolkit_gb300 import server
+    names = _declared_functions(SERVER_HEADER)
+    assert "hbt_server_submit" in names and "hbt_server_wait" in names
+    assert sorted(server.exported_symbols()) == names
+
+
+def test_server_create_reports_errors_without_crashing(lib):
+    """Without a GPU hbt_server_create returns HBT_ERR_CUDA; with one it
+    starts and stops cleanly."""
+    from hadronic_afterburner_toolkit_gb300 import server
+    L = server.load()
+    cfg = server.HbtServerConfig(device=0)
+    h = ctypes.c_void_p()
+    rc = L.hbt_server_create(ctypes.byref(cfg), ctypes.byref(h))
+    assert rc in (0, 2)
+    if rc == 0:
+        L.hbt_server_destroy(h)
+    assert L.hbt_server_last_error(None) == b"null server"
 
 
 def test_binding_loads_without_gpu(lib):
