@@ -1,7 +1,8 @@
 """Benchmark of the GB300 HBT pair-binning engine.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload central|small] [--precision fp64|fp32w]
+                    [--workload central|medium|small] [--precision fp64|fp32w]
+                    [--no-uneven] [--no-serving] [--serving-jobs J]
 
 Workload "central" (default): 1000 pi+ events, multiplicity Poisson(1500),
 emission source sigma_xy = 7 fm, tau0 = 12 fm/c, oversample factor 100
@@ -17,6 +18,17 @@ mixed-event pairs).  `value` times the device-resident entry points with
 CUDA events on the engine's stream; `e2e` times the host-buffer C-ABI calls
 (pinned host arrays copied in, histograms copied back every step) with the
 host clock.  The L2 is flushed (256 MB write) between timed steps.
+
+Two more legs are reported in the same JSON line.  "uneven": the
+uneven-multiplicity workload (4096 events, log-uniform multiplicity in
+[20, 3000], ~50k-particle groups, 10 partners, 41^3 grid, 4 K_T bins), all
+groups and partners in one batched launch per step, FP64 and FP32 weights,
+against the plain FP64 reference-chain kernel on a sample of groups.
+"serving": a Poisson stream of requests at 200 jobs/s (10-500 events each,
+mu in [50, 2000], pi+ or K+, qnpts in {21, 41, 61}, q_max in [0.1, 0.3] GeV,
+2-8 K_T bins; each event its own same-event list, one rotated partner per
+event) through the serving loop, with p50 / p99 request latency and pairs/s,
+against the plain per-job path.
 
 --impl reference times the reference algorithm on the host cores (the CPU
 oracle, multi-threaded) on a bounded sample of the same workload.
@@ -269,6 +281,182 @@ def run_reference(args) -> None:
     print(json.dumps(line))
 
 
+UNEVEN_PARAMS = dict(qnpts=41, q_min=-0.15, q_max=0.15, n_KT=5, KT_min=0.0, KT_max=1.0,
+                     n_Kphi=8, azimuthal_flag=0, invariant_radius_flag=0,
+                     long_comoving_boost=1, needed_number_of_pairs=1e18)
+
+
+def make_uneven(seed: int = 3, group_particles: int = 50_000, nmix: int = 10):
+    """The uneven-multiplicity workload: 4096 pi+ events with log-uniform
+    multiplicities in [20, 3000] (sigma_xy = 1.2 N^(1/3) fm), oversample
+    groups of ~50k particles, 10 rotated partners per event drawn inside
+    its group.  Returns the groups in make_workload's layout."""
+    from hadronic_afterburner_toolkit_gb300 import synth
+    ev = synth.uneven_pions(seed=seed)
+    rng = np.random.default_rng(seed + 1000)
+    groups = []
+    for (a, b) in synth.buffers(ev, group_particles):
+        g = synth.subset(ev, a, b)
+        cols = [np.ascontiguousarray(getattr(g, k)) for k in
+                ("px", "py", "pz", "E", "x", "y", "z", "t")]
+        mixed = []
+        for e in range(g.n_events):
+            lo, hi = g.offsets[e], g.offsets[e + 1]
+            ms = [int(m) for m in rng.integers(0, g.n_events, size=nmix)]
+            ms = [(m + 1) % g.n_events if (m == e and g.n_events > 1) else m for m in ms]
+            phis = rng.uniform(0, 2 * np.pi, size=nmix)
+            parts = []
+            for m, phi in zip(ms, phis):
+                c, s = np.cos(phi), np.sin(phi)
+                mlo, mhi = g.offsets[m], g.offsets[m + 1]
+                px, py = cols[0][mlo:mhi], cols[1][mlo:mhi]
+                parts.append((px * c - py * s, px * s + py * c, cols[2][mlo:mhi],
+                              cols[3][mlo:mhi]))
+            l1 = [c[lo:hi] for c in cols[:4]]
+            l2 = [np.concatenate([pp[f] for pp in parts]) for f in range(4)]
+            mixed.append((l1, l2))
+        groups.append((cols, mixed))
+    return groups
+
+
+def uneven_leg(E, torch, dev, stream, flush, local, steps=2) -> dict:
+    """All groups and partners of the uneven workload in one batched
+    persistent launch per step (FP64 and FP32 weights), against the plain
+    FP64 reference-chain kernel called list by list on a sample of groups."""
+    groups = make_uneven()
+    dgroups = [([torch.from_numpy(c).to(dev) for c in cols],
+                [([torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in l1],
+                  [torch.from_numpy(x).to(dev) for x in l2]) for l1, l2 in mixed])
+               for cols, mixed in groups]
+    total_pairs = sum(group_pairs(g) for g in groups)
+    jobs = []
+    for dc, dm in dgroups:
+        jobs.append(("same", dc))
+        jobs += [("mixed", l1, l2) for l1, l2 in dm]
+
+    def timed(fn, n):
+        ms = []
+        for k in range(n):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    out = {"events": 4096, "groups": len(groups), "group_particles": "~50k",
+           "mixed_partners": 10, "pairs_per_step": total_pairs, "qnpts": 41, "n_KT_bins": 4}
+    for label, prec in (("batched-fp64", E.PRECISION_FP64), ("batched-fp32w", E.PRECISION_FP32W)):
+        eng = E.Engine(device=local, precision=prec, kernel=E.KERNEL_SCREENED, **UNEVEN_PARAMS)
+        eng.set_stream(stream.cuda_stream)
+        timed(lambda: eng.bin_batch(jobs, device=True), 1)  # warm-up
+        ms = timed(lambda: eng.bin_batch(jobs, device=True), steps)
+        out[label] = {"value": total_pairs / (statistics.median(ms) * 1e-3), "unit": "pairs/s",
+                      "ms_per_step": statistics.median(ms), "steps": steps,
+                      "jobs_per_launch": len(jobs)}
+        eng.close()
+    # plain: the reference chain on every pair, one call per list, on the
+    # first groups (about 3e9 pairs)
+    eng = E.Engine(device=local, precision=E.PRECISION_FP64, kernel=E.KERNEL_REFERENCE_CHAIN,
+                   **UNEVEN_PARAMS)
+    eng.set_stream(stream.cuda_stream)
+    n_sample, acc = 0, 0
+    for g in groups:
+        if acc >= 3e9:
+            break
+        acc += group_pairs(g)
+        n_sample += 1
+
+    def plain_run():
+        for dc, dm in dgroups[:n_sample]:
+            eng.bin_same(dc, device=True)
+            for l1, l2 in dm:
+                eng.bin_mixed(l1, l2, device=True)
+
+    timed(lambda: eng.bin_same(dgroups[0][0], device=True), 1)
+    ms = timed(plain_run, 1)
+    out["plain-fp64"] = {"value": acc / (ms[0] * 1e-3), "unit": "pairs/s",
+                         "sample": "%d of %d groups (%.3g pairs)" % (n_sample, len(groups), acc),
+                         "kernel": "reference chain, one launch per list"}
+    eng.close()
+    for k in ("batched-fp64", "batched-fp32w"):
+        out[k]["speedup_vs_plain"] = out[k]["value"] / out["plain-fp64"]["value"]
+    return out
+
+
+def make_requests(n_jobs: int, seed: int = 5):
+    """Requests of the serving workload: 10-500 events each, multiplicity
+    Poisson(mu) with mu uniform in [50, 2000], pi+ or K+, qnpts in
+    {21, 41, 61} on [-q_max, q_max] with q_max uniform in [0.1, 0.3] GeV,
+    2-8 K_T bins on [0, 1] GeV."""
+    from hadronic_afterburner_toolkit_gb300 import synth
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(n_jobs):
+        nev = int(rng.integers(10, 501))
+        mu = float(rng.uniform(50, 2000))
+        kaon = bool(rng.random() < 0.5)
+        qnpts = int(rng.choice([21, 41, 61]))
+        qmax = float(rng.uniform(0.1, 0.3))
+        nkt = int(rng.integers(2, 9)) + 1
+        kw = dict(mass=synth.KAON_MASS, monval=321, T=0.30) if kaon else {}
+        ev = synth.generate(nev, mu, seed=seed * 100_000 + k, sigma_xy=5.0, tau_mean=10.0, **kw)
+        cols = [np.ascontiguousarray(getattr(ev, f)) for f in
+                ("px", "py", "pz", "E", "x", "y", "z", "t")]
+        prm = dict(qnpts=qnpts, q_min=-qmax, q_max=qmax, n_KT=nkt, KT_min=0.0, KT_max=1.0,
+                   n_Kphi=8, azimuthal_flag=0, invariant_radius_flag=0, long_comoving_boost=1,
+                   needed_number_of_pairs=1e18)
+        reqs.append((cols, np.ascontiguousarray(ev.offsets, dtype=np.int64), prm, k + 1))
+    return reqs
+
+
+def serving_leg(E, local, n_jobs=48, rate=200.0, seed=5) -> dict:
+    """A Poisson request stream at `rate` jobs/s through the serving loop:
+    continuous batching (FP64 and FP32 weights) against the plain per-job
+    path (reference-chain kernel, one request at a time, list by list)."""
+    from hadronic_afterburner_toolkit_gb300 import server
+    reqs = make_requests(n_jobs, seed)
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_jobs))
+
+    def stream_run(precision, kernel):
+        with server.Server(device=local) as srv:
+            ids = []
+            t0 = time.perf_counter()
+            for (cols, off, prm, sd), t in zip(reqs, arrivals):
+                now = time.perf_counter() - t0
+                if t > now:
+                    time.sleep(t - now)
+                ids.append(srv.submit(cols, off, dict(prm, precision=precision, kernel=kernel),
+                                      oversample=1, mixed_partners=1, seed=sd))
+            for j in ids:
+                srv.wait(j)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+            infos = [srv.info(j) for j in ids]
+        pairs = sum(i["pairs_same"] + i["pairs_mixed"] for i in infos)
+        return {"pairs_per_s": pairs / wall, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                "mean_ms": st["mean_ms"], "max_ms": st["max_ms"], "wall_s": wall,
+                "rounds": st["rounds"], "peak_active": st["peak_active"],
+                "peak_device_bytes": st["peak_bytes"], "gpu_busy_ms": st["gpu_busy_ms"],
+                "pairs": pairs}
+
+    out = {"jobs": n_jobs, "rate_jobs_per_s": rate, "oversample": 1, "mixed_partners": 1,
+           "arrival_span_s": float(arrivals[-1])}
+    out["batched-fp64"] = stream_run(E.PRECISION_FP64, E.KERNEL_SCREENED)
+    out["batched-fp32w"] = stream_run(E.PRECISION_FP32W, E.KERNEL_SCREENED)
+    out["plain-per-job-fp64"] = stream_run(E.PRECISION_FP64, E.KERNEL_REFERENCE_CHAIN)
+    out["offered_pairs_per_s"] = out["batched-fp64"]["pairs"] / float(arrivals[-1])
+    for k in ("batched-fp64", "batched-fp32w"):
+        out[k]["speedup_vs_plain"] = (out[k]["pairs_per_s"] /
+                                      out["plain-per-job-fp64"]["pairs_per_s"])
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -282,6 +470,11 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the one-step measurement of the plain reference-chain kernel")
+    ap.add_argument("--no-uneven", action="store_true",
+                    help="skip the uneven-multiplicity workload (one batched launch)")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the Poisson request stream through the serving loop")
+    ap.add_argument("--serving-jobs", type=int, default=48)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -464,6 +657,12 @@ def main() -> None:
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(groups[0], p, nthreads=1)
 
+    uneven = serving = None
+    if not args.no_uneven:
+        uneven = uneven_leg(E, torch, dev, stream, flush, local)
+    if not args.no_serving:
+        serving = serving_leg(E, local, n_jobs=args.serving_jobs)
+
     if rank == 0:
         st = eng.stats()
         line = {"metric": "candidate pairs binned per second (same + mixed event)",
@@ -492,6 +691,8 @@ def main() -> None:
                                      if plain else None) for k, v in variants.items()},
                 "e2e": e2e,
                 "cpu_baseline": cpu,
+                "uneven": uneven,
+                "serving": serving,
                 "stats": st}
         print(json.dumps(line))
     eng.close()
