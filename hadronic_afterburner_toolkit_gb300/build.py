@@ -86,7 +86,8 @@ def build_gpu(force: bool = False, verbose: bool = False) -> str:
         for unit, extra in GPU_UNITS.items():
             obj = os.path.join(OBJ, unit.replace(".cu", ".o"))
             objs.append(obj)
-            cmd = [nvcc] + NVCC_COMMON + extra + ["-Xptxas", "-v", "-c",
+            defines = os.environ.get("HBT_NVCC_DEFINES", "").split()
+            cmd = [nvcc] + NVCC_COMMON + extra + defines + ["-Xptxas", "-v", "-c",
                                                   os.path.join(CSRC, unit), "-o", obj]
             jobs.append(ex.submit(_run, cmd))
         logs = [j.result() for j in jobs]

@@ -203,11 +203,16 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
 
 // Same-event items [base, min(end, queued)) pulled by persistent CTAs.
 template <bool AZ, bool BOOST, int PREC>
-__global__ void __launch_bounds__(FT, 5) k_persistent_same(Device d, BatchDev b, unsigned base,
+#ifndef HBT_SAME_CTAS_PER_SM
+#define HBT_SAME_CTAS_PER_SM 5
+#endif
+__global__ void __launch_bounds__(FT, HBT_SAME_CTAS_PER_SM) k_persistent_same(Device d, BatchDev b, unsigned base,
                                                            unsigned end) {
     __shared__ TileSmem sm;
     __shared__ Device dsm;
     __shared__ unsigned item;
+    __shared__ double2 cs[COS_TABLE];
+    if (PREC == 0) fill_cos_table(cs);
     const unsigned stop = min(end, min(b.n_items[0], b.same_cap));
     for (;;) {
         if (threadIdx.x == 0) item = base + atomicAdd(b.item_next, 1u);
@@ -221,7 +226,7 @@ __global__ void __launch_bounds__(FT, 5) k_persistent_same(Device d, BatchDev b,
         const double *c[8];
 #pragma unroll
         for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
-        same_tile_pair<AZ, BOOST, PREC>(dd, sm, c, b.orig + la.off, la.n, (long long)it.ti * FT,
+        same_tile_pair<AZ, BOOST, PREC>(dd, sm, cs, c, b.orig + la.off, la.n, (long long)it.ti * FT,
                                         (long long)it.tj * FT);
         __syncthreads();
     }

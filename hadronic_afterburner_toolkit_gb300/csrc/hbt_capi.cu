@@ -330,11 +330,12 @@ void fill_screen(hbt_ctx *c) {
     s.qnpts = g.qnpts;
     s.n_KT = g.n_KT;
     s.n_Kphi = g.n_Kphi;
+    hbt::fill_prefilter(s);
 }
 
 bool screened_ok(const hbt_ctx *c) {
     return (c->prm.kernel == HBT_KERNEL_SCREENED || c->prm.kernel == HBT_KERNEL_SCREENED_GRID) &&
-           !c->d.g.qinv && c->d.g.n_KT <= 255 && c->d.g.qnpts <= 1024;
+           !c->d.g.qinv && c->d.g.n_KT <= 255 && c->d.g.qnpts <= 1024 && c->d.g.n_slots < 16384;
 }
 
 bool batched_ok(const hbt_ctx *c) {

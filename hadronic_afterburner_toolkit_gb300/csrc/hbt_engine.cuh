@@ -90,7 +90,22 @@ struct Screen {
     float KT_min, inv_dKT, kt_t_slack;
     float psi, psi_slack, two_pi, inv_dKphi;
     int qnpts, n_KT, n_Kphi;
+    // prefilter (hbt_tile.cuh prefilter()): Q = max(-lo, hi) + win_slack
+    // with margin, Q^2, 2 Q^2 and the coefficient of the input-rounding term
+    // of the q_T test
+    float pq, pq2, pqt2, pqt_c;
 };
+
+// Host: the prefilter constants of a screen whose window is filled in.
+inline void fill_prefilter(Screen &s) {
+    const double U = 5.9604644775390625e-8;  // 2^-24
+    const double Q = ((double)(-s.lo > s.hi ? -s.lo : s.hi) + (double)s.win_slack) * (1.0 + 1e-6);
+    s.pq = (float)(Q * (1.0 + 1e-5));
+    s.pq2 = (float)(Q * Q * (1.0 + 2e-4));
+    s.pqt2 = (float)(2.0 * Q * Q * (1.0 + 2e-4));
+    // (c + e)^2 <= c^2 + 2 c e (1 + 1e-4), c = sqrt(2) Q, e = 2.01 u L
+    s.pqt_c = (float)(2.0 * 1.4142135623730951 * Q * 2.01 * U * (1.0 + 2e-4));
+}
 
 struct Device {
     Grid g;

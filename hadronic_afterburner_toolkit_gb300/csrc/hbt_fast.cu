@@ -17,9 +17,11 @@ using namespace tile;
 template <bool AZ, bool BOOST, int PREC>
 __global__ void __launch_bounds__(FT) k_same_screened(Device d, long long n, Cols8 c) {
     __shared__ TileSmem sm;
+    __shared__ double2 cs[COS_TABLE];
+    if (PREC == 0) fill_cos_table(cs);
     long long ti, tj;
     tri_tile((long long)blockIdx.x + d.block_offset, ti, tj);
-    same_tile_pair<AZ, BOOST, PREC>(d, sm, c.p, nullptr, n, ti * FT, tj * FT);
+    same_tile_pair<AZ, BOOST, PREC>(d, sm, cs, c.p, nullptr, n, ti * FT, tj * FT);
 }
 
 template <bool AZ, bool BOOST>

@@ -156,6 +156,7 @@ extern "C" hbt_status hbt_bin_mixed_rotated_noalloc(const hbt_params *p, int64_t
     s.qnpts = g.qnpts;
     s.n_KT = g.n_KT;
     s.n_Kphi = g.n_Kphi;
+    fill_prefilter(s);
     d.h.den = reinterpret_cast<u64 *>(den);
     d.stats = stats;
 

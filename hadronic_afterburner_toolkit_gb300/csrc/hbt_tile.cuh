@@ -4,21 +4,29 @@
 // GB300 runs FP64 at 1/58 of its FP32 rate, so every pair is first screened
 // in FP32 and only the pairs that are binned pay for more work:
 //
-//  A. Window screen (every pair).  From FP32 copies of the momenta it forms
-//     K_perp^2, q_out, q_side, q_long and a rigorous bound on how far each
-//     lies from the value the reference computes in FP64 (error analysis
-//     below).  A pair is rejected when a window check fails by more than its
-//     bound; otherwise it is queued.
-//  B. Per-warp compaction.  Queued pairs are processed 32 at a time with all
-//     lanes active: the bin indices are decided in FP32 when every
-//     truncation is farther from its edge than its bound (they are then the
-//     reference's indices exactly), K_phi likewise with atan2f; any pair
-//     with an undecided window, index or angle runs the reference-order FP64
-//     chain of hbt_chain.cuh instead.
+//  A. Prefilter (every pair, ~30 FP32 operations).  Rejects only pairs
+//     certainly outside the window: q_out^2 + q_side^2 = q_x^2 + q_y^2 in
+//     real arithmetic, so a binned pair has q_x^2 + q_y^2 <= 2 Q^2, and
+//     |q_long| <= Q (with the boost: |S_E dq_z - S_z dq_E| <= Q sqrt(M^2),
+//     no division), Q = max(-lo, hi); each test carries the FP32 rounding of
+//     its inputs (2.01 u per sum) and a relative margin.  Other pairs are
+//     queued.
+//  B. Window screen and bins, per warp on 32 queued pairs with all lanes
+//     active.  From FP32 copies of the momenta: K_perp^2, q_out, q_side,
+//     q_long and a rigorous bound on how far each lies from the value the
+//     reference computes in FP64 (error analysis below).  A pair is dropped
+//     when a window check fails by more than its bound; the bin indices are
+//     decided in FP32 when every truncation is farther from its edge than
+//     its bound (they are then the reference's indices exactly), K_phi
+//     likewise with atan2f; any pair with an undecided window, index or
+//     angle runs the reference-order FP64 chain of hbt_chain.cuh instead.
+//     Same-event pairs that pass go to a second per-warp queue, so the FP64
+//     work of stage C again runs on 32 pairs at a time.
 //  C. Histogram update.  Mixed pairs add 1 to their denominator bin.
 //     Same-event pairs add q_out, q_side, q_long and cos(q.dx / hbarC):
 //       FP64 form  - FP64 values from algebraically identical expressions
-//                    (q_out = (q_x S_x + q_y S_y) / |S|, ...) and CUDA cos;
+//                    (q_out = (q_x S_x + q_y S_y) / |S|, ...) and a
+//                    table-driven FP64 cos (table_cos below);
 //       FP32W form - the FP32 screen values, and cos of the phase computed
 //                    and range-reduced in FP64, evaluated in FP32 by a Taylor
 //                    polynomial; added with one float4 vector atomic into
@@ -61,7 +69,34 @@ __device__ __forceinline__ int window_class(const Screen &S, float v, float err)
     return 2;
 }
 
-// Stage A: window checks.  Returns 0 (reject), 1 (all windows certainly
+// Stage A: false only when the pair certainly lies outside the q window.
+// a, b: FP32 momenta (px, py, pz, E); ga, gb: (|px| + |py|, |pz|) of each.
+template <bool BOOST>
+__device__ __forceinline__ bool prefilter(const Screen &S, float4 a, float2 ga, float4 b,
+                                          float2 gb) {
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    // |q_T| > sqrt(2) Q: |(dx, dy) - (q_x, q_y)| <= 2.01 u (|a.x|+|a.y|+|b.x|+|b.y|)
+    const float t = __fmaf_rn(dx, dx, dy * dy);
+    if (t > __fmaf_rn(S.pqt_c, ga.x + gb.x, S.pqt2)) return false;
+    const float Az = ga.y + gb.y;
+    if (BOOST) {
+        // q_long = (S_E dz - S_z dE) / sqrt((S_E - S_z)(S_E + S_z)); reject
+        // when (|nl| - e_nl)^2 > Q^2 * upper bound of (S_E - S_z)(S_E + S_z)
+        const float sE = a.w + b.w, sz = a.z + b.z, dE = a.w - b.w;
+        const float nl = __fmaf_rn(sE, dz, -(sz * dE));
+        const float low = fabsf(nl) - 17.0f * U * sE * Az;
+        const float em = 3.1f * U * (sE + Az);
+        const float m = sE - sz, p = sE + sz;
+        if (m > em && low > 0.0f &&
+            low * low > S.pq2 * ((m + em) * (p + em)) * (1.0f + 1e-5f))
+            return false;
+    } else {
+        if (fabsf(dz) > __fmaf_rn(2.1f * U, Az, S.pq)) return false;
+    }
+    return true;
+}
+
+// Stage B: window checks.  Returns 0 (reject), 1 (all windows certainly
 // passed), 2 (undecided).
 template <bool BOOST>
 __device__ __forceinline__ int screen_windows(const Screen &S, float4 a, float4 b, Q &q) {
@@ -166,11 +201,46 @@ __device__ __forceinline__ int kphi_screen(const Screen &S, const Q &q) {
     return (int)k;
 }
 
+// Table of cos and sin of 2 pi k / 256, k = 0..255, for table_cos, filled
+// by each CTA of the FP64-form same-event kernels.
+constexpr int COS_TABLE = 256;
+__device__ __forceinline__ void fill_cos_table(double2 *cs) {
+    for (int k = threadIdx.x; k < COS_TABLE; k += blockDim.x) {
+        double sn, cn;
+        sincospi(k / 128.0, &sn, &cn);
+        cs[k] = make_double2(cn, sn);
+    }
+}
+
+// cos(x), table-driven (the argument reduction of P. T. P. Tang's
+// table-driven elementary functions): x = k (2 pi / 256) + d with
+// k = rint(x 256 / 2 pi) and d from a two-part split of 2 pi / 256 (the
+// leading part has 26 significant bits, so k times it is exact for
+// |k| < 2^27), |d| <= pi / 256; then
+//   cos x = cos(2 pi k / 256) cos d - sin(2 pi k / 256) sin d
+// with cos d to d^6 and sin d to d^5 from their Taylor series (truncation
+// below 1e-17).  Absolute error about 3 ulp of 1.  |x| >= 2^20 (never on
+// this path: |q.dx| / hbarC is a few hundred at most) falls back to cos().
+__device__ __forceinline__ double table_cos(const double2 *cs, double x) {
+    if (!(fabs(x) < 1048576.0)) return cos(x);
+    const double kd = rint(x * 40.74366543152521);          // 256 / (2 pi)
+    double d = __fma_rn(-kd, 0.02454369282349944, x);       // leading part
+    d = __fma_rn(-kd, -2.173291814713612e-10, d);           // 2 pi / 256 - leading part
+    const int k = __double2int_rn(kd) & (COS_TABLE - 1);
+    const double d2 = d * d;
+    const double cd =
+        __fma_rn(d2, __fma_rn(d2, __fma_rn(d2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
+    const double sd = d * __fma_rn(d2, __fma_rn(d2, 1.0 / 120.0, -1.0 / 6.0), 1.0);
+    const double2 e = cs[k];
+    return __fma_rn(e.x, cd, -(e.y * sd));
+}
+
 // FP64 summed values of an accepted same-event pair (algebraically the
 // reference's q_out, q_side, q_long and cos(q.dx / hbarC)).
 template <bool BOOST>
-__device__ __forceinline__ void values64(const Grid &g, const double *a, const double *b,
-                                         double &qo, double &qs, double &ql, double &w) {
+__device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const double *a,
+                                         const double *b, double &qo, double &qs, double &ql,
+                                         double &w) {
     const double sx = a[0] + b[0], sy = a[1] + b[1];
     const double dx = a[0] - b[0], dy = a[1] - b[1];
     const double dz = a[2] - b[2], dE = a[3] - b[3];
@@ -185,7 +255,7 @@ __device__ __forceinline__ void values64(const Grid &g, const double *a, const d
     }
     const double ph = dE * (a[7] - b[7]) - dx * (a[4] - b[4]) - dy * (a[5] - b[5]) -
                       dz * (a[6] - b[6]);
-    w = cos(g.hbarC_inv * ph);
+    w = table_cos(cs, g.hbarC_inv * ph);
 }
 
 // Summed values of the FP32-weight form.  The momentum sums and differences
@@ -241,27 +311,47 @@ struct TileSmem {
     double sj[8][FT];  // FP64 j-tile (same-event)
     float4 fi[FT];     // FP32 momenta of the i-tile
     float4 fj[FT];     // FP32 momenta of the j-tile
+    float2 gi[FT];     // (|px| + |py|, |pz|) of the i-tile (prefilter)
+    float2 gj[FT];
     unsigned queue[FT / 32][QCAP];
+    // same-event pairs that passed the window screen: x = (i, j, swap,
+    // undecided, slot) bits, y = q bin (bin_entry)
+    uint2 queue2[FT / 32][QCAP];
     unsigned oi[FT], oj[FT];  // original list positions (pair orientation)
 };
 
-// Appends this lane's pair to the warp queue when `take`, and runs
-// `process` on 32 queued pairs whenever 32 are waiting.
-template <class F>
-__device__ __forceinline__ void enqueue(unsigned *q, int &count, bool take, unsigned entry,
-                                        int lane, F &process) {
+// Entry of the second same-event queue.
+__device__ __forceinline__ uint2 bin_entry(unsigned e, bool undecided, int slot, int bin) {
+    return make_uint2((e & 0x1ffffu) | (undecided ? 1u << 17 : 0u) | ((unsigned)slot << 18),
+                      (unsigned)bin);
+}
+
+// Appends this lane's entry to the warp queue when `take`, and runs
+// `process(entry, true)` on 32 queued entries whenever 32 are waiting (all
+// lanes of the warp call this in step; `count` is warp-uniform).
+template <class T, class F>
+__device__ __forceinline__ void enqueue(T *q, int &count, bool take, T entry, int lane,
+                                        F &process) {
     const unsigned m = __ballot_sync(0xffffffffu, take);
     if (!m) return;
     if (take) q[count + __popc(m & ((1u << lane) - 1u))] = entry;
     count += __popc(m);
     __syncwarp();
     if (count >= 32) {
-        process(q[lane]);
+        process(q[lane], true);
         __syncwarp();
         if (lane < count - 32) q[lane] = q[32 + lane];
         __syncwarp();
         count -= 32;
     }
+}
+
+// Runs `process(entry, valid)` on the entries left in the queue, all lanes
+// in step (lanes beyond the count pass valid = false).
+template <class T, class F>
+__device__ __forceinline__ void drain(T *q, int count, int lane, F &process) {
+    if (count > 0) process(q[lane < count ? lane : 0], lane < count);
+    __syncwarp();
 }
 
 // Same-event pairs of the tiles starting at i0 and j0 (i0 <= j0) of one list
@@ -272,7 +362,7 @@ __device__ __forceinline__ void enqueue(unsigned *q, int &count, bool take, unsi
 // the rows are in the caller's order.  Called by all FT threads of the CTA;
 // the caller syncs before reusing `sm`.
 template <bool AZ, bool BOOST, int PREC>
-__device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
+__device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, const double2 *cs,
                                                const double *const *c, const unsigned *orig,
                                                long long n, long long i0, long long j0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -287,31 +377,28 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
                              (float)sm.si[3][tid]);
     sm.fj[tid] = make_float4((float)sm.sj[0][tid], (float)sm.sj[1][tid], (float)sm.sj[2][tid],
                              (float)sm.sj[3][tid]);
+    sm.gi[tid] = make_float2(fabsf(sm.fi[tid].x) + fabsf(sm.fi[tid].y), fabsf(sm.fi[tid].z));
+    sm.gj[tid] = make_float2(fabsf(sm.fj[tid].x) + fabsf(sm.fj[tid].y), fabsf(sm.fj[tid].z));
     __syncthreads();
     const Screen &S = d.s;
     const int il = w * 32 + lane;
     const long long i = i0 + il;
     const float4 a = sm.fi[il];
+    const float2 ga = sm.gi[il];
     const unsigned oa = sm.oi[il];
     const int jend = (int)min((long long)FT, n - j0);
     unsigned *q = sm.queue[w];
-    int count = 0;
+    uint2 *q2 = sm.queue2[w];
+    int count = 0, count2 = 0;
 
-    // stages B and C for one queued pair (all lanes of the warp in step)
-    auto process = [&](unsigned e) {
+    // stage C for 32 screened pairs (all lanes of the warp in step)
+    auto values = [&](uint2 e2, bool valid) {
+        if (!valid) return;
+        const unsigned e = e2.x;
         const int qi = e & 0xff, qj = (e >> 8) & 0xff;
         const bool swap = (e >> 16) & 1u;
-        Q s;
-        const int wcls = swap ? screen_windows<BOOST>(S, sm.fj[qj], sm.fi[qi], s)
-                              : screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
-        int iK = 0, bin = 0, slot = -1;
-        if (wcls == 1 && decide_bins(S, s, iK, bin)) {
-            slot = iK;
-            if (AZ) {
-                const int ip = kphi_screen(S, s);
-                slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
-            }
-        }
+        const int slot = (e >> 17) & 1u ? -1 : (int)(e >> 18);
+        const int bin = (int)e2.y;
         double A[8], B[8];  // first and second particle of the pair
 #pragma unroll
         for (int f = 0; f < 8; f++) {
@@ -336,7 +423,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
         const long long at = (long long)slot * d.g.q3 + bin;
         if (PREC == 0) {
             double vo, vs, vl, vw;
-            values64<BOOST>(d.g, A, B, vo, vs, vl, vw);
+            values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
             Sums *h = d.h.sums + at;
             atomicAdd(&h->qo, vo);
             atomicAdd(&h->qs, vs);
@@ -348,19 +435,37 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm,
         atomicAdd(d.h.cnt + at, 1ull);
     };
 
+    // stage B for 32 prefiltered pairs: window screen and bins; the pairs
+    // inside the window (or undecided) go to the second queue
+    auto screen = [&](unsigned e, bool valid) {
+        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        const bool swap = (e >> 16) & 1u;
+        Q s;
+        int wcls = 0;
+        if (valid)
+            wcls = swap ? screen_windows<BOOST>(S, sm.fj[qj], sm.fi[qi], s)
+                        : screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+        int iK = 0, bin = 0, slot = -1;
+        if (wcls == 1 && decide_bins(S, s, iK, bin)) {
+            slot = iK;
+            if (AZ) {
+                const int ip = kphi_screen(S, s);
+                slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
+            }
+        }
+        enqueue(q2, count2, wcls != 0, bin_entry(e, slot < 0, slot < 0 ? 0 : slot, bin), lane,
+                values);
+    };
+
     for (int jj = 0; jj < jend; jj++) {
         const long long j = j0 + jj;
-        int cls = 0;
         const bool swap = oa > sm.oj[jj];
-        if (i < n && j > i) {
-            Q s;
-            cls = swap ? screen_windows<BOOST>(S, sm.fj[jj], a, s)
-                       : screen_windows<BOOST>(S, a, sm.fj[jj], s);
-        }
-        enqueue(q, count, cls != 0,
-                (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16), lane, process);
+        const bool take = i < n && j > i && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
+        enqueue(q, count, take,
+                (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16), lane, screen);
     }
-    if (lane < count) process(q[lane]);
+    drain(q, count, lane, screen);
+    drain(q2, count2, lane, values);
 }
 
 // Mixed-event pairs of the list-1 tile at i0 (n1 particles, columns l1 =
@@ -377,19 +482,24 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
     sm.fj[tid] = (j0 + tid < n2) ? make_float4((float)l2[0][j0 + tid], (float)l2[1][j0 + tid],
                                                (float)l2[2][j0 + tid], (float)l2[3][j0 + tid])
                                  : make_float4(0.f, 0.f, 0.f, 1.f);
+    sm.gi[tid] = make_float2(fabsf(sm.fi[tid].x) + fabsf(sm.fi[tid].y), fabsf(sm.fi[tid].z));
+    sm.gj[tid] = make_float2(fabsf(sm.fj[tid].x) + fabsf(sm.fj[tid].y), fabsf(sm.fj[tid].z));
     __syncthreads();
     const Screen &S = d.s;
     const int il = w * 32 + lane;
     const bool active = i0 + il < n1;
     const float4 a = sm.fi[il];
+    const float2 ga = sm.gi[il];
     const int jend = (int)min((long long)FT, n2 - j0);
     unsigned *q = sm.queue[w];
     int count = 0;
 
-    auto process = [&](unsigned e) {
+    auto process = [&](unsigned e, bool valid) {
+        if (!valid) return;
         const int qi = e & 0xff, qj = (e >> 8) & 0xff;
         Q s;
         const int wcls = screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+        if (wcls == 0) return;
         int iK = 0, bin = 0, slot = -1;
         if (wcls == 1 && decide_bins(S, s, iK, bin)) {
             slot = iK;
@@ -410,14 +520,10 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
     };
 
     for (int jj = 0; jj < jend; jj++) {
-        int cls = 0;
-        if (active) {
-            Q s;
-            cls = screen_windows<BOOST>(S, a, sm.fj[jj], s);
-        }
-        enqueue(q, count, cls != 0, (unsigned)il | ((unsigned)jj << 8), lane, process);
+        const bool take = active && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
+        enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process);
     }
-    if (lane < count) process(q[lane]);
+    drain(q, count, lane, process);
 }
 
 }  // namespace tile
