@@ -353,11 +353,19 @@ def uneven_leg(E, torch, dev, stream, flush, local, steps=2) -> dict:
     for label, prec in (("batched-fp64", E.PRECISION_FP64), ("batched-fp32w", E.PRECISION_FP32W)):
         eng = E.Engine(device=local, precision=prec, kernel=E.KERNEL_SCREENED, **UNEVEN_PARAMS)
         eng.set_stream(stream.cuda_stream)
-        timed(lambda: eng.bin_batch(jobs, device=True), 1)  # warm-up
+        default_ms = statistics.median(timed(lambda: eng.bin_batch(jobs, device=True), 2))
+        # autotune on a sample of the batch, then warm up: the second launch
+        # of the same batch is captured into a CUDA graph, later ones re-launch it
+        tuned, tune_ms = eng.autotune(jobs, max_pairs=4e9)
+        timed(lambda: eng.bin_batch(jobs, device=True), 2)
+        st0 = eng.stats()
         ms = timed(lambda: eng.bin_batch(jobs, device=True), steps)
+        st1 = eng.stats()
         out[label] = {"value": total_pairs / (statistics.median(ms) * 1e-3), "unit": "pairs/s",
                       "ms_per_step": statistics.median(ms), "steps": steps,
-                      "jobs_per_launch": len(jobs)}
+                      "jobs_per_launch": len(jobs), "tuning": tuned,
+                      "ms_per_step_default_tuning": default_ms,
+                      "graph_replays_timed": st1["graph_replays"] - st0["graph_replays"]}
         eng.close()
     # plain: the reference chain on every pair, one call per list, on the
     # first groups (about 3e9 pairs)

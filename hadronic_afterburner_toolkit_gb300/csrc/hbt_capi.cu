@@ -54,6 +54,8 @@ struct hbt_ctx {
     // batched path: tables, sorted particle table, sort scratch, boxes, queue
     hbt::BatchRunner runner;
     int persistent_grid = 152 * 4;
+    int sms = 152, max_blocks_per_sm = 5;
+    hbt_tuning tune = {0, 0.02, 0.05, 16384, 1};
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging
@@ -344,6 +346,19 @@ bool batched_ok(const hbt_ctx *c) {
 
 using hbt::FastJob;
 
+// The batched path's launch shape from the context's tuning.
+hbt::Tuning runner_tuning(const hbt_ctx *c, const hbt_tuning &t) {
+    hbt::Tuning r;
+    const int bps = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, c->max_blocks_per_sm)
+                                        : c->max_blocks_per_sm;
+    r.grid = c->sms * bps;
+    r.chunk = c->d.precision == HBT_PRECISION_FP32W ? (unsigned)t.merge_chunk : 0u;
+    r.cell_pt = t.cell_pt;
+    r.cell_y = t.cell_y;
+    r.graph = t.use_graph != 0;
+    return r;
+}
+
 // Sort, cull and bin fast jobs of this analysis in one persistent launch.
 hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs) {
     const double Q = std::max(std::fabs(c->d.g.q_lo), std::fabs(c->d.g.q_hi));
@@ -353,11 +368,42 @@ hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs) {
         j.boost = c->d.g.boost;
     }
     std::string err;
-    if (!c->runner.run(jobs, c->d, c->persistent_grid, (unsigned)c->d.merge_chunk_blocks,
-                       c->stream, err))
+    if (!c->runner.run(jobs, c->d, runner_tuning(c, c->tune), c->stream, err))
         return fail(c, HBT_ERR_CUDA, err);
     c->st.launches += 6;
+    if (c->runner.last_graph_reuse() == 0) c->st.graph_captures++;
+    if (c->runner.last_graph_reuse() == 1) c->st.graph_replays++;
     return HBT_OK;
+}
+
+// Device-array jobs of the C ABI as batch jobs.
+std::vector<FastJob> fast_jobs_of(int32_t n_jobs, const hbt_job *jobs) {
+    std::vector<FastJob> fj;
+    for (int k = 0; k < n_jobs; k++) {
+        const hbt_job &j = jobs[k];
+        FastJob f = {};
+        f.kind = j.kind;
+        f.na = j.na;
+        f.nb = j.nb;
+        const double *a[8] = {j.a.px, j.a.py, j.a.pz, j.a.E, j.a.x, j.a.y, j.a.z, j.a.t};
+        for (int q = 0; q < 8; q++) f.a[q] = a[q];
+        const double *b[4] = {j.b.px, j.b.py, j.b.pz, j.b.E};
+        for (int q = 0; q < 4; q++) f.b[q] = b[q];
+        fj.push_back(f);
+    }
+    return fj;
+}
+
+bool tuning_valid(const hbt_tuning &t) {
+    return t.blocks_per_sm >= 0 && t.cell_pt >= 0.0 && t.cell_y >= 0.0 && t.merge_chunk >= 0 &&
+           t.merge_chunk <= 16384 && (t.use_graph == 0 || t.use_graph == 1);
+}
+
+hbt_tuning tuning_defaults(hbt_tuning t) {
+    if (t.cell_pt == 0.0) t.cell_pt = 0.02;
+    if (t.cell_y == 0.0) t.cell_y = 0.05;
+    if (t.merge_chunk == 0) t.merge_chunk = 16384;
+    return t;
 }
 
 hbt_status bin_same_device(hbt_ctx *c, long long n, const double *const *c8) {
@@ -532,7 +578,9 @@ hbt_status ctx_create(const hbt_params *p, int device, cudaMemPool_t pool, hbt_c
     {
         int sms = 0;
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        c->persistent_grid = sms * hbt::persistent_blocks_per_sm();
+        c->sms = sms;
+        c->max_blocks_per_sm = hbt::persistent_blocks_per_sm();
+        c->persistent_grid = sms * c->max_blocks_per_sm;
     }
 
     const size_t nb = (size_t)g.n_slots * g.q3, nq = (size_t)g.n_KT * g.qnpts;
@@ -682,19 +730,7 @@ hbt_status hbt_bin_batch_dev(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs) {
         }
         return HBT_OK;
     }
-    std::vector<FastJob> fj;
-    for (int k = 0; k < n_jobs; k++) {
-        const hbt_job &j = jobs[k];
-        FastJob f = {};
-        f.kind = j.kind;
-        f.na = j.na;
-        f.nb = j.nb;
-        const double *a[8] = {j.a.px, j.a.py, j.a.pz, j.a.E, j.a.x, j.a.y, j.a.z, j.a.t};
-        for (int q = 0; q < 8; q++) f.a[q] = a[q];
-        const double *b[4] = {j.b.px, j.b.py, j.b.pz, j.b.E};
-        for (int q = 0; q < 4; q++) f.b[q] = b[q];
-        fj.push_back(f);
-    }
+    std::vector<FastJob> fj = fast_jobs_of(n_jobs, jobs);
     c->st.pairs_same += P_same;
     c->st.pairs_mixed += P_mixed;
     TRY(run_fast_jobs(c, fj));
@@ -740,6 +776,114 @@ hbt_status hbt_bin_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs) {
         }
     }
     return hbt_bin_batch_dev(c, n_jobs, dj.data());
+}
+
+hbt_status hbt_set_tuning(hbt_ctx *c, const hbt_tuning *t) {
+    if (!c || !t) return HBT_ERR_INVALID;
+    if (!tuning_valid(*t)) return fail(c, HBT_ERR_INVALID, "invalid tuning");
+    c->tune = tuning_defaults(*t);
+    return HBT_OK;
+}
+
+hbt_status hbt_get_tuning(hbt_ctx *c, hbt_tuning *t) {
+    if (!c || !t) return HBT_ERR_INVALID;
+    *t = c->tune;
+    return HBT_OK;
+}
+
+hbt_status hbt_autotune_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs, double max_pairs,
+                              hbt_tuning *best, double *best_ms) {
+    if (!c || n_jobs < 0 || (n_jobs > 0 && !jobs)) return HBT_ERR_INVALID;
+    if (!batched_ok(c)) return fail(c, HBT_ERR_STATE, "the batched path is not in use");
+    CU(cudaSetDevice(c->device));
+    for (int k = 0; k < n_jobs; k++)
+        if ((jobs[k].kind != 0 && jobs[k].kind != 1) || jobs[k].na < 0 || jobs[k].nb < 0)
+            return fail(c, HBT_ERR_INVALID, "invalid job");
+    // a sample of the batch: jobs in order up to max_pairs candidate pairs
+    if (!(max_pairs > 0)) max_pairs = 2e9;
+    std::vector<FastJob> all = fast_jobs_of(n_jobs, jobs), sample;
+    double pairs = 0.0;
+    for (const FastJob &f : all) {
+        if (!sample.empty() && pairs >= max_pairs) break;
+        sample.push_back(f);
+        pairs += f.kind == 0 ? 0.5 * (double)f.na * (double)(f.na - 1) : (double)f.na * f.nb;
+    }
+    // scratch histograms of the same analysis
+    hbt_ctx *t = nullptr;
+    const hbt_status s = hbt::ctx_create(&c->prm, c->device, nullptr, &t);
+    if (s != HBT_OK) return fail(c, s, "autotune: scratch context creation failed");
+    std::unique_ptr<hbt_ctx, void (*)(hbt_ctx *)> guard(t, hbt_destroy);
+    t->d.g.psi_ref = c->d.g.psi_ref;
+    fill_screen(t);
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    auto time_one = [&](const hbt_tuning &cand, double &ms) -> hbt_status {
+        t->tune = cand;
+        t->tune.use_graph = 0;
+        double bestv = 1e300;
+        for (int rep = 0; rep < 3; rep++) {  // the first run warms up
+            CU(cudaEventRecord(e0, t->stream));
+            TRY(run_fast_jobs(t, sample));
+            CU(cudaEventRecord(e1, t->stream));
+            CU(cudaEventSynchronize(e1));
+            float m = 0.f;
+            CU(cudaEventElapsedTime(&m, e0, e1));
+            if (rep > 0) bestv = std::min(bestv, (double)m);
+        }
+        ms = bestv;
+        return HBT_OK;
+    };
+    hbt_tuning cur = c->tune;
+    double cur_ms = 0.0;
+    hbt_status rs = time_one(cur, cur_ms);
+    // coordinate search: sort cells, then CTAs per SM, then the merge chunk
+    const double cells[][2] = {{0.01, 0.025}, {0.02, 0.05}, {0.04, 0.1}, {0.02, 0.1}, {0.04, 0.05},
+                               {0.01, 0.05}};
+    for (const auto &cl : cells) {
+        if (rs != HBT_OK) break;
+        hbt_tuning cand = cur;
+        cand.cell_pt = cl[0];
+        cand.cell_y = cl[1];
+        if (cand.cell_pt == cur.cell_pt && cand.cell_y == cur.cell_y) continue;
+        double ms = 0.0;
+        rs = time_one(cand, ms);
+        if (rs == HBT_OK && ms < cur_ms) {
+            cur = cand;
+            cur_ms = ms;
+        }
+    }
+    for (int bps = 2; bps <= c->max_blocks_per_sm && rs == HBT_OK; bps++) {
+        hbt_tuning cand = cur;
+        cand.blocks_per_sm = bps == c->max_blocks_per_sm ? 0 : bps;
+        if (cand.blocks_per_sm == cur.blocks_per_sm) continue;
+        double ms = 0.0;
+        rs = time_one(cand, ms);
+        if (rs == HBT_OK && ms < cur_ms) {
+            cur = cand;
+            cur_ms = ms;
+        }
+    }
+    if (c->d.precision == HBT_PRECISION_FP32W)
+        for (int chunk : {8192, 16384}) {
+            if (rs != HBT_OK || chunk == cur.merge_chunk) continue;
+            hbt_tuning cand = cur;
+            cand.merge_chunk = chunk;
+            double ms = 0.0;
+            rs = time_one(cand, ms);
+            if (rs == HBT_OK && ms < cur_ms) {
+                cur = cand;
+                cur_ms = ms;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rs != HBT_OK) return fail(c, rs, std::string("autotune: ") + hbt_last_error(t));
+    cur.use_graph = c->tune.use_graph;
+    c->tune = cur;
+    if (best) *best = cur;
+    if (best_ms) *best_ms = cur_ms;
+    return HBT_OK;
 }
 
 hbt_status hbt_sync(hbt_ctx *c, uint64_t timeout_us) {

@@ -3,10 +3,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 namespace hbt {
 
 BatchRunner::~BatchRunner() {
+    if (exec_) cudaGraphExecDestroy(exec_);
     Buf *all[] = {&lists_, &jobs_, &offs_, &table_, &keys_, &vals_, &sort_temp_, &boxes_,
                   &items_, &counters_, &devs_};
     for (Buf *b : all)
@@ -18,6 +20,9 @@ bool BatchRunner::grow(Buf &b, size_t bytes, std::string &err) {
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.bytes = 0;
+    // a cached graph refers to the old buffers
+    key_.clear();
+    last_key_.clear();
     if (bytes == 0) return true;
     // a little headroom so slowly growing batches do not reallocate each time
     const size_t want = bytes + bytes / 8;
@@ -30,13 +35,13 @@ bool BatchRunner::grow(Buf &b, size_t bytes, std::string &err) {
     return true;
 }
 
-bool BatchRunner::run(const std::vector<FastJob> &jobs, const Device &d, int grid,
-                      unsigned chunk, cudaStream_t st, std::string &err) {
-    return run_impl(jobs, d, nullptr, nullptr, 0, grid, chunk, st, err);
+bool BatchRunner::run(const std::vector<FastJob> &jobs, const Device &d, const Tuning &t,
+                      cudaStream_t st, std::string &err) {
+    return run_impl(jobs, d, nullptr, nullptr, 0, t, st, err);
 }
 
 bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<Device> &devs,
-                            int grid, unsigned chunk, cudaStream_t st, std::string &err) {
+                            const Tuning &t, cudaStream_t st, std::string &err) {
     if (devs.empty()) {
         err = "no analyses in the batch";
         return false;
@@ -59,12 +64,76 @@ bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<
         return false;
     }
     return run_impl(jobs, devs[0], static_cast<const Device *>(devs_.p), devs.data(),
-                    (int)devs.size(), grid, chunk, st, err);
+                    (int)devs.size(), t, st, err);
+}
+
+// The graph captured for one set of launch arguments stays valid while they
+// are unchanged: the batch tables it reads are re-uploaded before each
+// launch, into the same buffers.
+cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device *devs_host,
+                                int n_devs, const Tuning &t, cudaStream_t st) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (!t.graph || st == nullptr || cudaStreamIsCapturing(st, &cap) != cudaSuccess ||
+        cap != cudaStreamCaptureStatusNone) {
+        last_reuse_ = -1;
+        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st);
+    }
+    std::vector<unsigned char> key;
+    auto put = [&](const void *p, size_t n) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        key.insert(key.end(), c, c + n);
+    };
+    put(&d, sizeof(d));
+    put(&b, sizeof(b));
+    put(&t.grid, sizeof(t.grid));
+    put(&t.chunk, sizeof(t.chunk));
+    put(&n_devs, sizeof(n_devs));
+    if (n_devs > 0) put(devs_host, sizeof(Device) * n_devs);
+    if (exec_ && key == key_) {
+        last_reuse_ = 1;
+        return cudaGraphLaunch(exec_, st);
+    }
+    if (key != last_key_) {
+        // a new shape: run directly; capture if it comes again
+        last_key_.swap(key);
+        last_reuse_ = -1;
+        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st);
+    }
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const cudaError_t run_e = run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st, &g);
+    if (run_e != cudaSuccess || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        key_.clear();
+        return run_e != cudaSuccess ? run_e : e;
+    }
+    bool updated = false;
+    if (exec_) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(exec_, g, &info) == cudaSuccess;
+        if (!updated) {
+            cudaGetLastError();  // clear the update's error
+            cudaGraphExecDestroy(exec_);
+            exec_ = nullptr;
+        }
+    }
+    if (!updated) e = cudaGraphInstantiate(&exec_, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        exec_ = nullptr;
+        key_.clear();
+        return e;
+    }
+    key_.swap(key);
+    last_reuse_ = 0;
+    return cudaGraphLaunch(exec_, st);
 }
 
 bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
-                           const Device *devs_dev, const Device *devs_host, int n_devs, int grid,
-                           unsigned chunk, cudaStream_t st, std::string &err) {
+                           const Device *devs_dev, const Device *devs_host, int n_devs,
+                           const Tuning &t, cudaStream_t st, std::string &err) {
     std::vector<BatchList> lists;
     std::vector<BatchJob> bj;
     std::vector<long long> list_off, tile_off, pair_off;
@@ -138,7 +207,8 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
         err = "uploading the batch tables failed";
         return false;
     }
-    BatchDev b = {};
+    BatchDev b;
+    memset(&b, 0, sizeof(b));  // padding too: the bytes key the cached graph
     const long long *o = static_cast<const long long *>(offs_.p);
     b.lists = static_cast<const BatchList *>(lists_.p);
     b.jobs = static_cast<const BatchJob *>(jobs_.p);
@@ -165,13 +235,13 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
     b.mixed_cap = (unsigned)mixed_pairs;
     b.n_items = static_cast<unsigned *>(counters_.p);
     b.item_next = b.n_items + 2;
-    b.p_extent = 1024 * 0.02 / 2;
-    b.inv_cell_pt = 1.0 / 0.02;
-    b.y_extent = 1024 * 0.05 / 2;
-    b.inv_cell_y = 1.0 / 0.05;
+    b.p_extent = 1024 * t.cell_pt / 2;
+    b.inv_cell_pt = 1.0 / t.cell_pt;
+    b.y_extent = 1024 * t.cell_y / 2;
+    b.inv_cell_y = 1.0 / t.cell_y;
     b.devs = devs_dev;
     b.n_devs = n_devs;
-    const cudaError_t e = run_batch(d, b, grid, chunk, devs_host, n_devs, st);
+    const cudaError_t e = launch(d, b, devs_host, n_devs, t, st);
     if (e != cudaSuccess) {
         err = std::string("batch launch failed: ") + cudaGetErrorString(e);
         return false;

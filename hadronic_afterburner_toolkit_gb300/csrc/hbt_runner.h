@@ -24,6 +24,15 @@ struct FastJob {
     int boost;           // long_comoving_boost of the analysis
 };
 
+// Launch shape of a batch, chosen by hbt_set_tuning / hbt_autotune_batch.
+struct Tuning {
+    int grid = 0;            // persistent CTAs
+    unsigned chunk = 0;      // FP32-weight form: same-event items between merges (0: no chunks)
+    double cell_pt = 0.02;   // Morton cell of p_x, p_y (GeV)
+    double cell_y = 0.05;    // Morton cell of rapidity
+    bool graph = true;       // launch the pipeline as a CUDA graph
+};
+
 class BatchRunner {
   public:
     BatchRunner() = default;
@@ -34,19 +43,22 @@ class BatchRunner {
     // Runs the jobs of one analysis: every job bins into `d`.  Returns
     // false and sets `err` on failure.  Allocates scratch on first use and
     // when a batch outgrows it.
-    bool run(const std::vector<FastJob> &jobs, const Device &d, int grid, unsigned chunk,
-             cudaStream_t st, std::string &err);
+    bool run(const std::vector<FastJob> &jobs, const Device &d, const Tuning &t, cudaStream_t st,
+             std::string &err);
 
     // Runs jobs of several analyses in one launch: job.dev indexes `devs`,
     // whose entries must share azimuthal_flag, long_comoving_boost and
     // precision (they select the kernel).  The FP32-weight partials of
     // every analysis are merged after each chunk of `chunk` same-event
     // items and at the end.
-    bool run_multi(const std::vector<FastJob> &jobs, const std::vector<Device> &devs, int grid,
-                   unsigned chunk, cudaStream_t st, std::string &err);
+    bool run_multi(const std::vector<FastJob> &jobs, const std::vector<Device> &devs,
+                   const Tuning &t, cudaStream_t st, std::string &err);
 
-    // Candidate and kept tile pairs of the last batch (kept read lazily).
+    // Candidate tile pairs of the last batch.
     long long last_tile_pairs() const { return last_pairs_; }
+    // Graph launches of the last batch: 1 a cached graph was re-launched,
+    // 0 captured anew, -1 launched without a graph.
+    int last_graph_reuse() const { return last_reuse_; }
 
   private:
     struct Buf {
@@ -55,10 +67,18 @@ class BatchRunner {
     };
     bool grow(Buf &b, size_t bytes, std::string &err);
     bool run_impl(const std::vector<FastJob> &jobs, const Device &d, const Device *devs_dev,
-                  const Device *devs_host, int n_devs, int grid, unsigned chunk, cudaStream_t st,
+                  const Device *devs_host, int n_devs, const Tuning &t, cudaStream_t st,
                   std::string &err);
+    // Runs the device pipeline, through a cached CUDA graph when possible.
+    cudaError_t launch(const Device &d, const BatchDev &b, const Device *devs_host, int n_devs,
+                       const Tuning &t, cudaStream_t st);
     Buf lists_, jobs_, offs_, table_, keys_, vals_, sort_temp_, boxes_, items_, counters_, devs_;
     long long last_pairs_ = 0;
+    int last_reuse_ = -1;
+    // the cached graph and the launch arguments it was captured with; a
+    // graph is captured when the same arguments come twice in a row
+    cudaGraphExec_t exec_ = nullptr;
+    std::vector<unsigned char> key_, last_key_;
 };
 
 }  // namespace hbt

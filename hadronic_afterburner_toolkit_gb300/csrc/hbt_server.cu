@@ -551,8 +551,12 @@ bool issue_round(hbt_server *s) {
     r.end = take_event(s, true);
     cudaEventRecord(r.start, s->rounds);
     std::string err;
-    const unsigned chunk = ld.precision == HBT_PRECISION_FP32W ? (unsigned)ld.merge_chunk_blocks : 0;
-    const bool ok = s->runner.run_multi(jobs, devs, s->grid, chunk, s->rounds, err);
+    // rounds differ in shape: direct launches, no graph
+    hbt::Tuning tu;
+    tu.grid = s->grid;
+    tu.chunk = ld.precision == HBT_PRECISION_FP32W ? (unsigned)ld.merge_chunk_blocks : 0u;
+    tu.graph = false;
+    const bool ok = s->runner.run_multi(jobs, devs, tu, s->rounds, err);
     cudaEventRecord(r.end, s->rounds);
     for (Request *q : members)
         if (!ok || q->next >= q->work.size()) r.finishing.push_back(q);

@@ -56,9 +56,15 @@ class HbtJob(ctypes.Structure):
     _fields_ = [("kind", _I32), ("na", _I64), ("nb", _I64), ("a", HbtSoa8), ("b", HbtSoa8)]
 
 
+class HbtTuning(ctypes.Structure):
+    _fields_ = [("blocks_per_sm", _I32), ("cell_pt", _D), ("cell_y", _D),
+                ("merge_chunk", _I32), ("use_graph", _I32)]
+
+
 class HbtStats(ctypes.Structure):
     _fields_ = [(k, _U64) for k in ("pairs_same", "pairs_mixed", "launches",
-                                    "ordered_passes", "deferred_kphi", "anomalies")]
+                                    "ordered_passes", "deferred_kphi", "anomalies",
+                                    "graph_captures", "graph_replays")]
 
 
 # Every entry point of include/hbt_gpu.h: name -> (restype, argtypes)
@@ -77,6 +83,10 @@ _SIGNATURES = {
                                  ctypes.POINTER(HbtSoa4)]),
     "hbt_bin_batch": (_I32, [ctypes.c_void_p, _I32, ctypes.POINTER(HbtJob)]),
     "hbt_bin_batch_dev": (_I32, [ctypes.c_void_p, _I32, ctypes.POINTER(HbtJob)]),
+    "hbt_set_tuning": (_I32, [ctypes.c_void_p, ctypes.POINTER(HbtTuning)]),
+    "hbt_get_tuning": (_I32, [ctypes.c_void_p, ctypes.POINTER(HbtTuning)]),
+    "hbt_autotune_batch": (_I32, [ctypes.c_void_p, _I32, ctypes.POINTER(HbtJob), _D,
+                                  ctypes.POINTER(HbtTuning), ctypes.POINTER(_D)]),
     "hbt_sync": (_I32, [ctypes.c_void_p, _U64]),
     "hbt_n_bins": (_I64, [ctypes.c_void_p]),
     "hbt_read_hist": (_I32, [ctypes.c_void_p] + [_PD] * 6),
@@ -216,6 +226,35 @@ class Engine:
     def bin_batch(self, jobs: Sequence, device: bool = False):
         """Many jobs in one persistent launch.  Each job is ("same", cols8)
         or ("mixed", cols4_list1, cols4_list2)."""
+        arr, keep = self._job_array(jobs, device)
+        fn = self.L.hbt_bin_batch_dev if device else self.L.hbt_bin_batch
+        self._check(fn(self._h, len(jobs), arr))
+
+    # ------------------------------------------------------------- tuning
+    def set_tuning(self, **kw):
+        t = HbtTuning()
+        self._check(self.L.hbt_get_tuning(self._h, ctypes.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(self.L.hbt_set_tuning(self._h, ctypes.byref(t)))
+
+    def tuning(self) -> dict:
+        t = HbtTuning()
+        self._check(self.L.hbt_get_tuning(self._h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in HbtTuning._fields_}
+
+    def autotune(self, jobs: Sequence, max_pairs: float = 0.0):
+        """Autotune the batched path on device-array jobs (bin_batch layout);
+        returns (tuning dict, best time in ms)."""
+        arr, keep = self._job_array(jobs, True)
+        t = HbtTuning()
+        ms = _D()
+        self._check(self.L.hbt_autotune_batch(self._h, len(jobs), arr, max_pairs,
+                                              ctypes.byref(t), ctypes.byref(ms)))
+        return {k: getattr(t, k) for k, _ in HbtTuning._fields_}, ms.value
+
+    @staticmethod
+    def _job_array(jobs: Sequence, device: bool):
         arr = (HbtJob * max(len(jobs), 1))()
         keep = []
         for k, job in enumerate(jobs):
@@ -235,8 +274,7 @@ class Engine:
                 arr[k].nb = int(b[0].shape[0])
                 arr[k].a = HbtSoa8(*([_ptr(c) for c in a[:4]] + [0, 0, 0, 0]))
                 arr[k].b = HbtSoa8(*([_ptr(c) for c in b[:4]] + [0, 0, 0, 0]))
-        fn = self.L.hbt_bin_batch_dev if device else self.L.hbt_bin_batch
-        self._check(fn(self._h, len(jobs), arr))
+        return arr, keep
 
     # ------------------------------------------------------------ results
     def hist(self) -> dict:

@@ -102,6 +102,8 @@ typedef struct hbt_stats {
     uint64_t deferred_kphi;   /* pairs whose K_phi bin was decided on the host */
     uint64_t anomalies;       /* pairs skipped: NaN LCMS component (K_perp == 0)
                                  or a K_T index outside [0, n_KT) */
+    uint64_t graph_captures;  /* batched launches captured into a CUDA graph */
+    uint64_t graph_replays;   /* batched launches that re-launched a cached graph */
 } hbt_stats;
 
 /* Creates a context on `device` and allocates the zeroed histograms
@@ -156,6 +158,33 @@ typedef struct hbt_job {
  * order.  hbt_bin_batch takes host arrays, hbt_bin_batch_dev device arrays. */
 hbt_status hbt_bin_batch(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs);
 hbt_status hbt_bin_batch_dev(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs);
+
+/* Launch shape of the batched path (HBT_KERNEL_SCREENED).  No counterpart
+ * in the reference.  Every choice gives the same bins and counts; they
+ * differ in speed only (and, for the FP32-weight form, merge_chunk bounds
+ * how many pairs an FP32 partial accumulates). */
+typedef struct hbt_tuning {
+    int32_t blocks_per_sm;  /* persistent CTAs per SM (0: the occupancy limit) */
+    double cell_pt;         /* sort cell of p_x and p_y in GeV (0: 0.02) */
+    double cell_y;          /* sort cell of rapidity (0: 0.05) */
+    int32_t merge_chunk;    /* FP32-weight form: same-event tile pairs between two
+                               merges of the partials, <= 16384 (0: 16384) */
+    int32_t use_graph;      /* 1: launch the sort-cull-bin pipeline as a CUDA graph,
+                               captured when a batch of the same shape comes twice in
+                               a row and re-launched while it repeats; 0: direct
+                               launches */
+} hbt_tuning;
+
+hbt_status hbt_set_tuning(hbt_ctx *ctx, const hbt_tuning *t);
+hbt_status hbt_get_tuning(hbt_ctx *ctx, hbt_tuning *t);
+
+/* Autotuner.  No counterpart in the reference.  Times candidate tunings
+ * (sort cells, CTAs per SM, merge chunk) on up to `max_pairs` candidate
+ * pairs of the batch (device arrays, jobs taken in order; 0: 2e9) with
+ * scratch histograms, keeps the fastest for this context and returns it
+ * with its time.  The context's histograms are not touched. */
+hbt_status hbt_autotune_batch(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs,
+                              double max_pairs, hbt_tuning *best, double *best_ms);
 
 /* Waits for the context's stream, polling up to timeout_us microseconds
  * (0: wait without limit).  Returns HBT_ERR_TIMEOUT if work is still
