@@ -557,7 +557,11 @@ def main() -> None:
     torch.cuda.synchronize()
     launches = eng.stats()["launches"] - launches0
     t_ms = sum(ms_steps)
+    reduced_bins = None
     if world > 1:
+        # replicas: one histogram sum at the end (outside the timed region)
+        from hadronic_afterburner_toolkit_gb300 import replicas
+        reduced_bins = int(replicas.allreduce_hist(eng.hist(), device=dev)["count"].sum())
         t = torch.tensor([t_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_ms = float(t.item())
@@ -691,6 +695,7 @@ def main() -> None:
                 "pairs_per_step": pairs_all / args.steps / max(world, 1),
                 "binned_same_fraction": round(fr[4], 4),
                 "gpu_launches": launches,
+                "replica_reduction_binned_pairs": reduced_bins,
                 "clocks": clk.summary(),
                 "roofline": roofline,
                 "plain_kernel": plain,
