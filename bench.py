@@ -30,6 +30,9 @@ mu in [50, 2000], pi+ or K+, qnpts in {21, 41, 61}, q_max in [0.1, 0.3] GeV,
 event) through the serving loop, with p50 / p99 request latency and pairs/s,
 against the plain per-job path.
 
+"ingest": the sample reader on a 200-event central-like gzip file, the
+line-by-line reader against the block reader (parallel parse).
+
 --impl reference times the reference algorithm on the host cores (the CPU
 oracle, multi-threaded) on a bounded sample of the same workload.
 """
@@ -396,6 +399,70 @@ def uneven_leg(E, torch, dev, stream, flush, local, steps=2) -> dict:
     return out
 
 
+INGEST_PARAMS = """echo_level = 0
+read_in_mode = 10
+read_in_real_mixed_events = 0
+particle_monval = 211
+resonance_weak_feed_down_flag = 0
+resonance_feed_down_flag = 0
+event_buffer_size = 150000
+rapidity_shift = 0.0
+"""
+
+
+def ingest_leg(n_events: int = 200, seed: int = 3) -> dict:
+    """The reader (read_in_mode 10: gzip text, ~100 oversampled events per
+    150k-particle buffer as on the central workload): the line-by-line
+    reader (strtod per number, the reference's reading rule) against the
+    block reader (inflate on its own thread, parallel from_chars parse and
+    boost on all host threads) and the binary sidecar (written on a first
+    pass, replayed after); all give bit-identical particles
+    (tests/test_host_cpu.py).  text_MB_per_s counts the bytes each source
+    read (text, or the sidecar's records)."""
+    import ctypes
+    from hadronic_afterburner_toolkit_gb300 import build, synth
+    L = ctypes.CDLL(build.build_host())
+    L.hbt_host_time_reader.restype = ctypes.c_int
+    L.hbt_host_time_reader.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
+                                       ctypes.POINTER(ctypes.c_char_p),
+                                       ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64)]
+    d = tempfile.mkdtemp(prefix="hbt_ingest_")
+    res = os.path.join(d, "results")
+    os.makedirs(res)
+    ev = synth.central_pions(n_events=n_events, seed=seed)
+    synth.write_mode10(os.path.join(res, "particle_samples.gz"), ev)
+    pfile = os.path.join(d, "parameters.dat")
+    with open(pfile, "w") as f:
+        f.write(INGEST_PARAMS)
+    out = {"events": n_events, "particles": int(ev.px.size),
+           "gz_bytes": os.path.getsize(os.path.join(res, "particle_samples.gz")),
+           "host_threads": os.cpu_count()}
+    for label, args, reps in (("line-reader", ["hbt_fast_reader=0"], 2),
+                              ("block-reader", ["hbt_fast_reader=1"], 2),
+                              ("block-reader-writing-cache", ["hbt_binary_cache=1"], 1),
+                              ("binary-cache-replay", ["hbt_binary_cache=1"], 2)):
+        best = None
+        for _ in range(reps):
+            argv = (ctypes.c_char_p * len(args))(*[a.encode() for a in args])
+            sec, npart, nbytes = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+            rc = L.hbt_host_time_reader(pfile.encode(), res.encode(), len(args), argv,
+                                        ctypes.byref(sec), ctypes.byref(npart), ctypes.byref(nbytes))
+            if rc != 0:
+                raise RuntimeError("reader failed")
+            if best is None or sec.value < best[0]:
+                best = (sec.value, npart.value, nbytes.value)
+        out[label] = {"seconds": best[0], "particles_per_s": best[1] / best[0],
+                      "text_MB_per_s": best[2] / best[0] / 1e6}
+    out["speedup"] = out["line-reader"]["seconds"] / out["block-reader"]["seconds"]
+    out["speedup_cached"] = (out["line-reader"]["seconds"] /
+                             out["binary-cache-replay"]["seconds"])
+    import shutil
+    shutil.rmtree(d, ignore_errors=True)
+    return out
+
+
 def make_requests(n_jobs: int, seed: int = 5):
     """Requests of the serving workload: 10-500 events each, multiplicity
     Poisson(mu) with mu uniform in [50, 2000], pi+ or K+, qnpts in
@@ -483,6 +550,8 @@ def main() -> None:
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the Poisson request stream through the serving loop")
     ap.add_argument("--serving-jobs", type=int, default=48)
+    ap.add_argument("--no-ingest", action="store_true",
+                    help="skip the reader timing (line-by-line against block reader)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -669,7 +738,9 @@ def main() -> None:
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(groups[0], p, nthreads=1)
 
-    uneven = serving = None
+    uneven = serving = ingest = None
+    if not args.no_ingest and rank == 0:
+        ingest = ingest_leg()
     if not args.no_uneven:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
@@ -706,6 +777,7 @@ def main() -> None:
                 "cpu_baseline": cpu,
                 "uneven": uneven,
                 "serving": serving,
+                "ingest": ingest,
                 "stats": st}
         print(json.dumps(line))
     eng.close()

@@ -122,7 +122,7 @@ def build_host(force: bool = False) -> str | None:
     deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST)] + [gpu]
     if force or _newer(lib, deps) or _newer(exe, deps):
         cxx = os.environ.get("CXX", "g++")
-        flags = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+        flags = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-pthread",
                  "-I" + INCLUDE, "-I" + HOST]
         zlib = _has_zlib(cxx)
         if zlib:

@@ -1,4 +1,6 @@
 // C ABI of the drop-in host side (include/hbt_host.h).
+#include <chrono>
+#include <cstring>
 #include <iostream>
 #include <memory>
 #include <stdexcept>
@@ -64,6 +66,106 @@ int hbt_host_scan_buffers(const char *param_file, const char *results_path, int3
             b++;
         }
         return b;
+    } catch (const std::exception &e) {
+        std::cerr << "error: " << e.what() << std::endl;
+        return -1;
+    }
+}
+
+}  // extern "C"
+
+namespace {
+
+struct Fnv {
+    uint64_t h = 1469598103934665603ull;
+    void add(const void *p, size_t n) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        for (size_t k = 0; k < n; k++) {
+            h ^= c[k];
+            h *= 1099511628211ull;
+        }
+    }
+    template <class T>
+    void add(const T &v) {
+        add(&v, sizeof(v));
+    }
+};
+
+void hash_events(Fnv &f, const particleSamples &ps, bool mixed) {
+    const int ne = mixed ? ps.get_number_of_mixed_events() : ps.get_number_of_events();
+    f.add(ne);
+    for (int e = 0; e < ne; e++) {
+        const std::vector<particle_info> &ev = mixed ? ps.mixed_event(e) : ps.event(e);
+        f.add(static_cast<int64_t>(ev.size()));
+        for (const particle_info &p : ev) {
+            f.add(p.monval);
+            const double v[] = {p.mass, p.px, p.py, p.pz, p.E, p.x, p.y, p.z, p.t,
+                                p.rap_y, p.rap_eta, p.pT, p.phi_p};
+            f.add(v, sizeof(v));
+        }
+    }
+}
+
+void load_params(ParameterReader &prm, const char *param_file, int32_t n_args, char **args) {
+    prm.readFromFile(param_file);
+    if (n_args > 0) {
+        // readFromArguments skips argv[0]
+        std::vector<char *> argv(n_args + 1);
+        argv[0] = const_cast<char *>("hbt");
+        for (int k = 0; k < n_args; k++) argv[k + 1] = args[k];
+        prm.readFromArguments(n_args + 1, argv.data());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hbt_host_digest_buffers(const char *param_file, const char *results_path, int32_t n_args,
+                            char **args, int32_t cap, uint64_t *digest) {
+    try {
+        ParameterReader prm;
+        load_params(prm, param_file, n_args, args);
+        auto rng = std::make_shared<RandomUtil::Random>(1);
+        particleSamples ps(prm, results_path, rng);
+        int b = 0;
+        while (!ps.end_of_file()) {
+            ps.read_in_particle_samples_and_filter();
+            ps.read_in_particle_samples_mixed_event_and_filter();
+            if (b < cap) {
+                Fnv f;
+                hash_events(f, ps, false);
+                hash_events(f, ps, true);
+                digest[b] = f.h;
+            }
+            b++;
+        }
+        return b;
+    } catch (const std::exception &e) {
+        std::cerr << "error: " << e.what() << std::endl;
+        return -1;
+    }
+}
+
+int hbt_host_time_reader(const char *param_file, const char *results_path, int32_t n_args,
+                         char **args, double *seconds, int64_t *particles, int64_t *text_bytes) {
+    try {
+        ParameterReader prm;
+        load_params(prm, param_file, n_args, args);
+        auto rng = std::make_shared<RandomUtil::Random>(1);
+        const auto t0 = std::chrono::steady_clock::now();
+        particleSamples ps(prm, results_path, rng);
+        int64_t np = 0;
+        while (!ps.end_of_file()) {
+            ps.read_in_particle_samples_and_filter();
+            ps.read_in_particle_samples_mixed_event_and_filter();
+            np += ps.last_buffer_particles();
+        }
+        const auto t1 = std::chrono::steady_clock::now();
+        if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+        if (particles) *particles = np;
+        if (text_bytes) *text_bytes = ps.text_bytes();
+        return 0;
     } catch (const std::exception &e) {
         std::cerr << "error: " << e.what() << std::endl;
         return -1;

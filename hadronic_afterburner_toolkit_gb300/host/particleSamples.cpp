@@ -8,106 +8,6 @@
 #include <sstream>
 #include <stdexcept>
 
-#ifdef HBT_HAVE_ZLIB
-#include <zlib.h>
-#endif
-
-namespace hbt {
-
-// Line reader over a plain or gzip-compressed text file.  next() returns the
-// line without its '\n'; eof() is true once a read ran into the end of the
-// file, which is the condition the reference's readers test after reading an
-// event header (gzeof / ifstream::eof).
-class LineSource {
-  public:
-    LineSource(const std::string &path, bool gz) : gz_(gz) {
-        if (gz_) {
-#ifdef HBT_HAVE_ZLIB
-            gzf_ = gzopen(path.c_str(), "rb");
-            ok_ = gzf_ != nullptr;
-            if (ok_) gzbuffer(static_cast<gzFile>(gzf_), 1 << 20);
-#else
-            const std::string cmd = "gzip -dc '" + path + "'";
-            pipe_ = popen(cmd.c_str(), "r");
-            std::ifstream probe(path.c_str());
-            ok_ = pipe_ != nullptr && probe.good();
-#endif
-        } else {
-            fs_.open(path.c_str());
-            ok_ = fs_.is_open();
-        }
-        buf_.resize(1 << 16);
-    }
-    ~LineSource() {
-#ifdef HBT_HAVE_ZLIB
-        if (gzf_) gzclose(static_cast<gzFile>(gzf_));
-#else
-        if (pipe_) pclose(pipe_);
-#endif
-    }
-    bool ok() const { return ok_; }
-    bool eof() const { return eof_; }
-
-    std::string next() {
-        std::string line;
-        if (!gz_) {
-            if (!std::getline(fs_, line)) eof_ = true;
-            else if (fs_.eof()) eof_ = true;
-            return line;
-        }
-        for (;;) {
-            char *got = nullptr;
-#ifdef HBT_HAVE_ZLIB
-            got = gzgets(static_cast<gzFile>(gzf_), &buf_[0], static_cast<int>(buf_.size()));
-#else
-            got = fgets(&buf_[0], static_cast<int>(buf_.size()), pipe_);
-#endif
-            if (!got) {
-                eof_ = true;
-                return line;
-            }
-            const size_t len = strlen(got);
-            if (len > 0 && got[len - 1] == '\n') {
-                line.append(got, len - 1);
-                return line;
-            }
-            line.append(got, len);
-            if (len + 1 < buf_.size()) {  // short read without newline: end of file
-                eof_ = true;
-                return line;
-            }
-        }
-    }
-
-  private:
-    bool gz_;
-    bool ok_ = false;
-    bool eof_ = false;
-    std::ifstream fs_;
-    void *gzf_ = nullptr;
-    FILE *pipe_ = nullptr;
-    std::vector<char> buf_;
-};
-
-}  // namespace hbt
-
-namespace {
-
-// Parses `count` numbers separated by blanks; returns how many were read.
-int parse_numbers(const char *s, double *out, int count) {
-    int k = 0;
-    char *end = nullptr;
-    while (k < count) {
-        const double v = strtod(s, &end);
-        if (end == s) break;
-        out[k++] = v;
-        s = end;
-    }
-    return k;
-}
-
-}  // namespace
-
 particleSamples::particleSamples(ParameterReader &paraRdr, std::string path,
                                  std::shared_ptr<RandomUtil::Random> ran_gen)
     : paraRdr_(paraRdr), path_(path) {
@@ -136,20 +36,27 @@ particleSamples::particleSamples(ParameterReader &paraRdr, std::string path,
                                  std::to_string(read_in_mode_) +
                                  " is not supported by this build (0 and 10 are)");
     }
-    in_.reset(new hbt::LineSource(file, gz));
+    const bool fast =
+        !paraRdr_.exist("hbt_fast_reader") || paraRdr_.getVal("hbt_fast_reader") != 0;
+    reader_threads_ = paraRdr_.exist("hbt_reader_threads")
+                          ? static_cast<int>(paraRdr_.getVal("hbt_reader_threads"))
+                          : 0;
+    const int threads = reader_threads_;
+    const bool cache =
+        paraRdr_.exist("hbt_binary_cache") && paraRdr_.getVal("hbt_binary_cache") != 0;
+    auto open = [&](const std::string &f) {
+        if (!fast) return hbt::make_line_source(f, gz, read_in_mode_);
+        return cache ? hbt::make_cached_source(f, gz, read_in_mode_, threads)
+                     : hbt::make_block_source(f, gz, read_in_mode_, threads);
+    };
+    in_ = open(file);
     if (!in_->ok())
         throw std::runtime_error("particleSamples:: Error: input file: " + file + " can not open!");
     if (read_mixed_events_) {
-        in_mixed_.reset(new hbt::LineSource(file_mixed, gz));
+        in_mixed_ = open(file_mixed);
         if (!in_mixed_->ok())
             throw std::runtime_error("particleSamples:: Error: input file: " + file_mixed +
                                      " can not open!");
-    }
-    if (read_in_mode_ == 0) {  // OSCAR header
-        for (int k = 0; k < 3; k++) {
-            in_->next();
-            if (in_mixed_) in_mixed_->next();
-        }
     }
     list_ = &filtered_;
     mixed_list_ = read_mixed_events_ ? &filtered_mixed_ : &filtered_;
@@ -158,75 +65,28 @@ particleSamples::particleSamples(ParameterReader &paraRdr, std::string path,
 particleSamples::~particleSamples() = default;
 
 bool particleSamples::end_of_file() const { return in_->eof(); }
-bool particleSamples::end_of_file_mixed_event() const {
-    return in_mixed_ ? in_mixed_->eof() : in_->eof();
+
+long long particleSamples::last_buffer_particles() const {
+    long long n = 0;
+    for (const auto &ev : full_) n += static_cast<long long>(ev.size());
+    if (read_mixed_events_)
+        for (const auto &ev : full_mixed_) n += static_cast<long long>(ev.size());
+    return n;
 }
 
-// One buffer: whole events until the particle count reaches the buffer size
-// (src/particleSamples.cpp:1247-1286 for mode 10, :680-714 for mode 0).
-int particleSamples::read_buffer(hbt::LineSource &src, EventList &out) {
-    out.clear();
-    long num_particles = 0;
-    double v[11];
-    while (num_particles < event_buffer_size_) {
-        const std::string head = src.next();
-        if (src.eof()) break;
-        int n_particle = 0;
-        if (read_in_mode_ == 10) {
-            n_particle = std::atoi(head.c_str());
-        } else {
-            std::istringstream hs(head);
-            int event_id = 0;
-            hs >> event_id >> n_particle;
-        }
-        out.emplace_back();
-        std::vector<particle_info> &ev = out.back();
-        ev.reserve(n_particle);
-        for (int k = 0; k < n_particle; k++) {
-            const std::string line = src.next();
-            particle_info p;
-            std::memset(&p, 0, sizeof(p));
-            if (read_in_mode_ == 10) {
-                // monval mass t x y z E px py pz
-                if (parse_numbers(line.c_str(), v, 10) != 10)
-                    throw std::runtime_error("particleSamples: truncated or malformed particle line");
-                p.monval = static_cast<int>(v[0]);
-                p.mass = v[1];
-                p.t = v[2];
-                p.x = v[3];
-                p.y = v[4];
-                p.z = v[5];
-                p.E = v[6];
-                p.px = v[7];
-                p.py = v[8];
-                p.pz = v[9];
-            } else {
-                // index monval px py pz E mass x y z t
-                if (parse_numbers(line.c_str(), v, 11) != 11)
-                    throw std::runtime_error("particleSamples: truncated or malformed OSCAR line");
-                p.monval = static_cast<int>(v[1]);
-                p.px = v[2];
-                p.py = v[3];
-                p.pz = v[4];
-                p.E = v[5];
-                p.mass = v[6];
-                p.x = v[7];
-                p.y = v[8];
-                p.z = v[9];
-                p.t = v[10];
-            }
-            ev.push_back(p);
-        }
-        num_particles += n_particle;
-    }
-    return static_cast<int>(out.size());
+long long particleSamples::text_bytes() const {
+    return in_->text_bytes() + (in_mixed_ ? in_mixed_->text_bytes() : 0);
+}
+bool particleSamples::end_of_file_mixed_event() const {
+    return in_mixed_ ? in_mixed_->eof() : in_->eof();
 }
 
 // particleSamples::boostParticles (src/particleSamples.cpp:442-468).
 void particleSamples::boost(EventList &evs) const {
     const double ch = cosh(rap_shift_), sh = sinh(rap_shift_);
-    for (auto &ev : evs)
-        for (auto &p : ev) {
+    hbt::parallel_ranges(static_cast<long>(evs.size()), reader_threads_, 8, [&](long lo, long hi) {
+        for (long e = lo; e < hi; e++)
+            for (auto &p : evs[e]) {
             p.pT = sqrt(p.px * p.px + p.py * p.py);
             const double mT = sqrt(p.pT * p.pT + p.mass * p.mass);
             p.phi_p = atan2(p.py, p.px);
@@ -234,19 +94,20 @@ void particleSamples::boost(EventList &evs) const {
             const double pz = p.pz * ch + p.E * sh;
             p.E = E;
             p.pz = pz;
-            p.rap_y = asinh(p.pz / mT);
-            p.rap_eta = asinh(p.pz / p.pT);
-        }
+                p.rap_y = asinh(p.pz / mT);
+                p.rap_eta = asinh(p.pz / p.pT);
+            }
+    });
 }
 
 int particleSamples::read_in_particle_samples() {
-    read_buffer(*in_, full_);
+    in_->read_buffer(event_buffer_size_, full_);
     boost(full_);
     return static_cast<int>(full_.size());
 }
 
 int particleSamples::read_in_particle_samples_mixed_event() {
-    read_buffer(*in_mixed_, full_mixed_);
+    in_mixed_->read_buffer(event_buffer_size_, full_mixed_);
     boost(full_mixed_);
     return static_cast<int>(full_mixed_.size());
 }

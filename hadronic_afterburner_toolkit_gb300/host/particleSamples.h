@@ -7,7 +7,7 @@
 //    *_mixed_event files when read_in_real_mixed_events = 1;
 //  - buffering: whole events are read until the particle count reaches
 //    event_buffer_size (particleSamples.cpp:1256-1283, :689-712);
-//  - rapidity_shift boost of E and pz (:442-468);
+//  - rapidity_shift boost of E and pz (:442-468), on all host threads;
 //  - particle_monval filter (:1329-1346): a Monte-Carlo number, or the
 //    class codes 9999 / +-9998 / +-9997 / +-9996 (charged, charge sign,
 //    baryon sign, strangeness sign) looked up in EOS/pdg.dat.
@@ -23,11 +23,8 @@
 
 #include "ParameterReader.h"
 #include "Random.h"
+#include "SampleSource.h"
 #include "particle_info.h"
-
-namespace hbt {
-class LineSource;
-}
 
 class particleSamples {
   public:
@@ -42,6 +39,10 @@ class particleSamples {
 
     bool end_of_file() const;
     bool end_of_file_mixed_event() const;
+    // Particles of the last buffer read, before the species filter (same
+    // events plus a separate mixed pool), and text bytes read so far.
+    long long last_buffer_particles() const;
+    long long text_bytes() const;
     int get_event_buffer_size() const { return event_buffer_size_; }
 
     int get_number_of_events() const { return static_cast<int>(list_->size()); }
@@ -65,7 +66,7 @@ class particleSamples {
     }
 
   private:
-    typedef std::vector<std::vector<particle_info>> EventList;
+    typedef hbt::EventList EventList;
 
     const ParameterReader paraRdr_;
     const std::string path_;
@@ -76,7 +77,11 @@ class particleSamples {
     bool read_mixed_events_;
     int particle_monval_;
 
-    std::unique_ptr<hbt::LineSource> in_, in_mixed_;
+    // text sources: the block reader (parallel parse, key hbt_fast_reader =
+    // 1, the default; with hbt_binary_cache = 1 it writes and later replays
+    // a binary sidecar of the file) or the line-by-line reader
+    // (hbt_fast_reader = 0)
+    std::unique_ptr<hbt::SampleSource> in_, in_mixed_;
     EventList full_, full_mixed_, filtered_, filtered_mixed_;
     EventList *list_, *mixed_list_;
 
@@ -84,8 +89,8 @@ class particleSamples {
     // loaded on first use by a class code.
     std::map<int, int> charge_, baryon_, strange_;
     bool pdg_loaded_ = false;
+    int reader_threads_ = 0;  // host threads of the reader and boost (0: all)
 
-    int read_buffer(hbt::LineSource &src, EventList &out);
     void boost(EventList &evs) const;
     void filter(const EventList &full, EventList &out);
     bool pick(int monval);

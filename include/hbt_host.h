@@ -3,7 +3,7 @@
  *
  * The C++ classes ParameterReader, RandomUtil::Random, particleSamples,
  * HBT_correlation and Analysis under hadronic_afterburner_toolkit_gb300/host
- * are source-compatible with the reference's (src/*.h of
+ * are source-compatible with the reference's (the src/ headers of
  * chunshen1987/hadronic_afterburner_toolkit); C++ callers use them directly.
  * These entry points serve callers through an FFI.
  */
@@ -46,6 +46,25 @@ int hbt_host_write(const hbt_params *params, const char *path, int32_t eco_outpu
 int hbt_host_scan_buffers(const char *param_file, const char *results_path, int32_t cap,
                           int32_t *nev, int64_t *n_particles, int32_t *mixed_nev,
                           int64_t *n_mixed_particles);
+
+/* The reader's output, buffer by buffer, as a digest: for each buffer a
+ * 64-bit FNV-1a hash over the event count, every event's particle count and
+ * every field of every particle (bit patterns, after the species filter and
+ * the rapidity boost), same-event list then mixed pool.  `args` are extra
+ * "key=value" strings applied after the parameter file (e.g.
+ * "hbt_fast_reader=0" selects the line-by-line reader).  Fills up to `cap`
+ * digests; returns the number of buffers, or -1 on error.  No counterpart in
+ * the reference: it lets two readers be compared without moving the
+ * particles through the FFI. */
+int hbt_host_digest_buffers(const char *param_file, const char *results_path, int32_t n_args,
+                            char **args, int32_t cap, uint64_t *digest);
+
+/* Reads every buffer of the samples (same-event list and mixed pool, with
+ * the species filter and boost) and returns the wall time in seconds, the
+ * particles read (before the filter) and the bytes of decompressed text;
+ * `args` as above.  Returns 0, or -1 on error.  For timing the reader. */
+int hbt_host_time_reader(const char *param_file, const char *results_path, int32_t n_args,
+                         char **args, double *seconds, int64_t *particles, int64_t *text_bytes);
 
 #ifdef __cplusplus
 }

@@ -3,6 +3,7 @@ reference-format writer of libhbt_host.so, checked on the golden cases."""
 import ctypes
 import os
 import tarfile
+import zlib
 
 import numpy as np
 import pytest
@@ -101,3 +102,127 @@ def test_writer_reproduces_reference_files(host, name, tmp_path):
     assert sorted(got) == sorted(want)
     for f in want:
         assert got[f] == want[f], f
+
+
+# ------------------------------------------------------------------ readers
+
+def _bind_digest(L):
+    L.hbt_host_digest_buffers.restype = ctypes.c_int
+    L.hbt_host_digest_buffers.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
+                                          ctypes.POINTER(ctypes.c_char_p), ctypes.c_int32,
+                                          ctypes.POINTER(ctypes.c_uint64)]
+
+
+def _digests(L, pfile, res, args, cap=4096):
+    _bind_digest(L)
+    argv = (ctypes.c_char_p * max(len(args), 1))(*[a.encode() for a in args])
+    out = (ctypes.c_uint64 * cap)()
+    n = L.hbt_host_digest_buffers(pfile.encode(), res.encode(), len(args), argv, cap, out)
+    return n, list(out[:max(n, 0)])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_block_reader_equals_line_reader_on_golden_inputs(host, name, tmp_path):
+    """The parallel block reader gives bit-identical particles, buffer by
+    buffer, to the line-by-line reader (the reference's reading rule)."""
+    pfile, res = _stage(name, str(tmp_path))
+    n0, d0 = _digests(host, pfile, res, ["hbt_fast_reader=0"])
+    assert n0 > 0
+    for threads in (0, 1, 3):
+        n1, d1 = _digests(host, pfile, res, ["hbt_fast_reader=1",
+                                             "hbt_reader_threads=%d" % threads])
+        assert (n1, d1) == (n0, d0)
+
+
+def _write_text(path, text, gz):
+    if gz:
+        import gzip
+        with gzip.open(path, "wt", newline="") as f:
+            f.write(text)
+    else:
+        with open(path, "w", newline="") as f:
+            f.write(text)
+
+
+def _mode10_text(rng, mults, fmt="%.17g", eol="\n", final_newline=True, plus=False):
+    lines = []
+    for m in mults:
+        lines.append("%d" % m)
+        for _ in range(m):
+            v = [211, 0.13957] + list(rng.normal(0, 3, 4)) + [abs(rng.normal(1, 0.3)) + 0.2] + \
+                list(rng.normal(0, 0.4, 3))
+            tok = ["%d" % v[0]] + [fmt % x for x in v[1:]]
+            if plus:
+                tok = [("+" + t if not t.startswith("-") and k % 3 == 1 else t)
+                       for k, t in enumerate(tok)]
+            lines.append(" ".join(tok))
+    text = eol.join(lines)
+    return text + eol if final_newline else text
+
+
+@pytest.mark.parametrize("variant", ["plain", "no_final_newline", "crlf", "plus_signs",
+                                     "scientific", "empty_events", "exact_fill"])
+def test_block_reader_equals_line_reader_on_edge_files(host, variant, tmp_path):
+    rng = np.random.default_rng(zlib.crc32(variant.encode()))
+    mults = list(rng.integers(0, 40, size=23))
+    kw = {}
+    size = 100
+    if variant == "no_final_newline":
+        kw["final_newline"] = False
+    elif variant == "crlf":
+        kw["eol"] = "\r\n"
+    elif variant == "plus_signs":
+        kw["plus"] = True
+    elif variant == "scientific":
+        kw["fmt"] = "%.10E"
+    elif variant == "empty_events":
+        mults = [0, 0, 5, 0, 17, 0, 0, 3, 0]
+    elif variant == "exact_fill":
+        mults = [25] * 8   # buffers end exactly at the end of the file
+    res = tmp_path / "results"
+    res.mkdir()
+    _write_text(str(res / "particle_samples.gz"), _mode10_text(rng, mults, **kw), gz=True)
+    prm = open(os.path.join(oracle_lib.GOLDEN, "basic", "parameters.dat")).read()
+    prm = prm.replace("event_buffer_size = 120", "event_buffer_size = %d" % size)
+    pfile = tmp_path / "parameters.dat"
+    pfile.write_text(prm)
+    n0, d0 = _digests(host, str(pfile), str(res), ["hbt_fast_reader=0"])
+    n1, d1 = _digests(host, str(pfile), str(res), ["hbt_fast_reader=1", "hbt_reader_threads=4"])
+    assert n0 > 0
+    assert (n1, d1) == (n0, d0)
+    # the binary sidecar: written on the first pass, replayed on the second
+    cache = res / "particle_samples.gz.hbtcache"
+    assert not cache.exists()
+    n2, d2 = _digests(host, str(pfile), str(res), ["hbt_binary_cache=1"])
+    assert cache.exists()
+    n3, d3 = _digests(host, str(pfile), str(res), ["hbt_binary_cache=1"])
+    assert (n2, d2) == (n0, d0) and (n3, d3) == (n0, d0)
+    # a changed source file invalidates the sidecar
+    os.utime(res / "particle_samples.gz", ns=(1, 1))
+    n4, d4 = _digests(host, str(pfile), str(res), ["hbt_binary_cache=1"])
+    assert (n4, d4) == (n0, d0)
+
+
+def test_block_reader_reads_oscar_and_rejects_malformed_lines(host, tmp_path):
+    rng = np.random.default_rng(3)
+    ev = synth.generate(7, 30.0, seed=4)
+    res = tmp_path / "results"
+    res.mkdir()
+    synth.write_oscar(str(res / "OSCAR.DAT"), ev)
+    prm = open(os.path.join(oracle_lib.GOLDEN, "basic", "parameters.dat")).read()
+    prm = prm.replace("read_in_mode = 10", "read_in_mode = 0")
+    pfile = tmp_path / "parameters.dat"
+    pfile.write_text(prm)
+    n0, d0 = _digests(host, str(pfile), str(res), ["hbt_fast_reader=0"])
+    n1, d1 = _digests(host, str(pfile), str(res), ["hbt_fast_reader=1"])
+    assert n0 > 0 and (n1, d1) == (n0, d0)
+    # a particle line with a missing column: both readers fail
+    bad = _mode10_text(rng, [3, 4]).splitlines()
+    bad[3] = " ".join(bad[3].split()[:-1])
+    res2 = tmp_path / "bad"
+    res2.mkdir()
+    _write_text(str(res2 / "particle_samples.gz"), "\n".join(bad) + "\n", gz=True)
+    pfile.write_text(open(os.path.join(oracle_lib.GOLDEN, "basic", "parameters.dat")).read())
+    for fast in (0, 1):
+        n, _ = _digests(host, str(pfile), str(res2), ["hbt_fast_reader=%d" % fast])
+        assert n == -1
