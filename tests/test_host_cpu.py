@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import oracle_lib
+import parity
 from hadronic_afterburner_toolkit_gb300 import build, engine, synth
 
 CASES = sorted(d for d in os.listdir(oracle_lib.GOLDEN)
@@ -101,7 +102,7 @@ def test_writer_reproduces_reference_files(host, name, tmp_path):
     got = {f: open(os.path.join(out, f), "rb").read() for f in os.listdir(out)}
     assert sorted(got) == sorted(want)
     for f in want:
-        assert got[f] == want[f], f
+        parity.same_output_file(got[f], want[f], f)
 
 
 # ------------------------------------------------------------------ readers
