@@ -31,7 +31,10 @@ event) through the serving loop, with p50 / p99 request latency and pairs/s,
 against the plain per-job path.
 
 "ingest": the sample reader on a 200-event central-like gzip file, the
-line-by-line reader against the block reader (parallel parse).
+line-by-line reader against the block reader (parallel parse) and the
+binary sidecar, plus the writer on the central histograms.  "average": the
+event averaging of HBT files over event folders against a restatement of
+the reference's averaging script.
 
 --impl reference times the reference algorithm on the host cores (the CPU
 oracle, multi-threaded) on a bounded sample of the same workload.
@@ -455,12 +458,91 @@ def ingest_leg(n_events: int = 200, seed: int = 3) -> dict:
                 best = (sec.value, npart.value, nbytes.value)
         out[label] = {"seconds": best[0], "particles_per_s": best[1] / best[0],
                       "text_MB_per_s": best[2] / best[0] / 1e6}
+    # the writer: the central workload's 64 files (9 K_T edges x 8 K_phi,
+    # 41^3 rows each, ~408 MB of text) from random histograms
+    L.hbt_host_write.restype = ctypes.c_int
+    _PD = ctypes.POINTER(ctypes.c_double)
+    _PU = ctypes.POINTER(ctypes.c_uint64)
+    from hadronic_afterburner_toolkit_gb300 import engine as E
+    L.hbt_host_write.argtypes = [ctypes.POINTER(E.HbtParams), ctypes.c_char_p,
+                                 ctypes.c_int32] + [_PD] * 10 + [_PU] * 4
+    hp = E.HbtParams(qnpts=41, q_min=-0.15, q_max=0.15, n_KT=9, KT_min=0.0, KT_max=1.0,
+                     n_Kphi=8, azimuthal_flag=1, invariant_radius_flag=0)
+    nb = 72 * 41 ** 3
+    rng = np.random.default_rng(1)
+    arr = [rng.integers(0, 100, nb).astype(float)] + [rng.normal(0, 1, nb) for _ in range(4)] + \
+          [rng.integers(0, 200, nb).astype(float)] + [np.zeros(9 * 41) for _ in range(4)]
+    ctr = [np.full(72, 1000, np.uint64), np.full(72, 1200, np.uint64), np.zeros(9, np.uint64),
+           np.zeros(9, np.uint64)]
+    wdir = os.path.join(d, "written")
+    os.makedirs(wdir)
+    t0 = time.perf_counter()
+    rc = L.hbt_host_write(ctypes.byref(hp), wdir.encode(), 0, *[a.ctypes.data_as(_PD) for a in arr],
+                          *[c.ctypes.data_as(_PU) for c in ctr])
+    tw = time.perf_counter() - t0
+    wbytes = sum(os.path.getsize(os.path.join(wdir, f)) for f in os.listdir(wdir))
+    out["writer"] = {"ok": rc == 0, "files": len(os.listdir(wdir)), "MB": wbytes / 1e6,
+                     "seconds": tw, "MB_per_s": wbytes / 1e6 / tw}
     out["speedup"] = out["line-reader"]["seconds"] / out["block-reader"]["seconds"]
     out["speedup_cached"] = (out["line-reader"]["seconds"] /
                              out["binary-cache-replay"]["seconds"])
     import shutil
     shutil.rmtree(d, ignore_errors=True)
     return out
+
+
+def average_leg(n_events: int = 12, seed: int = 11) -> dict:
+    """Event averaging of the HBT files over event folders: 12 UrQMD*
+    folders, each with the 4 files of a 21^3 grid and 5 K_T edges
+    (9261 rows x 5 columns per file, written by the drop-in's writer from
+    random histograms): hbt_host_average_events on all host threads against
+    the CPU restatement of the reference's averaging script (numpy.loadtxt /
+    savetxt, oracle/average_events.py)."""
+    import ctypes
+    import shutil
+    from hadronic_afterburner_toolkit_gb300 import build, engine as E
+    L = ctypes.CDLL(build.build_host())
+    _PD = ctypes.POINTER(ctypes.c_double)
+    _PU = ctypes.POINTER(ctypes.c_uint64)
+    L.hbt_host_write.restype = ctypes.c_int
+    L.hbt_host_write.argtypes = [ctypes.POINTER(E.HbtParams), ctypes.c_char_p,
+                                 ctypes.c_int32] + [_PD] * 10 + [_PU] * 4
+    L.hbt_host_average_events.restype = ctypes.c_int
+    L.hbt_host_average_events.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32]
+    d = tempfile.mkdtemp(prefix="hbt_avg_")
+    work = os.path.join(d, "work")
+    hp = E.HbtParams(qnpts=21, q_min=-0.15, q_max=0.15, n_KT=5, KT_min=0.0, KT_max=1.0,
+                     n_Kphi=1, azimuthal_flag=0, invariant_radius_flag=0)
+    nb = 5 * 21 ** 3
+    rng = np.random.default_rng(seed)
+    for ev in range(n_events):
+        res = os.path.join(work, "UrQMDev_%d" % ev, "UrQMD_results")
+        os.makedirs(res)
+        arr = [rng.integers(0, 60, nb).astype(float)] + [rng.normal(0, 1, nb) for _ in range(4)] + \
+              [rng.integers(0, 90, nb).astype(float)] + [np.zeros(5 * 21) for _ in range(4)]
+        ctr = [np.full(5, 1000, np.uint64), np.full(5, 1100, np.uint64), np.zeros(5, np.uint64),
+               np.zeros(5, np.uint64)]
+        L.hbt_host_write(ctypes.byref(hp), res.encode(), 0, *[a.ctypes.data_as(_PD) for a in arr],
+                         *[c.ctypes.data_as(_PU) for c in ctr])
+    text_mb = sum(os.path.getsize(os.path.join(r, f)) for r, _, fs in os.walk(work)
+                  for f in fs) / 1e6
+    t0 = time.perf_counter()
+    n = L.hbt_host_average_events(work.encode(), os.path.join(d, "ours").encode(), 0)
+    t_ours = time.perf_counter() - t0
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import average_events
+    t0 = time.perf_counter()
+    average_events.average_events(work, os.path.join(d, "port"))
+    t_port = time.perf_counter() - t0
+    same = all(open(os.path.join(d, "ours", f), "rb").read() ==
+               open(os.path.join(d, "port", f), "rb").read()
+               for f in os.listdir(os.path.join(d, "port")))
+    shutil.rmtree(d, ignore_errors=True)
+    return {"folders": n_events, "files": n, "text_MB": text_mb, "seconds": t_ours,
+            "MB_per_s": text_mb / t_ours, "cpu_port_seconds": t_port,
+            "cpu_port": "numpy loadtxt/savetxt restatement of the reference script, 1 thread",
+            "speedup": t_port / t_ours, "outputs_identical": same,
+            "host_threads": os.cpu_count()}
 
 
 def make_requests(n_jobs: int, seed: int = 5):
@@ -738,9 +820,10 @@ def main() -> None:
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(groups[0], p, nthreads=1)
 
-    uneven = serving = ingest = None
+    uneven = serving = ingest = average = None
     if not args.no_ingest and rank == 0:
         ingest = ingest_leg()
+        average = average_leg()
     if not args.no_uneven:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
@@ -778,6 +861,7 @@ def main() -> None:
                 "uneven": uneven,
                 "serving": serving,
                 "ingest": ingest,
+                "average": average,
                 "stats": st}
         print(json.dumps(line))
     eng.close()

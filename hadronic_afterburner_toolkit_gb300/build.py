@@ -130,10 +130,14 @@ def build_host(force: bool = False) -> str | None:
         libs = ["-L" + LIB, "-lhbt_gpu", "-Wl,-rpath,$ORIGIN"] + (["-lz"] if zlib else [])
         lib_srcs = [s for s in srcs if not s.endswith("main.cpp")]
         _run([cxx] + flags + ["-shared", "-o", lib] + lib_srcs + libs)
-        main = [s for s in srcs if s.endswith("main.cpp")]
-        if main:
-            _run([cxx] + flags + ["-o", exe] + main + ["-L" + LIB, "-lhbt_host", "-lhbt_gpu",
-                                                       "-Wl,-rpath,$ORIGIN"])
+        # one executable per *main.cpp: main.cpp -> hbt_afterburner.e,
+        # average_main.cpp -> hbt_average.e
+        for m in (s for s in srcs if s.endswith("main.cpp")):
+            base = os.path.basename(m)
+            out = exe if base == "main.cpp" else os.path.join(
+                LIB, "hbt_" + base[:-len("_main.cpp")] + ".e")
+            _run([cxx] + flags + ["-o", out, m, "-L" + LIB, "-lhbt_host", "-lhbt_gpu",
+                                  "-Wl,-rpath,$ORIGIN"])
     return lib
 
 

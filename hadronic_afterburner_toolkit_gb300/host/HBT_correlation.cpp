@@ -1,7 +1,11 @@
 #include "HBT_correlation.h"
 
+#include <atomic>
+
+#include <charconv>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <iostream>
 #include <sstream>
 #include <stdexcept>
@@ -276,16 +280,45 @@ void HBT_correlation::output_correlation_function_Kphi_differential() { output_H
 
 namespace {
 
-void row5(FILE *f, bool eco, double a, double b, double c, double num, double den) {
-    // std::scientific, setprecision(8), setw(18) on the first field only
-    if (eco)
-        fprintf(f, "%18.8e    %.8e\n", num, den);
-    else
-        fprintf(f, "%18.8e    %.8e    %.8e    %.8e    %.8e\n", a, b, c, num, den);
+// "%W.8e" of printf: std::to_chars in scientific form with precision 8 is
+// specified to give printf's characters (exact decimal conversion, at least
+// two exponent digits, "inf" / "nan" with their sign), right-aligned in a
+// field of `width`.
+char *put_e(char *p, double v, int width) {
+    char tmp[48];
+    const std::to_chars_result r =
+        std::to_chars(tmp, tmp + sizeof(tmp), v, std::chars_format::scientific, 8);
+    const int len = static_cast<int>(r.ptr - tmp);
+    for (int k = len; k < width; k++) *p++ = ' ';
+    memcpy(p, tmp, len);
+    return p + len;
+}
+
+// One row: std::scientific, setprecision(8), setw(18) on the first field
+// only, four blanks between fields (the reference's writer).
+char *row(char *p, int nfield, const double *v) {
+    for (int k = 0; k < nfield; k++) {
+        if (k > 0) {
+            memcpy(p, "    ", 4);
+            p += 4;
+        }
+        p = put_e(p, v[k], k == 0 ? 18 : 0);
+    }
+    *p++ = '\n';
+    return p;
+}
+
+bool write_file(const std::string &fn, const std::string &text) {
+    FILE *f = fopen(fn.c_str(), "w");
+    if (!f) return false;
+    const bool ok = fwrite(text.data(), 1, text.size(), f) == text.size();
+    return fclose(f) == 0 && ok;
 }
 
 }  // namespace
 
+// The files are formatted in memory and written on all host threads, one
+// file per task.
 int hbt_write_outputs(const hbt_params &p, const std::string &path, int eco_output,
                       const hbt_host_hist_view &h) {
     const bool eco = eco_output == 1;
@@ -298,32 +331,36 @@ int hbt_write_outputs(const hbt_params &p, const std::string &path, int eco_outp
     for (int i = 0; i < p.n_KT; i++) KT[i] = p.KT_min + i * dKT;
     for (int i = 0; i < p.n_Kphi; i++) Kphi[i] = i * dKphi;
     const long long q3 = (long long)n * n * n;
+    std::atomic<bool> failed(false);
 
     // q_inv files (src/HBT_correlation.cpp:694-724)
     if (p.invariant_radius_flag == 1) {
-        for (int iK = 0; iK < p.n_KT - 1; iK++) {
-            const double ratio = static_cast<double>(h.ctr_num_qinv[iK]) /
-                                 static_cast<double>(h.ctr_den_qinv[iK]);
-            const std::string fn = path + "/HBT_correlation_function_inv_KT_" + fmt_edge(KT[iK]) +
-                                   "_" + fmt_edge(KT[iK + 1]) + ".dat";
-            FILE *f = fopen(fn.c_str(), "w");
-            if (!f) return -1;
-            for (int k = 0; k < n; k++) {
-                const long long at = (long long)iK * n + k;
-                const double qmean = h.qinv_sum[at] / h.qinv_count[at];
-                const double den = h.qinv_den[at] * ratio;
-                if (eco)
-                    fprintf(f, "%18.8e    %.8e\n", h.qinv_num[at], den);
-                else
-                    fprintf(f, "%18.8e    %.8e    %.8e\n", qmean, h.qinv_num[at], den);
+        hbt::parallel_ranges(p.n_KT - 1, 0, 1, [&](long lo, long hi) {
+            std::string text;
+            for (long iK = lo; iK < hi; iK++) {
+                const double ratio = static_cast<double>(h.ctr_num_qinv[iK]) /
+                                     static_cast<double>(h.ctr_den_qinv[iK]);
+                const std::string fn = path + "/HBT_correlation_function_inv_KT_" +
+                                       fmt_edge(KT[iK]) + "_" + fmt_edge(KT[iK + 1]) + ".dat";
+                text.assign(static_cast<size_t>(n) * 64, '\0');
+                char *o = &text[0];
+                for (int k = 0; k < n; k++) {
+                    const long long at = (long long)iK * n + k;
+                    const double v[3] = {h.qinv_sum[at] / h.qinv_count[at], h.qinv_num[at],
+                                         h.qinv_den[at] * ratio};
+                    o = eco ? row(o, 2, v + 1) : row(o, 3, v);
+                }
+                text.resize(o - text.data());
+                if (!write_file(fn, text)) failed = true;
             }
-            fclose(f);
-        }
+        });
     }
     // 3-D files (src/HBT_correlation.cpp:726-855)
     const int nphi = p.azimuthal_flag == 1 ? p.n_Kphi : 1;
-    for (int iK = 0; iK < p.n_KT - 1; iK++)
-        for (int ip = 0; ip < nphi; ip++) {
+    hbt::parallel_ranges(static_cast<long>(p.n_KT - 1) * nphi, 0, 1, [&](long lo, long hi) {
+        std::string text;
+        for (long task = lo; task < hi; task++) {
+            const int iK = static_cast<int>(task / nphi), ip = static_cast<int>(task % nphi);
             const int s = p.azimuthal_flag == 1 ? iK * p.n_Kphi + ip : iK;
             const double ratio =
                 static_cast<double>(h.ctr_num[s]) / static_cast<double>(h.ctr_den[s]);
@@ -331,22 +368,33 @@ int hbt_write_outputs(const hbt_params &p, const std::string &path, int eco_outp
                              fmt_edge(KT[iK + 1]);
             if (p.azimuthal_flag == 1) fn += "_Kphi_" + fmt_edge(Kphi[ip]);
             fn += ".dat";
-            FILE *f = fopen(fn.c_str(), "w");
-            if (!f) return -1;
+            text.assign(static_cast<size_t>(q3) * 96, '\0');
+            char *o = &text[0];
             for (int il = 0; il < n; il++)
                 for (int io = 0; io < n; io++)
                     for (int is = 0; is < n; is++) {
                         const long long at = s * q3 + ((long long)io * n + is) * n + il;
                         const int npart_num = static_cast<int>(h.num_count[at]);
                         const int npart_den = static_cast<int>(h.den[at]);
-                        if (npart_num < 2 || npart_den < 2)
-                            row5(f, eco, grid[io], grid[is], grid[il], 0.0,
-                                 static_cast<double>(npart_den));
-                        else
-                            row5(f, eco, h.q_out_sum[at] / npart_num, h.q_side_sum[at] / npart_num,
-                                 h.q_long_sum[at] / npart_num, h.num[at], ratio * h.den[at]);
+                        double v[5];
+                        if (npart_num < 2 || npart_den < 2) {
+                            v[0] = grid[io];
+                            v[1] = grid[is];
+                            v[2] = grid[il];
+                            v[3] = 0.0;
+                            v[4] = static_cast<double>(npart_den);
+                        } else {
+                            v[0] = h.q_out_sum[at] / npart_num;
+                            v[1] = h.q_side_sum[at] / npart_num;
+                            v[2] = h.q_long_sum[at] / npart_num;
+                            v[3] = h.num[at];
+                            v[4] = ratio * h.den[at];
+                        }
+                        o = eco ? row(o, 2, v + 3) : row(o, 5, v);
                     }
-            fclose(f);
+            text.resize(o - text.data());
+            if (!write_file(fn, text)) failed = true;
         }
-    return 0;
+    });
+    return failed ? -1 : 0;
 }

@@ -1,4 +1,5 @@
 #include "SampleSource.h"
+#include "TextNumbers.h"
 
 #include <sys/stat.h>
 
@@ -37,43 +38,6 @@ int parse_numbers(const char *s, double *out, int count) {
         if (end == s) break;
         out[k++] = v;
         s = end;
-    }
-    return k;
-}
-
-bool is_space(char c) {
-    return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
-}
-
-// parse_numbers on the span [b, e) (not NUL-terminated).  std::from_chars
-// and strtod are both correctly rounded, so a token both accept gives the
-// same double; any token from_chars does not take whole (a leading '+', hex,
-// overflow, trailing junk) is handed to strtod on a NUL-terminated copy, and
-// parsing resumes where strtod stopped, exactly as the strtod loop would.
-int parse_span(const char *b, const char *e, double *out, int count) {
-    int k = 0;
-    const char *s = b;
-    char tok[128];
-    while (k < count) {
-        while (s < e && is_space(*s)) s++;
-        if (s >= e) break;
-        double v = 0.0;
-        const std::from_chars_result r = std::from_chars(s, e, v);
-        if (r.ec == std::errc() && *s != '+' && (r.ptr == e || is_space(*r.ptr))) {
-            out[k++] = v;
-            s = r.ptr;
-            continue;
-        }
-        const char *t = s;
-        while (t < e && !is_space(*t)) t++;
-        const size_t n = std::min<size_t>(t - s, sizeof(tok) - 1);
-        memcpy(tok, s, n);
-        tok[n] = '\0';
-        char *end = nullptr;
-        v = strtod(tok, &end);
-        if (end == tok) break;
-        out[k++] = v;
-        s += end - tok;
     }
     return k;
 }

@@ -66,6 +66,16 @@ int hbt_host_digest_buffers(const char *param_file, const char *results_path, in
 int hbt_host_time_reader(const char *param_file, const char *results_path, int32_t n_args,
                          char **args, double *seconds, int64_t *particles, int64_t *text_bytes);
 
+/* Event averaging of the HBT correlation files (the reference's
+ * ebe_scripts/average_event_HBT_correlation_function.py): for every HBT*
+ * file of the first UrQMD* folder's UrQMD_results under `working_folder`,
+ * the element-wise mean over all UrQMD* folders (directory order, as the
+ * script's glob) written to `avg_folder` with "%.10e" and two blanks between
+ * columns.  Files are averaged on `threads` host threads (0: all).  Returns
+ * the number of files written, or -1 on error. */
+int hbt_host_average_events(const char *working_folder, const char *avg_folder,
+                            int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -227,3 +227,47 @@ def test_block_reader_reads_oscar_and_rejects_malformed_lines(host, tmp_path):
     for fast in (0, 1):
         n, _ = _digests(host, str(pfile), str(res2), ["hbt_fast_reader=%d" % fast])
         assert n == -1
+
+
+def test_writer_formats_special_values_like_printf(host, tmp_path):
+    """The in-memory writer's %.8e fields equal printf's for signed zeros,
+    infinities, subnormals, huge values and values that round at the 8th
+    digit (Python's '%e' formatting is correctly rounded, like glibc's)."""
+    n, nkt = 3, 2
+    nb = nkt * n ** 3
+    specials = [0.0, -0.0, float("inf"), -float("inf"), 5e-324, -2.2250738585072014e-308,
+                1.7976931348623157e308, 9.9999999950e5, 1.23456785e-7, 2.5e-1, -1.0 / 3.0,
+                6.02214076e23, 1.0, -9.99999999e-100, 123456789.0, 1e-5, 0.1, 7.0]
+    rng = np.random.default_rng(9)
+    cnt = np.full(nb, 2.0)
+    cnt[:3] = [0.0, 1.0, 5.0]
+    q = [np.array([specials[(k + j) % len(specials)] for k in range(nb)]) for j in range(3)]
+    num = np.array([specials[(k + 7) % len(specials)] for k in range(nb)])
+    den = rng.integers(0, 50, nb).astype(float)
+    den[5] = 1.0
+    zeros = [np.zeros(nkt * n) for _ in range(4)]
+    ctr = [np.array([3, 0], np.uint64), np.array([7, 1], np.uint64), np.zeros(nkt, np.uint64),
+           np.zeros(nkt, np.uint64)]
+    hp = engine.HbtParams(qnpts=n, q_min=-0.1, q_max=0.1, n_KT=nkt, KT_min=0.0, KT_max=1.0,
+                          n_Kphi=1, azimuthal_flag=0, invariant_radius_flag=0)
+    arrs = [cnt] + q + [num, den] + zeros
+    assert host.hbt_host_write(ctypes.byref(hp), str(tmp_path).encode(), 0,
+                               *[np.ascontiguousarray(a).ctypes.data_as(_PD) for a in arrs],
+                               *[c.ctypes.data_as(_PU) for c in ctr]) == 0
+    files = os.listdir(tmp_path)
+    assert len(files) == 1
+    got = open(os.path.join(tmp_path, files[0])).read().split("\n")[:-1]
+    grid = [-0.1 + i * 0.1 for i in range(n)]
+    ratio = 3.0 / 7.0
+    want = []
+    for il in range(n):
+        for io in range(n):
+            for is_ in range(n):
+                at = (io * n + is_) * n + il
+                if int(cnt[at]) < 2 or int(den[at]) < 2:
+                    v = (grid[io], grid[is_], grid[il], 0.0, float(int(den[at])))
+                else:
+                    c = int(cnt[at])
+                    v = (q[0][at] / c, q[1][at] / c, q[2][at] / c, num[at], ratio * den[at])
+                want.append("%18.8e    %.8e    %.8e    %.8e    %.8e" % v)
+    assert got == want
