@@ -94,6 +94,8 @@ struct Screen {
     // with margin, Q^2, 2 Q^2 and the coefficient of the input-rounding term
     // of the q_T test
     float pq, pq2, pqt2, pqt_c;
+    // 1 / hbarC as a double-float pair (FP32-weight phase)
+    float hc_h, hc_l;
 };
 
 // Host: the prefilter constants of a screen whose window is filled in.
@@ -105,6 +107,9 @@ inline void fill_prefilter(Screen &s) {
     s.pqt2 = (float)(2.0 * Q * Q * (1.0 + 2e-4));
     // (c + e)^2 <= c^2 + 2 c e (1 + 1e-4), c = sqrt(2) Q, e = 2.01 u L
     s.pqt_c = (float)(2.0 * 1.4142135623730951 * Q * 2.01 * U * (1.0 + 2e-4));
+    const double hc = 1.0 / 0.197327053;  // 1 / hbarC [1 / (GeV fm)]
+    s.hc_h = (float)hc;
+    s.hc_l = (float)(hc - (double)s.hc_h);
 }
 
 struct Device {

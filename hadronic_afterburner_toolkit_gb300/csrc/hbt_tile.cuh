@@ -27,11 +27,18 @@
 //       FP64 form  - FP64 values from algebraically identical expressions
 //                    (q_out = (q_x S_x + q_y S_y) / |S|, ...) and a
 //                    table-driven FP64 cos (table_cos below);
-//       FP32W form - the FP32 screen values, and cos of the phase computed
-//                    and range-reduced in FP64, evaluated in FP32 by a Taylor
-//                    polynomial; added with one float4 vector atomic into
-//                    FP32 partial bins that hbt_capi.cu merges into the FP64
+//       FP32W form - each FP64 column split once per tile into hi + lo
+//                    FP32 parts; differences and the phase in double-float
+//                    arithmetic on the FP32 pipe, q values in FP32, cos by
+//                    quadrant reduction and FP32 Taylor polynomials
+//                    (values32_split); added with one float4 vector atomic
+//                    into FP32 partial bins that are merged into the FP64
 //                    bins with Kahan compensation.
+//     In the FP32-weight form a pair is evaluated as stored (i, j) and
+//     oriented afterwards: swapping first and second negates every momentum
+//     and position difference, so it negates q_out, q_side, q_long exactly
+//     (IEEE rounding is symmetric in sign) and leaves the phase and its cos
+//     unchanged.
 //
 // Error analysis (u = 2^-24).  Inputs are FP64 values v rounded once to
 // FP32: |v32 - v| <= u|v|.  For s = a +- b in FP32, |s - S| <= 2.01 u A with
@@ -305,10 +312,129 @@ __device__ __forceinline__ float4 values32(const Grid &g, const double *a, const
     return v;
 }
 
+// ---- double-float arithmetic (value = hi + lo, two FP32 numbers) on the
+// FP32 pipe, for the FP32-weight form's per-pair values.  The error-free
+// transformations are Knuth's two-sum and the FMA two-product (as in
+// Dekker's and Shewchuk's double-length arithmetic).
+struct FF {
+    float h, l;
+};
+
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return FF{s, e};
+}
+
+// a + b with |a| >= |b| (or a == 0).
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// (ah + al) - (bh + bl) of two split FP64 values.  A split holds its value
+// to 2^-48 relative; the high parts' difference is exact (two-sum) and the
+// low parts add one FP32 rounding of a term below 2^-47 of the inputs.
+__device__ __forceinline__ FF ff_diff(float2 a, float2 b) {
+    const FF s = two_sum(a.x, -b.x);
+    return two_sum(s.h, __fadd_rn(s.l, __fsub_rn(a.y, b.y)));
+}
+
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const FF s = two_sum(a.h, b.h);
+    return two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.h, -a.l}; }
+
+// Splits an FP64 value into hi = nearest FP32 and lo = nearest FP32 to the
+// rest (done once per particle and tile).
+__device__ __forceinline__ float2 split(double x) {
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+
+// cos of a phase given as a double-float: reduction by quadrant with pi/2
+// split into three parts (12 + 12 significant bits and the rest, so that
+// j times either leading part is exact for |j| < 2^11), then the FP32
+// Taylor polynomials of values32.  Absolute error below 2e-7.
+__device__ __forceinline__ float ff_cos(FF ph) {
+    const float j = rintf(ph.h * 0.63661977f);  // 2 / pi
+    float x;
+    if (fabsf(j) < 2048.0f) {
+        const float t1 = __fmaf_rn(-j, 1.57080078125f, ph.h);       // exact
+        const FF t2 = two_sum(t1, __fmul_rn(-j, -4.453584551811218e-06f));
+        x = __fadd_rn(t2.h, __fadd_rn(t2.l, __fmaf_rn(-j, -8.705515752716053e-10f, ph.l)));
+    } else {
+        // never on this path (|q.dx| / hbarC is a few hundred at most)
+        const double r = (double)ph.h + (double)ph.l;
+        const double k = rint(r * 0.6366197723675814);
+        x = (float)(r - k * 1.5707963267948966);
+        return cosf(x + (float)(fmod(k, 4.0)) * 1.5707964f);
+    }
+    const float x2 = __fmul_rn(x, x);
+    const float c = __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, 2.48015873e-5f,
+                                                                    -1.38888889e-3f),
+                                                        4.16666667e-2f),
+                                          -0.5f),
+                              1.0f);
+    const float s = x * __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, __fmaf_rn(x2, 2.75573192e-6f,
+                                                                        -1.98412698e-4f),
+                                                            8.33333333e-3f),
+                                              -1.66666667e-1f),
+                                1.0f);
+    const int quad = ((int)j) & 3;  // cos(x + j pi/2)
+    return quad == 0 ? c : quad == 1 ? -s : quad == 2 ? -c : s;
+}
+
+// Summed values of the FP32-weight form from split FP64 inputs, all on the
+// FP32 pipe: momentum and position differences in double-float (their
+// rounding relative to the difference, not to the momenta), q_out, q_side,
+// q_long in FP32 (a few 1e-7 relative), the phase (q.dx)/hbarC in
+// double-float and its cos by ff_cos.  a, b: the eight split columns of the
+// pair's first and second particle.
+template <bool BOOST>
+__device__ __forceinline__ float4 values32_split(const Screen &S, const float2 *a,
+                                                 const float2 *b) {
+    const FF dx = ff_diff(a[0], b[0]), dy = ff_diff(a[1], b[1]);
+    const FF dz = ff_diff(a[2], b[2]), dE = ff_diff(a[3], b[3]);
+    const float sx = __fadd_rn(__fadd_rn(a[0].x, b[0].x), __fadd_rn(a[0].y, b[0].y));
+    const float sy = __fadd_rn(__fadd_rn(a[1].x, b[1].x), __fadd_rn(a[1].y, b[1].y));
+    const float inv = rsqrtf(__fmaf_rn(sx, sx, sy * sy));
+    float4 v;
+    v.x = __fmaf_rn(dx.h, sx, dy.h * sy) * inv;
+    v.y = __fmaf_rn(dy.h, sx, -(dx.h * sy)) * inv;
+    if (BOOST) {
+        const float sE = __fadd_rn(__fadd_rn(a[3].x, b[3].x), __fadd_rn(a[3].y, b[3].y));
+        const float sz = __fadd_rn(__fadd_rn(a[2].x, b[2].x), __fadd_rn(a[2].y, b[2].y));
+        v.z = __fmaf_rn(sE, dz.h, -(sz * dE.h)) * rsqrtf((sE - sz) * (sE + sz));
+    } else {
+        v.z = dz.h;
+    }
+    FF ph = ff_mul(dE, ff_diff(a[7], b[7]));
+    ph = ff_add(ph, ff_neg(ff_mul(dx, ff_diff(a[4], b[4]))));
+    ph = ff_add(ph, ff_neg(ff_mul(dy, ff_diff(a[5], b[5]))));
+    ph = ff_add(ph, ff_neg(ff_mul(dz, ff_diff(a[6], b[6]))));
+    ph = ff_mul(ph, FF{S.hc_h, S.hc_l});
+    v.w = ff_cos(ph);
+    return v;
+}
+
 // Shared memory of one tile pair.
 struct TileSmem {
-    double si[8][FT];  // FP64 i-tile (same-event)
-    double sj[8][FT];  // FP64 j-tile (same-event)
+    // same-event tiles: FP64 columns (FP64 form) or split columns (hi, lo
+    // FP32 pairs, FP32-weight form), px py pz E x y z t
+    double si[8][FT];
+    double sj[8][FT];
     float4 fi[FT];     // FP32 momenta of the i-tile
     float4 fj[FT];     // FP32 momenta of the j-tile
     float2 gi[FT];     // (|px| + |py|, |pz|) of the i-tile (prefilter)
@@ -366,17 +492,29 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
                                                const double *const *c, const unsigned *orig,
                                                long long n, long long i0, long long j0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    for (int f = 0; f < 8; f++) {
-        sm.si[f][tid] = (i0 + tid < n) ? c[f][i0 + tid] : 0.0;
-        sm.sj[f][tid] = (j0 + tid < n) ? c[f][j0 + tid] : 0.0;
+    // split columns of the FP32-weight form, in the FP64 tiles' place
+    float2(*spi)[FT] = reinterpret_cast<float2(*)[FT]>(&sm.si[0][0]);
+    float2(*spj)[FT] = reinterpret_cast<float2(*)[FT]>(&sm.sj[0][0]);
+    if (PREC == 0) {
+        for (int f = 0; f < 8; f++) {
+            sm.si[f][tid] = (i0 + tid < n) ? c[f][i0 + tid] : 0.0;
+            sm.sj[f][tid] = (j0 + tid < n) ? c[f][j0 + tid] : 0.0;
+        }
+        sm.fi[tid] = make_float4((float)sm.si[0][tid], (float)sm.si[1][tid], (float)sm.si[2][tid],
+                                 (float)sm.si[3][tid]);
+        sm.fj[tid] = make_float4((float)sm.sj[0][tid], (float)sm.sj[1][tid], (float)sm.sj[2][tid],
+                                 (float)sm.sj[3][tid]);
+    } else {
+        for (int f = 0; f < 8; f++) {
+            spi[f][tid] = split((i0 + tid < n) ? c[f][i0 + tid] : 0.0);
+            spj[f][tid] = split((j0 + tid < n) ? c[f][j0 + tid] : 0.0);
+        }
+        // the high parts are the FP32 roundings of the momenta
+        sm.fi[tid] = make_float4(spi[0][tid].x, spi[1][tid].x, spi[2][tid].x, spi[3][tid].x);
+        sm.fj[tid] = make_float4(spj[0][tid].x, spj[1][tid].x, spj[2][tid].x, spj[3][tid].x);
     }
     sm.oi[tid] = orig ? (i0 + tid < n ? orig[i0 + tid] : 0u) : (unsigned)(i0 + tid);
     sm.oj[tid] = orig ? (j0 + tid < n ? orig[j0 + tid] : 0u) : (unsigned)(j0 + tid);
-    __syncthreads();
-    sm.fi[tid] = make_float4((float)sm.si[0][tid], (float)sm.si[1][tid], (float)sm.si[2][tid],
-                             (float)sm.si[3][tid]);
-    sm.fj[tid] = make_float4((float)sm.sj[0][tid], (float)sm.sj[1][tid], (float)sm.sj[2][tid],
-                             (float)sm.sj[3][tid]);
     sm.gi[tid] = make_float2(fabsf(sm.fi[tid].x) + fabsf(sm.fi[tid].y), fabsf(sm.fi[tid].z));
     sm.gj[tid] = make_float2(fabsf(sm.fj[tid].x) + fabsf(sm.fj[tid].y), fabsf(sm.fj[tid].z));
     __syncthreads();
@@ -399,14 +537,50 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
         const bool swap = (e >> 16) & 1u;
         const int slot = (e >> 17) & 1u ? -1 : (int)(e >> 18);
         const int bin = (int)e2.y;
+        if (PREC == 1 && slot >= 0) {
+            // the pair as stored (i, j); swapping first and second negates
+            // q_out, q_side, q_long exactly and leaves the phase unchanged
+            float2 a[8], b[8];
+#pragma unroll
+            for (int f = 0; f < 8; f++) {
+                a[f] = spi[f][qi];
+                b[f] = spj[f][qj];
+            }
+            float4 v = values32_split<BOOST>(d.s, a, b);
+            if (swap) {
+                v.x = -v.x;
+                v.y = -v.y;
+                v.z = -v.z;
+            }
+            const long long at = (long long)slot * d.g.q3 + bin;
+            atomicAdd(d.part + at, v);
+            atomicAdd(d.h.cnt + at, 1ull);
+            return;
+        }
+        // FP64 form, or a pair the window screen left undecided: the pair in
+        // the reference's orientation, from the FP64 tile or (FP32-weight
+        // form) the FP64 columns themselves
         double A[8], B[8];  // first and second particle of the pair
 #pragma unroll
         for (int f = 0; f < 8; f++) {
-            const double u = sm.si[f][qi], v = sm.sj[f][qj];
+            const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+            const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
             A[f] = swap ? v : u;
             B[f] = swap ? u : v;
         }
-        if (slot < 0) {
+        if (PREC == 0 && slot >= 0) {
+            double vo, vs, vl, vw;
+            values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
+            const long long at = (long long)slot * d.g.q3 + bin;
+            Sums *h = d.h.sums + at;
+            atomicAdd(&h->qo, vo);
+            atomicAdd(&h->qs, vs);
+            atomicAdd(&h->ql, vl);
+            atomicAdd(&h->w, vw);
+            atomicAdd(d.h.cnt + at, 1ull);
+            return;
+        }
+        {
             // undecided somewhere: the reference chain decides (and may hand
             // a K_phi edge to the host)
             const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2],
@@ -418,21 +592,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
                 atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
                 atomicAdd(d.h.cnt + at, 1ull);
             }
-            return;
         }
-        const long long at = (long long)slot * d.g.q3 + bin;
-        if (PREC == 0) {
-            double vo, vs, vl, vw;
-            values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
-            Sums *h = d.h.sums + at;
-            atomicAdd(&h->qo, vo);
-            atomicAdd(&h->qs, vs);
-            atomicAdd(&h->ql, vl);
-            atomicAdd(&h->w, vw);
-        } else {
-            atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
-        }
-        atomicAdd(d.h.cnt + at, 1ull);
     };
 
     // stage B for 32 prefiltered pairs: window screen and bins; the pairs
