@@ -771,8 +771,14 @@ def main() -> None:
            sum(o * f for o, f in zip(STAGE_OPS_MIXED, fr)) * P_mixed)
     t_step = statistics.median(ms_steps) * 1e-3
     achieved = ops / t_step / 1e12
+    # DRAM bytes per launch of k_persistent_same on this workload (ncu,
+    # profiles/k_persistent_central_dram.md; not measured in this run)
+    traffic = 1.44e9 if (args.workload == "central" and args.precision == "fp64" and batched) \
+        else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"], "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"], "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                  "k_persistent_same, one central launch" if traffic else None,
                 "kernel": "k_persistent (batched screened pair binning)" if batched
                           else "pair-binning kernels",
                 "peak_source": "measured live: FP64 FMA probe (lib/libhbt_probe.so)",
