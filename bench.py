@@ -670,8 +670,10 @@ def main() -> None:
     kern = E.KERNEL_SCREENED if args.kernel == "screened" else E.KERNEL_REFERENCE_CHAIN
     eng = E.Engine(device=local, precision=prec, kernel=kern, **p)
     eng.set_stream(stream.cuda_stream)
-
     batched = kern == E.KERNEL_SCREENED
+    if batched:
+        # CUDA events around the persistent kernels (the roofline's kernel time)
+        eng.set_tuning(time_kernels=1)
 
     def run_group(engine, grp, batch, device=True):
         """One oversample group: its same-event pairs and every event's
@@ -691,7 +693,7 @@ def main() -> None:
     if world > 1:
         torch.distributed.barrier()
     launches0 = eng.stats()["launches"]
-    ms_steps, pairs = [], 0
+    ms_steps, pairs, same_ms, mixed_ms = [], 0, [], []
     with ClockSampler(local) as clk:
         for k in range(args.steps):
             g = args.warmup + k
@@ -705,6 +707,10 @@ def main() -> None:
             e1.synchronize()
             ms_steps.append(e0.elapsed_time(e1))
             pairs += group_pairs(groups[g % len(groups)])
+            if batched:
+                kst = eng.stats()
+                same_ms.append(kst["same_kernel_ms"])
+                mixed_ms.append(kst["mixed_kernel_ms"])
     torch.cuda.synchronize()
     launches = eng.stats()["launches"] - launches0
     t_ms = sum(ms_steps)
@@ -770,17 +776,33 @@ def main() -> None:
     ops = (sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)) * P_same +
            sum(o * f for o, f in zip(STAGE_OPS_MIXED, fr)) * P_mixed)
     t_step = statistics.median(ms_steps) * 1e-3
-    achieved = ops / t_step / 1e12
+    step_achieved = ops / t_step / 1e12
+    # the dominant kernel: same-event pairs' FP64 work over its own time
+    ops_same = sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)) * P_same
+    t_same = statistics.median(same_ms) * 1e-3 if same_ms and min(same_ms) > 0 else t_step
+    achieved = ops_same / t_same / 1e12
     # DRAM bytes per launch of k_persistent_same on this workload (ncu,
     # profiles/k_persistent_central_dram.md; not measured in this run)
     traffic = 1.44e9 if (args.workload == "central" and args.precision == "fp64" and batched) \
         else None
+    try:
+        hbm_peak = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, ValueError, KeyError):
+        hbm_peak = 6800.0
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
                 "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"], "traffic": traffic,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
                                   "k_persistent_same, one central launch" if traffic else None,
-                "kernel": "k_persistent (batched screened pair binning)" if batched
-                          else "pair-binning kernels",
+                "kernel": "k_persistent_same (same-event pairs; CUDA events around its "
+                          "launch)" if batched and same_ms else "pair-binning kernels",
+                "kernel_ms": t_same * 1e3,
+                "mixed_kernel_ms": statistics.median(mixed_ms) if mixed_ms else None,
+                "algorithmic_work": "FP64 ops of the reference chain per same-event pair "
+                                    "(stage counts 11, 12, 5, 11, 15 of the reference loop x measured survival) x pairs",
+                "hbm": {"achieved_gbs": traffic / t_same / 1e9 if traffic else None,
+                        "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json",
+                        "frac": (traffic / t_same / 1e9 / hbm_peak) if traffic else None},
+                "step_achieved": step_achieved,
                 "peak_source": "measured live: FP64 FMA probe (lib/libhbt_probe.so)",
                 "ops_per_pair_same": round(sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)), 2),
                 "ops_per_pair_mixed": round(sum(o * f for o, f in zip(STAGE_OPS_MIXED, fr)), 2),

@@ -292,7 +292,8 @@ size_t batch_sort_temp_bytes(long long cap) {
 }
 
 cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
-                      const Device *host_devs, int n_host_devs, cudaStream_t st) {
+                      const Device *host_devs, int n_host_devs, cudaStream_t st,
+                      cudaEvent_t *marks) {
     cudaError_t e;
     const int gs = 152 * 8;
     if (b.total > 0) {
@@ -320,6 +321,7 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
     // same-event items (chunked for the FP32-weight form)
     const unsigned upper = b.same_cap;
     if (chunk == 0 || prec == 0) chunk = upper;
+    if (marks && (e = cudaEventRecord(marks[0], st)) != cudaSuccess) return e;
     for (unsigned base = 0; base < upper; base += chunk) {
         const unsigned end =
             (unsigned)min((unsigned long long)base + chunk, (unsigned long long)upper);
@@ -346,6 +348,8 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
                 if ((e = launch_merge(host_devs[k], st)) != cudaSuccess) return e;
         }
     }
+    if (marks && (e = cudaEventRecord(marks[1], st)) != cudaSuccess) return e;
+    if (marks && (e = cudaEventRecord(marks[2], st)) != cudaSuccess) return e;
     // mixed-event items
     if (b.mixed_cap > 0) {
         if (az && boost) e = launch_mixed_items<true, true>(d, b, grid, st);
@@ -354,6 +358,7 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
         else e = launch_mixed_items<false, false>(d, b, grid, st);
         if (e != cudaSuccess) return e;
     }
+    if (marks && (e = cudaEventRecord(marks[3], st)) != cudaSuccess) return e;
     return cudaSuccess;
 }
 

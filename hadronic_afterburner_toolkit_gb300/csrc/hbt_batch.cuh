@@ -81,7 +81,10 @@ size_t batch_sort_temp_bytes(long long cap);
 // form's same-event queue into chunks of that many items with a merge of
 // the FP32 partials after each: of `d` for a one-analysis batch, of every
 // host_devs[k] (the host copies of b.devs) for a batch of many analyses.
+// marks (optional, 4 events): recorded before and after the same-event
+// kernels (with their merges) and before and after the mixed-event kernel.
 cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
-                      const Device *host_devs, int n_host_devs, cudaStream_t st);
+                      const Device *host_devs, int n_host_devs, cudaStream_t st,
+                      cudaEvent_t *marks = nullptr);
 
 }  // namespace hbt

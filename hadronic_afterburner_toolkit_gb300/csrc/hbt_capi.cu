@@ -55,7 +55,7 @@ struct hbt_ctx {
     hbt::BatchRunner runner;
     int persistent_grid = 152 * 4;
     int sms = 152, max_blocks_per_sm = 5;
-    hbt_tuning tune = {0, 0.02, 0.05, 16384, 1};
+    hbt_tuning tune = {0, 0.02, 0.05, 16384, 1, 0};
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging
@@ -356,6 +356,7 @@ hbt::Tuning runner_tuning(const hbt_ctx *c, const hbt_tuning &t) {
     r.cell_pt = t.cell_pt;
     r.cell_y = t.cell_y;
     r.graph = t.use_graph != 0;
+    r.time_kernels = t.time_kernels != 0;
     return r;
 }
 
@@ -396,7 +397,8 @@ std::vector<FastJob> fast_jobs_of(int32_t n_jobs, const hbt_job *jobs) {
 
 bool tuning_valid(const hbt_tuning &t) {
     return t.blocks_per_sm >= 0 && t.cell_pt >= 0.0 && t.cell_y >= 0.0 && t.merge_chunk >= 0 &&
-           t.merge_chunk <= 16384 && (t.use_graph == 0 || t.use_graph == 1);
+           t.merge_chunk <= 16384 && (t.use_graph == 0 || t.use_graph == 1) &&
+           (t.time_kernels == 0 || t.time_kernels == 1);
 }
 
 hbt_tuning tuning_defaults(hbt_tuning t) {
@@ -991,6 +993,11 @@ hbt_status hbt_get_stats(hbt_ctx *c, hbt_stats *out) {
     CU(cudaMemcpy(stats, c->stats.p, sizeof(stats), cudaMemcpyDeviceToHost));
     *out = c->st;
     out->anomalies = stats[hbt::STAT_ANOMALY];
+    float sm = 0.f, mm = 0.f;
+    if (c->tune.time_kernels && c->runner.kernel_times(sm, mm)) {
+        out->same_kernel_ms = sm;
+        out->mixed_kernel_ms = mm;
+    }
     return HBT_OK;
 }
 

@@ -9,6 +9,8 @@ namespace hbt {
 
 BatchRunner::~BatchRunner() {
     if (exec_) cudaGraphExecDestroy(exec_);
+    for (cudaEvent_t e : marks_)
+        if (e) cudaEventDestroy(e);
     Buf *all[] = {&lists_, &jobs_, &offs_, &table_, &keys_, &vals_, &sort_temp_, &boxes_,
                   &items_, &counters_, &devs_};
     for (Buf *b : all)
@@ -70,13 +72,27 @@ bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<
 // The graph captured for one set of launch arguments stays valid while they
 // are unchanged: the batch tables it reads are re-uploaded before each
 // launch, into the same buffers.
+bool BatchRunner::kernel_times(float &same_ms, float &mixed_ms) {
+    same_ms = mixed_ms = 0.f;
+    if (!timed_ || cudaEventSynchronize(marks_[3]) != cudaSuccess) return false;
+    return cudaEventElapsedTime(&same_ms, marks_[0], marks_[1]) == cudaSuccess &&
+           cudaEventElapsedTime(&mixed_ms, marks_[2], marks_[3]) == cudaSuccess;
+}
+
 cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device *devs_host,
                                 int n_devs, const Tuning &t, cudaStream_t st) {
+    cudaEvent_t *marks = nullptr;
+    if (t.time_kernels) {
+        for (cudaEvent_t &e : marks_)
+            if (!e && cudaEventCreate(&e) != cudaSuccess) return cudaErrorMemoryAllocation;
+        marks = marks_;
+    }
+    timed_ = marks != nullptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (!t.graph || st == nullptr || cudaStreamIsCapturing(st, &cap) != cudaSuccess ||
         cap != cudaStreamCaptureStatusNone) {
         last_reuse_ = -1;
-        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st);
+        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks);
     }
     std::vector<unsigned char> key;
     auto put = [&](const void *p, size_t n) {
@@ -88,6 +104,7 @@ cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device
     put(&t.grid, sizeof(t.grid));
     put(&t.chunk, sizeof(t.chunk));
     put(&n_devs, sizeof(n_devs));
+    put(&timed_, sizeof(timed_));
     if (n_devs > 0) put(devs_host, sizeof(Device) * n_devs);
     if (exec_ && key == key_) {
         last_reuse_ = 1;
@@ -97,11 +114,11 @@ cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device
         // a new shape: run directly; capture if it comes again
         last_key_.swap(key);
         last_reuse_ = -1;
-        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st);
+        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks);
     }
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    const cudaError_t run_e = run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st);
+    const cudaError_t run_e = run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(st, &g);
     if (run_e != cudaSuccess || e != cudaSuccess) {

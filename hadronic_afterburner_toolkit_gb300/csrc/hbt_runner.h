@@ -31,6 +31,7 @@ struct Tuning {
     double cell_pt = 0.02;   // Morton cell of p_x, p_y (GeV)
     double cell_y = 0.05;    // Morton cell of rapidity
     bool graph = true;       // launch the pipeline as a CUDA graph
+    bool time_kernels = false;  // record events around the persistent kernels
 };
 
 class BatchRunner {
@@ -59,6 +60,10 @@ class BatchRunner {
     // Graph launches of the last batch: 1 a cached graph was re-launched,
     // 0 captured anew, -1 launched without a graph.
     int last_graph_reuse() const { return last_reuse_; }
+    // Device time of the last timed batch's same-event kernels (with their
+    // merges) and mixed-event kernel, ms (waits for them); false when the
+    // last batch was not timed.
+    bool kernel_times(float &same_ms, float &mixed_ms);
 
   private:
     struct Buf {
@@ -79,6 +84,8 @@ class BatchRunner {
     // graph is captured when the same arguments come twice in a row
     cudaGraphExec_t exec_ = nullptr;
     std::vector<unsigned char> key_, last_key_;
+    cudaEvent_t marks_[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool timed_ = false;
 };
 
 }  // namespace hbt

@@ -58,13 +58,14 @@ class HbtJob(ctypes.Structure):
 
 class HbtTuning(ctypes.Structure):
     _fields_ = [("blocks_per_sm", _I32), ("cell_pt", _D), ("cell_y", _D),
-                ("merge_chunk", _I32), ("use_graph", _I32)]
+                ("merge_chunk", _I32), ("use_graph", _I32), ("time_kernels", _I32)]
 
 
 class HbtStats(ctypes.Structure):
     _fields_ = [(k, _U64) for k in ("pairs_same", "pairs_mixed", "launches",
                                     "ordered_passes", "deferred_kphi", "anomalies",
-                                    "graph_captures", "graph_replays")]
+                                    "graph_captures", "graph_replays")] + \
+        [("same_kernel_ms", _D), ("mixed_kernel_ms", _D)]
 
 
 # Every entry point of include/hbt_gpu.h: name -> (restype, argtypes)
@@ -301,4 +302,5 @@ class Engine:
     def stats(self) -> dict:
         s = HbtStats()
         self._check(self.L.hbt_get_stats(self._h, ctypes.byref(s)))
-        return {k: int(getattr(s, k)) for k, _ in HbtStats._fields_}
+        return {k: (getattr(s, k) if t is _D else int(getattr(s, k)))
+                for k, t in HbtStats._fields_}

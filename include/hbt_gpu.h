@@ -104,6 +104,10 @@ typedef struct hbt_stats {
                                  or a K_T index outside [0, n_KT) */
     uint64_t graph_captures;  /* batched launches captured into a CUDA graph */
     uint64_t graph_replays;   /* batched launches that re-launched a cached graph */
+    /* device time of the last batched launch's persistent kernels, ms, when
+     * hbt_tuning.time_kernels is set (0 otherwise): the same-event kernels
+     * with their FP32 merges, and the mixed-event kernel */
+    double same_kernel_ms, mixed_kernel_ms;
 } hbt_stats;
 
 /* Creates a context on `device` and allocates the zeroed histograms
@@ -173,6 +177,8 @@ typedef struct hbt_tuning {
                                captured when a batch of the same shape comes twice in
                                a row and re-launched while it repeats; 0: direct
                                launches */
+    int32_t time_kernels;   /* 1: time the persistent kernels with CUDA events
+                               (hbt_stats.same_kernel_ms / mixed_kernel_ms) */
 } hbt_tuning;
 
 hbt_status hbt_set_tuning(hbt_ctx *ctx, const hbt_tuning *t);
