@@ -60,6 +60,8 @@ struct hbt_ctx {
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging
     DevBuf in;
+    // readback: two FP64 arrays of the histogram size, used in turn
+    DevBuf exp;
     // upper bounds of the four counter families (num 3-D, den 3-D, num
     // q_inv, den q_inv): max counter <= bound
     u64 ub[4] = {0, 0, 0, 0};
@@ -617,7 +619,7 @@ void hbt_destroy(hbt_ctx *c) {
     DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
-                      &c->apply_iphi, &c->in, &c->part, &c->comp};
+                      &c->apply_iphi, &c->in, &c->part, &c->comp, &c->exp};
     for (DevBuf *b : bufs) dfree(c, *b);
     if (c->staged) cudaEventDestroy(c->staged);
     if (c->own) cudaStreamDestroy(c->own);
@@ -924,25 +926,20 @@ hbt_status hbt_read_hist(hbt_ctx *c, double *num_count, double *q_out_sum, doubl
     TRY(drain_deferrals(c));
     TRY(hbt_sync(c, 0));
     const size_t nb = (size_t)hbt_n_bins(c);
-    if (q_out_sum || q_side_sum || q_long_sum || num) {
-        std::vector<hbt::Sums> s(nb);
-        CU(cudaMemcpy(s.data(), c->sums.p, nb * sizeof(hbt::Sums), cudaMemcpyDeviceToHost));
-        for (size_t k = 0; k < nb; k++) {
-            if (q_out_sum) q_out_sum[k] = s[k].qo;
-            if (q_side_sum) q_side_sum[k] = s[k].qs;
-            if (q_long_sum) q_long_sum[k] = s[k].ql;
-            if (num) num[k] = s[k].w;
-        }
+    // each array is laid out as FP64 on the device (k_export), then copied
+    // straight into the caller's array; two device buffers in turn keep the
+    // next export running while a copy is in flight
+    double *dst[6] = {q_out_sum, q_side_sum, q_long_sum, num, num_count, den};
+    TRY(dalloc(c, c->exp, 2 * nb * sizeof(double)));
+    int used = 0;
+    for (int f = 0; f < 6; f++) {
+        if (!dst[f]) continue;
+        double *buf = ptr<double>(c->exp) + (size_t)(used++ & 1) * nb;
+        CU(hbt::launch_export(c->d, f, buf, (long long)nb, c->stream));
+        CU(cudaMemcpyAsync(dst[f], buf, nb * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
-    std::vector<u64> v(nb);
-    if (num_count) {
-        CU(cudaMemcpy(v.data(), c->cnt.p, nb * sizeof(u64), cudaMemcpyDeviceToHost));
-        for (size_t k = 0; k < nb; k++) num_count[k] = (double)v[k];
-    }
-    if (den) {
-        CU(cudaMemcpy(v.data(), c->den.p, nb * sizeof(u64), cudaMemcpyDeviceToHost));
-        for (size_t k = 0; k < nb; k++) den[k] = (double)v[k];
-    }
+    CU(cudaStreamSynchronize(c->stream));
+    c->st.launches += used;
     return HBT_OK;
 }
 
@@ -1027,8 +1024,9 @@ cudaError_t ctx_merge(hbt_ctx *c, cudaStream_t st) {
 size_t ctx_device_bytes(const hbt_params &p) {
     const size_t slots = (size_t)p.n_KT * (p.azimuthal_flag == 1 ? p.n_Kphi : 1);
     const size_t nb = slots * p.qnpts * p.qnpts * p.qnpts, nq = (size_t)p.n_KT * p.qnpts;
-    size_t bytes = nb * (sizeof(Sums) + 2 * sizeof(u64)) + nq * (sizeof(QiSums) + 2 * sizeof(u64)) +
-                   kDeferCap * sizeof(Deferral) + 4096;
+    // bins, counts, the readback buffers, the q_inv bins, the deferrals
+    size_t bytes = nb * (sizeof(Sums) + 2 * sizeof(u64) + 2 * sizeof(double)) +
+                   nq * (sizeof(QiSums) + 2 * sizeof(u64)) + kDeferCap * sizeof(Deferral) + 4096;
     if (p.precision == HBT_PRECISION_FP32W) bytes += nb * (sizeof(float4) + sizeof(Sums));
     return bytes;
 }

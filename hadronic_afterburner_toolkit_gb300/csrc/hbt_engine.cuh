@@ -150,6 +150,11 @@ cudaError_t launch_apply(const Device &d, const Deferral *rec, const int *iphi, 
 cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, int n_res,
                                cudaStream_t st);
 cudaError_t launch_counters(const Device &d, unsigned long long *out, cudaStream_t st);
+// One output array of hbt_read_hist as FP64 in `out` (nbins doubles):
+// field 0..3 = q_out, q_side, q_long, cos sums; 4 = numerator count;
+// 5 = denominator count.
+cudaError_t launch_export(const Device &d, int field, double *out, long long nbins,
+                          cudaStream_t st);
 
 // Merge of the FP32-weight partial sums into the FP64 bins (hbt_fast.cu).
 cudaError_t launch_merge(const Device &d, cudaStream_t st);

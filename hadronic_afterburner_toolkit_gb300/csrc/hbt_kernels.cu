@@ -17,6 +17,8 @@
 //  ORDER - admit rows before each stream bin's cut row; the cut row itself
 //          is admitted in pair order by the straddle kernel.
 #include "hbt_engine.cuh"
+#include <algorithm>
+
 #include "hbt_chain.cuh"
 
 namespace hbt {
@@ -328,6 +330,30 @@ cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, 
                                cudaStream_t st) {
     if (n_res <= 0) return cudaSuccess;
     k_defer_count<<<(n_res + 127) / 128, 128, 0, st>>>(d, rows, cols, n_res);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) k_export(Device d, int field, double *out,
+                                                long long nbins) {
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nbins;
+         k += (long long)gridDim.x * blockDim.x) {
+        double v;
+        switch (field) {
+            case 0: v = d.h.sums[k].qo; break;
+            case 1: v = d.h.sums[k].qs; break;
+            case 2: v = d.h.sums[k].ql; break;
+            case 3: v = d.h.sums[k].w; break;
+            case 4: v = (double)d.h.cnt[k]; break;
+            default: v = (double)d.h.den[k]; break;
+        }
+        out[k] = v;
+    }
+}
+
+cudaError_t launch_export(const Device &d, int field, double *out, long long nbins,
+                          cudaStream_t st) {
+    const long long blocks = std::min<long long>((nbins + 255) / 256, 152 * 16);
+    k_export<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, st>>>(d, field, out, nbins);
     return cudaGetLastError();
 }
 

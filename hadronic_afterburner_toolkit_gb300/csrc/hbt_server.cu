@@ -2,8 +2,10 @@
 // of many analyses into the batched persistent pair-binning launches.
 //
 // Threads: callers submit and wait; one worker admits requests, uploads
-// their particles, builds rounds and completes requests; one solo thread
-// runs the requests that must go through the per-analysis path.  Streams:
+// their particles, builds and issues rounds and retires them; one
+// completion thread copies the results of finished requests out and frees
+// their memory; one solo thread runs the requests that must go through the
+// per-analysis path.  Streams:
 // uploads and rotations on `upload_`, rounds on `rounds_`, each request's
 // histograms live on its context's own stream.  All device memory of the
 // requests is stream-ordered from one pool, so admitting and finishing
@@ -120,12 +122,21 @@ struct hbt_server {
     std::condition_variable cv_work;  // worker: new requests or stop
     std::condition_variable cv_done;  // waiters
     std::condition_variable cv_solo;
-    bool stop = false;
+    std::condition_variable cv_complete;  // completion thread: finished rounds
+    bool stop = false, worker_done = false;
     std::string err;
     uint64_t next_id = 1;
     std::map<uint64_t, std::unique_ptr<Request>> jobs;
     std::deque<Request *> queued;
     std::deque<Request *> solo_queue;
+    // requests whose last round retired, with the round's status, waiting
+    // for their results to be copied out (completion thread)
+    struct Done {
+        Request *q;
+        hbt_status st;
+        std::string err;
+    };
+    std::deque<Done> done_queue;
 
     // statistics (under mu)
     u64 submitted = 0, completed = 0, failed = 0, n_rounds = 0, pairs = 0;
@@ -139,7 +150,7 @@ struct hbt_server {
     std::deque<Round> in_flight;
     std::vector<cudaEvent_t> spare_events;
 
-    std::thread worker, solo;
+    std::thread worker, solo, completer;
 };
 
 namespace {
@@ -434,6 +445,7 @@ void finish(hbt_server *s, Request &q, hbt_status st) {
         s->failed++;
     }
     s->cv_done.notify_all();
+    s->cv_work.notify_all();  // memory and a slot are free for the queue
 }
 
 void solo_main(hbt_server *s) {
@@ -471,6 +483,30 @@ void solo_main(hbt_server *s) {
     }
 }
 
+// Copies out the results of requests whose last round retired and frees
+// their device memory.
+void completer_main(hbt_server *s) {
+    cudaSetDevice(s->cfg.device);
+    for (;;) {
+        hbt_server::Done d;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_complete.wait(lk, [&] { return s->worker_done || !s->done_queue.empty(); });
+            if (s->done_queue.empty()) return;
+            d = std::move(s->done_queue.front());
+            s->done_queue.pop_front();
+        }
+        hbt_status st = d.st;
+        std::string err = d.err;
+        if (st == HBT_OK) {
+            hbt::ctx_add_pairs(d.q->ctx, d.q->pairs_same, d.q->pairs_mixed);
+            st = collect(s, *d.q, err);
+        }
+        if (st != HBT_OK) set_err(s, "request " + std::to_string(d.q->id) + ": " + err);
+        finish(s, *d.q, st);
+    }
+}
+
 // Completes the oldest round in flight (waits for it when `block`).
 bool retire_round(hbt_server *s, bool block) {
     if (s->in_flight.empty()) return false;
@@ -479,15 +515,14 @@ bool retire_round(hbt_server *s, bool block) {
     const cudaError_t e = cudaEventSynchronize(r.end);
     float ms = 0.f;
     if (e == cudaSuccess) cudaEventElapsedTime(&ms, r.start, r.end);
-    for (Request *q : r.finishing) {
-        hbt_status st = e == cudaSuccess ? HBT_OK : HBT_ERR_CUDA;
-        std::string err = e == cudaSuccess ? "" : cudaGetErrorString(e);
-        if (st == HBT_OK) {
-            hbt::ctx_add_pairs(q->ctx, q->pairs_same, q->pairs_mixed);
-            st = collect(s, *q, err);
-        }
-        if (st != HBT_OK) set_err(s, "request " + std::to_string(q->id) + ": " + err);
-        finish(s, *q, st);
+    {
+        // the completion thread copies the results out, so that the worker
+        // goes on issuing rounds meanwhile
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (Request *q : r.finishing)
+            s->done_queue.push_back({q, e == cudaSuccess ? HBT_OK : HBT_ERR_CUDA,
+                                     e == cudaSuccess ? "" : cudaGetErrorString(e)});
+        if (!r.finishing.empty()) s->cv_complete.notify_one();
     }
     cudaEventDestroy(r.start);
     cudaEventDestroy(r.end);
@@ -610,9 +645,9 @@ void admit_queued(hbt_server *s) {
         } else if (q->work.empty()) {
             // nothing to bin: results are the zero histograms
             cudaEventSynchronize(q->ready);
-            std::string e2;
-            const hbt_status s2 = collect(s, *q, e2);
-            finish(s, *q, s2);
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->done_queue.push_back({q, HBT_OK, ""});
+            s->cv_complete.notify_one();
         } else {
             s->batched.push_back(q);
         }
@@ -704,6 +739,7 @@ hbt_status hbt_server_create(const hbt_server_config *cfg, hbt_server **out) {
     hbt_server *raw = s.release();
     raw->worker = std::thread(worker_main, raw);
     raw->solo = std::thread(solo_main, raw);
+    raw->completer = std::thread(completer_main, raw);
     *out = raw;
     return HBT_OK;
 }
@@ -718,9 +754,12 @@ void hbt_server_destroy(hbt_server *s) {
     if (s->worker.joinable()) s->worker.join();
     {
         std::lock_guard<std::mutex> lk(s->mu);
+        s->worker_done = true;
         s->cv_solo.notify_all();
+        s->cv_complete.notify_all();
     }
     if (s->solo.joinable()) s->solo.join();
+    if (s->completer.joinable()) s->completer.join();
     cudaSetDevice(s->cfg.device);
     for (cudaEvent_t e : s->spare_events) cudaEventDestroy(e);
     if (s->upload) cudaStreamSynchronize(s->upload);
