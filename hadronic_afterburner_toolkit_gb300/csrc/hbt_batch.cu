@@ -201,12 +201,19 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
     return dsm;
 }
 
+// Resident CTAs per SM (register budget 65536 / (128 x CTAs)): measured on
+// GB300, the FP64 form of the same-event kernel is fastest at 5 (its FP64
+// values need the registers), the FP32-weight form and the mixed-event
+// kernel at 6.
+template <int PREC>
+struct SameCtas {
+    static constexpr int value = PREC == 0 ? 5 : 6;
+};
+constexpr int kMixedCtas = 6;
+
 // Same-event items [base, min(end, queued)) pulled by persistent CTAs.
 template <bool AZ, bool BOOST, int PREC>
-#ifndef HBT_SAME_CTAS_PER_SM
-#define HBT_SAME_CTAS_PER_SM 5
-#endif
-__global__ void __launch_bounds__(FT, HBT_SAME_CTAS_PER_SM) k_persistent_same(Device d, BatchDev b, unsigned base,
+__global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(Device d, BatchDev b, unsigned base,
                                                            unsigned end) {
     __shared__ TileSmem sm;
     __shared__ Device dsm;
@@ -234,7 +241,7 @@ __global__ void __launch_bounds__(FT, HBT_SAME_CTAS_PER_SM) k_persistent_same(De
 
 // Mixed-event items, all in one launch.
 template <bool AZ, bool BOOST>
-__global__ void __launch_bounds__(FT, 5) k_persistent_mixed(Device d, BatchDev b) {
+__global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, BatchDev b) {
     __shared__ TileSmem sm;
     __shared__ Device dsm;
     __shared__ unsigned item;
@@ -260,15 +267,38 @@ __global__ void __launch_bounds__(FT, 5) k_persistent_mixed(Device d, BatchDev b
     }
 }
 
+int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+    }
+    return sms;
+}
+
+// grid > 0: that many CTAs; otherwise one CTA per resident slot.
+template <class K>
+int persistent_grid(K kernel, int grid) {
+    if (grid > 0) return grid;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, FT, 0) != cudaSuccess || nb < 1)
+        nb = 4;
+    return sm_count() * nb;
+}
+
 template <bool AZ, bool BOOST, int PREC>
 cudaError_t launch_same_items(const Device &d, const BatchDev &b, unsigned base, unsigned end,
                               int grid, cudaStream_t st) {
+    grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC>, grid);
     k_persistent_same<AZ, BOOST, PREC><<<grid, FT, 0, st>>>(d, b, base, end);
     return cudaGetLastError();
 }
 
 template <bool AZ, bool BOOST>
 cudaError_t launch_mixed_items(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
+    grid = persistent_grid(k_persistent_mixed<AZ, BOOST>, grid);
     k_persistent_mixed<AZ, BOOST><<<grid, FT, 0, st>>>(d, b);
     return cudaGetLastError();
 }

@@ -351,9 +351,8 @@ using hbt::FastJob;
 // The batched path's launch shape from the context's tuning.
 hbt::Tuning runner_tuning(const hbt_ctx *c, const hbt_tuning &t) {
     hbt::Tuning r;
-    const int bps = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, c->max_blocks_per_sm)
-                                        : c->max_blocks_per_sm;
-    r.grid = c->sms * bps;
+    // 0: each persistent kernel at its own occupancy
+    r.grid = t.blocks_per_sm > 0 ? c->sms * std::min(t.blocks_per_sm, 8) : 0;
     r.chunk = c->d.precision == HBT_PRECISION_FP32W ? (unsigned)t.merge_chunk : 0u;
     r.cell_pt = t.cell_pt;
     r.cell_y = t.cell_y;
@@ -857,9 +856,9 @@ hbt_status hbt_autotune_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs, d
             cur_ms = ms;
         }
     }
-    for (int bps = 2; bps <= c->max_blocks_per_sm && rs == HBT_OK; bps++) {
+    for (int bps = 3; bps <= 6 && rs == HBT_OK; bps++) {
         hbt_tuning cand = cur;
-        cand.blocks_per_sm = bps == c->max_blocks_per_sm ? 0 : bps;
+        cand.blocks_per_sm = bps;
         if (cand.blocks_per_sm == cur.blocks_per_sm) continue;
         double ms = 0.0;
         rs = time_one(cand, ms);

@@ -588,7 +588,7 @@ bool issue_round(hbt_server *s) {
     std::string err;
     // rounds differ in shape: direct launches, no graph
     hbt::Tuning tu;
-    tu.grid = s->grid;
+    tu.grid = 0;  // each persistent kernel at its own occupancy
     tu.chunk = ld.precision == HBT_PRECISION_FP32W ? (unsigned)ld.merge_chunk_blocks : 0u;
     tu.graph = false;
     const bool ok = s->runner.run_multi(jobs, devs, tu, s->rounds, err);

@@ -168,7 +168,8 @@ hbt_status hbt_bin_batch_dev(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs);
  * differ in speed only (and, for the FP32-weight form, merge_chunk bounds
  * how many pairs an FP32 partial accumulates). */
 typedef struct hbt_tuning {
-    int32_t blocks_per_sm;  /* persistent CTAs per SM (0: the occupancy limit) */
+    int32_t blocks_per_sm;  /* persistent CTAs per SM, at most 8 (0: each kernel at
+                               its occupancy limit) */
     double cell_pt;         /* sort cell of p_x and p_y in GeV (0: 0.02) */
     double cell_y;          /* sort cell of rapidity (0: 0.05) */
     int32_t merge_chunk;    /* FP32-weight form: same-event tile pairs between two
