@@ -989,6 +989,13 @@ hbt_status hbt_get_stats(hbt_ctx *c, hbt_stats *out) {
     CU(cudaMemcpy(stats, c->stats.p, sizeof(stats), cudaMemcpyDeviceToHost));
     *out = c->st;
     out->anomalies = stats[hbt::STAT_ANOMALY];
+    long long cs = 0, cm = 0, ks = 0, km = 0;
+    if (c->runner.tile_counts(cs, cm, ks, km)) {
+        out->tiles_same = cs;
+        out->tiles_mixed = cm;
+        out->tiles_same_kept = ks;
+        out->tiles_mixed_kept = km;
+    }
     float sm = 0.f, mm = 0.f;
     if (c->tune.time_kernels && c->runner.kernel_times(sm, mm)) {
         out->same_kernel_ms = sm;

@@ -72,6 +72,22 @@ bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<
 // The graph captured for one set of launch arguments stays valid while they
 // are unchanged: the batch tables it reads are re-uploaded before each
 // launch, into the same buffers.
+bool BatchRunner::tile_counts(long long &cand_same, long long &cand_mixed, long long &kept_same,
+                              long long &kept_mixed) {
+    cand_same = last_same_;
+    cand_mixed = last_mixed_;
+    kept_same = kept_mixed = 0;
+    if (!counters_.p || last_pairs_ == 0) return last_pairs_ == 0;
+    unsigned n[2] = {0, 0};
+    if (cudaMemcpyAsync(n, counters_.p, sizeof(n), cudaMemcpyDeviceToHost, last_stream_) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(last_stream_) != cudaSuccess)
+        return false;
+    kept_same = std::min<long long>(n[0], last_same_);
+    kept_mixed = std::min<long long>(n[1], last_mixed_);
+    return true;
+}
+
 bool BatchRunner::kernel_times(float &same_ms, float &mixed_ms) {
     same_ms = mixed_ms = 0.f;
     if (!timed_ || cudaEventSynchronize(marks_[3]) != cudaSuccess) return false;
@@ -196,6 +212,9 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
         bj.push_back(b);
     }
     last_pairs_ = pairs;
+    last_same_ = same_pairs;
+    last_mixed_ = mixed_pairs;
+    last_stream_ = st;
     if (bj.empty()) return true;
     if (same_pairs > 0xffffffffLL || mixed_pairs > 0xffffffffLL || total > 0x7fffffffLL) {
         err = "batch too large (tile pairs or particles)";

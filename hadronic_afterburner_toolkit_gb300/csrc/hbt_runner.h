@@ -57,6 +57,10 @@ class BatchRunner {
 
     // Candidate tile pairs of the last batch.
     long long last_tile_pairs() const { return last_pairs_; }
+    // Candidate and culled (kept) same-event and mixed-event tile pairs of
+    // the last batch (reads the kept counts back: waits for the batch).
+    bool tile_counts(long long &cand_same, long long &cand_mixed, long long &kept_same,
+                     long long &kept_mixed);
     // Graph launches of the last batch: 1 a cached graph was re-launched,
     // 0 captured anew, -1 launched without a graph.
     int last_graph_reuse() const { return last_reuse_; }
@@ -78,7 +82,8 @@ class BatchRunner {
     cudaError_t launch(const Device &d, const BatchDev &b, const Device *devs_host, int n_devs,
                        const Tuning &t, cudaStream_t st);
     Buf lists_, jobs_, offs_, table_, keys_, vals_, sort_temp_, boxes_, items_, counters_, devs_;
-    long long last_pairs_ = 0;
+    long long last_pairs_ = 0, last_same_ = 0, last_mixed_ = 0;
+    cudaStream_t last_stream_ = nullptr;
     int last_reuse_ = -1;
     // the cached graph and the launch arguments it was captured with; a
     // graph is captured when the same arguments come twice in a row

@@ -65,7 +65,8 @@ class HbtStats(ctypes.Structure):
     _fields_ = [(k, _U64) for k in ("pairs_same", "pairs_mixed", "launches",
                                     "ordered_passes", "deferred_kphi", "anomalies",
                                     "graph_captures", "graph_replays")] + \
-        [("same_kernel_ms", _D), ("mixed_kernel_ms", _D)]
+        [("same_kernel_ms", _D), ("mixed_kernel_ms", _D)] + \
+        [(k, _U64) for k in ("tiles_same", "tiles_mixed", "tiles_same_kept", "tiles_mixed_kept")]
 
 
 # Every entry point of include/hbt_gpu.h: name -> (restype, argtypes)

@@ -108,6 +108,9 @@ typedef struct hbt_stats {
      * hbt_tuning.time_kernels is set (0 otherwise): the same-event kernels
      * with their FP32 merges, and the mixed-event kernel */
     double same_kernel_ms, mixed_kernel_ms;
+    /* the last batched launch's 128 x 128 tile pairs: candidates and those
+     * the momentum-space cull kept, same-event and mixed-event */
+    uint64_t tiles_same, tiles_mixed, tiles_same_kept, tiles_mixed_kept;
 } hbt_stats;
 
 /* Creates a context on `device` and allocates the zeroed histograms

@@ -54,6 +54,9 @@ def test_graph_capture_and_relaunch():
         eng.bin_batch(djobs, device=True)
     st = eng.stats()
     assert st["graph_captures"] == 1 and st["graph_replays"] == 1
+    # the cull's statistics of the last batch
+    assert 0 < st["tiles_same_kept"] <= st["tiles_same"]
+    assert 0 < st["tiles_mixed_kept"] <= st["tiles_mixed"]
     orc = oracle_lib.Oracle(**BASE)
     for _ in range(3):
         for j in jobs:
