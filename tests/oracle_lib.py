@@ -323,3 +323,122 @@ def run_golden_case_through_oracle(name: str, out_dir: str) -> Oracle:
         orc.process_buffer(buf, mbuf)
     orc.write(out_dir, int(prm.get("ecooutput", 0)))
     return orc
+
+
+# ------------------------------------------------------- balance function
+
+GOLDEN_BF = os.path.join(REPO, "tests", "golden_bf")
+
+
+class OrcBfParams(ctypes.Structure):
+    _fields_ = [("particle_alpha", _I32), ("particle_beta", _I32), ("BpT_min", _D),
+                ("BpT_max", _D), ("Bnpts", _I32), ("Brap_max", _D), ("rap_type", _I32),
+                ("seed", _I32)]
+
+
+def _bf_lib():
+    L = lib()
+    if getattr(L, "_bf_bound", False):
+        return L
+    _PI32 = ctypes.POINTER(_I32)
+    L.orc_bf_create.restype = ctypes.c_void_p
+    L.orc_bf_create.argtypes = [ctypes.POINTER(OrcBfParams)]
+    L.orc_bf_destroy.argtypes = [ctypes.c_void_p]
+    L.orc_bf_boost.argtypes = [_I64] + [_PD] * 5 + [_D] + [_PD] * 4
+    L.orc_bf_process_buffer.argtypes = [ctypes.c_void_p, _I32, ctypes.POINTER(_I64), _PI32] + \
+        [_PD] * 4 + [_I32, ctypes.POINTER(_I64), _PI32] + [_PD] * 4
+    L.orc_bf_bin.argtypes = [ctypes.c_void_p, _I32, _I64, _PD, _PD, _PD, _I64, _PD, _PD, _PD,
+                             _I32, _D]
+    L.orc_bf_get_hist.argtypes = [ctypes.c_void_p, _I32, _PD]
+    L.orc_bf_get_norm.argtypes = [ctypes.c_void_p, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
+    L.orc_bf_write.restype = ctypes.c_int
+    L.orc_bf_write.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    L._bf_bound = True
+    return L
+
+
+def bf_boost(ev, shift: float = 0.0) -> dict:
+    """pT, phi_p, rap_y, rap_eta of every particle (the reader's boost)."""
+    n = ev.px.size
+    out = {k: np.zeros(n) for k in ("pT", "phi", "y", "eta")}
+    cols = [np.ascontiguousarray(getattr(ev, k), dtype=np.float64)
+            for k in ("mass", "px", "py", "pz", "E")]
+    _bf_lib().orc_bf_boost(n, *[_pd(c) for c in cols], shift,
+                           *[_pd(out[k]) for k in ("pT", "phi", "y", "eta")])
+    return out
+
+
+class BfOracle:
+    def __init__(self, **kw):
+        p = OrcBfParams(**kw)
+        self.p = dict(kw)
+        self._h = _bf_lib().orc_bf_create(ctypes.byref(p))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _bf_lib().orc_bf_destroy(self._h)
+            self._h = None
+
+    def process_buffer(self, ev, kin, mev=None, mkin=None):
+        """ev: events of one buffer; kin: bf_boost of it (likewise the pool)."""
+        if mev is None:
+            mev, mkin = ev, kin
+        keep = []
+
+        def args(e, k):
+            off = np.ascontiguousarray(e.offsets, dtype=np.int64)
+            mon = np.ascontiguousarray(e.monval, dtype=np.int32)
+            cols = [np.ascontiguousarray(k[x]) for x in ("pT", "phi", "y", "eta")]
+            keep.append((off, mon, cols))
+            return ([e.n_events, off.ctypes.data_as(ctypes.POINTER(_I64)),
+                     mon.ctypes.data_as(ctypes.POINTER(_I32))] + [_pd(c) for c in cols])
+        _bf_lib().orc_bf_process_buffer(self._h, *args(ev, kin), *args(mev, mkin))
+
+    def hist(self, which: int) -> np.ndarray:
+        out = np.zeros(self.p["Bnpts"] * 20)
+        _bf_lib().orc_bf_get_hist(self._h, which, _pd(out))
+        return out.reshape(self.p["Bnpts"], 20)
+
+    def write(self, path: str):
+        assert _bf_lib().orc_bf_write(self._h, path.encode()) == 0
+
+
+def bf_golden_case(name: str):
+    d = os.path.join(GOLDEN_BF, name)
+    prm = read_params(os.path.join(d, "parameters.dat"))
+    if int(prm["read_in_mode"]) == 10:
+        ev = read_mode10(os.path.join(d, "particle_samples.gz"))
+        mp = os.path.join(d, "particle_samples_mixed_event.gz")
+        mixed = read_mode10(mp) if os.path.exists(mp) else None
+    else:
+        ev = read_oscar(os.path.join(d, "OSCAR.DAT"))
+        mp = os.path.join(d, "OSCAR_mixed_event.DAT")
+        mixed = read_oscar(mp) if os.path.exists(mp) else None
+    return prm, ev, mixed
+
+
+def bf_params_from(prm: dict) -> dict:
+    return dict(particle_alpha=int(prm["particle_alpha"]), particle_beta=int(prm["particle_beta"]),
+                BpT_min=prm["bpt_min"], BpT_max=prm["bpt_max"], Bnpts=int(prm["bnpts"]),
+                Brap_max=prm["brap_max"], rap_type=int(prm["rap_type"]),
+                seed=int(prm["randomseed"]))
+
+
+def run_bf_golden_case_through_oracle(name: str, out_dir: str) -> BfOracle:
+    from hadronic_afterburner_toolkit_gb300 import synth
+    prm, ev, mixed = bf_golden_case(name)
+    shift = prm.get("rapidity_shift", 0.0)
+    size = int(prm["event_buffer_size"])
+    orc = BfOracle(**bf_params_from(prm))
+    rng_same = buffer_ranges(ev.multiplicities(), size)
+    rng_mixed = buffer_ranges(mixed.multiplicities(), size) if mixed is not None else None
+    for b, (s, e) in enumerate(rng_same):
+        buf = synth.subset(ev, s, e)
+        if mixed is not None:
+            ms, me = rng_mixed[b]
+            mbuf = synth.subset(mixed, ms, me)
+            orc.process_buffer(buf, bf_boost(buf, shift), mbuf, bf_boost(mbuf, shift))
+        else:
+            orc.process_buffer(buf, bf_boost(buf, shift))
+    orc.write(out_dir)
+    return orc

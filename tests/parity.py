@@ -63,6 +63,8 @@ def compare(eng_h, orc_h, q_scale, rtol=RTOL, exact_sums=False):
 def _parse_table(text):
     rows = []
     for line in text.strip().split("\n"):
+        if line.lstrip().startswith("#"):
+            continue
         rows.append([float("nan") if "nan" in tok else float(tok) for tok in line.split()])
     return np.array(rows)
 
