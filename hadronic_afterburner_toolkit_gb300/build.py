@@ -42,6 +42,7 @@ GPU_UNITS = {
     "hbt_batch.cu": ["--fmad=false"],
     "hbt_runner.cu": [],
     "hbt_server.cu": ["--fmad=false"],
+    "hbt_bf.cu": ["--fmad=false"],
 }
 
 

@@ -3,6 +3,7 @@
 #include <fstream>
 #include <iostream>
 
+#include "BalanceFunction.h"
 #include "HBT_correlation.h"
 
 Analysis::Analysis(std::string path) : path_(path) {}
@@ -48,9 +49,12 @@ void Analysis::PerformAnalysis() {
         HBTAnalysis();
         particle_list_.reset();
     }
-    if (paraRdr_.getVal("analyze_balance_function") == 1)
-        std::cout << "[Warning] analyze_balance_function: not part of this build; skipped"
-                  << std::endl;
+    if (paraRdr_.getVal("analyze_balance_function") == 1) {
+        std::cout << "[Info] Analyze balance functions ..." << std::endl;
+        particle_list_ = std::make_shared<particleSamples>(paraRdr_, path_, ran_gen_ptr_);
+        BalanceFunctionAnalysis();
+        particle_list_.reset();
+    }
     if (paraRdr_.getVal("analyze_ebe_yield") == 1)
         std::cout << "[Warning] analyze_ebe_yield: not part of this build; skipped" << std::endl;
 }
@@ -73,4 +77,20 @@ void Analysis::HBTAnalysis() {
     std::cout << "[Info] HBT pairs: " << st.pairs_same << " same-event, " << st.pairs_mixed
               << " mixed-event; " << st.launches << " GPU launches, " << st.deferred_kphi
               << " K_phi edge pairs decided on the host" << std::endl;
+}
+
+// src/Analysis.cpp:856-874
+void Analysis::BalanceFunctionAnalysis() {
+    BalanceFunction bf(paraRdr_, path_, ran_gen_ptr_);
+    int event_id = 0;
+    while (!particle_list_->end_of_file()) {
+        particle_list_->read_in_particle_samples_and_filter();
+        particle_list_->read_in_particle_samples_mixed_event_and_filter();
+        const int nev = particle_list_->get_number_of_events();
+        std::cout << "[Info] Reading event: " << event_id + 1 << " ... nev = " << nev
+                  << std::endl;
+        bf.calculate_balance_function(particle_list_);
+        event_id += nev;
+    }
+    bf.output_balance_function();
 }

@@ -1,8 +1,9 @@
-// Driver of the HBT analysis (the HBT part of the reference's Analysis
-// class, src/Analysis.{h,cpp}: parameter dictionary, RNG seeding and the
-// buffer loop of Analysis::HBTAnalysis, src/Analysis.cpp:817-835).  The
-// flow, balance-function and yield analyses are not part of this build and
-// are skipped with a warning.
+// Driver of the HBT and balance-function analyses (those parts of the
+// reference's Analysis class, src/Analysis.{h,cpp}: parameter dictionary,
+// RNG seeding and the buffer loops of Analysis::HBTAnalysis and
+// Analysis::BalanceFunctionAnalysis, src/Analysis.cpp:817-874).  The flow
+// and yield analyses are not part of this build and are skipped with a
+// warning.
 #pragma once
 
 #include <memory>
@@ -20,6 +21,7 @@ class Analysis {
     void InitializeAnalysis();
     void PerformAnalysis();
     void HBTAnalysis();
+    void BalanceFunctionAnalysis();
     ParameterReader &parameters() { return paraRdr_; }
 
   private:

@@ -18,6 +18,17 @@ particleSamples::particleSamples(ParameterReader &paraRdr, std::string path,
     rap_shift_ = paraRdr_.getVal("rapidity_shift", 0);
     read_mixed_events_ = paraRdr_.getVal("read_in_real_mixed_events") == 1;
     particle_monval_ = static_cast<int>(paraRdr_.getVal("particle_monval"));
+    analyze_bf_ = paraRdr_.exist("analyze_balance_function") &&
+                  paraRdr_.getVal("analyze_balance_function") == 1;
+    if (analyze_bf_) {
+        // src/particleSamples.cpp:66-71
+        const int a = static_cast<int>(paraRdr_.getVal("particle_alpha"));
+        const int b = static_cast<int>(paraRdr_.getVal("particle_beta"));
+        bf_monval_[0] = a;
+        bf_monval_[1] = -a;
+        bf_monval_[2] = b;
+        bf_monval_[3] = -b;
+    }
     if (paraRdr_.getVal("resonance_feed_down_flag") == 1 ||
         paraRdr_.getVal("resonance_weak_feed_down_flag") == 1)
         throw std::runtime_error("particleSamples: resonance decays are not part of this build");
@@ -115,6 +126,8 @@ int particleSamples::read_in_particle_samples_mixed_event() {
 void particleSamples::read_in_particle_samples_and_filter() {
     read_in_particle_samples();
     filter(full_, filtered_);
+    if (analyze_bf_)
+        for (int s = 0; s < 4; s++) filter_code(bf_monval_[s], full_, bf_[s]);
 }
 
 void particleSamples::read_in_particle_samples_mixed_event_and_filter() {
@@ -125,6 +138,8 @@ void particleSamples::read_in_particle_samples_mixed_event_and_filter() {
     read_in_particle_samples_mixed_event();
     filter(full_mixed_, filtered_mixed_);
     mixed_list_ = &filtered_mixed_;
+    if (analyze_bf_)
+        for (int s = 0; s < 4; s++) filter_code(bf_monval_[s], full_mixed_, bf_mixed_[s]);
 }
 
 void particleSamples::filter(const EventList &full, EventList &out) {
@@ -135,9 +150,16 @@ void particleSamples::filter(const EventList &full, EventList &out) {
             if (pick(p.monval)) out[e].push_back(p);
 }
 
+void particleSamples::filter_code(int poi, const EventList &full, EventList &out) {
+    out.clear();
+    out.resize(full.size());
+    for (size_t e = 0; e < full.size(); e++)
+        for (const auto &p : full[e])
+            if (pick_code(poi, p.monval)) out[e].push_back(p);
+}
+
 // decide_to_pick_OSCAR (src/particleSamples.cpp:625-678).
-bool particleSamples::pick(int monval) {
-    const int poi = particle_monval_;
+bool particleSamples::pick_code(int poi, int monval) {
     if (poi == 99999) return true;
     const bool klass = poi == 9999 || poi == 9998 || poi == -9998 || poi == 9997 ||
                        poi == -9997 || poi == 9996 || poi == -9996;

@@ -10,7 +10,8 @@
 //  - rapidity_shift boost of E and pz (:442-468), on all host threads;
 //  - particle_monval filter (:1329-1346): a Monte-Carlo number, or the
 //    class codes 9999 / +-9998 / +-9997 / +-9996 (charged, charge sign,
-//    baryon sign, strangeness sign) looked up in EOS/pdg.dat.
+//    baryon sign, strangeness sign) looked up in EOS/pdg.dat;
+//  - the balance-function species lists (:1300-1330, :1370-1460, :538-551).
 // Other reader modes (UrQMD, JAM, SMASH, iSS binary) and resonance decays
 // are not part of this build; asking for them throws.
 #pragma once
@@ -65,6 +66,16 @@ class particleSamples {
         return (*mixed_list_)[event_id];
     }
 
+    // Balance-function species lists (analyze_balance_function = 1; the
+    // reference's get_balance_function_particle_list_*): s = 0 a, 1 abar,
+    // 2 b, 3 bbar with a = particle_alpha, b = particle_beta, abar = -a,
+    // bbar = -b; the mixed-event lists come from the mixed-event pool (the
+    // buffer itself when read_in_real_mixed_events = 0).
+    const hbt::EventList &balance_function_list(int s) const { return bf_[s]; }
+    const hbt::EventList &balance_function_list_mixed_event(int s) const {
+        return read_mixed_events_ ? bf_mixed_[s] : bf_[s];
+    }
+
   private:
     typedef hbt::EventList EventList;
 
@@ -90,9 +101,14 @@ class particleSamples {
     std::map<int, int> charge_, baryon_, strange_;
     bool pdg_loaded_ = false;
     int reader_threads_ = 0;  // host threads of the reader and boost (0: all)
+    bool analyze_bf_ = false;
+    int bf_monval_[4] = {0, 0, 0, 0};
+    EventList bf_[4], bf_mixed_[4];
 
     void boost(EventList &evs) const;
     void filter(const EventList &full, EventList &out);
-    bool pick(int monval);
+    void filter_code(int poi, const EventList &full, EventList &out);
+    bool pick(int monval) { return pick_code(particle_monval_, monval); }
+    bool pick_code(int poi, int monval);
     void load_pdg();
 };

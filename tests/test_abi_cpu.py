@@ -11,6 +11,7 @@ from hadronic_afterburner_toolkit_gb300 import build, engine
 INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
 HEADER = os.path.join(INCLUDE, "hbt_gpu.h")
 SERVER_HEADER = os.path.join(INCLUDE, "hbt_server.h")
+BF_HEADER = os.path.join(INCLUDE, "hbt_bf.h")
 
 
 def _declared_functions(path):
@@ -34,8 +35,16 @@ def test_header_declares_the_engine_api():
 
 
 def test_library_exports_every_declared_symbol(lib):
-    for name in _declared_functions(HEADER) + _declared_functions(SERVER_HEADER):
+    for name in (_declared_functions(HEADER) + _declared_functions(SERVER_HEADER) +
+                 _declared_functions(BF_HEADER)):
         assert hasattr(lib, name), name
+
+
+def test_bf_header_matches_its_binding(lib):
+    from hadronic_afterburner_toolkit_gb300 import bf
+    names = _declared_functions(BF_HEADER)
+    assert "hbt_bf_bin" in names and "hbt_bf_read" in names
+    assert sorted(bf.exported_symbols()) == names
 
 
 def test_server_header_matches_its_binding(lib):

@@ -10,7 +10,7 @@ import oracle_lib
 import parity
 
 CASES = sorted(d for d in os.listdir(oracle_lib.GOLDEN_BF)
-               if os.path.isdir(os.path.join(oracle_lib.GOLDEN_BF, d)))
+               if os.path.exists(os.path.join(oracle_lib.GOLDEN_BF, d, "parameters.dat")))
 
 
 @pytest.mark.parametrize("name", CASES)

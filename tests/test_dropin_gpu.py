@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 EXE = os.path.join(oracle_lib.REPO, "hadronic_afterburner_toolkit_gb300", "lib",
                    "hbt_afterburner.e")
 CASES = sorted(d for d in os.listdir(oracle_lib.GOLDEN)
-               if os.path.isdir(os.path.join(oracle_lib.GOLDEN, d)))
+               if os.path.exists(os.path.join(oracle_lib.GOLDEN, d, "parameters.dat")))
 
 
 def _parse(text):

@@ -13,7 +13,7 @@ import parity
 from hadronic_afterburner_toolkit_gb300 import build, engine, synth
 
 CASES = sorted(d for d in os.listdir(oracle_lib.GOLDEN)
-               if os.path.isdir(os.path.join(oracle_lib.GOLDEN, d)))
+               if os.path.exists(os.path.join(oracle_lib.GOLDEN, d, "parameters.dat")))
 _PD = ctypes.POINTER(ctypes.c_double)
 _PU = ctypes.POINTER(ctypes.c_uint64)
 

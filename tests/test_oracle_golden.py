@@ -16,7 +16,7 @@ import oracle_lib
 import parity
 
 CASES = sorted(d for d in os.listdir(oracle_lib.GOLDEN)
-               if os.path.isdir(os.path.join(oracle_lib.GOLDEN, d)))
+               if os.path.exists(os.path.join(oracle_lib.GOLDEN, d, "parameters.dat")))
 
 
 def _golden_files(name):
