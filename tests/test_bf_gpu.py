@@ -125,7 +125,7 @@ def test_bf_bin_edges_and_tiles():
                      *[oracle_lib._pd(c) for c in cols[3:]], mx, rot)
     for h in range(5):
         assert np.array_equal(eng.hist(h), orc.hist(h)), h
-    assert eng.hist(0).sum() > 60000
+    assert eng.hist(0).sum() > 30000  # most of the 300 x 200 tile pairs fall in the Delta y window
 
 
 def test_bf_rejects_bad_jobs():
