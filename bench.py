@@ -545,6 +545,74 @@ def average_leg(n_events: int = 12, seed: int = 11) -> dict:
             "host_threads": os.cpu_count()}
 
 
+def bf_leg(n_events: int = 200, seed: int = 21) -> dict:
+    """Balance function (pi+ / pi-): 200 events with Poisson(700) pi+ and
+    pi-, Poisson(120) K+ and K-; Bnpts = 41 on |Delta y| <= 2, pT in
+    [0.2, 2] GeV; every event against itself (4 same-event histograms) and
+    against a drawn partner event with a random rotation (4 mixed-event
+    histograms): all 8 x 200 event pairs in one hbt_bf_bin call, against
+    the CPU oracle's restatement of the reference loop on a sample."""
+    import ctypes
+    from hadronic_afterburner_toolkit_gb300 import bf, synth
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    rng = np.random.default_rng(seed)
+    kinds = [(211, synth.PION_MASS, 0.25, 700.0), (-211, synth.PION_MASS, 0.25, 700.0),
+             (321, synth.KAON_MASS, 0.30, 120.0), (-321, synth.KAON_MASS, 0.30, 120.0)]
+    gens = [synth.generate(n_events, mu, seed=seed + k, mass=m, monval=mon, T=T, y_max=2.0)
+            for k, (mon, m, T, mu) in enumerate(kinds)]
+    # species lists a = pi+, abar = pi-, b = pi-, bbar = pi+ (alpha 211, beta -211)
+    lists = []
+    for g in (gens[0], gens[1], gens[1], gens[0]):
+        kin = oracle_lib.bf_boost(g)
+        keep = ~((kin["pT"] < 0.2) | (kin["pT"] > 2.0))
+        evid = np.repeat(np.arange(g.n_events), g.multiplicities())
+        off = np.zeros(g.n_events + 1, np.int64)
+        np.cumsum(np.bincount(evid[keep], minlength=g.n_events), out=off[1:])
+        lists.append((off, kin["phi"][keep], kin["y"][keep]))
+    lists = lists + lists  # the mixed-event pool is the buffer itself
+    pairs_of = [(0, 2), (1, 3), (0, 3), (1, 2)]
+    jobs = []
+    for h, (la, lb) in enumerate(pairs_of):
+        for e in range(n_events):
+            jobs.append((h, la, e, lb, e, 0, 0.0))
+            jobs.append((4 + h, la, e, 4 + lb, int(rng.integers(n_events)), 1,
+                         float(rng.uniform(0, 2 * np.pi))))
+    n_pairs = sum(int((lists[la][0][ea + 1] - lists[la][0][ea]) *
+                      (lists[lb][0][eb + 1] - lists[lb][0][eb]))
+                  for (h, la, ea, lb, eb, mx, rot) in jobs)
+    eng = bf.BfEngine(41, 2.0)
+    eng.bin(lists, jobs)  # warm-up
+    eng.reset()
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        eng.bin(lists, jobs)
+        times.append(time.perf_counter() - t0)
+    t_gpu = min(times)
+    # CPU: the oracle's pair loop on the first jobs, ~5 s
+    orc = oracle_lib.BfOracle(particle_alpha=211, particle_beta=-211, BpT_min=0.2, BpT_max=2.0,
+                              Bnpts=41, Brap_max=2.0, rap_type=1, seed=1)
+    L = oracle_lib._bf_lib()
+    done, t0 = 0, time.perf_counter()
+    for (h, la, ea, lb, eb, mx, rot) in jobs:
+        A, B = lists[la], lists[lb]
+        a0, a1, b0, b1 = A[0][ea], A[0][ea + 1], B[0][eb], B[0][eb + 1]
+        cols = [np.ascontiguousarray(x) for x in (np.ones(a1 - a0), A[1][a0:a1], A[2][a0:a1],
+                                                   np.ones(b1 - b0), B[1][b0:b1], B[2][b0:b1])]
+        L.orc_bf_bin(orc._h, h, a1 - a0, *[oracle_lib._pd(c) for c in cols[:3]], b1 - b0,
+                     *[oracle_lib._pd(c) for c in cols[3:]], mx, rot)
+        done += int((a1 - a0) * (b1 - b0))
+        if time.perf_counter() - t0 > 5.0:
+            break
+    t_cpu = time.perf_counter() - t0
+    return {"events": n_events, "event_pairs": len(jobs), "pairs": n_pairs,
+            "seconds": t_gpu, "pairs_per_s": n_pairs / t_gpu,
+            "timing": "host clock around hbt_bf_bin (list upload, kernel, sync)",
+            "cpu_oracle_pairs_per_s": done / t_cpu, "cpu_cores": 1,
+            "cpu_sample_pairs": done, "speedup_vs_cpu_core": (n_pairs / t_gpu) / (done / t_cpu)}
+
+
 def make_requests(n_jobs: int, seed: int = 5):
     """Requests of the serving workload: 10-500 events each, multiplicity
     Poisson(mu) with mu uniform in [50, 2000], pi+ or K+, qnpts in
@@ -632,6 +700,8 @@ def main() -> None:
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the Poisson request stream through the serving loop")
     ap.add_argument("--serving-jobs", type=int, default=48)
+    ap.add_argument("--no-bf", action="store_true",
+                    help="skip the balance-function leg")
     ap.add_argument("--no-ingest", action="store_true",
                     help="skip the reader timing (line-by-line against block reader)")
     args = ap.parse_args()
@@ -849,9 +919,12 @@ def main() -> None:
         cpu = cpu_baseline(groups[0], p, nthreads=1)
 
     uneven = serving = ingest = average = None
+    balance = None
     if not args.no_ingest and rank == 0:
         ingest = ingest_leg()
         average = average_leg()
+    if not args.no_bf and rank == 0:
+        balance = bf_leg()
     if not args.no_uneven:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
@@ -890,6 +963,7 @@ def main() -> None:
                 "serving": serving,
                 "ingest": ingest,
                 "average": average,
+                "balance_function": balance,
                 "stats": st}
         print(json.dumps(line))
     eng.close()

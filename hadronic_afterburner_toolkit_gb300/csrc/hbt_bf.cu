@@ -2,9 +2,11 @@
 //
 // One CTA per event pair (job): the particles of list A in registers (one
 // per thread), those of list B staged through shared memory in tiles of
-// 128, every pair binned with the reference's FP64 expressions
-// (src/BalanceFunction.cpp:136-160 and :183-204, this unit is compiled
-// with --fmad=false) into a shared-memory histogram of Bnpts x 20 counts,
+// 128.  Every pair is binned in FP32 with rigorous error bounds (bin32);
+// the pairs within those bounds of a bin edge or a cut run the reference's
+// FP64 expressions (bin64, src/BalanceFunction.cpp:136-160 and :183-204;
+// this unit is compiled with --fmad=false), so every bin is the
+// reference's.  Counts go to a shared-memory histogram of Bnpts x 20,
 // whose non-zero bins are added to the global histogram when the job is
 // done.  The bins are few and every pair lands in one, so privatising the
 // histogram in shared memory turns the pair rate's worth of global atomics
@@ -28,44 +30,99 @@ struct BfJob {
     int hist, mixed;
 };
 
-// The reference's binning constants (src/BalanceFunction.cpp:29-35).
+// The reference's binning constants (src/BalanceFunction.cpp:29-35) and
+// their FP32 copies for the screen.
 struct BfConst {
     double drap, Brap_min, dphi, Bphi_min;
     int Bnpts;
+    float f_Brap_min, f_inv_drap, f_Bphi_min, f_inv_dphi;
 };
+
+constexpr float kU = 5.9604645e-8f;  // 2^-24
+
+// The reference's FP64 binning of one pair (src/BalanceFunction.cpp
+// :183-204; the same-event loop :136-157 has no rotation term, and adding
+// a zero rotation changes no value): the flat bin, or -1 when skipped.
+__device__ __forceinline__ int bin64(const BfConst &c, double pa, double ya, double pb, double yb,
+                                     int mixed, double rot) {
+    const double d = mixed ? (pa - pb) + rot : pa - pb;
+    int ip = static_cast<int>(floor((d - c.Bphi_min) / c.dphi)) % kNphi;
+    if (ip < 0) ip += kNphi;
+    const double dy = ya - yb;
+    if (fabs(dy) < 1e-10) return -1;
+    if (dy < c.Brap_min) return -1;
+    const int iy = static_cast<int>((dy - c.Brap_min) / c.drap);
+    if (iy >= 0 && iy < c.Bnpts) return iy * kNphi + ip;
+    return -1;
+}
+
+// The same decision from FP32 copies with rigorous error bounds (u =
+// 2^-24 per rounding, every input rounded once from FP64, bounds widened by
+// a factor for the FP32 constants and the reference's own FP64 rounding):
+// the bin, -1 (skipped) or -2 (undecided: the caller runs bin64).
+__device__ __forceinline__ int bin32(const BfConst &c, float pa, float ya, float pb, float yb,
+                                     int mixed, float rot) {
+    const float s1 = pa - pb;
+    const float d = mixed ? s1 + rot : s1;
+    const float ed = 3.0f * kU * (fabsf(d) + fabsf(pa) + fabsf(pb) + fabsf(rot));
+    const float t = (d - c.f_Bphi_min) * c.f_inv_dphi;
+    const float et = (ed + 3.0f * kU * (fabsf(d) + fabsf(c.f_Bphi_min))) * c.f_inv_dphi * 1.01f +
+                     3.0f * kU * fabsf(t) + 1e-6f;
+    const float kp = floorf(t), fp = t - kp;
+    if (!(fp > et) || !(fp < 1.0f - et)) return -2;
+    const float dy = ya - yb;
+    const float ey = 3.0f * kU * (fabsf(ya) + fabsf(yb) + fabsf(dy)) + 1e-12f;
+    const float ady = fabsf(dy);
+    // 1e-10f rounds above 1e-10: both tests keep a relative margin
+    if (ady + ey < 0.9999e-10f) return -1;  // |dy| < 1e-10 for certain
+    if (!(ady - ey > 1.0001e-10f)) return -2;
+    const float eb = ey + 3.0f * kU * fabsf(c.f_Brap_min);
+    if (dy + eb < c.f_Brap_min) return -1;  // dy < Brap_min for certain
+    if (!(dy - eb > c.f_Brap_min)) return -2;
+    const float ty = (dy - c.f_Brap_min) * c.f_inv_drap;
+    const float ety = (eb + 3.0f * kU * fabsf(dy - c.f_Brap_min)) * c.f_inv_drap * 1.01f +
+                      3.0f * kU * fabsf(ty) + 1e-6f;
+    const float ky = floorf(ty), fy = ty - ky;
+    if (!(fy > ety) || !(fy < 1.0f - ety)) return -2;
+    const int iy = (int)ky;
+    if (iy < 0 || iy >= c.Bnpts) return -1;
+    int ip = ((int)kp) % kNphi;
+    if (ip < 0) ip += kNphi;
+    return iy * kNphi + ip;
+}
 
 __global__ void __launch_bounds__(kTile) k_bf(const BfJob *jobs, long long n_jobs,
                                               const double *phi, const double *y, BfConst c,
                                               unsigned long long *hist) {
     extern __shared__ unsigned sh[];  // [Bnpts][kNphi]
     __shared__ double sphi[kTile], sy[kTile];
+    __shared__ float fphi[kTile], fy[kTile];
     const int nbins = c.Bnpts * kNphi;
     for (long long job = blockIdx.x; job < n_jobs; job += gridDim.x) {
         for (int k = threadIdx.x; k < nbins; k += blockDim.x) sh[k] = 0u;
         __syncthreads();
         const BfJob J = jobs[job];
+        const float frot = (float)J.rotation;
         for (long long a = J.a0; a < J.a1; a += kTile) {
             const long long ia = a + threadIdx.x;
             const bool have = ia < J.a1;
             const double pa = have ? phi[ia] : 0.0, ya = have ? y[ia] : 0.0;
+            const float fpa = (float)pa, fya = (float)ya;
             for (long long b = J.b0; b < J.b1; b += kTile) {
                 __syncthreads();
                 if (b + threadIdx.x < J.b1) {
                     sphi[threadIdx.x] = phi[b + threadIdx.x];
                     sy[threadIdx.x] = y[b + threadIdx.x];
+                    fphi[threadIdx.x] = (float)sphi[threadIdx.x];
+                    fy[threadIdx.x] = (float)sy[threadIdx.x];
                 }
                 __syncthreads();
                 const int nb = (int)min((long long)kTile, J.b1 - b);
                 if (!have) continue;
                 for (int j = 0; j < nb; j++) {
-                    const double d = J.mixed ? (pa - sphi[j]) + J.rotation : pa - sphi[j];
-                    int ip = static_cast<int>(floor((d - c.Bphi_min) / c.dphi)) % kNphi;
-                    if (ip < 0) ip += kNphi;
-                    const double dy = ya - sy[j];
-                    if (fabs(dy) < 1e-10) continue;
-                    if (dy < c.Brap_min) continue;
-                    const int iy = static_cast<int>((dy - c.Brap_min) / c.drap);
-                    if (iy >= 0 && iy < c.Bnpts) atomicAdd(&sh[iy * kNphi + ip], 1u);
+                    int k = bin32(c, fpa, fya, fphi[j], fy[j], J.mixed, frot);
+                    if (k == -2) k = bin64(c, pa, ya, sphi[j], sy[j], J.mixed, J.rotation);
+                    if (k >= 0) atomicAdd(&sh[k], 1u);
                 }
             }
         }
@@ -132,6 +189,10 @@ hbt_status hbt_bf_create(const hbt_bf_params *p, int device, hbt_bf_ctx **out) {
     c->c.dphi = 2. * M_PI / kNphi;
     c->c.Bphi_min = -M_PI / 2.;
     c->c.Bnpts = p->Bnpts;
+    c->c.f_Brap_min = (float)c->c.Brap_min;
+    c->c.f_inv_drap = (float)(1.0 / c->c.drap);
+    c->c.f_Bphi_min = (float)c->c.Bphi_min;
+    c->c.f_inv_dphi = (float)(1.0 / c->c.dphi);
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         !grow(c->hist, (size_t)8 * p->Bnpts * kNphi * sizeof(unsigned long long))) {

@@ -1,7 +1,7 @@
 """Balance-function pair binning on the GPU (include/hbt_bf.h) against the
 oracle's restatement of the reference's loops, histogram by histogram:
-counts must be identical (the bins are decided in FP64 in the reference's
-operation order).  Inputs: the golden balance-function cases with their
+counts must be identical (an FP32 screen with rigorous bounds decides most
+pairs; the rest are binned in FP64 in the reference's operation order).  Inputs: the golden balance-function cases with their
 species lists, and hand-made lists whose differences sit on bin edges."""
 import math
 
@@ -163,3 +163,48 @@ def test_bf_dropin_matches_reference_files(name, tmp_path):
         want = {m.name: tar.extractfile(m).read() for m in tar.getmembers()}
     for f in want:
         parity.same_output_file(open(res / f, "rb").read(), want[f], f)
+
+
+def test_bf_fp32_screen_near_edges():
+    """Differences a few FP32 ulps either side of every Delta y and Delta
+    phi edge and of the Delta y cuts, at rapidities and angles of several
+    magnitudes: the FP32 screen must hand every pair it cannot decide to
+    the FP64 expressions, so the counts stay the oracle's."""
+    from hadronic_afterburner_toolkit_gb300 import bf
+    Bnpts, Brap_max = 41, 2.0
+    drap = 2.0 * Brap_max / (Bnpts - 1)
+    ymin = -Brap_max - 0.5 * drap
+    dphi = 2.0 * math.pi / 20
+    rng = np.random.default_rng(11)
+    edges_y = np.array([ymin + k * drap for k in range(Bnpts + 1)])
+    edges_p = np.array([-math.pi / 2 + k * dphi for k in range(41)])
+    offs = np.concatenate([[0.0], np.outer([1, -1], [1e-9, 3e-8, 1e-7, 4e-7, 2e-6]).ravel()])
+    yb = np.array([0.0, 0.75, -3.2, 1e-11])
+    pb = np.array([0.0, 1.3, -2.9, 3.1])
+    ya, pa = [], []
+    for y0, p0 in zip(yb, pb):
+        for o in offs:
+            ya.append(edges_y + y0 + o * (1.0 + abs(y0)))
+            pa.append(np.resize(edges_p, edges_y.size) + p0 + o * (1.0 + abs(p0)))
+    ya = np.concatenate(ya + [yb, yb + 1e-10, yb - 2e-10])
+    pa = np.concatenate(pa + [pb, pb + 1e-7, pb - dphi])
+    A = (np.array([0, ya.size], np.int64), pa, ya)
+    B = (np.array([0, yb.size], np.int64), pb, yb)
+    jobs = [(0, 0, 0, 1, 0, 0, 0.0)]
+    for r, rot in enumerate([dphi, 2 * math.pi - dphi, 0.5 + 1e-8, 4 * dphi - 1e-9,
+                             rng.uniform(0, 2 * math.pi), 1e-300, 6.0]):
+        jobs.append((1 + r, 0, 0, 1, 0, 1, rot))
+    eng = bf.BfEngine(Bnpts, Brap_max)
+    eng.bin([A, B], jobs)
+    orc = oracle_lib.BfOracle(particle_alpha=1, particle_beta=2, BpT_min=-1.0, BpT_max=10.0,
+                              Bnpts=Bnpts, Brap_max=Brap_max, rap_type=1, seed=1)
+    L = oracle_lib._bf_lib()
+    for (h, la, ea, lb, eb, mx, rot) in jobs:
+        cols = [np.ascontiguousarray(x) for x in (np.ones(ya.size), pa, ya,
+                                                   np.ones(yb.size), pb, yb)]
+        L.orc_bf_bin(orc._h, h, ya.size, *[oracle_lib._pd(c) for c in cols[:3]], yb.size,
+                     *[oracle_lib._pd(c) for c in cols[3:]], mx, rot)
+    for h in range(len(jobs)):
+        g, o = eng.hist(h), orc.hist(h)
+        assert np.array_equal(g, o), "histogram %d differs at %s" % (h, np.argwhere(g != o)[:5])
+    assert eng.hist(0).sum() > 1000
