@@ -582,14 +582,16 @@ def bf_leg(n_events: int = 200, seed: int = 21) -> dict:
                       (lists[lb][0][eb + 1] - lists[lb][0][eb]))
                   for (h, la, ea, lb, eb, mx, rot) in jobs)
     eng = bf.BfEngine(41, 2.0)
-    eng.bin(lists, jobs)  # warm-up
+    jarr = bf.job_array(jobs)
+    eng.bin(lists, jarr)  # warm-up
     eng.reset()
     times = []
     for _ in range(3):
         t0 = time.perf_counter()
-        eng.bin(lists, jobs)
+        eng.bin(lists, jarr)
         times.append(time.perf_counter() - t0)
     t_gpu = min(times)
+    st = eng.stats()
     # CPU: the oracle's pair loop on the first jobs, ~5 s
     orc = oracle_lib.BfOracle(particle_alpha=211, particle_beta=-211, BpT_min=0.2, BpT_max=2.0,
                               Bnpts=41, Brap_max=2.0, rap_type=1, seed=1)
@@ -609,6 +611,10 @@ def bf_leg(n_events: int = 200, seed: int = 21) -> dict:
     return {"events": n_events, "event_pairs": len(jobs), "pairs": n_pairs,
             "seconds": t_gpu, "pairs_per_s": n_pairs / t_gpu,
             "timing": "host clock around hbt_bf_bin (list upload, kernel, sync)",
+            "kernel_ms": st["kernel_ms"], "upload_ms": st["upload_ms"],
+            "kernel_pairs_per_s": n_pairs / (st["kernel_ms"] * 1e-3),
+            "bytes_uploaded": st["bytes_uploaded"],
+            "fp64_fallback_fraction": st["fp64_pairs"] / max(n_pairs, 1),
             "cpu_oracle_pairs_per_s": done / t_cpu, "cpu_cores": 1,
             "cpu_sample_pairs": done, "speedup_vs_cpu_core": (n_pairs / t_gpu) / (done / t_cpu)}
 

@@ -36,6 +36,21 @@ class HbtBfJob(ctypes.Structure):
                 ("mixed", _I32), ("rotation", _D)]
 
 
+JOB_DTYPE = np.dtype([("hist", "<i4"), ("la", "<i4"), ("ea", "<i4"), ("lb", "<i4"),
+                      ("eb", "<i4"), ("mixed", "<i4"), ("rotation", "<f8")], align=True)
+
+
+def job_array(jobs) -> np.ndarray:
+    """(hist, la, ea, lb, eb, mixed, rotation) tuples as an array laid out
+    like ``hbt_bf_job``, which ``BfEngine.bin`` passes without conversion."""
+    return np.array([tuple(j) for j in jobs], dtype=JOB_DTYPE)
+
+
+class HbtBfStats(ctypes.Structure):
+    _fields_ = [("pairs", _I64), ("bytes_uploaded", _I64), ("fp64_pairs", _I64),
+                ("upload_ms", _D), ("kernel_ms", _D)]
+
+
 SIGNATURES = {
     "hbt_bf_create": (_I32, [ctypes.POINTER(HbtBfParams), ctypes.c_int, ctypes.POINTER(_VP)]),
     "hbt_bf_destroy": (None, [_VP]),
@@ -43,6 +58,7 @@ SIGNATURES = {
     "hbt_bf_reset": (_I32, [_VP]),
     "hbt_bf_bin": (_I32, [_VP, _I32, ctypes.POINTER(HbtBfList), _I32, ctypes.POINTER(HbtBfJob)]),
     "hbt_bf_read": (_I32, [_VP, _I32, _PD]),
+    "hbt_bf_get_stats": (_I32, [_VP, ctypes.POINTER(HbtBfStats)]),
 }
 
 _bound = None
@@ -95,7 +111,7 @@ class BfEngine:
 
     def bin(self, lists: Sequence, jobs: Sequence):
         """lists: (offsets, phi, y) per species list; jobs: (hist, la, ea, lb,
-        eb, mixed, rotation) tuples."""
+        eb, mixed, rotation) tuples, or an array made by ``job_array``."""
         keep = []
         arr = (HbtBfList * max(len(lists), 1))()
         for k, (off, phi, y) in enumerate(lists):
@@ -105,7 +121,11 @@ class BfEngine:
             keep += [off, phi, y]
             arr[k] = HbtBfList(len(off) - 1, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                phi.ctypes.data_as(_PD), y.ctypes.data_as(_PD))
-        jarr = (HbtBfJob * max(len(jobs), 1))(*[HbtBfJob(*j) for j in jobs])
+        if isinstance(jobs, np.ndarray) and jobs.dtype == JOB_DTYPE:
+            ja = np.ascontiguousarray(jobs)
+            jarr = ctypes.cast(ja.ctypes.data, ctypes.POINTER(HbtBfJob))
+        else:
+            jarr = (HbtBfJob * max(len(jobs), 1))(*[HbtBfJob(*j) for j in jobs])
         self._check(self.L.hbt_bf_bin(self._h, len(lists), arr, len(jobs), jarr), "hbt_bf_bin")
 
     def hist(self, which: int) -> np.ndarray:
@@ -115,3 +135,10 @@ class BfEngine:
 
     def reset(self):
         self._check(self.L.hbt_bf_reset(self._h), "hbt_bf_reset")
+
+    def stats(self) -> dict:
+        """Pairs, uploaded bytes, FP64-fallback pairs and device times of the
+        last ``bin`` call."""
+        st = HbtBfStats()
+        self._check(self.L.hbt_bf_get_stats(self._h, ctypes.byref(st)), "hbt_bf_get_stats")
+        return {k: getattr(st, k) for k, _ in HbtBfStats._fields_}

@@ -13,7 +13,9 @@
 // into one per non-zero bin and job.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/hbt_bf.h"
@@ -23,6 +25,11 @@ namespace {
 constexpr int kTile = 128;
 constexpr int kNphi = HBT_BF_NPHI;
 
+// Resident CTAs per SM the kernel is compiled for (register budget).
+#ifndef HBT_BF_MIN_BLOCKS
+#define HBT_BF_MIN_BLOCKS 10
+#endif
+
 // A job with its particle ranges resolved in the concatenated arrays.
 struct BfJob {
     long long a0, a1, b0, b1;
@@ -31,14 +38,12 @@ struct BfJob {
 };
 
 // The reference's binning constants (src/BalanceFunction.cpp:29-35) and
-// their FP32 copies for the screen.
+// the reciprocals the screen multiplies by.
 struct BfConst {
     double drap, Brap_min, dphi, Bphi_min;
+    double inv_drap, inv_dphi;
     int Bnpts;
-    float f_Brap_min, f_inv_drap, f_Bphi_min, f_inv_dphi;
 };
-
-constexpr float kU = 5.9604645e-8f;  // 2^-24
 
 // The reference's FP64 binning of one pair (src/BalanceFunction.cpp
 // :183-204; the same-event loop :136-157 has no rotation term, and adding
@@ -56,82 +61,153 @@ __device__ __forceinline__ int bin64(const BfConst &c, double pa, double ya, dou
     return -1;
 }
 
-// The same decision from FP32 copies with rigorous error bounds (u =
-// 2^-24 per rounding, every input rounded once from FP64, bounds widened by
-// a factor for the FP32 constants and the reference's own FP64 rounding):
-// the bin, -1 (skipped) or -2 (undecided: the caller runs bin64).
-__device__ __forceinline__ int bin32(const BfConst &c, float pa, float ya, float pb, float yb,
-                                     int mixed, float rot) {
-    const float s1 = pa - pb;
-    const float d = mixed ? s1 + rot : s1;
-    const float ed = 3.0f * kU * (fabsf(d) + fabsf(pa) + fabsf(pb) + fabsf(rot));
-    const float t = (d - c.f_Bphi_min) * c.f_inv_dphi;
-    const float et = (ed + 3.0f * kU * (fabsf(d) + fabsf(c.f_Bphi_min))) * c.f_inv_dphi * 1.01f +
-                     3.0f * kU * fabsf(t) + 1e-6f;
-    const float kp = floorf(t), fp = t - kp;
-    if (!(fp > et) || !(fp < 1.0f - et)) return -2;
-    const float dy = ya - yb;
-    const float ey = 3.0f * kU * (fabsf(ya) + fabsf(yb) + fabsf(dy)) + 1e-12f;
-    const float ady = fabsf(dy);
-    // 1e-10f rounds above 1e-10: both tests keep a relative margin
-    if (ady + ey < 0.9999e-10f) return -1;  // |dy| < 1e-10 for certain
-    if (!(ady - ey > 1.0001e-10f)) return -2;
-    const float eb = ey + 3.0f * kU * fabsf(c.f_Brap_min);
-    if (dy + eb < c.f_Brap_min) return -1;  // dy < Brap_min for certain
-    if (!(dy - eb > c.f_Brap_min)) return -2;
-    const float ty = (dy - c.f_Brap_min) * c.f_inv_drap;
-    const float ety = (eb + 3.0f * kU * fabsf(dy - c.f_Brap_min)) * c.f_inv_drap * 1.01f +
-                      3.0f * kU * fabsf(ty) + 1e-6f;
-    const float ky = floorf(ty), fy = ty - ky;
-    if (!(fy > ety) || !(fy < 1.0f - ety)) return -2;
-    const int iy = (int)ky;
-    if (iy < 0 || iy >= c.Bnpts) return -1;
-    int ip = ((int)kp) % kNphi;
-    if (ip < 0) ip += kNphi;
-    return iy * kNphi + ip;
+// A pair the FP32 screen leaves undecided, from the particles' FP64 values
+// in global memory: equal rapidities (a particle with itself, when the two
+// lists hold the same species) give dy = 0, which the reference skips;
+// everything else runs the reference's expressions.  Out of line: it runs
+// for about one pair in a thousand and keeps the loop's registers free.
+__device__ __noinline__ int bin_slow(const BfConst &c, const double *phi, const double *y,
+                                     long long ia, long long ib, int mixed, double rot) {
+    const double ya = y[ia], yb = y[ib];
+    if (ya == yb && fabs(ya) < INFINITY) return -1;
+    return bin64(c, phi[ia], ya, phi[ib], yb, mixed, rot);
 }
 
-__global__ void __launch_bounds__(kTile) k_bf(const BfJob *jobs, long long n_jobs,
-                                              const double *phi, const double *y, BfConst c,
-                                              unsigned long long *hist) {
+// The screen.  A pair's bins are the floors of two quotients,
+//   T_phi = (phi_a - phi_b + rot - Bphi_min) / dphi   (taken mod 20),
+//   T_y   = (y_a - y_b - Brap_min) / drap              (T_y < 0 is the
+//           reference's dy < Brap_min cut),
+// each the difference of a term of particle a and a term of particle b.
+// The terms are computed once per particle in FP64, the phi term reduced
+// mod 20 into [0, 20), and rounded to FP32 (error <= u |term|, u = 2^-24),
+// so a pair costs one FP32 subtraction per quotient (error <= u (|term a| +
+// |term b|)).  Each term carries a bound: 2.0001 u |term| for those
+// roundings, 2^-46 times the magnitudes it was made of for the FP64
+// arithmetic here and in the reference's own quotient, and on particle a
+// 2e-7 for the FP32 rounding of 1 - bound.  When the fraction of both FP32
+// differences clears the summed bounds, their floors are the reference's.
+// A term of magnitude >= 1e9 (or NaN) becomes NaN: every pair of that
+// particle then fails the screen and takes the FP64 path.
+constexpr double kU64 = 0x1p-24;
+constexpr float kU = 0x1p-24f;
+
+__device__ __forceinline__ double wrap20(double x) {
+    double r = x - 20.0 * floor(x * 0.05);
+    if (r < 0.0) r += 20.0;
+    if (r >= 20.0) r -= 20.0;
+    return r;
+}
+
+__device__ __forceinline__ float4 pack_terms(double xp, double mp, double xy, double my,
+                                             double slack) {
+    if (!(fabs(xp) < 1e9 && fabs(xy) < 1e9)) return make_float4(NAN, 0.f, NAN, 0.f);
+    const float tp = (float)wrap20(xp), ty = (float)xy;
+    const float ep = (float)(2.0001 * kU64 * fabs((double)tp) + 0x1p-46 * (mp + 40.0) + slack);
+    const float ey = (float)(2.0001 * kU64 * fabs((double)ty) + 0x1p-46 * my + slack);
+    return make_float4(tp, ep, ty, ey);
+}
+
+// Particle a: (phi + rot - Bphi_min) / dphi and (y - Brap_min) / drap.
+__device__ __forceinline__ float4 terms_a(const BfConst &c, double phi, double y, double rot) {
+    return pack_terms(((phi + rot) - c.Bphi_min) * c.inv_dphi,
+                      (fabs(phi) + fabs(rot) + fabs(c.Bphi_min)) * c.inv_dphi,
+                      (y - c.Brap_min) * c.inv_drap, (fabs(y) + fabs(c.Brap_min)) * c.inv_drap,
+                      2e-7);
+}
+
+// Particle b: phi / dphi and y / drap.
+__device__ __forceinline__ float4 terms_b(const BfConst &c, double phi, double y) {
+    return pack_terms(phi * c.inv_dphi, fabs(phi) * c.inv_dphi, y * c.inv_drap,
+                      fabs(y) * c.inv_drap, 0.0);
+}
+
+// The |dy| < 1e-10 cut: |dy| from FP32 copies errs by at most u (|y_a| +
+// |y_b| + |dy|); the pair certainly passes when |dy| exceeds 7 u per
+// magnitude plus 1.0001e-10 (1e-10f itself rounds above 1e-10).
+__device__ __forceinline__ float2 dy_terms(double y, float slack) {
+    const float fy = (float)y;
+    return make_float2(fy, 7.0f * kU * fabsf(fy) + slack);
+}
+
+// Every particle's b terms, once per call.
+__global__ void k_bf_terms(long long n, const double *phi, const double *y, BfConst c,
+                           float4 *tb, float2 *yb) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        tb[i] = terms_b(c, phi[i], y[i]);
+        yb[i] = dy_terms(y[i], 0.f);
+    }
+}
+
+// One work item per (job, tile of up to 128 particles of list A): a job of
+// n_a particles is ceil(n_a / 128) items, so the grid holds several waves
+// of similar items instead of one CTA per event pair.  A's terms sit in
+// registers (one particle per thread), B's are staged through shared memory
+// 128 at a time; the histogram is privatised in shared memory and its
+// non-zero bins are added to the global one when the item is done.
+__global__ void __launch_bounds__(kTile, HBT_BF_MIN_BLOCKS)
+    k_bf(const BfJob *jobs, const int2 *items, long long n_items, const double *phi,
+         const double *y, const float4 *tb, const float2 *yb, BfConst c,
+         unsigned long long *hist, unsigned long long *n_slow) {
     extern __shared__ unsigned sh[];  // [Bnpts][kNphi]
-    __shared__ double sphi[kTile], sy[kTile];
-    __shared__ float fphi[kTile], fy[kTile];
+    __shared__ float4 sb[kTile];
+    __shared__ float2 sd[kTile];
+    __shared__ BfJob sj;
     const int nbins = c.Bnpts * kNphi;
-    for (long long job = blockIdx.x; job < n_jobs; job += gridDim.x) {
+    unsigned slow = 0;
+    for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const int2 item = items[it];
         for (int k = threadIdx.x; k < nbins; k += blockDim.x) sh[k] = 0u;
+        if (threadIdx.x == 0) sj = jobs[item.x];
         __syncthreads();
-        const BfJob J = jobs[job];
-        const float frot = (float)J.rotation;
-        for (long long a = J.a0; a < J.a1; a += kTile) {
-            const long long ia = a + threadIdx.x;
-            const bool have = ia < J.a1;
-            const double pa = have ? phi[ia] : 0.0, ya = have ? y[ia] : 0.0;
-            const float fpa = (float)pa, fya = (float)ya;
-            for (long long b = J.b0; b < J.b1; b += kTile) {
-                __syncthreads();
-                if (b + threadIdx.x < J.b1) {
-                    sphi[threadIdx.x] = phi[b + threadIdx.x];
-                    sy[threadIdx.x] = y[b + threadIdx.x];
-                    fphi[threadIdx.x] = (float)sphi[threadIdx.x];
-                    fy[threadIdx.x] = (float)sy[threadIdx.x];
-                }
-                __syncthreads();
-                const int nb = (int)min((long long)kTile, J.b1 - b);
-                if (!have) continue;
+        const long long ia = sj.a0 + item.y + threadIdx.x;
+        const bool have = ia < sj.a1;
+        float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 Ay = make_float2(0.f, 0.f);
+        if (have) {
+            A = terms_a(c, phi[ia], y[ia], sj.mixed ? sj.rotation : 0.0);
+            Ay = dy_terms(y[ia], 1.0001e-10f);
+        }
+        for (long long b = sj.b0; b < sj.b1; b += kTile) {
+            if (b + threadIdx.x < sj.b1) {
+                sb[threadIdx.x] = tb[b + threadIdx.x];
+                sd[threadIdx.x] = yb[b + threadIdx.x];
+            }
+            __syncthreads();
+            const int nb = (int)min((long long)kTile, sj.b1 - b);
+            if (have) {
+#pragma unroll 2
                 for (int j = 0; j < nb; j++) {
-                    int k = bin32(c, fpa, fya, fphi[j], fy[j], J.mixed, frot);
-                    if (k == -2) k = bin64(c, pa, ya, sphi[j], sy[j], J.mixed, J.rotation);
-                    if (k >= 0) atomicAdd(&sh[k], 1u);
+                    const float4 B = sb[j];
+                    const float2 By = sd[j];
+                    const float t = A.x - B.x, et = A.y + B.y;
+                    const float ty = A.z - B.z, ety = A.w + B.w;
+                    const float kp = floorf(t), fp = t - kp;
+                    const float ky = floorf(ty), fy = ty - ky;
+                    int k;
+                    if (fp > et && fp < 1.0f - et && fy > ety && fy < 1.0f - ety &&
+                        fabsf(Ay.x - By.x) > Ay.y + By.y) {
+                        // t lies in (-20, 20): kp in [-20, 19], its class mod 20
+                        // in [0, 19]; ky beyond [0, Bnpts) puts k outside the
+                        // histogram (|ty| < 2^23 here, so k fits an int)
+                        const float ipf = kp < 0.0f ? kp + 20.0f : kp;
+                        k = (int)(ky * 20.0f + ipf);
+                    } else {
+                        k = bin_slow(c, phi, y, ia, b + j, sj.mixed, sj.rotation);
+                        slow++;
+                    }
+                    if ((unsigned)k < (unsigned)nbins) atomicAdd(&sh[k], 1u);
                 }
             }
+            __syncthreads();
         }
-        __syncthreads();
-        unsigned long long *h = hist + (long long)J.hist * nbins;
+        unsigned long long *h = hist + (long long)sj.hist * nbins;
         for (int k = threadIdx.x; k < nbins; k += blockDim.x)
             if (sh[k]) atomicAdd(h + k, (unsigned long long)sh[k]);
         __syncthreads();
     }
+    for (int o = 16; o > 0; o >>= 1) slow += __shfl_xor_sync(0xffffffffu, slow, o);
+    if ((threadIdx.x & 31) == 0 && slow) atomicAdd(n_slow, (unsigned long long)slow);
 }
 
 struct Buf {
@@ -160,7 +236,9 @@ struct hbt_bf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     BfConst c;
-    Buf hist, jobs, phi, y;
+    Buf hist, jobs, items, phi, y, tb, yb, counter;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    hbt_bf_stats stats{};
     std::string err;
 };
 
@@ -189,13 +267,14 @@ hbt_status hbt_bf_create(const hbt_bf_params *p, int device, hbt_bf_ctx **out) {
     c->c.dphi = 2. * M_PI / kNphi;
     c->c.Bphi_min = -M_PI / 2.;
     c->c.Bnpts = p->Bnpts;
-    c->c.f_Brap_min = (float)c->c.Brap_min;
-    c->c.f_inv_drap = (float)(1.0 / c->c.drap);
-    c->c.f_Bphi_min = (float)c->c.Bphi_min;
-    c->c.f_inv_dphi = (float)(1.0 / c->c.dphi);
+    c->c.inv_drap = 1.0 / c->c.drap;
+    c->c.inv_dphi = 1.0 / c->c.dphi;
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        !grow(c->hist, (size_t)8 * p->Bnpts * kNphi * sizeof(unsigned long long))) {
+        cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
+        cudaEventCreate(&c->ev[2]) != cudaSuccess ||
+        !grow(c->hist, (size_t)8 * p->Bnpts * kNphi * sizeof(unsigned long long)) ||
+        !grow(c->counter, sizeof(unsigned long long))) {
         hbt_bf_destroy(c);
         return HBT_ERR_CUDA;
     }
@@ -212,8 +291,10 @@ void hbt_bf_destroy(hbt_bf_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    for (Buf *b : {&c->hist, &c->jobs, &c->phi, &c->y})
+    for (Buf *b : {&c->hist, &c->jobs, &c->items, &c->phi, &c->y, &c->tb, &c->yb, &c->counter})
         if (b->p) cudaFree(b->p);
+    for (cudaEvent_t e : c->ev)
+        if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -235,16 +316,32 @@ hbt_status hbt_bf_bin(hbt_bf_ctx *c, int32_t n_lists, const hbt_bf_list *lists, 
         return HBT_ERR_INVALID;
     if (n_jobs == 0) return HBT_OK;
     if (cudaSetDevice(c->device) != cudaSuccess) return bf_fail(c, HBT_ERR_CUDA, "cudaSetDevice");
-    // concatenate the lists, resolve every job's particle ranges
-    std::vector<long long> base(n_lists + 1, 0);
+    // concatenate the lists (a list passed again with the same arrays, as the
+    // mixed-event pool is when it is the buffer itself, shares the first
+    // copy), resolve every job's particle ranges
+    std::vector<long long> base(n_lists, 0);
+    std::vector<int> copy_of(n_lists, -1);
+    std::map<std::tuple<const void *, const void *, const void *, int32_t>, int> first;
+    long long total = 0;
     for (int l = 0; l < n_lists; l++) {
         const hbt_bf_list &L = lists[l];
         if (L.n_events < 0 || (L.n_events > 0 && !L.offsets))
             return bf_fail(c, HBT_ERR_INVALID, "list without offsets");
         const long long n = L.n_events > 0 ? L.offsets[L.n_events] : 0;
         if (n > 0 && (!L.phi || !L.y)) return bf_fail(c, HBT_ERR_INVALID, "list without columns");
-        base[l + 1] = base[l] + n;
+        const auto key = std::make_tuple(static_cast<const void *>(L.offsets),
+                                         static_cast<const void *>(L.phi),
+                                         static_cast<const void *>(L.y), L.n_events);
+        const auto seen = first.emplace(key, l);
+        if (!seen.second) copy_of[l] = seen.first->second;
+        if (copy_of[l] >= 0) {
+            base[l] = base[copy_of[l]];
+        } else {
+            base[l] = total;
+            total += n;
+        }
     }
+    long long pairs = 0;
     std::vector<BfJob> dj(n_jobs);
     for (int k = 0; k < n_jobs; k++) {
         const hbt_bf_job &J = jobs[k];
@@ -255,32 +352,79 @@ hbt_status hbt_bf_bin(hbt_bf_ctx *c, int32_t n_lists, const hbt_bf_list *lists, 
         const int64_t *oa = lists[J.la].offsets, *ob = lists[J.lb].offsets;
         dj[k] = BfJob{base[J.la] + oa[J.ea], base[J.la] + oa[J.ea + 1], base[J.lb] + ob[J.eb],
                       base[J.lb] + ob[J.eb + 1], J.rotation, J.hist, J.mixed ? 1 : 0};
+        pairs += (oa[J.ea + 1] - oa[J.ea]) * (ob[J.eb + 1] - ob[J.eb]);
     }
-    const long long total = base[n_lists];
-    if (!grow(c->jobs, dj.size() * sizeof(BfJob)) || !grow(c->phi, total * sizeof(double)) ||
-        !grow(c->y, total * sizeof(double)))
+    std::vector<int2> items;
+    for (int k = 0; k < n_jobs; k++)
+        if (dj[k].b1 > dj[k].b0)
+            for (long long a = 0; a < dj[k].a1 - dj[k].a0; a += kTile)
+                items.push_back(make_int2(k, (int)a));
+    if (items.empty()) {
+        c->stats = hbt_bf_stats{};
+        return HBT_OK;
+    }
+    if (!grow(c->jobs, dj.size() * sizeof(BfJob)) || !grow(c->items, items.size() * sizeof(int2)) ||
+        !grow(c->phi, total * sizeof(double)) || !grow(c->y, total * sizeof(double)) ||
+        !grow(c->tb, total * sizeof(float4)) || !grow(c->yb, total * sizeof(float2)))
         return bf_fail(c, HBT_ERR_NOMEM, "device allocation failed");
-    cudaError_t e = cudaMemcpyAsync(c->jobs.p, dj.data(), dj.size() * sizeof(BfJob),
-                                    cudaMemcpyHostToDevice, c->stream);
+    cudaError_t e = cudaEventRecord(c->ev[0], c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->jobs.p, dj.data(), dj.size() * sizeof(BfJob),
+                            cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->items.p, items.data(), items.size() * sizeof(int2),
+                            cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(c->counter.p, 0, sizeof(unsigned long long), c->stream);
     for (int l = 0; l < n_lists && e == cudaSuccess; l++) {
-        const long long n = base[l + 1] - base[l];
-        if (n == 0) continue;
+        const long long n = lists[l].n_events > 0 ? lists[l].offsets[lists[l].n_events] : 0;
+        if (n == 0 || copy_of[l] >= 0) continue;
         e = cudaMemcpyAsync(static_cast<double *>(c->phi.p) + base[l], lists[l].phi,
                             n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(static_cast<double *>(c->y.p) + base[l], lists[l].y,
                                 n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
     }
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev[1], c->stream);
     if (e != cudaSuccess) return bf_fail(c, HBT_ERR_CUDA, "upload failed");
-    const long long grid = std::min<long long>(n_jobs, 152LL * 32);
+    const double *dphi_p = static_cast<const double *>(c->phi.p);
+    const double *dy_p = static_cast<const double *>(c->y.p);
+    if (total > 0)
+        k_bf_terms<<<(unsigned)std::min<long long>((total + 255) / 256, 152LL * 16), 256, 0,
+                     c->stream>>>(total, dphi_p, dy_p, c->c, static_cast<float4 *>(c->tb.p),
+                                  static_cast<float2 *>(c->yb.p));
+    const long long n_items = (long long)items.size();
+    const long long grid = std::min<long long>(n_items, 1LL << 30);
     k_bf<<<(unsigned)grid, kTile, (size_t)c->p.Bnpts * kNphi * sizeof(unsigned), c->stream>>>(
-        static_cast<const BfJob *>(c->jobs.p), n_jobs, static_cast<const double *>(c->phi.p),
-        static_cast<const double *>(c->y.p), c->c, static_cast<unsigned long long *>(c->hist.p));
+        static_cast<const BfJob *>(c->jobs.p), static_cast<const int2 *>(c->items.p), n_items,
+        dphi_p, dy_p, static_cast<const float4 *>(c->tb.p), static_cast<const float2 *>(c->yb.p),
+        c->c, static_cast<unsigned long long *>(c->hist.p),
+        static_cast<unsigned long long *>(c->counter.p));
     if ((e = cudaGetLastError()) != cudaSuccess)
         return bf_fail(c, HBT_ERR_CUDA, std::string("k_bf: ") + cudaGetErrorString(e));
+    unsigned long long slow = 0;
+    if ((e = cudaEventRecord(c->ev[2], c->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&slow, c->counter.p, sizeof slow, cudaMemcpyDeviceToHost,
+                             c->stream)) != cudaSuccess)
+        return bf_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
     // the host arrays may be reused once the copies are done
     if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
         return bf_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
+    float up = 0.f, ker = 0.f;
+    cudaEventElapsedTime(&up, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&ker, c->ev[1], c->ev[2]);
+    c->stats.pairs = pairs;
+    c->stats.bytes_uploaded = (int64_t)(dj.size() * sizeof(BfJob) + items.size() * sizeof(int2) +
+                                        2 * total * sizeof(double));
+    c->stats.fp64_pairs = (int64_t)slow;
+    c->stats.upload_ms = up;
+    c->stats.kernel_ms = ker;
+    return HBT_OK;
+}
+
+hbt_status hbt_bf_get_stats(const hbt_bf_ctx *c, hbt_bf_stats *out) {
+    if (!c || !out) return HBT_ERR_INVALID;
+    *out = c->stats;
     return HBT_OK;
 }
 

@@ -8,8 +8,9 @@
  * with a global rotation added to the azimuthal difference), binned in
  * (Delta y, Delta phi) into one of eight histograms (ab, abar bbar, a bbar,
  * abar b; then the same four with mixed events).  The bins and counts are
- * the reference's exactly: the bin-deciding arithmetic runs in FP64 in the
- * reference's operation order.
+ * the reference's exactly: an FP32 screen with rigorous error bounds decides
+ * a pair's bin unless it lies near a bin edge or a cut, where the reference's
+ * FP64 expressions run in its operation order.
  *
  * The host side (species lists, pT cut, random partner events and
  * rotations, output files) stays in C++ above this boundary.
@@ -67,6 +68,20 @@ hbt_status hbt_bf_bin(hbt_bf_ctx *ctx, int32_t n_lists, const hbt_bf_list *lists
 /* Counts of histogram `hist`, Bnpts x HBT_BF_NPHI doubles, [y bin][phi bin]
  * (the reference's C_ab ... C_mixed_abarb arrays). */
 hbt_status hbt_bf_read(hbt_bf_ctx *ctx, int32_t hist, double *out);
+
+/* What the last hbt_bf_bin did: candidate pairs, bytes copied to the device
+ * (lists passed more than once with the same pointers are copied once), and
+ * the device time of the copies and of the binning kernel (CUDA events on
+ * the context's stream). */
+typedef struct hbt_bf_stats {
+    int64_t pairs;
+    int64_t bytes_uploaded;
+    int64_t fp64_pairs; /* pairs the FP32 screen left to the FP64 path */
+    double upload_ms;
+    double kernel_ms;
+} hbt_bf_stats;
+
+hbt_status hbt_bf_get_stats(const hbt_bf_ctx *ctx, hbt_bf_stats *out);
 
 #ifdef __cplusplus
 }

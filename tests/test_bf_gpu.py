@@ -195,7 +195,7 @@ def test_bf_fp32_screen_near_edges():
                              rng.uniform(0, 2 * math.pi), 1e-300, 6.0]):
         jobs.append((1 + r, 0, 0, 1, 0, 1, rot))
     eng = bf.BfEngine(Bnpts, Brap_max)
-    eng.bin([A, B], jobs)
+    eng.bin([A, B], bf.job_array(jobs))
     orc = oracle_lib.BfOracle(particle_alpha=1, particle_beta=2, BpT_min=-1.0, BpT_max=10.0,
                               Bnpts=Bnpts, Brap_max=Brap_max, rap_type=1, seed=1)
     L = oracle_lib._bf_lib()
@@ -208,3 +208,11 @@ def test_bf_fp32_screen_near_edges():
         g, o = eng.hist(h), orc.hist(h)
         assert np.array_equal(g, o), "histogram %d differs at %s" % (h, np.argwhere(g != o)[:5])
     assert eng.hist(0).sum() > 1000
+    st = eng.stats()
+    assert st["pairs"] == len(jobs) * ya.size * yb.size
+    assert 0 < st["fp64_pairs"] < st["pairs"]  # the edges reach the FP64 path
+    assert st["kernel_ms"] > 0
+    # a list passed twice with the same arrays is uploaded once
+    eng.bin([A, B, A, B], [(0, 2, 0, 3, 0, 0, 0.0)])
+    n_items = -(-ya.size // 128)
+    assert eng.stats()["bytes_uploaded"] == 48 + 8 * n_items + 16 * (ya.size + yb.size)
