@@ -619,6 +619,78 @@ def bf_leg(n_events: int = 200, seed: int = 21) -> dict:
             "cpu_sample_pairs": done, "speedup_vs_cpu_core": (n_pairs / t_gpu) / (done / t_cpu)}
 
 
+def fit_tables_synthetic(n_tables: int, seed: int = 31, nq: int = 41, q_max: float = 0.15):
+    """Eight-column correlation tables of a 41^3 q grid on [-0.15, 0.15] GeV
+    (the shape the HBT writer gives per K_T bin), pair-averaged q jitter,
+    C from a Gaussian source with random radii plus noise."""
+    rng = np.random.default_rng(seed)
+    q = np.linspace(-q_max, q_max, nq)
+    dq = q[1] - q[0]
+    ql, qo, qs = [a.ravel() for a in np.meshgrid(q, q, q, indexing="ij")]
+    out = []
+    for _ in range(n_tables):
+        lam, ro, rs, rl, ros, rol = (rng.uniform(0.3, 0.9), rng.uniform(3, 8), rng.uniform(3, 7),
+                                     rng.uniform(3, 9), rng.uniform(0.6, 2.0), rng.uniform(0.5, 1.6))
+        t = np.empty((qo.size, 8))
+        t[:, 0] = qo + 0.1 * dq * rng.uniform(-1, 1, qo.size)
+        t[:, 1] = qs + 0.1 * dq * rng.uniform(-1, 1, qo.size)
+        t[:, 2] = ql + 0.1 * dq * rng.uniform(-1, 1, qo.size)
+        a = np.array([ro, rs, rl, ros, rol]) / 0.19733
+        c0 = lam * np.exp(-((a[0] * t[:, 0]) ** 2 + (a[1] * t[:, 1]) ** 2 + (a[2] * t[:, 2]) ** 2
+                            + 2 * t[:, 0] * t[:, 1] * a[3] ** 2 + 2 * t[:, 0] * t[:, 2] * a[4] ** 2))
+        err = 0.004 + 0.03 * c0
+        t[:, 3] = 1000.0
+        t[:, 5] = 1000.0
+        t[:, 6] = c0 + err * rng.standard_normal(qo.size)
+        t[:, 4] = 1000.0 * t[:, 6]
+        t[:, 7] = err
+        out.append(t)
+    return out
+
+
+def fit_leg(n_tables: int = 256, cpu_seconds: float = 8.0) -> dict:
+    """Radii fits: 256 correlation tables (64 events x 4 K_T bins) of 41^3
+    rows, five q cuts each (1280 fits) in one hbt_fit_radii call, against
+    the oracle's scipy curve_fit loop (the reference script's) on one host
+    core for a bounded sample of tables."""
+    from hadronic_afterburner_toolkit_gb300 import radii
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    tabs = fit_tables_synthetic(n_tables)
+    f = radii.Fitter()
+    f.fit(tabs[:8])  # warm-up
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        rows = f.fit(tabs)
+        times.append(time.perf_counter() - t0)
+    st = f.stats()
+    n_fits = n_tables * len(radii.Q_CUT_MAX_LIST)
+    res = {"tables": n_tables, "rows_per_table": int(tabs[0].shape[0]), "fits": n_fits,
+           "seconds": min(times), "fits_per_s": n_fits / min(times),
+           "timing": "host clock around hbt_fit_radii (packing, upload, fits, results)",
+           "kernel_ms": st["kernel_ms"], "upload_ms": st["upload_ms"],
+           "points": st["points"], "passes": st["passes"],
+           "converged": int((f.last["status"] == 0).sum())}
+    try:
+        import fit_radii
+    except ImportError as exc:  # scipy missing
+        res["cpu_oracle"] = "unavailable: %s" % exc
+        return res
+    done, t0 = 0, time.perf_counter()
+    worst = 0.0
+    for k, t in enumerate(tabs):
+        o = fit_radii.fit_table(t)
+        done += o.shape[0]
+        worst = max(worst, float(np.max(np.abs(o[:, 1::2] - rows[k, :, 1::2]) / o[:, 2::2])))
+        if time.perf_counter() - t0 > cpu_seconds:
+            break
+    t_cpu = time.perf_counter() - t0
+    res.update({"cpu_oracle_fits_per_s": done / t_cpu, "cpu_cores": 1, "cpu_sample_fits": done,
+                "speedup_vs_cpu_core": (n_fits / min(times)) / (done / t_cpu),
+                "max_param_diff_in_errors_vs_oracle": worst})
+    return res
+
+
 def make_requests(n_jobs: int, seed: int = 5):
     """Requests of the serving workload: 10-500 events each, multiplicity
     Poisson(mu) with mu uniform in [50, 2000], pi+ or K+, qnpts in
@@ -708,6 +780,8 @@ def main() -> None:
     ap.add_argument("--serving-jobs", type=int, default=48)
     ap.add_argument("--no-bf", action="store_true",
                     help="skip the balance-function leg")
+    ap.add_argument("--no-fit", action="store_true",
+                    help="skip the radii-fit leg")
     ap.add_argument("--no-ingest", action="store_true",
                     help="skip the reader timing (line-by-line against block reader)")
     args = ap.parse_args()
@@ -925,12 +999,14 @@ def main() -> None:
         cpu = cpu_baseline(groups[0], p, nthreads=1)
 
     uneven = serving = ingest = average = None
-    balance = None
+    balance = fits = None
     if not args.no_ingest and rank == 0:
         ingest = ingest_leg()
         average = average_leg()
     if not args.no_bf and rank == 0:
         balance = bf_leg()
+    if not args.no_fit and rank == 0:
+        fits = fit_leg()
     if not args.no_uneven:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
@@ -970,6 +1046,7 @@ def main() -> None:
                 "ingest": ingest,
                 "average": average,
                 "balance_function": balance,
+                "radii_fit": fits,
                 "stats": st}
         print(json.dumps(line))
     eng.close()

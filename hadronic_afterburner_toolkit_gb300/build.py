@@ -43,6 +43,7 @@ GPU_UNITS = {
     "hbt_runner.cu": [],
     "hbt_server.cu": ["--fmad=false"],
     "hbt_bf.cu": ["--fmad=false"],
+    "hbt_fit.cu": [],
 }
 
 

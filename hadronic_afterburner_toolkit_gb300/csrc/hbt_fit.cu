@@ -1,0 +1,645 @@
+// Batched Gaussian HBT radii fits (include/hbt_fit.h).
+//
+// The reference fits each correlation table with scipy's curve_fit, one
+// table and one q_cut at a time (ebe_scripts/fit_HBT_radii.py:60-92).  Here
+// every (table, q_cut) of a call is one CTA of one launch:
+//
+//  * k_fit_select (one CTA per table) applies the script's preprocessing
+//    (numpy nan_to_num, C_err + 1e-15, weight 1 / sigma) and keeps the rows
+//    with q_cut_min < |q| < the largest cut, ordered by the smallest cut
+//    they pass, so the rows of cut k are a prefix of the table's kept rows.
+//    Per row it stores the five q products of the exponent, C and the
+//    weight (7 doubles).
+//  * k_fit_lm (one CTA per fit) runs Levenberg-Marquardt in FP64: each pass
+//    over the rows accumulates chi^2, J^T r and J^T J (28 sums, analytic
+//    Jacobian) with a block reduction; one thread solves the damped 6 x 6
+//    system by Cholesky and decides the next trial point.  At the minimum
+//    the errors are sqrt(diag((J^T J)^-1)) (curve_fit, absolute_sigma).
+//
+// The rows a fit touches are read once per pass: 56 bytes per row against
+// about 60 FP64 operations, so the fits are bound by the FP64 pipe.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/hbt_fit.h"
+
+namespace {
+
+constexpr double kHbarC = 0.19733;  // fit_HBT_radii.py:10
+constexpr double kEps = 1e-15;      // fit_HBT_radii.py:11
+constexpr int kMaxCuts = 16;
+constexpr int kSelThreads = 256;
+constexpr int kFitThreads = 128;
+constexpr int kSums = 28;  // chi2, J^T r (6), J^T J (21, packed lower)
+
+struct FitConst {
+    double cut_sorted[kMaxCuts];  // ascending
+    int rank[kMaxCuts];           // position of cut k in cut_sorted
+    int n_cuts;
+    double q_cut_min;
+    double p0[6];
+    int max_iter;
+};
+
+// Where a table's columns sit in the batch's input buffer: column k of row
+// i at in[base + col[k] + i * stride].  An interleaved host table (all five
+// columns in one row-major block) is copied as that block; other tables are
+// packed column by column (stride 1).
+struct TabDesc {
+    long long base, stride, col[5];
+};
+
+// Device rows of a batch: the kept rows of table t start at row_off[t];
+// cls[t * (n_cuts + 1) + c] = rows of t whose smallest passed cut is c.
+struct Rows {
+    double *qoo, *qss, *qll, *qos, *qol, *C, *w;
+};
+
+__device__ __forceinline__ double nan_to_num(double v) {
+    if (isnan(v)) return 0.0;
+    if (isinf(v)) return v > 0 ? DBL_MAX : -DBL_MAX;
+    return v;
+}
+
+// numpy's sqrt(q_out**2. + q_side**2. + q_long**2.), without contraction.
+__device__ __forceinline__ double qabs(double qo, double qs, double ql) {
+    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(qo, qo), __dmul_rn(qs, qs)), __dmul_rn(ql, ql)));
+}
+
+__device__ __forceinline__ int cut_class(const FitConst &fc, double r) {
+    if (!(r > fc.q_cut_min)) return -1;
+    for (int c = 0; c < fc.n_cuts; c++)
+        if (r < fc.cut_sorted[c]) return c;
+    return -1;
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+    k_fit_select(FitConst fc, const long long *tab_off, const TabDesc *desc, const double *in,
+                 Rows out, int *cls) {
+    __shared__ int warp_tot[kSelThreads / 32];
+    __shared__ int base;
+    const int t = blockIdx.x;
+    const long long r0 = tab_off[t], n = tab_off[t + 1] - r0;
+    const TabDesc d = desc[t];
+    const double *qo_in = in + d.base + d.col[0], *qs_in = in + d.base + d.col[1],
+                 *ql_in = in + d.base + d.col[2], *c_in = in + d.base + d.col[3],
+                 *e_in = in + d.base + d.col[4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (int c = 0; c < fc.n_cuts; c++) {
+        const int before = base;
+        for (long long i0 = 0; i0 < n; i0 += kSelThreads) {
+            const long long i = i0 + threadIdx.x;
+            double qo = 0, qs = 0, ql = 0;
+            bool take = false;
+            if (i < n) {
+                qo = nan_to_num(qo_in[i * d.stride]);
+                qs = nan_to_num(qs_in[i * d.stride]);
+                ql = nan_to_num(ql_in[i * d.stride]);
+                take = cut_class(fc, qabs(qo, qs, ql)) == c;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, take);
+            if (lane == 0) warp_tot[warp] = __popc(m);
+            __syncthreads();
+            int off = base, tot = 0;
+            for (int w = 0; w < kSelThreads / 32; w++) {
+                if (w < warp) off += warp_tot[w];
+                tot += warp_tot[w];
+            }
+            if (take) {
+                const long long o = r0 + off + __popc(m & ((1u << lane) - 1u));
+                const double cc = nan_to_num(c_in[i * d.stride]);
+                const double sigma = nan_to_num(e_in[i * d.stride]) + kEps;
+                out.qoo[o] = qo * qo;
+                out.qss[o] = qs * qs;
+                out.qll[o] = ql * ql;
+                out.qos[o] = 2.0 * qo * qs;
+                out.qol[o] = 2.0 * qo * ql;
+                out.C[o] = cc;
+                out.w[o] = 1.0 / sigma;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) base += tot;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) cls[t * (fc.n_cuts + 1) + c] = base - before;
+    }
+    if (threadIdx.x == 0) cls[t * (fc.n_cuts + 1) + fc.n_cuts] = base;
+}
+
+// One pass at parameters p: chi^2, J^T r, J^T J of the rows [0, n) of the
+// fit, reduced over the block into red[0..27] (valid in thread 0).
+// Residual r = w (f - C), J = w df/dp with f = lambda exp(-E),
+// E = sum_k (R_k / hbar c)^2 Q_k over the five q products Q_k.
+__device__ void fit_pass(const Rows &rw, long long r0, int n, const double *p, double *red) {
+    __shared__ double part[kFitThreads / 32][kSums];
+    double a[5], cdf[5];
+    for (int k = 0; k < 5; k++) {
+        a[k] = p[k + 1] / kHbarC;
+        cdf[k] = 2.0 * a[k] / kHbarC;  // dE/dR_k = 2 a_k Q_k / hbar c
+    }
+    const double lam = p[0];
+    double s[kSums];
+#pragma unroll
+    for (int k = 0; k < kSums; k++) s[k] = 0.0;
+    for (int i = threadIdx.x; i < n; i += kFitThreads) {
+        const long long o = r0 + i;
+        const double q[5] = {rw.qoo[o], rw.qss[o], rw.qll[o], rw.qos[o], rw.qol[o]};
+        const double w = rw.w[o];
+        double E = 0.0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) E += a[k] * a[k] * q[k];
+        const double e = exp(-E);
+        const double f = lam * e;
+        const double r = w * (f - rw.C[o]);
+        double J[6];
+        J[0] = w * e;
+        const double u = -w * f;
+#pragma unroll
+        for (int k = 0; k < 5; k++) J[k + 1] = u * cdf[k] * q[k];
+        s[0] += r * r;
+#pragma unroll
+        for (int k = 0; k < 6; k++) s[1 + k] += J[k] * r;
+        int m = 7;
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+#pragma unroll
+            for (int k = 0; k <= j; k++) s[m++] += J[j] * J[k];
+    }
+#pragma unroll
+    for (int k = 0; k < kSums; k++) {
+        double v = s[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        s[k] = v;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < kSums; k++) part[warp][k] = s[k];
+    __syncthreads();
+    if (threadIdx.x < kSums) {
+        double v = 0.0;
+        for (int w = 0; w < kFitThreads / 32; w++) v += part[w][threadIdx.x];
+        red[threadIdx.x] = v;
+    }
+    __syncthreads();
+}
+
+// Cholesky of the packed symmetric 6 x 6 matrix M (lower, row-major
+// packed: M[j(j+1)/2 + k], k <= j) in place; false if not positive definite.
+__device__ bool cholesky6(double *M) {
+    for (int j = 0; j < 6; j++) {
+        for (int k = 0; k <= j; k++) {
+            double s = M[j * (j + 1) / 2 + k];
+            for (int l = 0; l < k; l++) s -= M[j * (j + 1) / 2 + l] * M[k * (k + 1) / 2 + l];
+            if (k == j) {
+                if (!(s > 0.0)) return false;
+                M[j * (j + 1) / 2 + j] = sqrt(s);
+            } else {
+                M[j * (j + 1) / 2 + k] = s / M[k * (k + 1) / 2 + k];
+            }
+        }
+    }
+    return true;
+}
+
+// Solves L L^T x = b with the factor of cholesky6.
+__device__ void chol_solve6(const double *L, const double *b, double *x) {
+    double y[6];
+    for (int j = 0; j < 6; j++) {
+        double s = b[j];
+        for (int l = 0; l < j; l++) s -= L[j * (j + 1) / 2 + l] * y[l];
+        y[j] = s / L[j * (j + 1) / 2 + j];
+    }
+    for (int j = 5; j >= 0; j--) {
+        double s = y[j];
+        for (int l = j + 1; l < 6; l++) s -= L[l * (l + 1) / 2 + j] * x[l];
+        x[j] = s / L[j * (j + 1) / 2 + j];
+    }
+}
+
+// Levenberg-Marquardt state of one fit, in shared memory, advanced by one
+// thread between the block's passes over the rows.
+struct LmState {
+    double x[6], trial[6];
+    double S, g[6], A[21], D[6], mu, nu;
+    int iter, status, stop, go;
+    long long passes;
+};
+
+// After the pass at the start point.
+__device__ __noinline__ void lm_init(LmState &st, const double *red) {
+    st.S = red[0];
+    for (int j = 0; j < 6; j++) st.g[j] = red[1 + j];
+    for (int j = 0; j < 21; j++) st.A[j] = red[7 + j];
+    // Marquardt's scaling: the damping adds mu times the diagonal of J^T J
+    // (dimensionless mu), so every parameter is damped on its own scale
+    for (int j = 0; j < 6; j++) {
+        const double d = st.A[j * (j + 1) / 2 + j];
+        st.D[j] = d > 0 ? d : 1.0;
+    }
+    st.mu = 1e-3;
+    st.nu = 2;
+    st.iter = 0;
+    st.status = HBT_FIT_CONVERGED;
+    st.stop = 0;
+    st.passes = 1;
+}
+
+// The next trial point: solve (A + mu D) delta = -g (D: the largest
+// diagonal of J^T J seen, Marquardt's scaling), raising mu while the damped
+// matrix is not positive definite.  go = 0 when the step no longer moves
+// the point, the damping overflowed or the iterations ran out.
+__device__ __noinline__ void lm_propose(LmState &st, int max_iter) {
+    st.go = 0;
+    while (!st.stop) {
+        if (st.iter >= max_iter) {
+            st.status = HBT_FIT_MAX_ITER;
+            return;
+        }
+        st.iter++;
+        double M[21], delta[6], mg[6];
+        for (int j = 0; j < 21; j++) M[j] = st.A[j];
+        for (int j = 0; j < 6; j++) {
+            M[j * (j + 1) / 2 + j] += st.mu * st.D[j];
+            mg[j] = -st.g[j];
+        }
+        if (!cholesky6(M)) {
+            st.mu *= st.nu;
+            st.nu *= 2;
+            st.stop = !(st.mu < 1e300);
+            continue;
+        }
+        chol_solve6(M, mg, delta);
+        bool small = true;
+        for (int j = 0; j < 6; j++) {
+            st.trial[j] = st.x[j] + delta[j];
+            if (fabs(delta[j]) > 1e-12 * (fabs(st.x[j]) + 1e-12)) small = false;
+        }
+        if (small) {
+            st.stop = 1;
+            return;
+        }
+        st.go = 1;
+        return;
+    }
+}
+
+// After the pass at the trial point: accept it when chi^2 fell (gain ratio
+// rho > 0, Nielsen's update of mu), else raise mu.  Converged when an
+// accepted step changed chi^2 by less than 1e-14 of it, predicted and
+// actual.
+__device__ __noinline__ void lm_update(LmState &st, const double *red) {
+    st.passes++;
+    const double Sn = red[0];
+    double pred = 0;
+    for (int j = 0; j < 6; j++) {
+        const double dj = st.trial[j] - st.x[j];
+        pred += dj * (st.mu * st.D[j] * dj - st.g[j]);
+    }
+    const double rho = (isfinite(Sn) && pred > 0) ? (st.S - Sn) / pred : -1.0;
+    if (rho > 0) {
+        const double drop = st.S - Sn;
+        for (int j = 0; j < 6; j++) st.x[j] = st.trial[j];
+        st.S = Sn;
+        for (int j = 0; j < 6; j++) st.g[j] = red[1 + j];
+        for (int j = 0; j < 21; j++) st.A[j] = red[7 + j];
+        for (int j = 0; j < 6; j++) st.D[j] = fmax(st.D[j], st.A[j * (j + 1) / 2 + j]);
+        const double q = 2 * rho - 1;
+        st.mu *= fmax(1.0 / 3.0, 1.0 - q * q * q);
+        st.nu = 2;
+        st.stop = drop <= 1e-14 * st.S && pred <= 1e-14 * st.S;
+    } else {
+        st.mu *= st.nu;
+        st.nu *= 2;
+        st.stop = !(st.mu < 1e300);
+    }
+}
+
+// Results: the point, chi^2 and the errors sqrt(diag((J^T J)^-1)).
+__device__ __noinline__ void lm_finish(const LmState &st, double q_cut, int n,
+                                       hbt_fit_result *out) {
+    out->q_cut = q_cut;
+    for (int j = 0; j < 6; j++) out->p[j] = st.x[j];
+    out->chi2 = st.S;
+    out->n_points = n;
+    out->iterations = st.iter;
+    out->reserved = 0;
+    int status = st.status;
+    double L[21];
+    for (int j = 0; j < 21; j++) L[j] = st.A[j];
+    if (cholesky6(L)) {
+        for (int j = 0; j < 6; j++) {
+            double e[6] = {0, 0, 0, 0, 0, 0}, col[6];
+            e[j] = 1.0;
+            chol_solve6(L, e, col);
+            out->err[j] = sqrt(col[j]);
+        }
+    } else {
+        for (int j = 0; j < 6; j++) out->err[j] = INFINITY;
+        if (status == HBT_FIT_CONVERGED) status = HBT_FIT_SINGULAR;
+    }
+    out->status = status;
+}
+
+__global__ void __launch_bounds__(kFitThreads)
+    k_fit_lm(FitConst fc, int first_table, const long long *tab_off, const int *cls, Rows rw,
+             hbt_fit_result *res, unsigned long long *n_passes) {
+    __shared__ double red[kSums];
+    __shared__ LmState st;
+    const int fit = blockIdx.x;
+    const int t = fit / fc.n_cuts, k = fit % fc.n_cuts;
+    const long long r0 = tab_off[t];
+    int n = 0;
+    for (int c = 0; c <= fc.rank[k]; c++) n += cls[t * (fc.n_cuts + 1) + c];
+    hbt_fit_result *out = res + (long long)(first_table + t) * fc.n_cuts + k;
+    const double q_cut = fc.cut_sorted[fc.rank[k]];
+    if (n < 6) {
+        if (threadIdx.x == 0) {
+            out->q_cut = q_cut;
+            for (int j = 0; j < 6; j++) out->p[j] = out->err[j] = NAN;
+            out->chi2 = NAN;
+            out->n_points = n;
+            out->iterations = 0;
+            out->status = HBT_FIT_TOO_FEW;
+            out->reserved = 0;
+        }
+        return;
+    }
+    if (threadIdx.x < 6) st.x[threadIdx.x] = fc.p0[threadIdx.x];
+    __syncthreads();
+    // one pass per trial point: the first at the start point
+    for (bool first = true;; first = false) {
+        fit_pass(rw, r0, n, first ? st.x : st.trial, red);
+        if (threadIdx.x == 0) {
+            if (first)
+                lm_init(st, red);
+            else
+                lm_update(st, red);
+            lm_propose(st, fc.max_iter);
+        }
+        __syncthreads();
+        if (!st.go) break;
+    }
+    if (threadIdx.x == 0) {
+        lm_finish(st, q_cut, n, out);
+        atomicAdd(n_passes, (unsigned long long)st.passes);
+    }
+}
+
+struct Buf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+bool grow(Buf &b, size_t bytes) {
+    if (b.p && b.bytes >= bytes) return true;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (bytes == 0) return true;
+    if (cudaMalloc(&b.p, bytes + bytes / 8) != cudaSuccess) {
+        b.p = nullptr;
+        return false;
+    }
+    b.bytes = bytes + bytes / 8;
+    return true;
+}
+
+// Per launch: at most 16 M table rows (7 doubles each once kept) and 64 M
+// doubles of input, which bounds the device memory of a call to 1.4 GB.
+constexpr long long kBatchRows = 16LL << 20;
+constexpr long long kBatchIn = 64LL << 20;
+
+// The input doubles of a table and, for an interleaved one, where its
+// block starts: the five columns within one row-major block of n rows.
+long long table_span(const hbt_fit_table &T, const double **lo_out) {
+    const double *col[5] = {T.q_out, T.q_side, T.q_long, T.C, T.C_err};
+    const uintptr_t b0 = reinterpret_cast<uintptr_t>(col[0]);
+    uintptr_t lo = b0, hi = b0;
+    bool aligned = true;
+    for (const double *c : col) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(c);
+        lo = std::min(lo, a);
+        hi = std::max(hi, a);
+        aligned = aligned && (a - b0) % sizeof(double) == 0;
+    }
+    const long long width = (long long)((hi - lo) / sizeof(double)) + 1;
+    if (T.stride > 1 && aligned && width <= T.stride && T.n_rows > 0) {
+        *lo_out = reinterpret_cast<const double *>(lo);
+        return (T.n_rows - 1) * T.stride + width;
+    }
+    *lo_out = nullptr;
+    return 5 * T.n_rows;
+}
+
+}  // namespace
+
+struct hbt_fit_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    Buf in, rows[7], tab_off, desc, cls, res, counter;
+    hbt_fit_stats stats{};
+    std::string err;
+};
+
+namespace {
+
+hbt_status fit_fail(hbt_fit_ctx *c, hbt_status s, const std::string &m) {
+    if (c) c->err = m;
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+hbt_status hbt_fit_create(int device, hbt_fit_ctx **out) {
+    if (!out) return HBT_ERR_INVALID;
+    *out = nullptr;
+    hbt_fit_ctx *c = new hbt_fit_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
+        cudaEventCreate(&c->ev[2]) != cudaSuccess || !grow(c->counter, 8)) {
+        hbt_fit_destroy(c);
+        return HBT_ERR_CUDA;
+    }
+    *out = c;
+    return HBT_OK;
+}
+
+void hbt_fit_destroy(hbt_fit_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (Buf &b : c->rows)
+        if (b.p) cudaFree(b.p);
+    for (Buf *b : {&c->in, &c->tab_off, &c->desc, &c->cls, &c->res, &c->counter})
+        if (b->p) cudaFree(b->p);
+    for (cudaEvent_t e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *hbt_fit_last_error(const hbt_fit_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+hbt_status hbt_fit_get_stats(const hbt_fit_ctx *c, hbt_fit_stats *out) {
+    if (!c || !out) return HBT_ERR_INVALID;
+    *out = c->stats;
+    return HBT_OK;
+}
+
+hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *tables,
+                         const hbt_fit_options *opt, hbt_fit_result *out) {
+    if (!c || n_tables < 0 || (n_tables > 0 && (!tables || !out)) || !opt)
+        return HBT_ERR_INVALID;
+    if (opt->n_cuts < 1 || opt->n_cuts > kMaxCuts || !opt->q_cut_max)
+        return fit_fail(c, HBT_ERR_INVALID, "n_cuts must be 1..16");
+    FitConst fc{};
+    fc.n_cuts = opt->n_cuts;
+    fc.q_cut_min = opt->q_cut_min;
+    fc.max_iter = opt->max_iterations > 0 ? opt->max_iterations : 500;
+    for (int j = 0; j < 6; j++) fc.p0[j] = opt->p0[j];
+    std::vector<int> order(opt->n_cuts);
+    for (int k = 0; k < opt->n_cuts; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return opt->q_cut_max[a] < opt->q_cut_max[b]; });
+    for (int s = 0; s < opt->n_cuts; s++) {
+        fc.cut_sorted[s] = opt->q_cut_max[order[s]];
+        fc.rank[order[s]] = s;
+    }
+    for (int t = 0; t < n_tables; t++) {
+        const hbt_fit_table &T = tables[t];
+        if (T.n_rows < 0 || T.stride < 1 ||
+            (T.n_rows > 0 && (!T.q_out || !T.q_side || !T.q_long || !T.C || !T.C_err)))
+            return fit_fail(c, HBT_ERR_INVALID, "table " + std::to_string(t) + " is invalid");
+        const double *lo = nullptr;
+        if (T.n_rows > kBatchRows || table_span(T, &lo) > kBatchIn)
+            return fit_fail(c, HBT_ERR_INVALID, "table larger than a launch's row budget");
+    }
+    if (cudaSetDevice(c->device) != cudaSuccess) return fit_fail(c, HBT_ERR_CUDA, "cudaSetDevice");
+    c->stats = hbt_fit_stats{};
+    c->stats.fits = (int64_t)n_tables * opt->n_cuts;
+    if (n_tables == 0) return HBT_OK;
+    if (!grow(c->res, (size_t)n_tables * opt->n_cuts * sizeof(hbt_fit_result)))
+        return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
+    cudaError_t e = cudaMemsetAsync(c->counter.p, 0, 8, c->stream);
+    float up_ms = 0.f, fit_ms = 0.f;
+    std::vector<double> packed;
+    std::vector<long long> off;
+    std::vector<TabDesc> desc;
+    std::vector<const double *> block;
+    for (int t0 = 0; t0 < n_tables && e == cudaSuccess;) {
+        // the batch: tables [t0, t1) within the row and input budgets
+        int t1 = t0;
+        long long rows = 0, in_total = 0, n_packed = 0;
+        off.assign(1, 0);
+        desc.clear();
+        block.clear();
+        while (t1 < n_tables) {
+            const hbt_fit_table &T = tables[t1];
+            const double *lo = nullptr;
+            const long long span = table_span(T, &lo);
+            if (t1 > t0 && (rows + T.n_rows > kBatchRows || in_total + span > kBatchIn)) break;
+            TabDesc d{};
+            d.base = in_total;
+            if (lo) {
+                d.stride = T.stride;
+                const double *col[5] = {T.q_out, T.q_side, T.q_long, T.C, T.C_err};
+                for (int k = 0; k < 5; k++) d.col[k] = col[k] - lo;
+            } else {
+                d.stride = 1;
+                for (int k = 0; k < 5; k++) d.col[k] = k * T.n_rows;
+                n_packed += span;
+            }
+            desc.push_back(d);
+            block.push_back(lo);
+            in_total += span;
+            rows += T.n_rows;
+            off.push_back(rows);
+            t1++;
+        }
+        const int nt = t1 - t0;
+        bool ok = grow(c->tab_off, (nt + 1) * sizeof(long long)) &&
+                  grow(c->desc, nt * sizeof(TabDesc)) &&
+                  grow(c->cls, (size_t)nt * (opt->n_cuts + 1) * sizeof(int)) &&
+                  grow(c->in, in_total * sizeof(double));
+        for (int k = 0; k < 7; k++) ok = ok && grow(c->rows[k], rows * sizeof(double));
+        if (!ok) return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
+        // tables that are not one interleaved block are packed on the host
+        packed.resize((size_t)std::max<long long>(n_packed, 1));
+        long long pk = 0;
+        std::vector<long long> packed_at(nt, -1);
+        for (int t = t0; t < t1; t++) {
+            if (block[t - t0]) continue;
+            const hbt_fit_table &T = tables[t];
+            const double *col[5] = {T.q_out, T.q_side, T.q_long, T.C, T.C_err};
+            packed_at[t - t0] = pk;
+            for (int k = 0; k < 5; k++)
+                for (long long i = 0; i < T.n_rows; i++) packed[pk++] = col[k][i * T.stride];
+        }
+        double *din = static_cast<double *>(c->in.p);
+        e = cudaEventRecord(c->ev[0], c->stream);
+        for (int t = t0; t < t1 && e == cudaSuccess; t++) {
+            const long long span = (t + 1 < t1 ? desc[t - t0 + 1].base : in_total) - desc[t - t0].base;
+            if (span == 0) continue;
+            const double *src = block[t - t0] ? block[t - t0] : packed.data() + packed_at[t - t0];
+            e = cudaMemcpyAsync(din + desc[t - t0].base, src, span * sizeof(double),
+                                cudaMemcpyHostToDevice, c->stream);
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->tab_off.p, off.data(), off.size() * sizeof(long long),
+                                cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->desc.p, desc.data(), desc.size() * sizeof(TabDesc),
+                                cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) break;
+        Rows rw;
+        double **dst[7] = {&rw.qoo, &rw.qss, &rw.qll, &rw.qos, &rw.qol, &rw.C, &rw.w};
+        for (int k = 0; k < 7; k++) *dst[k] = static_cast<double *>(c->rows[k].p);
+        k_fit_select<<<nt, kSelThreads, 0, c->stream>>>(
+            fc, static_cast<const long long *>(c->tab_off.p),
+            static_cast<const TabDesc *>(c->desc.p), din, rw, static_cast<int *>(c->cls.p));
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if ((e = cudaEventRecord(c->ev[1], c->stream)) != cudaSuccess) break;
+        k_fit_lm<<<nt * opt->n_cuts, kFitThreads, 0, c->stream>>>(
+            fc, t0, static_cast<const long long *>(c->tab_off.p),
+            static_cast<const int *>(c->cls.p), rw, static_cast<hbt_fit_result *>(c->res.p),
+            static_cast<unsigned long long *>(c->counter.p));
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if ((e = cudaEventRecord(c->ev[2], c->stream)) != cudaSuccess) break;
+        // the host staging is reused by the next batch
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) break;
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+        up_ms += a;
+        fit_ms += b;
+        c->stats.rows += rows;
+        t0 = t1;
+    }
+    if (e != cudaSuccess) return fit_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
+    unsigned long long passes = 0;
+    if ((e = cudaMemcpyAsync(out, c->res.p, (size_t)n_tables * opt->n_cuts * sizeof(hbt_fit_result),
+                             cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&passes, c->counter.p, 8, cudaMemcpyDeviceToHost, c->stream)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+        return fit_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
+    for (long long f = 0; f < (long long)n_tables * opt->n_cuts; f++)
+        c->stats.points += out[f].n_points;
+    c->stats.passes = (int64_t)passes;
+    c->stats.upload_ms = up_ms;
+    c->stats.kernel_ms = fit_ms;
+    return HBT_OK;
+}
+
+}  // extern "C"

@@ -12,6 +12,7 @@ INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 HEADER = os.path.join(INCLUDE, "hbt_gpu.h")
 SERVER_HEADER = os.path.join(INCLUDE, "hbt_server.h")
 BF_HEADER = os.path.join(INCLUDE, "hbt_bf.h")
+FIT_HEADER = os.path.join(INCLUDE, "hbt_fit.h")
 
 
 def _declared_functions(path):
@@ -36,7 +37,7 @@ def test_header_declares_the_engine_api():
 
 def test_library_exports_every_declared_symbol(lib):
     for name in (_declared_functions(HEADER) + _declared_functions(SERVER_HEADER) +
-                 _declared_functions(BF_HEADER)):
+                 _declared_functions(BF_HEADER) + _declared_functions(FIT_HEADER)):
         assert hasattr(lib, name), name
 
 
@@ -45,6 +46,23 @@ def test_bf_header_matches_its_binding(lib):
     names = _declared_functions(BF_HEADER)
     assert "hbt_bf_bin" in names and "hbt_bf_read" in names
     assert sorted(bf.exported_symbols()) == names
+
+
+def test_fit_header_matches_its_binding(lib):
+    from hadronic_afterburner_toolkit_gb300 import radii
+    names = _declared_functions(FIT_HEADER)
+    assert "hbt_fit_radii" in names and "hbt_fit_create" in names
+    assert sorted(radii.exported_symbols()) == names
+    # the ctypes mirrors have the C structs' sizes
+    assert ctypes.sizeof(radii.HbtFitResult) == 8 * 14 + 16
+    assert ctypes.sizeof(radii.HbtFitTable) == 8 * 7
+
+
+def test_fit_rejects_bad_options_without_a_device_call(lib):
+    from hadronic_afterburner_toolkit_gb300 import radii
+    L = radii.load()
+    assert L.hbt_fit_radii(None, 0, None, None, None) == 1
+    assert L.hbt_fit_last_error(None) == b"null context"
 
 
 def test_server_header_matches_its_binding(lib):
