@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/hbt_fit.h"
@@ -39,6 +40,7 @@ constexpr int kSums = 28;  // chi2, J^T r (6), J^T J (21, packed lower)
 struct FitConst {
     double cut_sorted[kMaxCuts];  // ascending
     int rank[kMaxCuts];           // position of cut k in cut_sorted
+    int by_rank[kMaxCuts];        // the cut at position s of cut_sorted
     int n_cuts;
     double q_cut_min;
     double p0[6];
@@ -57,6 +59,7 @@ struct TabDesc {
 // cls[t * (n_cuts + 1) + c] = rows of t whose smallest passed cut is c.
 struct Rows {
     double *qoo, *qss, *qll, *qos, *qol, *C, *w;
+    float *fq[5];  // FP32 copies of the five q products
 };
 
 __device__ __forceinline__ double nan_to_num(double v) {
@@ -115,11 +118,13 @@ __global__ void __launch_bounds__(kSelThreads)
                 const long long o = r0 + off + __popc(m & ((1u << lane) - 1u));
                 const double cc = nan_to_num(c_in[i * d.stride]);
                 const double sigma = nan_to_num(e_in[i * d.stride]) + kEps;
-                out.qoo[o] = qo * qo;
-                out.qss[o] = qs * qs;
-                out.qll[o] = ql * ql;
-                out.qos[o] = 2.0 * qo * qs;
-                out.qol[o] = 2.0 * qo * ql;
+                const double q5[5] = {qo * qo, qs * qs, ql * ql, 2.0 * qo * qs, 2.0 * qo * ql};
+                out.qoo[o] = q5[0];
+                out.qss[o] = q5[1];
+                out.qll[o] = q5[2];
+                out.qos[o] = q5[3];
+                out.qol[o] = q5[4];
+                for (int k = 0; k < 5; k++) out.fq[k][o] = (float)q5[k];
                 out.C[o] = cc;
                 out.w[o] = 1.0 / sigma;
             }
@@ -135,56 +140,90 @@ __global__ void __launch_bounds__(kSelThreads)
 // One pass at parameters p: chi^2, J^T r, J^T J of the rows [0, n) of the
 // fit, reduced over the block into red[0..27] (valid in thread 0).
 // Residual r = w (f - C), J = w df/dp with f = lambda exp(-E),
-// E = sum_k (R_k / hbar c)^2 Q_k over the five q products Q_k.
+// E = sum_k a_k^2 Q_k over the five q products Q_k (a_k = R_k / hbar c), so
+// J_0 = w e and J_k = -w f (2 a_k / hbar c) Q_k: the constant factors
+// 2 a_k / hbar c are applied after the sums.  chi^2 and J^T r, which fix
+// where the minimum is, are summed in FP64.  J^T J only shapes the steps
+// while iterating (kExact = false: FP32 products and per-thread sums over
+// at most a few hundred rows, 1e-5 relative); the pass at the minimum that
+// gives the covariance sums it in FP64 (kExact = true).
+template <bool kExact>
 __device__ void fit_pass(const Rows &rw, long long r0, int n, const double *p, double *red) {
+    using AccT = typename std::conditional<kExact, double, float>::type;
     __shared__ double part[kFitThreads / 32][kSums];
-    double a[5], cdf[5];
+    double a2[5], cdf[7];
+    cdf[0] = 1.0;
     for (int k = 0; k < 5; k++) {
-        a[k] = p[k + 1] / kHbarC;
-        cdf[k] = 2.0 * a[k] / kHbarC;  // dE/dR_k = 2 a_k Q_k / hbar c
+        const double a = p[k + 1] / kHbarC;
+        a2[k] = a * a;
+        cdf[k + 1] = -2.0 * a / kHbarC;
     }
     const double lam = p[0];
-    double s[kSums];
+    double s[7];
+    AccT sa[21];
 #pragma unroll
-    for (int k = 0; k < kSums; k++) s[k] = 0.0;
+    for (int k = 0; k < 7; k++) s[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 21; k++) sa[k] = 0;
     for (int i = threadIdx.x; i < n; i += kFitThreads) {
         const long long o = r0 + i;
         const double q[5] = {rw.qoo[o], rw.qss[o], rw.qll[o], rw.qos[o], rw.qol[o]};
         const double w = rw.w[o];
         double E = 0.0;
 #pragma unroll
-        for (int k = 0; k < 5; k++) E += a[k] * a[k] * q[k];
+        for (int k = 0; k < 5; k++) E += a2[k] * q[k];
         const double e = exp(-E);
         const double f = lam * e;
         const double r = w * (f - rw.C[o]);
-        double J[6];
-        J[0] = w * e;
-        const double u = -w * f;
+        const double u = w * f;
+        double v[6];  // J without its constant factors
+        v[0] = w * e;
 #pragma unroll
-        for (int k = 0; k < 5; k++) J[k + 1] = u * cdf[k] * q[k];
+        for (int k = 0; k < 5; k++) v[k + 1] = u * q[k];
         s[0] += r * r;
 #pragma unroll
-        for (int k = 0; k < 6; k++) s[1 + k] += J[k] * r;
-        int m = 7;
+        for (int k = 0; k < 6; k++) s[1 + k] += v[k] * r;
+        AccT va[6];
+        if (kExact) {
+#pragma unroll
+            for (int k = 0; k < 6; k++) va[k] = (AccT)v[k];
+        } else {
+            const float uf = (float)u;
+            va[0] = (AccT)v[0];
+#pragma unroll
+            for (int k = 0; k < 5; k++) va[k + 1] = (AccT)(uf * rw.fq[k][o]);
+        }
+        int m = 0;
 #pragma unroll
         for (int j = 0; j < 6; j++)
 #pragma unroll
-            for (int k = 0; k <= j; k++) s[m++] += J[j] * J[k];
+            for (int k = 0; k <= j; k++) sa[m++] += va[j] * va[k];
+    }
+    double tot[kSums];
+    tot[0] = s[0];
+#pragma unroll
+    for (int k = 0; k < 6; k++) tot[1 + k] = s[1 + k] * cdf[k];
+    {
+        int m = 0;
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+#pragma unroll
+            for (int k = 0; k <= j; k++, m++) tot[7 + m] = (double)sa[m] * (cdf[j] * cdf[k]);
     }
 #pragma unroll
     for (int k = 0; k < kSums; k++) {
-        double v = s[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        s[k] = v;
+        double x = tot[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        tot[k] = x;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0)
-        for (int k = 0; k < kSums; k++) part[warp][k] = s[k];
+        for (int k = 0; k < kSums; k++) part[warp][k] = tot[k];
     __syncthreads();
     if (threadIdx.x < kSums) {
-        double v = 0.0;
-        for (int w = 0; w < kFitThreads / 32; w++) v += part[w][threadIdx.x];
-        red[threadIdx.x] = v;
+        double x = 0.0;
+        for (int w = 0; w < kFitThreads / 32; w++) x += part[w][threadIdx.x];
+        red[threadIdx.x] = x;
     }
     __syncthreads();
 }
@@ -320,18 +359,27 @@ __device__ __noinline__ void lm_update(LmState &st, const double *red) {
     }
 }
 
-// Results: the point, chi^2 and the errors sqrt(diag((J^T J)^-1)).
+// Results of the iterations: the point and chi^2 (the errors follow in
+// k_fit_cov).
 __device__ __noinline__ void lm_finish(const LmState &st, double q_cut, int n,
                                        hbt_fit_result *out) {
     out->q_cut = q_cut;
-    for (int j = 0; j < 6; j++) out->p[j] = st.x[j];
+    for (int j = 0; j < 6; j++) {
+        out->p[j] = st.x[j];
+        out->err[j] = NAN;
+    }
     out->chi2 = st.S;
     out->n_points = n;
     out->iterations = st.iter;
     out->reserved = 0;
-    int status = st.status;
+    out->status = st.status;
+}
+
+// The errors: sqrt(diag((J^T J)^-1)) with J^T J summed in FP64 at the
+// minimum (inf and the singular status when it is not positive definite).
+__device__ __noinline__ void cov_finish(const double *red, hbt_fit_result *out) {
     double L[21];
-    for (int j = 0; j < 21; j++) L[j] = st.A[j];
+    for (int j = 0; j < 21; j++) L[j] = red[7 + j];
     if (cholesky6(L)) {
         for (int j = 0; j < 6; j++) {
             double e[6] = {0, 0, 0, 0, 0, 0}, col[6];
@@ -341,9 +389,22 @@ __device__ __noinline__ void lm_finish(const LmState &st, double q_cut, int n,
         }
     } else {
         for (int j = 0; j < 6; j++) out->err[j] = INFINITY;
-        if (status == HBT_FIT_CONVERGED) status = HBT_FIT_SINGULAR;
+        if (out->status == HBT_FIT_CONVERGED) out->status = HBT_FIT_SINGULAR;
     }
-    out->status = status;
+}
+
+// The fit of a block: the largest cuts first (they have the most rows), so
+// a launch's tail is made of the small fits.
+__device__ __forceinline__ void fit_of_block(const FitConst &fc, int &t, int &k) {
+    const int nt = gridDim.x / fc.n_cuts;
+    t = blockIdx.x % nt;
+    k = fc.by_rank[fc.n_cuts - 1 - blockIdx.x / nt];
+}
+
+__device__ __forceinline__ int rows_of_fit(const FitConst &fc, const int *cls, int t, int k) {
+    int n = 0;
+    for (int c = 0; c <= fc.rank[k]; c++) n += cls[t * (fc.n_cuts + 1) + c];
+    return n;
 }
 
 __global__ void __launch_bounds__(kFitThreads)
@@ -351,11 +412,10 @@ __global__ void __launch_bounds__(kFitThreads)
              hbt_fit_result *res, unsigned long long *n_passes) {
     __shared__ double red[kSums];
     __shared__ LmState st;
-    const int fit = blockIdx.x;
-    const int t = fit / fc.n_cuts, k = fit % fc.n_cuts;
+    int t, k;
+    fit_of_block(fc, t, k);
     const long long r0 = tab_off[t];
-    int n = 0;
-    for (int c = 0; c <= fc.rank[k]; c++) n += cls[t * (fc.n_cuts + 1) + c];
+    const int n = rows_of_fit(fc, cls, t, k);
     hbt_fit_result *out = res + (long long)(first_table + t) * fc.n_cuts + k;
     const double q_cut = fc.cut_sorted[fc.rank[k]];
     if (n < 6) {
@@ -374,7 +434,7 @@ __global__ void __launch_bounds__(kFitThreads)
     __syncthreads();
     // one pass per trial point: the first at the start point
     for (bool first = true;; first = false) {
-        fit_pass(rw, r0, n, first ? st.x : st.trial, red);
+        fit_pass<false>(rw, r0, n, first ? st.x : st.trial, red);
         if (threadIdx.x == 0) {
             if (first)
                 lm_init(st, red);
@@ -387,8 +447,27 @@ __global__ void __launch_bounds__(kFitThreads)
     }
     if (threadIdx.x == 0) {
         lm_finish(st, q_cut, n, out);
-        atomicAdd(n_passes, (unsigned long long)st.passes);
+        atomicAdd(n_passes, (unsigned long long)st.passes + 1);  // + k_fit_cov's pass
     }
+}
+
+// One pass at each fit's minimum with J^T J in FP64, for the errors.  A
+// kernel of its own so that the iterations' kernel keeps the FP32 sums'
+// register budget.
+__global__ void __launch_bounds__(kFitThreads)
+    k_fit_cov(FitConst fc, int first_table, const long long *tab_off, const int *cls, Rows rw,
+              hbt_fit_result *res) {
+    __shared__ double red[kSums];
+    __shared__ double x[6];
+    int t, k;
+    fit_of_block(fc, t, k);
+    const int n = rows_of_fit(fc, cls, t, k);
+    if (n < 6) return;
+    hbt_fit_result *out = res + (long long)(first_table + t) * fc.n_cuts + k;
+    if (threadIdx.x < 6) x[threadIdx.x] = out->p[threadIdx.x];
+    __syncthreads();
+    fit_pass<true>(rw, tab_off[t], n, x, red);
+    if (threadIdx.x == 0) cov_finish(red, out);
 }
 
 struct Buf {
@@ -443,7 +522,7 @@ struct hbt_fit_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-    Buf in, rows[7], tab_off, desc, cls, res, counter;
+    Buf in, rows[7], frows[5], tab_off, desc, cls, res, counter;
     hbt_fit_stats stats{};
     std::string err;
 };
@@ -481,6 +560,8 @@ void hbt_fit_destroy(hbt_fit_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (Buf &b : c->rows)
         if (b.p) cudaFree(b.p);
+    for (Buf &b : c->frows)
+        if (b.p) cudaFree(b.p);
     for (Buf *b : {&c->in, &c->tab_off, &c->desc, &c->cls, &c->res, &c->counter})
         if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : c->ev)
@@ -515,6 +596,7 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
     for (int s = 0; s < opt->n_cuts; s++) {
         fc.cut_sorted[s] = opt->q_cut_max[order[s]];
         fc.rank[order[s]] = s;
+        fc.by_rank[s] = order[s];
     }
     for (int t = 0; t < n_tables; t++) {
         const hbt_fit_table &T = tables[t];
@@ -573,6 +655,7 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
                   grow(c->cls, (size_t)nt * (opt->n_cuts + 1) * sizeof(int)) &&
                   grow(c->in, in_total * sizeof(double));
         for (int k = 0; k < 7; k++) ok = ok && grow(c->rows[k], rows * sizeof(double));
+        for (int k = 0; k < 5; k++) ok = ok && grow(c->frows[k], rows * sizeof(float));
         if (!ok) return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
         // tables that are not one interleaved block are packed on the host
         packed.resize((size_t)std::max<long long>(n_packed, 1));
@@ -605,6 +688,7 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
         Rows rw;
         double **dst[7] = {&rw.qoo, &rw.qss, &rw.qll, &rw.qos, &rw.qol, &rw.C, &rw.w};
         for (int k = 0; k < 7; k++) *dst[k] = static_cast<double *>(c->rows[k].p);
+        for (int k = 0; k < 5; k++) rw.fq[k] = static_cast<float *>(c->frows[k].p);
         k_fit_select<<<nt, kSelThreads, 0, c->stream>>>(
             fc, static_cast<const long long *>(c->tab_off.p),
             static_cast<const TabDesc *>(c->desc.p), din, rw, static_cast<int *>(c->cls.p));
@@ -614,6 +698,10 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
             fc, t0, static_cast<const long long *>(c->tab_off.p),
             static_cast<const int *>(c->cls.p), rw, static_cast<hbt_fit_result *>(c->res.p),
             static_cast<unsigned long long *>(c->counter.p));
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        k_fit_cov<<<nt * opt->n_cuts, kFitThreads, 0, c->stream>>>(
+            fc, t0, static_cast<const long long *>(c->tab_off.p),
+            static_cast<const int *>(c->cls.p), rw, static_cast<hbt_fit_result *>(c->res.p));
         if ((e = cudaGetLastError()) != cudaSuccess) break;
         if ((e = cudaEventRecord(c->ev[2], c->stream)) != cudaSuccess) break;
         // the host staging is reused by the next batch
