@@ -2,7 +2,8 @@
 //
 // The reference fits each correlation table with scipy's curve_fit, one
 // table and one q_cut at a time (ebe_scripts/fit_HBT_radii.py:60-92).  Here
-// every (table, q_cut) of a call is one CTA of one launch:
+// every (table, q_cut) of a batch is one CTA of one launch, and two batches
+// are in flight on two streams (one copying while the other fits):
 //
 //  * k_fit_select (one CTA per table) applies the script's preprocessing
 //    (numpy nan_to_num, C_err + 1e-15, weight 1 / sigma) and keeps the rows
@@ -489,10 +490,12 @@ bool grow(Buf &b, size_t bytes) {
     return true;
 }
 
-// Per launch: at most 16 M table rows (7 doubles each once kept) and 64 M
-// doubles of input, which bounds the device memory of a call to 1.4 GB.
-constexpr long long kBatchRows = 16LL << 20;
-constexpr long long kBatchIn = 64LL << 20;
+// Per batch: at most 4 M table rows (7 doubles and 5 floats each once
+// kept) and 32 M doubles of input; two batches are in flight (one copying
+// while the other fits), which bounds the device memory of a call to
+// 1.1 GB.  A batch of 41^3-row tables holds 58 of them (290 fits).
+constexpr long long kBatchRows = 4LL << 20;
+constexpr long long kBatchIn = 32LL << 20;
 
 // The input doubles of a table and, for an interleaved one, where its
 // block starts: the five columns within one row-major block of n rows.
@@ -518,11 +521,22 @@ long long table_span(const hbt_fit_table &T, const double **lo_out) {
 
 }  // namespace
 
+// One of the two batches in flight: its device buffers, its stream (copies,
+// row selection, fits, errors in order) and the host arrays its copies read.
+struct FitSlot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr, t2 = nullptr;
+    Buf in, rows[7], frows[5], tab_off, desc, cls;
+    std::vector<double> packed;
+    std::vector<long long> off;
+    std::vector<TabDesc> desc_h;
+    bool busy = false;
+};
+
 struct hbt_fit_ctx {
     int device = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-    Buf in, rows[7], frows[5], tab_off, desc, cls, res, counter;
+    FitSlot slot[2];
+    Buf res, counter;
     hbt_fit_stats stats{};
     std::string err;
 };
@@ -543,10 +557,12 @@ hbt_status hbt_fit_create(int device, hbt_fit_ctx **out) {
     *out = nullptr;
     hbt_fit_ctx *c = new hbt_fit_ctx();
     c->device = device;
-    if (cudaSetDevice(device) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
-        cudaEventCreate(&c->ev[2]) != cudaSuccess || !grow(c->counter, 8)) {
+    bool ok = cudaSetDevice(device) == cudaSuccess && grow(c->counter, 8);
+    for (FitSlot &sl : c->slot)
+        ok = ok && cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreate(&sl.t0) == cudaSuccess && cudaEventCreate(&sl.t1) == cudaSuccess &&
+             cudaEventCreate(&sl.t2) == cudaSuccess;
+    if (!ok) {
         hbt_fit_destroy(c);
         return HBT_ERR_CUDA;
     }
@@ -557,16 +573,20 @@ hbt_status hbt_fit_create(int device, hbt_fit_ctx **out) {
 void hbt_fit_destroy(hbt_fit_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    for (Buf &b : c->rows)
-        if (b.p) cudaFree(b.p);
-    for (Buf &b : c->frows)
-        if (b.p) cudaFree(b.p);
-    for (Buf *b : {&c->in, &c->tab_off, &c->desc, &c->cls, &c->res, &c->counter})
+    for (FitSlot &sl : c->slot) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        for (Buf &b : sl.rows)
+            if (b.p) cudaFree(b.p);
+        for (Buf &b : sl.frows)
+            if (b.p) cudaFree(b.p);
+        for (Buf *b : {&sl.in, &sl.tab_off, &sl.desc, &sl.cls})
+            if (b->p) cudaFree(b->p);
+        for (cudaEvent_t e : {sl.t0, sl.t1, sl.t2})
+            if (e) cudaEventDestroy(e);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    for (Buf *b : {&c->res, &c->counter})
         if (b->p) cudaFree(b->p);
-    for (cudaEvent_t e : c->ev)
-        if (e) cudaEventDestroy(e);
-    if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
 
@@ -613,18 +633,37 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
     if (n_tables == 0) return HBT_OK;
     if (!grow(c->res, (size_t)n_tables * opt->n_cuts * sizeof(hbt_fit_result)))
         return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
-    cudaError_t e = cudaMemsetAsync(c->counter.p, 0, 8, c->stream);
+    FitSlot *S = c->slot;
+    cudaError_t e = cudaMemsetAsync(c->counter.p, 0, 8, S[0].stream);
+    // slot 1 starts after the counter is cleared
+    if (e == cudaSuccess) e = cudaEventRecord(S[0].t2, S[0].stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(S[1].stream, S[0].t2, 0);
     float up_ms = 0.f, fit_ms = 0.f;
-    std::vector<double> packed;
-    std::vector<long long> off;
-    std::vector<TabDesc> desc;
+    // a slot's previous batch must be done before its buffers and host
+    // arrays are reused; its times are collected then
+    auto retire = [&](FitSlot &sl) -> cudaError_t {
+        if (!sl.busy) return cudaSuccess;
+        const cudaError_t r = cudaEventSynchronize(sl.t2);
+        if (r != cudaSuccess) return r;
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, sl.t0, sl.t1);
+        cudaEventElapsedTime(&b, sl.t1, sl.t2);
+        up_ms += a;
+        fit_ms += b;
+        sl.busy = false;
+        return cudaSuccess;
+    };
     std::vector<const double *> block;
-    for (int t0 = 0; t0 < n_tables && e == cudaSuccess;) {
+    std::vector<long long> packed_at;
+    int batch = 0;
+    for (int t0 = 0; t0 < n_tables && e == cudaSuccess; batch++) {
+        FitSlot &sl = S[batch & 1];
+        if ((e = retire(sl)) != cudaSuccess) break;
         // the batch: tables [t0, t1) within the row and input budgets
         int t1 = t0;
         long long rows = 0, in_total = 0, n_packed = 0;
-        off.assign(1, 0);
-        desc.clear();
+        sl.off.assign(1, 0);
+        sl.desc_h.clear();
         block.clear();
         while (t1 < n_tables) {
             const hbt_fit_table &T = tables[t1];
@@ -642,85 +681,90 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
                 for (int k = 0; k < 5; k++) d.col[k] = k * T.n_rows;
                 n_packed += span;
             }
-            desc.push_back(d);
+            sl.desc_h.push_back(d);
             block.push_back(lo);
             in_total += span;
             rows += T.n_rows;
-            off.push_back(rows);
+            sl.off.push_back(rows);
             t1++;
         }
         const int nt = t1 - t0;
-        bool ok = grow(c->tab_off, (nt + 1) * sizeof(long long)) &&
-                  grow(c->desc, nt * sizeof(TabDesc)) &&
-                  grow(c->cls, (size_t)nt * (opt->n_cuts + 1) * sizeof(int)) &&
-                  grow(c->in, in_total * sizeof(double));
-        for (int k = 0; k < 7; k++) ok = ok && grow(c->rows[k], rows * sizeof(double));
-        for (int k = 0; k < 5; k++) ok = ok && grow(c->frows[k], rows * sizeof(float));
-        if (!ok) return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
+        bool ok = grow(sl.tab_off, (nt + 1) * sizeof(long long)) &&
+                  grow(sl.desc, nt * sizeof(TabDesc)) &&
+                  grow(sl.cls, (size_t)nt * (opt->n_cuts + 1) * sizeof(int)) &&
+                  grow(sl.in, in_total * sizeof(double));
+        for (int k = 0; k < 7; k++) ok = ok && grow(sl.rows[k], rows * sizeof(double));
+        for (int k = 0; k < 5; k++) ok = ok && grow(sl.frows[k], rows * sizeof(float));
+        if (!ok) {
+            for (FitSlot &x : c->slot) cudaStreamSynchronize(x.stream);
+            return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
+        }
         // tables that are not one interleaved block are packed on the host
-        packed.resize((size_t)std::max<long long>(n_packed, 1));
+        sl.packed.resize((size_t)std::max<long long>(n_packed, 1));
         long long pk = 0;
-        std::vector<long long> packed_at(nt, -1);
+        packed_at.assign(nt, -1);
         for (int t = t0; t < t1; t++) {
             if (block[t - t0]) continue;
             const hbt_fit_table &T = tables[t];
             const double *col[5] = {T.q_out, T.q_side, T.q_long, T.C, T.C_err};
             packed_at[t - t0] = pk;
             for (int k = 0; k < 5; k++)
-                for (long long i = 0; i < T.n_rows; i++) packed[pk++] = col[k][i * T.stride];
+                for (long long i = 0; i < T.n_rows; i++) sl.packed[pk++] = col[k][i * T.stride];
         }
-        double *din = static_cast<double *>(c->in.p);
-        e = cudaEventRecord(c->ev[0], c->stream);
+        double *din = static_cast<double *>(sl.in.p);
+        e = cudaEventRecord(sl.t0, sl.stream);
         for (int t = t0; t < t1 && e == cudaSuccess; t++) {
-            const long long span = (t + 1 < t1 ? desc[t - t0 + 1].base : in_total) - desc[t - t0].base;
+            const long long span =
+                (t + 1 < t1 ? sl.desc_h[t - t0 + 1].base : in_total) - sl.desc_h[t - t0].base;
             if (span == 0) continue;
-            const double *src = block[t - t0] ? block[t - t0] : packed.data() + packed_at[t - t0];
-            e = cudaMemcpyAsync(din + desc[t - t0].base, src, span * sizeof(double),
-                                cudaMemcpyHostToDevice, c->stream);
+            const double *src = block[t - t0] ? block[t - t0] : sl.packed.data() + packed_at[t - t0];
+            e = cudaMemcpyAsync(din + sl.desc_h[t - t0].base, src, span * sizeof(double),
+                                cudaMemcpyHostToDevice, sl.stream);
         }
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(c->tab_off.p, off.data(), off.size() * sizeof(long long),
-                                cudaMemcpyHostToDevice, c->stream);
+            e = cudaMemcpyAsync(sl.tab_off.p, sl.off.data(), sl.off.size() * sizeof(long long),
+                                cudaMemcpyHostToDevice, sl.stream);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(c->desc.p, desc.data(), desc.size() * sizeof(TabDesc),
-                                cudaMemcpyHostToDevice, c->stream);
+            e = cudaMemcpyAsync(sl.desc.p, sl.desc_h.data(), sl.desc_h.size() * sizeof(TabDesc),
+                                cudaMemcpyHostToDevice, sl.stream);
         if (e != cudaSuccess) break;
         Rows rw;
         double **dst[7] = {&rw.qoo, &rw.qss, &rw.qll, &rw.qos, &rw.qol, &rw.C, &rw.w};
-        for (int k = 0; k < 7; k++) *dst[k] = static_cast<double *>(c->rows[k].p);
-        for (int k = 0; k < 5; k++) rw.fq[k] = static_cast<float *>(c->frows[k].p);
-        k_fit_select<<<nt, kSelThreads, 0, c->stream>>>(
-            fc, static_cast<const long long *>(c->tab_off.p),
-            static_cast<const TabDesc *>(c->desc.p), din, rw, static_cast<int *>(c->cls.p));
+        for (int k = 0; k < 7; k++) *dst[k] = static_cast<double *>(sl.rows[k].p);
+        for (int k = 0; k < 5; k++) rw.fq[k] = static_cast<float *>(sl.frows[k].p);
+        const long long *d_off = static_cast<const long long *>(sl.tab_off.p);
+        k_fit_select<<<nt, kSelThreads, 0, sl.stream>>>(
+            fc, d_off, static_cast<const TabDesc *>(sl.desc.p), din, rw,
+            static_cast<int *>(sl.cls.p));
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        if ((e = cudaEventRecord(c->ev[1], c->stream)) != cudaSuccess) break;
-        k_fit_lm<<<nt * opt->n_cuts, kFitThreads, 0, c->stream>>>(
-            fc, t0, static_cast<const long long *>(c->tab_off.p),
-            static_cast<const int *>(c->cls.p), rw, static_cast<hbt_fit_result *>(c->res.p),
-            static_cast<unsigned long long *>(c->counter.p));
+        if ((e = cudaEventRecord(sl.t1, sl.stream)) != cudaSuccess) break;
+        k_fit_lm<<<nt * opt->n_cuts, kFitThreads, 0, sl.stream>>>(
+            fc, t0, d_off, static_cast<const int *>(sl.cls.p), rw,
+            static_cast<hbt_fit_result *>(c->res.p), static_cast<unsigned long long *>(c->counter.p));
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        k_fit_cov<<<nt * opt->n_cuts, kFitThreads, 0, c->stream>>>(
-            fc, t0, static_cast<const long long *>(c->tab_off.p),
-            static_cast<const int *>(c->cls.p), rw, static_cast<hbt_fit_result *>(c->res.p));
+        k_fit_cov<<<nt * opt->n_cuts, kFitThreads, 0, sl.stream>>>(
+            fc, t0, d_off, static_cast<const int *>(sl.cls.p), rw,
+            static_cast<hbt_fit_result *>(c->res.p));
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        if ((e = cudaEventRecord(c->ev[2], c->stream)) != cudaSuccess) break;
-        // the host staging is reused by the next batch
-        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) break;
-        float a = 0.f, b = 0.f;
-        cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
-        cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
-        up_ms += a;
-        fit_ms += b;
+        if ((e = cudaEventRecord(sl.t2, sl.stream)) != cudaSuccess) break;
+        sl.busy = true;
         c->stats.rows += rows;
         t0 = t1;
     }
-    if (e != cudaSuccess) return fit_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
+    for (FitSlot &sl : c->slot) {
+        const cudaError_t r = retire(sl);
+        if (e == cudaSuccess) e = r;
+    }
+    if (e != cudaSuccess) {
+        for (FitSlot &sl : c->slot) cudaStreamSynchronize(sl.stream);
+        return fit_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
+    }
     unsigned long long passes = 0;
     if ((e = cudaMemcpyAsync(out, c->res.p, (size_t)n_tables * opt->n_cuts * sizeof(hbt_fit_result),
-                             cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(&passes, c->counter.p, 8, cudaMemcpyDeviceToHost, c->stream)) !=
+                             cudaMemcpyDeviceToHost, S[0].stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&passes, c->counter.p, 8, cudaMemcpyDeviceToHost, S[0].stream)) !=
             cudaSuccess ||
-        (e = cudaStreamSynchronize(c->stream)) != cudaSuccess)
+        (e = cudaStreamSynchronize(S[0].stream)) != cudaSuccess)
         return fit_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
     for (long long f = 0; f < (long long)n_tables * opt->n_cuts; f++)
         c->stats.points += out[f].n_points;

@@ -15,8 +15,9 @@
  * nan_to_num).  Each fit is a Levenberg-Marquardt minimisation in FP64
  * from the given start point with the analytic Jacobian; the errors are
  * the square roots of the diagonal of (J^T J)^-1 at the minimum (scipy's
- * curve_fit with absolute_sigma=True).  All fits of a call run in one
- * launch, one CTA per (table, q_cut).
+ * curve_fit with absolute_sigma=True).  The fits of a call run one CTA per
+ * (table, q_cut), in batches of up to 32 M input doubles with two batches
+ * in flight: one copying to the device while the other fits.
  */
 #ifndef HBT_FIT_H
 #define HBT_FIT_H
@@ -73,8 +74,8 @@ typedef struct hbt_fit_stats {
     int64_t rows;          /* table rows uploaded */
     int64_t points;        /* sum over fits of the rows fitted */
     int64_t passes;        /* sum over fits of the passes over their rows */
-    double upload_ms;      /* device time: copies and row selection */
-    double kernel_ms;      /* device time: the fits */
+    double upload_ms;      /* device time of the copies and row selection, summed over batches */
+    double kernel_ms;      /* device time of the fits, summed over batches (two overlap) */
 } hbt_fit_stats;
 
 hbt_status hbt_fit_create(int device, hbt_fit_ctx **out);
