@@ -38,6 +38,11 @@ constexpr int kSelThreads = 256;
 constexpr int kFitThreads = 128;
 constexpr int kSums = 28;  // chi2, J^T r (6), J^T J (21, packed lower)
 
+// Resident fitting CTAs per SM the iterations' kernel is compiled for.
+#ifndef HBT_FIT_MIN_BLOCKS
+#define HBT_FIT_MIN_BLOCKS 4
+#endif
+
 struct FitConst {
     double cut_sorted[kMaxCuts];  // ascending
     int rank[kMaxCuts];           // position of cut k in cut_sorted
@@ -58,10 +63,16 @@ struct TabDesc {
 
 // Device rows of a batch: the kept rows of table t start at row_off[t];
 // cls[t * (n_cuts + 1) + c] = rows of t whose smallest passed cut is c.
+// Column k of kept row o: d[k * ld + o] for the doubles (the five q
+// products q_out^2, q_side^2, q_long^2, 2 q_out q_side, 2 q_out q_long, then
+// C and the weight), f[k * ld + o] for the FP32 copies of the q products.
+// One base pointer each keeps the fitting loop's registers for its sums.
 struct Rows {
-    double *qoo, *qss, *qll, *qos, *qol, *C, *w;
-    float *fq[5];  // FP32 copies of the five q products
+    double *d;
+    float *f;
+    long long ld;
 };
+constexpr int kColC = 5, kColW = 6;
 
 __device__ __forceinline__ double nan_to_num(double v) {
     if (isnan(v)) return 0.0;
@@ -120,14 +131,12 @@ __global__ void __launch_bounds__(kSelThreads)
                 const double cc = nan_to_num(c_in[i * d.stride]);
                 const double sigma = nan_to_num(e_in[i * d.stride]) + kEps;
                 const double q5[5] = {qo * qo, qs * qs, ql * ql, 2.0 * qo * qs, 2.0 * qo * ql};
-                out.qoo[o] = q5[0];
-                out.qss[o] = q5[1];
-                out.qll[o] = q5[2];
-                out.qos[o] = q5[3];
-                out.qol[o] = q5[4];
-                for (int k = 0; k < 5; k++) out.fq[k][o] = (float)q5[k];
-                out.C[o] = cc;
-                out.w[o] = 1.0 / sigma;
+                for (int k = 0; k < 5; k++) {
+                    out.d[k * out.ld + o] = q5[k];
+                    out.f[k * out.ld + o] = (float)q5[k];
+                }
+                out.d[kColC * out.ld + o] = cc;
+                out.d[kColW * out.ld + o] = 1.0 / sigma;
             }
             __syncthreads();
             if (threadIdx.x == 0) base += tot;
@@ -168,14 +177,17 @@ __device__ void fit_pass(const Rows &rw, long long r0, int n, const double *p, d
     for (int k = 0; k < 21; k++) sa[k] = 0;
     for (int i = threadIdx.x; i < n; i += kFitThreads) {
         const long long o = r0 + i;
-        const double q[5] = {rw.qoo[o], rw.qss[o], rw.qll[o], rw.qos[o], rw.qol[o]};
-        const double w = rw.w[o];
+        const double *dp = rw.d + o;
+        double q[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) q[k] = dp[k * rw.ld];
+        const double w = dp[kColW * rw.ld];
         double E = 0.0;
 #pragma unroll
         for (int k = 0; k < 5; k++) E += a2[k] * q[k];
         const double e = exp(-E);
         const double f = lam * e;
-        const double r = w * (f - rw.C[o]);
+        const double r = w * (f - dp[kColC * rw.ld]);
         const double u = w * f;
         double v[6];  // J without its constant factors
         v[0] = w * e;
@@ -192,7 +204,7 @@ __device__ void fit_pass(const Rows &rw, long long r0, int n, const double *p, d
             const float uf = (float)u;
             va[0] = (AccT)v[0];
 #pragma unroll
-            for (int k = 0; k < 5; k++) va[k + 1] = (AccT)(uf * rw.fq[k][o]);
+            for (int k = 0; k < 5; k++) va[k + 1] = (AccT)(uf * rw.f[k * rw.ld + o]);
         }
         int m = 0;
 #pragma unroll
@@ -408,7 +420,7 @@ __device__ __forceinline__ int rows_of_fit(const FitConst &fc, const int *cls, i
     return n;
 }
 
-__global__ void __launch_bounds__(kFitThreads)
+__global__ void __launch_bounds__(kFitThreads, HBT_FIT_MIN_BLOCKS)
     k_fit_lm(FitConst fc, int first_table, const long long *tab_off, const int *cls, Rows rw,
              hbt_fit_result *res, unsigned long long *n_passes) {
     __shared__ double red[kSums];
@@ -526,7 +538,7 @@ long long table_span(const hbt_fit_table &T, const double **lo_out) {
 struct FitSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr, t2 = nullptr;
-    Buf in, rows[7], frows[5], tab_off, desc, cls;
+    Buf in, rows, frows, tab_off, desc, cls;
     std::vector<double> packed;
     std::vector<long long> off;
     std::vector<TabDesc> desc_h;
@@ -575,11 +587,7 @@ void hbt_fit_destroy(hbt_fit_ctx *c) {
     cudaSetDevice(c->device);
     for (FitSlot &sl : c->slot) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
-        for (Buf &b : sl.rows)
-            if (b.p) cudaFree(b.p);
-        for (Buf &b : sl.frows)
-            if (b.p) cudaFree(b.p);
-        for (Buf *b : {&sl.in, &sl.tab_off, &sl.desc, &sl.cls})
+        for (Buf *b : {&sl.in, &sl.rows, &sl.frows, &sl.tab_off, &sl.desc, &sl.cls})
             if (b->p) cudaFree(b->p);
         for (cudaEvent_t e : {sl.t0, sl.t1, sl.t2})
             if (e) cudaEventDestroy(e);
@@ -693,8 +701,8 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
                   grow(sl.desc, nt * sizeof(TabDesc)) &&
                   grow(sl.cls, (size_t)nt * (opt->n_cuts + 1) * sizeof(int)) &&
                   grow(sl.in, in_total * sizeof(double));
-        for (int k = 0; k < 7; k++) ok = ok && grow(sl.rows[k], rows * sizeof(double));
-        for (int k = 0; k < 5; k++) ok = ok && grow(sl.frows[k], rows * sizeof(float));
+        ok = ok && grow(sl.rows, 7 * rows * sizeof(double)) &&
+             grow(sl.frows, 5 * rows * sizeof(float));
         if (!ok) {
             for (FitSlot &x : c->slot) cudaStreamSynchronize(x.stream);
             return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
@@ -728,10 +736,7 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
             e = cudaMemcpyAsync(sl.desc.p, sl.desc_h.data(), sl.desc_h.size() * sizeof(TabDesc),
                                 cudaMemcpyHostToDevice, sl.stream);
         if (e != cudaSuccess) break;
-        Rows rw;
-        double **dst[7] = {&rw.qoo, &rw.qss, &rw.qll, &rw.qos, &rw.qol, &rw.C, &rw.w};
-        for (int k = 0; k < 7; k++) *dst[k] = static_cast<double *>(sl.rows[k].p);
-        for (int k = 0; k < 5; k++) rw.fq[k] = static_cast<float *>(sl.frows[k].p);
+        Rows rw{static_cast<double *>(sl.rows.p), static_cast<float *>(sl.frows.p), rows};
         const long long *d_off = static_cast<const long long *>(sl.tab_off.p);
         k_fit_select<<<nt, kSelThreads, 0, sl.stream>>>(
             fc, d_off, static_cast<const TabDesc *>(sl.desc.p), din, rw,
