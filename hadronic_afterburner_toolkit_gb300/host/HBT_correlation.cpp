@@ -133,14 +133,10 @@ void HBT_correlation::calculate_HBT_correlation_function(
 // src/HBT_correlation.cpp:233-249
 void HBT_correlation::calculate_flow_event_plane_angle(int n_order) {
     const int nev = particle_list->get_number_of_events();
-    double vn_real = 0.0, vn_imag = 0.0;
+    EventPlaneSums sums;
     for (int iev = 0; iev < nev; iev++)
-        for (const particle_info &p : particle_list->event(iev)) {
-            const double phi = atan2(p.py, p.px);
-            vn_real += cos(n_order * phi);
-            vn_imag += sin(n_order * phi);
-        }
-    psi_ref = atan2(vn_imag, vn_real) / n_order;
+        for (const particle_info &p : particle_list->event(iev)) sums.add(p.px, p.py, n_order);
+    psi_ref = sums.angle(n_order);
 }
 
 // Gather of src/HBT_correlation.cpp:254-285, pair loop on the GPU.

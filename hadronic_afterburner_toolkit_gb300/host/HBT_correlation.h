@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cmath>
 #include <memory>
 #include <string>
 #include <vector>
@@ -22,6 +23,19 @@
 #include "Random.h"
 #include "hbt_gpu.h"
 #include "particleSamples.h"
+
+// The event-plane sums of src/HBT_correlation.cpp:233-249: over the
+// particles in order, phi = atan2(py, px), sum cos(n phi) and sin(n phi);
+// psi_ref = atan2(sum sin, sum cos) / n.
+struct EventPlaneSums {
+    double re = 0.0, im = 0.0;
+    void add(double px, double py, int n_order) {
+        const double phi = atan2(py, px);
+        re += cos(n_order * phi);
+        im += sin(n_order * phi);
+    }
+    double angle(int n_order) const { return atan2(im, re) / n_order; }
+};
 
 class HBT_correlation {
   public:

@@ -1,5 +1,6 @@
 // C ABI of the drop-in host side (include/hbt_host.h).
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <iostream>
 #include <memory>
@@ -39,6 +40,14 @@ int hbt_host_write(const hbt_params *params, const char *path, int32_t eco_outpu
                                   den,       qinv_sum,   qinv_num,   qinv_count, qinv_den,
                                   ctr_num,   ctr_den,    ctr_num_qinv, ctr_den_qinv};
     return hbt_write_outputs(*params, path, eco_output, v);
+}
+
+double hbt_host_event_plane_angle(int64_t n, const double *px, const double *py,
+                                  int32_t n_order) {
+    if (n < 0 || (n > 0 && (!px || !py)) || n_order == 0) return NAN;
+    EventPlaneSums sums;
+    for (int64_t i = 0; i < n; i++) sums.add(px[i], py[i], n_order);
+    return sums.angle(n_order);
 }
 
 int hbt_host_scan_buffers(const char *param_file, const char *results_path, int32_t cap,

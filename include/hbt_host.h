@@ -38,6 +38,14 @@ int hbt_host_write(const hbt_params *params, const char *path, int32_t eco_outpu
                    const double *qinv_den, const uint64_t *ctr_num, const uint64_t *ctr_den,
                    const uint64_t *ctr_num_qinv, const uint64_t *ctr_den_qinv);
 
+/* psi_ref of the reference's calculate_flow_event_plane_angle(n_order)
+ * (src/HBT_correlation.cpp:233-249, what get_psi_ref() returns after it):
+ * atan2(sum sin(n phi), sum cos(n phi)) / n over the n particles in order,
+ * phi = atan2(py, px).  The drop-in's HBT_correlation computes it with the
+ * same sums.  NaN for invalid arguments. */
+double hbt_host_event_plane_angle(int64_t n, const double *px, const double *py,
+                                  int32_t n_order);
+
 /* Reads the samples of a parameter file's HBT setup buffer by buffer with
  * the reference's reader rules (particleSamples, src/particleSamples.cpp),
  * without binning anything: for each buffer, the event count and particle

@@ -271,3 +271,15 @@ def test_writer_formats_special_values_like_printf(host, tmp_path):
                     v = (q[0][at] / c, q[1][at] / c, q[2][at] / c, num[at], ratio * den[at])
                 want.append("%18.8e    %.8e    %.8e    %.8e    %.8e" % v)
     assert got == want
+
+
+def test_host_library_exports_every_declared_symbol(host):
+    """libhbt_host.so exports every entry point include/hbt_host.h declares."""
+    import re
+    text = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                             "include", "hbt_host.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = sorted(set(re.findall(r"\b(hbt_host_[a-z_0-9]+)\s*\(", text)))
+    assert "hbt_host_run" in names and "hbt_host_event_plane_angle" in names
+    for name in names:
+        assert hasattr(host, name), name
