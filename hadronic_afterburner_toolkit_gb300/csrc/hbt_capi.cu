@@ -62,6 +62,14 @@ struct hbt_ctx {
     DevBuf in;
     // readback: two FP64 arrays of the histogram size, used in turn
     DevBuf exp;
+    // overlapped readback (hbt_read_hist_async): a snapshot of the six
+    // arrays and the error flag, copied to the host on `copy` while later
+    // work runs on `stream`
+    DevBuf snap;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t snap_ev = nullptr, copy_ev = nullptr;
+    u64 *flag_host = nullptr;  // pinned
+    bool read_pending = false;
     // upper bounds of the four counter families (num 3-D, den 3-D, num
     // q_inv, den q_inv): max counter <= bound
     u64 ub[4] = {0, 0, 0, 0};
@@ -619,7 +627,13 @@ void hbt_destroy(hbt_ctx *c) {
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
                       &c->apply_iphi, &c->in, &c->part, &c->comp, &c->exp};
+    if (c->copy) cudaStreamSynchronize(c->copy);
     for (DevBuf *b : bufs) dfree(c, *b);
+    dfree(c, c->snap);
+    if (c->snap_ev) cudaEventDestroy(c->snap_ev);
+    if (c->copy_ev) cudaEventDestroy(c->copy_ev);
+    if (c->copy) cudaStreamDestroy(c->copy);
+    if (c->flag_host) cudaFreeHost(c->flag_host);
     if (c->staged) cudaEventDestroy(c->staged);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
@@ -938,6 +952,55 @@ hbt_status hbt_read_hist(hbt_ctx *c, double *num_count, double *q_out_sum, doubl
         CU(cudaMemcpyAsync(dst[f], buf, nb * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     }
     CU(cudaStreamSynchronize(c->stream));
+    c->st.launches += used;
+    return HBT_OK;
+}
+
+hbt_status hbt_read_hist_wait(hbt_ctx *c) {
+    if (!c) return HBT_ERR_INVALID;
+    if (!c->read_pending) return HBT_OK;
+    CU(cudaSetDevice(c->device));
+    CU(cudaEventSynchronize(c->copy_ev));
+    c->read_pending = false;
+    if (*c->flag_host != 0) return fail(c, HBT_ERR_DEVICE, "a kernel raised its error flag");
+    return HBT_OK;
+}
+
+hbt_status hbt_read_hist_async(hbt_ctx *c, double *num_count, double *q_out_sum,
+                               double *q_side_sum, double *q_long_sum, double *num, double *den) {
+    if (!c) return HBT_ERR_INVALID;
+    CU(cudaSetDevice(c->device));
+    TRY(hbt_read_hist_wait(c));  // one read in flight: the snapshot is reused
+    TRY(drain_deferrals(c));
+    if (!c->copy) {
+        CU(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&c->snap_ev, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&c->copy_ev, cudaEventDisableTiming));
+        CU(cudaMallocHost(&c->flag_host, sizeof(u64)));
+    }
+    const size_t nb = (size_t)hbt_n_bins(c);
+    double *dst[6] = {q_out_sum, q_side_sum, q_long_sum, num, num_count, den};
+    TRY(dalloc(c, c->snap, 6 * nb * sizeof(double) + sizeof(u64)));
+    double *snap = ptr<double>(c->snap);
+    u64 *flag = reinterpret_cast<u64 *>(snap + 6 * nb);
+    // the snapshot is stream-ordered after everything binned so far
+    int used = 0;
+    for (int f = 0; f < 6; f++) {
+        if (!dst[f]) continue;
+        CU(hbt::launch_export(c->d, f, snap + (size_t)f * nb, (long long)nb, c->stream));
+        used++;
+    }
+    CU(cudaMemcpyAsync(flag, ptr<u64>(c->stats) + hbt::STAT_ERROR, sizeof(u64),
+                       cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaEventRecord(c->snap_ev, c->stream));
+    CU(cudaStreamWaitEvent(c->copy, c->snap_ev, 0));
+    for (int f = 0; f < 6; f++)
+        if (dst[f])
+            CU(cudaMemcpyAsync(dst[f], snap + (size_t)f * nb, nb * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->copy));
+    CU(cudaMemcpyAsync(c->flag_host, flag, sizeof(u64), cudaMemcpyDeviceToHost, c->copy));
+    CU(cudaEventRecord(c->copy_ev, c->copy));
+    c->read_pending = true;
     c->st.launches += used;
     return HBT_OK;
 }

@@ -92,6 +92,8 @@ _SIGNATURES = {
     "hbt_sync": (_I32, [ctypes.c_void_p, _U64]),
     "hbt_n_bins": (_I64, [ctypes.c_void_p]),
     "hbt_read_hist": (_I32, [ctypes.c_void_p] + [_PD] * 6),
+    "hbt_read_hist_async": (_I32, [ctypes.c_void_p] + [_PD] * 6),
+    "hbt_read_hist_wait": (_I32, [ctypes.c_void_p]),
     "hbt_read_qinv": (_I32, [ctypes.c_void_p] + [_PD] * 4),
     "hbt_read_counters": (_I32, [ctypes.c_void_p] + [_PU64] * 4),
     "hbt_get_stats": (_I32, [ctypes.c_void_p, ctypes.POINTER(HbtStats)]),

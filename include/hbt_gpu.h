@@ -216,6 +216,19 @@ hbt_status hbt_read_hist(hbt_ctx *ctx, double *num_count, double *q_out_sum,
                          double *q_side_sum, double *q_long_sum, double *num,
                          double *den);
 
+/* hbt_read_hist without waiting for the copies: the arrays are snapshotted
+ * on the device (stream-ordered after everything binned so far) and copied
+ * to the caller's arrays on a copy stream, so the next bin calls run while
+ * the copies are in flight.  The arrays hold the snapshot once
+ * hbt_read_hist_wait returns; with pinned host arrays the copies overlap the
+ * binning.  One read is in flight at a time: a second call first waits for
+ * the previous one.  The device error flag travels with the snapshot and
+ * is reported by hbt_read_hist_wait (HBT_ERR_DEVICE). */
+hbt_status hbt_read_hist_async(hbt_ctx *ctx, double *num_count, double *q_out_sum,
+                               double *q_side_sum, double *q_long_sum, double *num,
+                               double *den);
+hbt_status hbt_read_hist_wait(hbt_ctx *ctx);
+
 /* q_inv histograms, n_KT * qnpts doubles each (q_inv_mean,
  * correl_1d_inv_num, correl_1d_inv_num_count, correl_1d_inv_denorm). */
 hbt_status hbt_read_qinv(hbt_ctx *ctx, double *qinv_sum, double *num,

@@ -129,3 +129,33 @@ def test_batch_device_resident():
     ha, hb = a.hist(), b.hist()
     for k in ("count", "den"):
         assert np.array_equal(ha[k], hb[k])
+
+
+def test_async_readback_is_a_snapshot():
+    """hbt_read_hist_async: the arrays equal hbt_read_hist at the time of the
+    call, although more pairs are binned while the copies are in flight; a
+    second call waits for the first; K_phi slots (deferred edges drained)."""
+    from hadronic_afterburner_toolkit_gb300 import engine as E
+    p = dict(BASE, azimuthal_flag=1)
+    jobs = _uneven_jobs(seed=17)
+    eng = E.Engine(**p)
+    eng.set_psi_ref(0.3)
+    eng.bin_batch(jobs[:len(jobs) // 2])
+    n = int(eng.L.hbt_n_bins(eng.handle))
+    sync = [np.zeros(n) for _ in range(6)]
+    eng._check(eng.L.hbt_read_hist(eng.handle, *[a.ctypes.data_as(E._PD) for a in sync]))
+    snap = [np.full(n, -1.0) for _ in range(6)]
+    eng._check(eng.L.hbt_read_hist_async(eng.handle, *[a.ctypes.data_as(E._PD) for a in snap]))
+    eng.bin_batch(jobs[len(jobs) // 2:])  # binning goes on while the copy is in flight
+    eng._check(eng.L.hbt_read_hist_wait(eng.handle))
+    for a, b in zip(snap, sync):
+        np.testing.assert_array_equal(a, b)
+    # the second snapshot holds all jobs and equals the oracle's binning
+    full = [np.zeros(n) for _ in range(6)]
+    eng._check(eng.L.hbt_read_hist_async(eng.handle, *[a.ctypes.data_as(E._PD) for a in full]))
+    eng._check(eng.L.hbt_read_hist_wait(eng.handle))
+    eng._check(eng.L.hbt_read_hist_wait(eng.handle))  # nothing pending: returns at once
+    h = eng.hist()
+    for a, k in zip(full, ("count", "q_out", "q_side", "q_long", "num", "den")):
+        np.testing.assert_array_equal(a, h[k])
+    assert full[0].sum() > sync[0].sum()
