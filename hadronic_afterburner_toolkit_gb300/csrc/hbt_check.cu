@@ -1,0 +1,37 @@
+// Device evaluation of the table-driven FP64 functions (include/hbt_check.h).
+#include "../../include/hbt_check.h"
+#include "hbt_math.cuh"
+
+namespace {
+
+__global__ void k_check_math(int which, long long n, const double *x, double *out) {
+    __shared__ double2 cs[COS_TABLE];
+    __shared__ double et[EXP_TABLE];
+    fill_cos_table(cs);
+    fill_exp_table(et);
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = which == HBT_CHECK_COS ? table_cos(cs, x[i]) : table_exp(et, x[i]);
+}
+
+}  // namespace
+
+extern "C" hbt_status hbt_check_math(int device, int32_t which, int64_t n, const double *x,
+                                     double *out) {
+    if (n < 0 || (n > 0 && (!x || !out)) || (which != HBT_CHECK_COS && which != HBT_CHECK_EXP))
+        return HBT_ERR_INVALID;
+    if (n == 0) return HBT_OK;
+    if (cudaSetDevice(device) != cudaSuccess) return HBT_ERR_CUDA;
+    double *d = nullptr;
+    if (cudaMalloc(&d, 2 * n * sizeof(double)) != cudaSuccess) return HBT_ERR_NOMEM;
+    cudaError_t e = cudaMemcpy(d, x, n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const long long blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+        k_check_math<<<(unsigned)blocks, 256>>>(which, n, d, d + n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? HBT_OK : HBT_ERR_CUDA;
+}

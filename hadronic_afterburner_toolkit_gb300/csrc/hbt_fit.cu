@@ -17,8 +17,9 @@
 //    system by Cholesky and decides the next trial point.  At the minimum
 //    the errors are sqrt(diag((J^T J)^-1)) (curve_fit, absolute_sigma).
 //
-// The rows a fit touches are read once per pass: 56 bytes per row against
-// about 60 FP64 operations, so the fits are bound by the FP64 pipe.
+// The rows a fit touches are read once per pass: 76 bytes per row against
+// about 35 FP64 operations (exp table-driven, hbt_math.cuh), so the fits
+// are bound by the FP64 pipe.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -28,6 +29,7 @@
 #include <vector>
 
 #include "../../include/hbt_fit.h"
+#include "hbt_math.cuh"
 
 namespace {
 
@@ -158,7 +160,8 @@ __global__ void __launch_bounds__(kSelThreads)
 // at most a few hundred rows, 1e-5 relative); the pass at the minimum that
 // gives the covariance sums it in FP64 (kExact = true).
 template <bool kExact>
-__device__ void fit_pass(const Rows &rw, long long r0, int n, const double *p, double *red) {
+__device__ void fit_pass(const Rows &rw, long long r0, int n, const double *p, const double *etab,
+                         double *red) {
     using AccT = typename std::conditional<kExact, double, float>::type;
     __shared__ double part[kFitThreads / 32][kSums];
     double a2[5], cdf[7];
@@ -185,7 +188,7 @@ __device__ void fit_pass(const Rows &rw, long long r0, int n, const double *p, d
         double E = 0.0;
 #pragma unroll
         for (int k = 0; k < 5; k++) E += a2[k] * q[k];
-        const double e = exp(-E);
+        const double e = table_exp(etab, -E);
         const double f = lam * e;
         const double r = w * (f - dp[kColC * rw.ld]);
         const double u = w * f;
@@ -425,6 +428,7 @@ __global__ void __launch_bounds__(kFitThreads, HBT_FIT_MIN_BLOCKS)
              hbt_fit_result *res, unsigned long long *n_passes) {
     __shared__ double red[kSums];
     __shared__ LmState st;
+    __shared__ double etab[EXP_TABLE];
     int t, k;
     fit_of_block(fc, t, k);
     const long long r0 = tab_off[t];
@@ -444,10 +448,11 @@ __global__ void __launch_bounds__(kFitThreads, HBT_FIT_MIN_BLOCKS)
         return;
     }
     if (threadIdx.x < 6) st.x[threadIdx.x] = fc.p0[threadIdx.x];
+    fill_exp_table(etab);
     __syncthreads();
     // one pass per trial point: the first at the start point
     for (bool first = true;; first = false) {
-        fit_pass<false>(rw, r0, n, first ? st.x : st.trial, red);
+        fit_pass<false>(rw, r0, n, first ? st.x : st.trial, etab, red);
         if (threadIdx.x == 0) {
             if (first)
                 lm_init(st, red);
@@ -472,14 +477,16 @@ __global__ void __launch_bounds__(kFitThreads)
               hbt_fit_result *res) {
     __shared__ double red[kSums];
     __shared__ double x[6];
+    __shared__ double etab[EXP_TABLE];
     int t, k;
     fit_of_block(fc, t, k);
     const int n = rows_of_fit(fc, cls, t, k);
     if (n < 6) return;
     hbt_fit_result *out = res + (long long)(first_table + t) * fc.n_cuts + k;
     if (threadIdx.x < 6) x[threadIdx.x] = out->p[threadIdx.x];
+    fill_exp_table(etab);
     __syncthreads();
-    fit_pass<true>(rw, tab_off[t], n, x, red);
+    fit_pass<true>(rw, tab_off[t], n, x, etab, red);
     if (threadIdx.x == 0) cov_finish(red, out);
 }
 

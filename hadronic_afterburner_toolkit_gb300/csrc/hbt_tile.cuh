@@ -26,7 +26,7 @@
 //     Same-event pairs add q_out, q_side, q_long and cos(q.dx / hbarC):
 //       FP64 form  - FP64 values from algebraically identical expressions
 //                    (q_out = (q_x S_x + q_y S_y) / |S|, ...) and a
-//                    table-driven FP64 cos (table_cos below);
+//                    table-driven FP64 cos (table_cos, hbt_math.cuh);
 //       FP32W form - each FP64 column split once per tile into hi + lo
 //                    FP32 parts; differences and the phase in double-float
 //                    arithmetic on the FP32 pipe, q values in FP32, cos by
@@ -52,6 +52,7 @@
 #pragma once
 
 #include "hbt_chain.cuh"
+#include "hbt_math.cuh"
 
 namespace hbt {
 namespace tile {
@@ -206,39 +207,6 @@ __device__ __forceinline__ int kphi_screen(const Screen &S, const Q &q) {
     const float fr = r - k;
     if (!(fr > er) || !(fr < 1.0f - er) || k < 0.0f || k >= (float)S.n_Kphi) return -2;
     return (int)k;
-}
-
-// Table of cos and sin of 2 pi k / 512, k = 0..511, for table_cos, filled
-// by each CTA of the FP64-form same-event kernels.
-constexpr int COS_TABLE = 512;
-__device__ __forceinline__ void fill_cos_table(double2 *cs) {
-    for (int k = threadIdx.x; k < COS_TABLE; k += blockDim.x) {
-        double sn, cn;
-        sincospi(k / 256.0, &sn, &cn);
-        cs[k] = make_double2(cn, sn);
-    }
-}
-
-// cos(x), table-driven (the argument reduction of P. T. P. Tang's
-// table-driven elementary functions): x = k (2 pi / 512) + d with
-// k = rint(x 512 / 2 pi) and d from a two-part split of 2 pi / 512 (the
-// leading part has 26 significant bits, so k times it is exact for
-// |k| < 2^27), |d| <= pi / 512 = 6.2e-3; then
-//   cos x = cos(2 pi k / 512) cos d - sin(2 pi k / 512) sin d
-// with cos d to d^4 and sin d to d^3 from their Taylor series (truncation
-// below 1e-16 and 8e-14).  |x| >= 2^20 (never on this path: |q.dx| / hbarC
-// is a few hundred at most) falls back to cos().
-__device__ __forceinline__ double table_cos(const double2 *cs, double x) {
-    if (!(fabs(x) < 1048576.0)) return cos(x);
-    const double kd = rint(x * 81.48733086305042);          // 512 / (2 pi)
-    double d = __fma_rn(-kd, 0.01227184641174972, x);       // leading part
-    d = __fma_rn(-kd, -1.086645907356806e-10, d);           // 2 pi / 512 - leading part
-    const int k = __double2int_rn(kd) & (COS_TABLE - 1);
-    const double d2 = d * d;
-    const double cd = __fma_rn(d2, __fma_rn(d2, 1.0 / 24.0, -0.5), 1.0);
-    const double sd = d * __fma_rn(d2, -1.0 / 6.0, 1.0);
-    const double2 e = cs[k];
-    return __fma_rn(e.x, cd, -(e.y * sd));
 }
 
 // FP64 summed values of an accepted same-event pair (algebraically the

@@ -13,6 +13,7 @@ HEADER = os.path.join(INCLUDE, "hbt_gpu.h")
 SERVER_HEADER = os.path.join(INCLUDE, "hbt_server.h")
 BF_HEADER = os.path.join(INCLUDE, "hbt_bf.h")
 FIT_HEADER = os.path.join(INCLUDE, "hbt_fit.h")
+CHECK_HEADER = os.path.join(INCLUDE, "hbt_check.h")
 
 
 def _declared_functions(path):
@@ -37,7 +38,8 @@ def test_header_declares_the_engine_api():
 
 def test_library_exports_every_declared_symbol(lib):
     for name in (_declared_functions(HEADER) + _declared_functions(SERVER_HEADER) +
-                 _declared_functions(BF_HEADER) + _declared_functions(FIT_HEADER)):
+                 _declared_functions(BF_HEADER) + _declared_functions(FIT_HEADER) +
+                 _declared_functions(CHECK_HEADER)):
         assert hasattr(lib, name), name
 
 

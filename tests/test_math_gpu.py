@@ -1,0 +1,64 @@
+"""The engine's table-driven FP64 functions (csrc/hbt_math.cuh), run on the
+device through hbt_check_math, against the host's libm (numpy): cos, used
+for the same-event numerators, and exp, used by the radii fits.
+
+Bounds: cos within 3e-16 absolute over |x| < 1000 (the phases of the pair
+kernels are a few hundred at most) and 1e-15 absolute near 2^20; exp within
+4 ulp relative over |x| < 700 and within 1e-15 relative of libm outside
+(there it calls the device's exp())."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+_PD = ctypes.POINTER(ctypes.c_double)
+
+
+def _dev(which, x):
+    from hadronic_afterburner_toolkit_gb300 import engine
+    L = engine.load()
+    L.hbt_check_math.restype = ctypes.c_int32
+    L.hbt_check_math.argtypes = [ctypes.c_int, ctypes.c_int32, ctypes.c_int64, _PD, _PD]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    assert L.hbt_check_math(0, which, x.size, x.ctypes.data_as(_PD), out.ctypes.data_as(_PD)) == 0
+    return out
+
+
+def test_table_cos_against_libm():
+    rng = np.random.default_rng(1)
+    step = 2 * np.pi / 512
+    k = np.arange(-4000, 4000)
+    x = np.concatenate([rng.uniform(-1000, 1000, 200000), rng.uniform(-1, 1, 50000),
+                        k * step, k * step + step / 2, np.nextafter(k * step + step / 2, 0),
+                        [0.0, -0.0, 1e-300, 5e-324, np.pi, -np.pi, 2 * np.pi]])
+    got = _dev(0, x)
+    assert np.max(np.abs(got - np.cos(x))) < 3e-16
+    big = rng.uniform(-1048575, 1048575, 20000)
+    assert np.max(np.abs(_dev(0, big) - np.cos(big))) < 1e-15
+    tail = np.array([1048576.0, -3e6, 1e10])
+    np.testing.assert_array_equal(np.isnan(_dev(0, [np.nan, np.inf])), [True, True])
+    assert np.max(np.abs(_dev(0, tail) - np.cos(tail))) < 1e-15
+
+
+def test_table_exp_against_libm():
+    rng = np.random.default_rng(2)
+    ln2_64 = np.log(2) / 64
+    k = np.arange(-64000, 64000, 7)
+    x = np.concatenate([rng.uniform(-700, 700, 200000), rng.uniform(-1, 1, 50000),
+                        -rng.exponential(30, 50000), k * ln2_64, k * ln2_64 + ln2_64 / 2,
+                        [0.0, -0.0, 1e-300, -1e-300, 699.99, -699.99]])
+    got = _dev(1, x)
+    ref = np.exp(x)
+    ulp = np.spacing(ref)
+    assert np.max(np.abs(got - ref) / ulp) <= 4
+    tail = np.array([700.0, -700.0, 709.7, -708.0, -800.0, 800.0, -np.inf, np.inf])
+    with np.errstate(over="ignore"):
+        want = np.exp(tail)
+    got = _dev(1, tail)
+    fin = np.isfinite(want)
+    np.testing.assert_allclose(got[fin], want[fin], rtol=1e-15, atol=1e-320)
+    np.testing.assert_array_equal(got[~fin], want[~fin])
+    assert np.isnan(_dev(1, [np.nan])[0])
