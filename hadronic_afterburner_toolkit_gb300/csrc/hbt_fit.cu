@@ -36,7 +36,7 @@ namespace {
 constexpr double kHbarC = 0.19733;  // fit_HBT_radii.py:10
 constexpr double kEps = 1e-15;      // fit_HBT_radii.py:11
 constexpr int kMaxCuts = 16;
-constexpr int kSelThreads = 256;
+constexpr int kSelThreads = 512;
 constexpr int kFitThreads = 128;
 constexpr int kSums = 28;  // chi2, J^T r (6), J^T J (21, packed lower)
 
@@ -94,59 +94,94 @@ __device__ __forceinline__ int cut_class(const FitConst &fc, double r) {
     return -1;
 }
 
+// Two sweeps over a table's rows: the first counts the rows of each cut
+// class (the smallest cut a row passes, or none), the second writes every
+// kept row at its class's running position: within a class, rows keep
+// their table order (the same arrays and sums on every run).
 __global__ void __launch_bounds__(kSelThreads)
     k_fit_select(FitConst fc, const long long *tab_off, const TabDesc *desc, const double *in,
                  Rows out, int *cls) {
-    __shared__ int warp_tot[kSelThreads / 32];
-    __shared__ int base;
+    __shared__ int cnt[kSelThreads / 32][kMaxCuts];
+    __shared__ int base[kMaxCuts];
     const int t = blockIdx.x;
     const long long r0 = tab_off[t], n = tab_off[t + 1] - r0;
     const TabDesc d = desc[t];
     const double *qo_in = in + d.base + d.col[0], *qs_in = in + d.base + d.col[1],
                  *ql_in = in + d.base + d.col[2], *c_in = in + d.base + d.col[3],
                  *e_in = in + d.base + d.col[4];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) base = 0;
-    __syncthreads();
-    for (int c = 0; c < fc.n_cuts; c++) {
-        const int before = base;
-        for (long long i0 = 0; i0 < n; i0 += kSelThreads) {
-            const long long i = i0 + threadIdx.x;
-            double qo = 0, qs = 0, ql = 0;
-            bool take = false;
-            if (i < n) {
-                qo = nan_to_num(qo_in[i * d.stride]);
-                qs = nan_to_num(qs_in[i * d.stride]);
-                ql = nan_to_num(ql_in[i * d.stride]);
-                take = cut_class(fc, qabs(qo, qs, ql)) == c;
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, take);
-            if (lane == 0) warp_tot[warp] = __popc(m);
-            __syncthreads();
-            int off = base, tot = 0;
-            for (int w = 0; w < kSelThreads / 32; w++) {
-                if (w < warp) off += warp_tot[w];
-                tot += warp_tot[w];
-            }
-            if (take) {
-                const long long o = r0 + off + __popc(m & ((1u << lane) - 1u));
-                const double cc = nan_to_num(c_in[i * d.stride]);
-                const double sigma = nan_to_num(e_in[i * d.stride]) + kEps;
-                const double q5[5] = {qo * qo, qs * qs, ql * ql, 2.0 * qo * qs, 2.0 * qo * ql};
-                for (int k = 0; k < 5; k++) {
-                    out.d[k * out.ld + o] = q5[k];
-                    out.f[k * out.ld + o] = (float)q5[k];
-                }
-                out.d[kColC * out.ld + o] = cc;
-                out.d[kColW * out.ld + o] = 1.0 / sigma;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) base += tot;
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) cls[t * (fc.n_cuts + 1) + c] = base - before;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nc = fc.n_cuts;
+    const unsigned below = (1u << lane) - 1u;
+    // sweep 1: rows per class (per-thread counters, then the block's sums)
+    int mine[kMaxCuts];
+#pragma unroll
+    for (int c = 0; c < kMaxCuts; c++) mine[c] = 0;
+    for (long long i = threadIdx.x; i < n; i += kSelThreads) {
+        const int c = cut_class(fc, qabs(nan_to_num(qo_in[i * d.stride]),
+                                         nan_to_num(qs_in[i * d.stride]),
+                                         nan_to_num(ql_in[i * d.stride])));
+#pragma unroll
+        for (int k = 0; k < kMaxCuts; k++) mine[k] += (c == k);
     }
-    if (threadIdx.x == 0) cls[t * (fc.n_cuts + 1) + fc.n_cuts] = base;
+#pragma unroll
+    for (int k = 0; k < kMaxCuts; k++) {
+        if (k >= nc) break;
+        int v = mine[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) cnt[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int k = 0; k < nc; k++) {
+            int tot = 0;
+            for (int w = 0; w < kSelThreads / 32; w++) tot += cnt[w][k];
+            base[k] = run;
+            cls[t * (nc + 1) + k] = tot;
+            run += tot;
+        }
+        cls[t * (nc + 1) + nc] = run;
+    }
+    __syncthreads();
+    // sweep 2: chunk by chunk, rank each row among its class in row order
+    for (long long i0 = 0; i0 < n; i0 += kSelThreads) {
+        const long long i = i0 + threadIdx.x;
+        double qo = 0, qs = 0, ql = 0;
+        int c = -1;
+        if (i < n) {
+            qo = nan_to_num(qo_in[i * d.stride]);
+            qs = nan_to_num(qs_in[i * d.stride]);
+            ql = nan_to_num(ql_in[i * d.stride]);
+            c = cut_class(fc, qabs(qo, qs, ql));
+        }
+        // this warp's rows per class: zeroed, then each class group's first
+        // lane writes the group's size
+        for (int k = lane; k < nc; k += 32) cnt[warp][k] = 0;
+        __syncwarp();
+        const unsigned same = __match_any_sync(0xffffffffu, c);
+        if (c >= 0 && lane == __ffs(same) - 1) cnt[warp][c] = __popc(same);
+        __syncthreads();
+        if (c >= 0) {
+            int off = base[c] + __popc(same & below);
+            for (int w = 0; w < warp; w++) off += cnt[w][c];
+            const long long o = r0 + off;
+            const double cc = nan_to_num(c_in[i * d.stride]);
+            const double sigma = nan_to_num(e_in[i * d.stride]) + kEps;
+            const double q5[5] = {qo * qo, qs * qs, ql * ql, 2.0 * qo * qs, 2.0 * qo * ql};
+            for (int k = 0; k < 5; k++) {
+                out.d[k * out.ld + o] = q5[k];
+                out.f[k * out.ld + o] = (float)q5[k];
+            }
+            out.d[kColC * out.ld + o] = cc;
+            out.d[kColW * out.ld + o] = 1.0 / sigma;
+        }
+        __syncthreads();
+        if (threadIdx.x < nc) {
+            int tot = 0;
+            for (int w = 0; w < kSelThreads / 32; w++) tot += cnt[w][threadIdx.x];
+            base[threadIdx.x] += tot;
+        }
+        __syncthreads();
+    }
 }
 
 // One pass at parameters p: chi^2, J^T r, J^T J of the rows [0, n) of the
