@@ -2,24 +2,27 @@
 //
 // The reference fits each correlation table with scipy's curve_fit, one
 // table and one q_cut at a time (ebe_scripts/fit_HBT_radii.py:60-92).  Here
-// every (table, q_cut) of a batch is one CTA of one launch, and two batches
-// are in flight on two streams (one copying while the other fits):
+// all fits of a batch of tables advance together:
 //
 //  * k_fit_select (one CTA per table) applies the script's preprocessing
 //    (numpy nan_to_num, C_err + 1e-15, weight 1 / sigma) and keeps the rows
 //    with q_cut_min < |q| < the largest cut, ordered by the smallest cut
 //    they pass, so the rows of cut k are a prefix of the table's kept rows.
-//    Per row it stores the five q products of the exponent, C and the
-//    weight (7 doubles).
-//  * k_fit_lm (one CTA per fit) runs Levenberg-Marquardt in FP64: each pass
-//    over the rows accumulates chi^2, J^T r and J^T J (28 sums, analytic
-//    Jacobian) with a block reduction; one thread solves the damped 6 x 6
-//    system by Cholesky and decides the next trial point.  At the minimum
-//    the errors are sqrt(diag((J^T J)^-1)) (curve_fit, absolute_sigma).
+//    Per row it stores the five q products of the exponent (FP64 and FP32),
+//    C and the weight.
+//  * Each fit's rows are cut into work items of up to 8192 rows.  A pass
+//    (k_fit_pass, one CTA per item) sums chi^2, J^T r and J^T J of every
+//    active fit's items at its trial point; a step (k_fit_step, one thread
+//    per fit) adds its items' sums and makes one Levenberg-Marquardt step:
+//    damped 6 x 6 system by Cholesky, accept or reject, next trial point.
+//    Passes and steps alternate until no fit has a trial point; work is
+//    balanced over the GPU whatever the fits' sizes, and finished fits cost
+//    nothing in later passes.
+//  * A last pass sums J^T J in FP64 at each minimum; k_fit_finish inverts
+//    it for the errors sqrt(diag((J^T J)^-1)) (curve_fit, absolute_sigma).
 //
-// The rows a fit touches are read once per pass: 76 bytes per row against
-// about 35 FP64 operations (exp table-driven, hbt_math.cuh), so the fits
-// are bound by the FP64 pipe.
+// A pass reads 76 bytes per row against about 35 FP64 operations (exp
+// table-driven, hbt_math.cuh): the fits are bound by the FP64 pipe.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -40,7 +43,7 @@ constexpr int kSelThreads = 512;
 constexpr int kFitThreads = 128;
 constexpr int kSums = 28;  // chi2, J^T r (6), J^T J (21, packed lower)
 
-// Resident fitting CTAs per SM the iterations' kernel is compiled for.
+// Resident pass CTAs per SM the pass kernel is compiled for.
 #ifndef HBT_FIT_MIN_BLOCKS
 #define HBT_FIT_MIN_BLOCKS 4
 #endif
@@ -312,12 +315,13 @@ __device__ void chol_solve6(const double *L, const double *b, double *x) {
     }
 }
 
-// Levenberg-Marquardt state of one fit, in shared memory, advanced by one
-// thread between the block's passes over the rows.
+// Levenberg-Marquardt state of one fit, in device memory, advanced by one
+// thread (k_fit_step) between the passes over the fit's rows.
 struct LmState {
     double x[6], trial[6];
     double S, g[6], A[21], D[6], mu, nu;
     int iter, status, stop, go;
+    int use_x;  // the next pass evaluates x (the start point), not trial
     long long passes;
 };
 
@@ -410,25 +414,110 @@ __device__ __noinline__ void lm_update(LmState &st, const double *red) {
     }
 }
 
-// Results of the iterations: the point and chi^2 (the errors follow in
-// k_fit_cov).
-__device__ __noinline__ void lm_finish(const LmState &st, double q_cut, int n,
-                                       hbt_fit_result *out) {
-    out->q_cut = q_cut;
-    for (int j = 0; j < 6; j++) {
-        out->p[j] = st.x[j];
-        out->err[j] = NAN;
-    }
-    out->chi2 = st.S;
-    out->n_points = n;
-    out->iterations = st.iter;
-    out->reserved = 0;
-    out->status = st.status;
+// A fit of a batch: table t, cut k, its n kept rows and its work items
+// [item0, item1).
+struct FitInfo {
+    int t, k, n, item0, item1;
+};
+
+// A work item: up to kItemRows consecutive kept rows of one fit.
+struct FitItem {
+    int fit, rows;
+    long long row0;
+};
+constexpr int kItemRows = 8192;
+
+__global__ void k_fit_init(FitConst fc, const FitInfo *fits, int n_fits, LmState *st) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_fits) return;
+    LmState &s = st[f];
+    for (int j = 0; j < 6; j++) s.x[j] = s.trial[j] = fc.p0[j];
+    s.use_x = 1;
+    s.iter = 0;
+    s.passes = 0;
+    s.stop = 0;
+    s.S = NAN;
+    const bool enough = fits[f].n >= 6;
+    s.go = enough;
+    s.status = enough ? HBT_FIT_CONVERGED : HBT_FIT_TOO_FEW;
 }
 
-// The errors: sqrt(diag((J^T J)^-1)) with J^T J summed in FP64 at the
-// minimum (inf and the singular status when it is not positive definite).
-__device__ __noinline__ void cov_finish(const double *red, hbt_fit_result *out) {
+// One pass over every active fit's rows: each item's chi^2, J^T r and
+// J^T J (at the fit's trial point, its start point on the first pass, or
+// with kExact at its minimum for the covariance) into partial[item].
+// Items of finished fits return at once.
+template <bool kExact>
+__global__ void __launch_bounds__(kFitThreads, HBT_FIT_MIN_BLOCKS)
+    k_fit_pass(const FitItem *items, int n_items, Rows rw, const LmState *st, double *partial) {
+    __shared__ double etab[EXP_TABLE];
+    __shared__ double red[kSums];
+    __shared__ double p[6];
+    fill_exp_table(etab);
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const FitItem I = items[it];
+        const LmState &s = st[I.fit];
+        if (kExact ? s.status == HBT_FIT_TOO_FEW : !s.go) continue;  // uniform in the block
+        __syncthreads();  // the previous item's p and red are read
+        if (threadIdx.x < 6) p[threadIdx.x] = (kExact || s.use_x) ? s.x[threadIdx.x] : s.trial[threadIdx.x];
+        __syncthreads();
+        fit_pass<kExact>(rw, I.row0, I.rows, p, etab, red);
+        if (threadIdx.x < kSums) partial[(long long)it * kSums + threadIdx.x] = red[threadIdx.x];
+    }
+}
+
+// The fit's sums: its items' partials added in item order.
+__device__ __forceinline__ void fit_sums(const FitInfo &fi, const double *partial, double *red) {
+    for (int k = 0; k < kSums; k++) red[k] = 0.0;
+    for (int it = fi.item0; it < fi.item1; it++)
+        for (int k = 0; k < kSums; k++) red[k] += partial[(long long)it * kSums + k];
+}
+
+// One Levenberg-Marquardt step of every active fit (one thread per fit);
+// `active` is set while any fit has another trial point.
+__global__ void k_fit_step(FitConst fc, const FitInfo *fits, int n_fits, LmState *st,
+                           const double *partial, int *active) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_fits) return;
+    LmState &s = st[f];
+    if (!s.go) return;
+    double red[kSums];
+    fit_sums(fits[f], partial, red);
+    if (s.use_x) {
+        lm_init(s, red);
+        s.use_x = 0;
+    } else {
+        lm_update(s, red);
+    }
+    lm_propose(s, fc.max_iter);
+    if (s.go) atomicOr(active, 1);
+}
+
+// Results: the point, chi^2, the errors sqrt(diag((J^T J)^-1)) from the
+// exact pass at the minimum (inf and the singular status when J^T J is not
+// positive definite), rows, iterations, status.
+__global__ void k_fit_finish(FitConst fc, int first_table, const FitInfo *fits, int n_fits,
+                             const LmState *st, const double *partial, hbt_fit_result *res,
+                             unsigned long long *n_passes) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_fits) return;
+    const FitInfo fi = fits[f];
+    const LmState &s = st[f];
+    hbt_fit_result *out = res + (long long)(first_table + fi.t) * fc.n_cuts + fi.k;
+    out->q_cut = fc.cut_sorted[fc.rank[fi.k]];
+    out->n_points = fi.n;
+    out->iterations = s.iter;
+    out->reserved = 0;
+    if (s.status == HBT_FIT_TOO_FEW) {
+        for (int j = 0; j < 6; j++) out->p[j] = out->err[j] = NAN;
+        out->chi2 = NAN;
+        out->status = HBT_FIT_TOO_FEW;
+        return;
+    }
+    for (int j = 0; j < 6; j++) out->p[j] = s.x[j];
+    out->chi2 = s.S;
+    int status = s.status;
+    double red[kSums];
+    fit_sums(fi, partial, red);
     double L[21];
     for (int j = 0; j < 21; j++) L[j] = red[7 + j];
     if (cholesky6(L)) {
@@ -440,89 +529,10 @@ __device__ __noinline__ void cov_finish(const double *red, hbt_fit_result *out) 
         }
     } else {
         for (int j = 0; j < 6; j++) out->err[j] = INFINITY;
-        if (out->status == HBT_FIT_CONVERGED) out->status = HBT_FIT_SINGULAR;
+        if (status == HBT_FIT_CONVERGED) status = HBT_FIT_SINGULAR;
     }
-}
-
-// The fit of a block: the largest cuts first (they have the most rows), so
-// a launch's tail is made of the small fits.
-__device__ __forceinline__ void fit_of_block(const FitConst &fc, int &t, int &k) {
-    const int nt = gridDim.x / fc.n_cuts;
-    t = blockIdx.x % nt;
-    k = fc.by_rank[fc.n_cuts - 1 - blockIdx.x / nt];
-}
-
-__device__ __forceinline__ int rows_of_fit(const FitConst &fc, const int *cls, int t, int k) {
-    int n = 0;
-    for (int c = 0; c <= fc.rank[k]; c++) n += cls[t * (fc.n_cuts + 1) + c];
-    return n;
-}
-
-__global__ void __launch_bounds__(kFitThreads, HBT_FIT_MIN_BLOCKS)
-    k_fit_lm(FitConst fc, int first_table, const long long *tab_off, const int *cls, Rows rw,
-             hbt_fit_result *res, unsigned long long *n_passes) {
-    __shared__ double red[kSums];
-    __shared__ LmState st;
-    __shared__ double etab[EXP_TABLE];
-    int t, k;
-    fit_of_block(fc, t, k);
-    const long long r0 = tab_off[t];
-    const int n = rows_of_fit(fc, cls, t, k);
-    hbt_fit_result *out = res + (long long)(first_table + t) * fc.n_cuts + k;
-    const double q_cut = fc.cut_sorted[fc.rank[k]];
-    if (n < 6) {
-        if (threadIdx.x == 0) {
-            out->q_cut = q_cut;
-            for (int j = 0; j < 6; j++) out->p[j] = out->err[j] = NAN;
-            out->chi2 = NAN;
-            out->n_points = n;
-            out->iterations = 0;
-            out->status = HBT_FIT_TOO_FEW;
-            out->reserved = 0;
-        }
-        return;
-    }
-    if (threadIdx.x < 6) st.x[threadIdx.x] = fc.p0[threadIdx.x];
-    fill_exp_table(etab);
-    __syncthreads();
-    // one pass per trial point: the first at the start point
-    for (bool first = true;; first = false) {
-        fit_pass<false>(rw, r0, n, first ? st.x : st.trial, etab, red);
-        if (threadIdx.x == 0) {
-            if (first)
-                lm_init(st, red);
-            else
-                lm_update(st, red);
-            lm_propose(st, fc.max_iter);
-        }
-        __syncthreads();
-        if (!st.go) break;
-    }
-    if (threadIdx.x == 0) {
-        lm_finish(st, q_cut, n, out);
-        atomicAdd(n_passes, (unsigned long long)st.passes + 1);  // + k_fit_cov's pass
-    }
-}
-
-// One pass at each fit's minimum with J^T J in FP64, for the errors.  A
-// kernel of its own so that the iterations' kernel keeps the FP32 sums'
-// register budget.
-__global__ void __launch_bounds__(kFitThreads)
-    k_fit_cov(FitConst fc, int first_table, const long long *tab_off, const int *cls, Rows rw,
-              hbt_fit_result *res) {
-    __shared__ double red[kSums];
-    __shared__ double x[6];
-    __shared__ double etab[EXP_TABLE];
-    int t, k;
-    fit_of_block(fc, t, k);
-    const int n = rows_of_fit(fc, cls, t, k);
-    if (n < 6) return;
-    hbt_fit_result *out = res + (long long)(first_table + t) * fc.n_cuts + k;
-    if (threadIdx.x < 6) x[threadIdx.x] = out->p[threadIdx.x];
-    fill_exp_table(etab);
-    __syncthreads();
-    fit_pass<true>(rw, tab_off[t], n, x, etab, red);
-    if (threadIdx.x == 0) cov_finish(red, out);
+    out->status = status;
+    atomicAdd(n_passes, (unsigned long long)s.passes + 1);
 }
 
 struct Buf {
@@ -544,12 +554,13 @@ bool grow(Buf &b, size_t bytes) {
     return true;
 }
 
-// Per batch: at most 4 M table rows (7 doubles and 5 floats each once
-// kept) and 32 M doubles of input; two batches are in flight (one copying
-// while the other fits), which bounds the device memory of a call to
-// 1.1 GB.  A batch of 41^3-row tables holds 58 of them (290 fits).
-constexpr long long kBatchRows = 4LL << 20;
-constexpr long long kBatchIn = 32LL << 20;
+// Per batch: at most 32 M table rows (7 doubles and 5 floats each once
+// kept) and 256 M doubles of input, which bounds the device memory of a
+// call to about 4.5 GB; a batch of 41^3-row tables holds 464 of them.
+constexpr long long kBatchRows = 32LL << 20;
+constexpr long long kBatchIn = 256LL << 20;
+// Iterations launched between two reads of the any-fit-active flag.
+constexpr int kStepsPerCheck = 4;
 
 // The input doubles of a table and, for an interleaved one, where its
 // block starts: the five columns within one row-major block of n rows.
@@ -575,22 +586,13 @@ long long table_span(const hbt_fit_table &T, const double **lo_out) {
 
 }  // namespace
 
-// One of the two batches in flight: its device buffers, its stream (copies,
-// row selection, fits, errors in order) and the host arrays its copies read.
-struct FitSlot {
-    cudaStream_t stream = nullptr;
-    cudaEvent_t t0 = nullptr, t1 = nullptr, t2 = nullptr;
-    Buf in, rows, frows, tab_off, desc, cls;
-    std::vector<double> packed;
-    std::vector<long long> off;
-    std::vector<TabDesc> desc_h;
-    bool busy = false;
-};
-
 struct hbt_fit_ctx {
     int device = 0;
-    FitSlot slot[2];
-    Buf res, counter;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    Buf in, rows, frows, tab_off, desc, cls, fits, items, state, partial, res, counter, active;
+    int *active_host = nullptr;  // pinned
+    std::vector<double> packed;
     hbt_fit_stats stats{};
     std::string err;
 };
@@ -611,12 +613,12 @@ hbt_status hbt_fit_create(int device, hbt_fit_ctx **out) {
     *out = nullptr;
     hbt_fit_ctx *c = new hbt_fit_ctx();
     c->device = device;
-    bool ok = cudaSetDevice(device) == cudaSuccess && grow(c->counter, 8);
-    for (FitSlot &sl : c->slot)
-        ok = ok && cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
-             cudaEventCreate(&sl.t0) == cudaSuccess && cudaEventCreate(&sl.t1) == cudaSuccess &&
-             cudaEventCreate(&sl.t2) == cudaSuccess;
-    if (!ok) {
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
+        cudaEventCreate(&c->ev[2]) != cudaSuccess || !grow(c->counter, 8) ||
+        !grow(c->active, sizeof(int)) ||
+        cudaMallocHost(&c->active_host, sizeof(int)) != cudaSuccess) {
         hbt_fit_destroy(c);
         return HBT_ERR_CUDA;
     }
@@ -627,16 +629,14 @@ hbt_status hbt_fit_create(int device, hbt_fit_ctx **out) {
 void hbt_fit_destroy(hbt_fit_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
-    for (FitSlot &sl : c->slot) {
-        if (sl.stream) cudaStreamSynchronize(sl.stream);
-        for (Buf *b : {&sl.in, &sl.rows, &sl.frows, &sl.tab_off, &sl.desc, &sl.cls})
-            if (b->p) cudaFree(b->p);
-        for (cudaEvent_t e : {sl.t0, sl.t1, sl.t2})
-            if (e) cudaEventDestroy(e);
-        if (sl.stream) cudaStreamDestroy(sl.stream);
-    }
-    for (Buf *b : {&c->res, &c->counter})
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (Buf *b : {&c->in, &c->rows, &c->frows, &c->tab_off, &c->desc, &c->cls, &c->fits,
+                   &c->items, &c->state, &c->partial, &c->res, &c->counter, &c->active})
         if (b->p) cudaFree(b->p);
+    for (cudaEvent_t e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->active_host) cudaFreeHost(c->active_host);
+    if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
 
@@ -681,39 +681,25 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
     c->stats = hbt_fit_stats{};
     c->stats.fits = (int64_t)n_tables * opt->n_cuts;
     if (n_tables == 0) return HBT_OK;
-    if (!grow(c->res, (size_t)n_tables * opt->n_cuts * sizeof(hbt_fit_result)))
+    const int nc = opt->n_cuts;
+    if (!grow(c->res, (size_t)n_tables * nc * sizeof(hbt_fit_result)))
         return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
-    FitSlot *S = c->slot;
-    cudaError_t e = cudaMemsetAsync(c->counter.p, 0, 8, S[0].stream);
-    // slot 1 starts after the counter is cleared
-    if (e == cudaSuccess) e = cudaEventRecord(S[0].t2, S[0].stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(S[1].stream, S[0].t2, 0);
+    cudaStream_t st = c->stream;
+    cudaError_t e = cudaMemsetAsync(c->counter.p, 0, 8, st);
     float up_ms = 0.f, fit_ms = 0.f;
-    // a slot's previous batch must be done before its buffers and host
-    // arrays are reused; its times are collected then
-    auto retire = [&](FitSlot &sl) -> cudaError_t {
-        if (!sl.busy) return cudaSuccess;
-        const cudaError_t r = cudaEventSynchronize(sl.t2);
-        if (r != cudaSuccess) return r;
-        float a = 0.f, b = 0.f;
-        cudaEventElapsedTime(&a, sl.t0, sl.t1);
-        cudaEventElapsedTime(&b, sl.t1, sl.t2);
-        up_ms += a;
-        fit_ms += b;
-        sl.busy = false;
-        return cudaSuccess;
-    };
+    std::vector<long long> off;
+    std::vector<TabDesc> desc;
     std::vector<const double *> block;
     std::vector<long long> packed_at;
-    int batch = 0;
-    for (int t0 = 0; t0 < n_tables && e == cudaSuccess; batch++) {
-        FitSlot &sl = S[batch & 1];
-        if ((e = retire(sl)) != cudaSuccess) break;
+    std::vector<int> cls_h;
+    std::vector<FitInfo> fits;
+    std::vector<FitItem> items;
+    for (int t0 = 0; t0 < n_tables && e == cudaSuccess;) {
         // the batch: tables [t0, t1) within the row and input budgets
         int t1 = t0;
         long long rows = 0, in_total = 0, n_packed = 0;
-        sl.off.assign(1, 0);
-        sl.desc_h.clear();
+        off.assign(1, 0);
+        desc.clear();
         block.clear();
         while (t1 < n_tables) {
             const hbt_fit_table &T = tables[t1];
@@ -731,26 +717,23 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
                 for (int k = 0; k < 5; k++) d.col[k] = k * T.n_rows;
                 n_packed += span;
             }
-            sl.desc_h.push_back(d);
+            desc.push_back(d);
             block.push_back(lo);
             in_total += span;
             rows += T.n_rows;
-            sl.off.push_back(rows);
+            off.push_back(rows);
             t1++;
         }
         const int nt = t1 - t0;
-        bool ok = grow(sl.tab_off, (nt + 1) * sizeof(long long)) &&
-                  grow(sl.desc, nt * sizeof(TabDesc)) &&
-                  grow(sl.cls, (size_t)nt * (opt->n_cuts + 1) * sizeof(int)) &&
-                  grow(sl.in, in_total * sizeof(double));
-        ok = ok && grow(sl.rows, 7 * rows * sizeof(double)) &&
-             grow(sl.frows, 5 * rows * sizeof(float));
-        if (!ok) {
-            for (FitSlot &x : c->slot) cudaStreamSynchronize(x.stream);
-            return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
-        }
+        bool ok = grow(c->tab_off, (nt + 1) * sizeof(long long)) &&
+                  grow(c->desc, nt * sizeof(TabDesc)) &&
+                  grow(c->cls, (size_t)nt * (nc + 1) * sizeof(int)) &&
+                  grow(c->in, in_total * sizeof(double)) &&
+                  grow(c->rows, 7 * rows * sizeof(double)) &&
+                  grow(c->frows, 5 * rows * sizeof(float));
+        if (!ok) return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
         // tables that are not one interleaved block are packed on the host
-        sl.packed.resize((size_t)std::max<long long>(n_packed, 1));
+        c->packed.resize((size_t)std::max<long long>(n_packed, 1));
         long long pk = 0;
         packed_at.assign(nt, -1);
         for (int t = t0; t < t1; t++) {
@@ -759,62 +742,116 @@ hbt_status hbt_fit_radii(hbt_fit_ctx *c, int32_t n_tables, const hbt_fit_table *
             const double *col[5] = {T.q_out, T.q_side, T.q_long, T.C, T.C_err};
             packed_at[t - t0] = pk;
             for (int k = 0; k < 5; k++)
-                for (long long i = 0; i < T.n_rows; i++) sl.packed[pk++] = col[k][i * T.stride];
+                for (long long i = 0; i < T.n_rows; i++) c->packed[pk++] = col[k][i * T.stride];
         }
-        double *din = static_cast<double *>(sl.in.p);
-        e = cudaEventRecord(sl.t0, sl.stream);
+        double *din = static_cast<double *>(c->in.p);
+        Rows rw{static_cast<double *>(c->rows.p), static_cast<float *>(c->frows.p), rows};
+        const long long *d_off = static_cast<const long long *>(c->tab_off.p);
+        if ((e = cudaEventRecord(c->ev[0], st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(c->tab_off.p, off.data(), off.size() * sizeof(long long),
+                                 cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(c->desc.p, desc.data(), desc.size() * sizeof(TabDesc),
+                                 cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            break;
+        // all copies first (copies from pageable memory wait for the stream's
+        // earlier work, so a kernel between them would serialise them), then
+        // the row selection of every table
         for (int t = t0; t < t1 && e == cudaSuccess; t++) {
             const long long span =
-                (t + 1 < t1 ? sl.desc_h[t - t0 + 1].base : in_total) - sl.desc_h[t - t0].base;
+                (t + 1 < t1 ? desc[t - t0 + 1].base : in_total) - desc[t - t0].base;
             if (span == 0) continue;
-            const double *src = block[t - t0] ? block[t - t0] : sl.packed.data() + packed_at[t - t0];
-            e = cudaMemcpyAsync(din + sl.desc_h[t - t0].base, src, span * sizeof(double),
-                                cudaMemcpyHostToDevice, sl.stream);
+            const double *src = block[t - t0] ? block[t - t0] : c->packed.data() + packed_at[t - t0];
+            e = cudaMemcpyAsync(din + desc[t - t0].base, src, span * sizeof(double),
+                                cudaMemcpyHostToDevice, st);
         }
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(sl.tab_off.p, sl.off.data(), sl.off.size() * sizeof(long long),
-                                cudaMemcpyHostToDevice, sl.stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(sl.desc.p, sl.desc_h.data(), sl.desc_h.size() * sizeof(TabDesc),
-                                cudaMemcpyHostToDevice, sl.stream);
         if (e != cudaSuccess) break;
-        Rows rw{static_cast<double *>(sl.rows.p), static_cast<float *>(sl.frows.p), rows};
-        const long long *d_off = static_cast<const long long *>(sl.tab_off.p);
-        k_fit_select<<<nt, kSelThreads, 0, sl.stream>>>(
-            fc, d_off, static_cast<const TabDesc *>(sl.desc.p), din, rw,
-            static_cast<int *>(sl.cls.p));
+        k_fit_select<<<nt, kSelThreads, 0, st>>>(fc, d_off, static_cast<const TabDesc *>(c->desc.p),
+                                                din, rw, static_cast<int *>(c->cls.p));
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        if ((e = cudaEventRecord(sl.t1, sl.stream)) != cudaSuccess) break;
-        k_fit_lm<<<nt * opt->n_cuts, kFitThreads, 0, sl.stream>>>(
-            fc, t0, d_off, static_cast<const int *>(sl.cls.p), rw,
-            static_cast<hbt_fit_result *>(c->res.p), static_cast<unsigned long long *>(c->counter.p));
+        // the fits and their work items, from the selected row counts
+        cls_h.resize((size_t)nt * (nc + 1));
+        if ((e = cudaMemcpyAsync(cls_h.data(), c->cls.p, cls_h.size() * sizeof(int),
+                                 cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaEventRecord(c->ev[1], st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            break;
+        fits.clear();
+        items.clear();
+        for (int t = 0; t < nt; t++)
+            for (int k = 0; k < nc; k++) {
+                FitInfo fi{t, k, 0, (int)items.size(), 0};
+                for (int r = 0; r <= fc.rank[k]; r++) fi.n += cls_h[(size_t)t * (nc + 1) + r];
+                if (fi.n >= 6)
+                    for (int r = 0; r < fi.n; r += kItemRows)
+                        items.push_back(FitItem{(int)fits.size(), std::min(kItemRows, fi.n - r),
+                                                off[t] + r});
+                fi.item1 = (int)items.size();
+                fits.push_back(fi);
+            }
+        const int nf = (int)fits.size(), ni = (int)items.size();
+        ok = grow(c->fits, nf * sizeof(FitInfo)) && grow(c->items, std::max(ni, 1) * sizeof(FitItem)) &&
+             grow(c->state, nf * sizeof(LmState)) &&
+             grow(c->partial, (size_t)std::max(ni, 1) * kSums * sizeof(double));
+        if (!ok) return fit_fail(c, HBT_ERR_NOMEM, "device allocation failed");
+        if ((e = cudaMemcpyAsync(c->fits.p, fits.data(), nf * sizeof(FitInfo),
+                                 cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (ni > 0 && (e = cudaMemcpyAsync(c->items.p, items.data(), ni * sizeof(FitItem),
+                                            cudaMemcpyHostToDevice, st)) != cudaSuccess))
+            break;
+        const FitInfo *d_fits = static_cast<const FitInfo *>(c->fits.p);
+        const FitItem *d_items = static_cast<const FitItem *>(c->items.p);
+        LmState *d_state = static_cast<LmState *>(c->state.p);
+        double *d_part = static_cast<double *>(c->partial.p);
+        int *d_active = static_cast<int *>(c->active.p);
+        const unsigned fb = (unsigned)((nf + 127) / 128);
+        const unsigned pg = (unsigned)std::max(1, std::min(ni, 152 * HBT_FIT_MIN_BLOCKS * 8));
+        k_fit_init<<<fb, 128, 0, st>>>(fc, d_fits, nf, d_state);
+        e = cudaGetLastError();
+        // Levenberg-Marquardt: a pass over all active fits' rows, then one
+        // step of every active fit; the flag is read every few iterations
+        for (int done = 0; e == cudaSuccess && ni > 0 && done <= fc.max_iter + 1;
+             done += kStepsPerCheck) {
+            for (int r = 0; r < kStepsPerCheck && e == cudaSuccess; r++) {
+                if ((e = cudaMemsetAsync(d_active, 0, sizeof(int), st)) != cudaSuccess) break;
+                k_fit_pass<false><<<pg, kFitThreads, 0, st>>>(d_items, ni, rw, d_state, d_part);
+                k_fit_step<<<fb, 128, 0, st>>>(fc, d_fits, nf, d_state, d_part, d_active);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(c->active_host, d_active, sizeof(int), cudaMemcpyDeviceToHost,
+                                    st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess || *c->active_host == 0) break;
+        }
+        if (e != cudaSuccess) break;
+        // J^T J in FP64 at each minimum, then the results
+        if (ni > 0) k_fit_pass<true><<<pg, kFitThreads, 0, st>>>(d_items, ni, rw, d_state, d_part);
+        k_fit_finish<<<fb, 128, 0, st>>>(fc, t0, d_fits, nf, d_state, d_part,
+                                          static_cast<hbt_fit_result *>(c->res.p),
+                                          static_cast<unsigned long long *>(c->counter.p));
         if ((e = cudaGetLastError()) != cudaSuccess) break;
-        k_fit_cov<<<nt * opt->n_cuts, kFitThreads, 0, sl.stream>>>(
-            fc, t0, d_off, static_cast<const int *>(sl.cls.p), rw,
-            static_cast<hbt_fit_result *>(c->res.p));
-        if ((e = cudaGetLastError()) != cudaSuccess) break;
-        if ((e = cudaEventRecord(sl.t2, sl.stream)) != cudaSuccess) break;
-        sl.busy = true;
+        if ((e = cudaEventRecord(c->ev[2], st)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+        up_ms += a;
+        fit_ms += b;
         c->stats.rows += rows;
         t0 = t1;
     }
-    for (FitSlot &sl : c->slot) {
-        const cudaError_t r = retire(sl);
-        if (e == cudaSuccess) e = r;
-    }
     if (e != cudaSuccess) {
-        for (FitSlot &sl : c->slot) cudaStreamSynchronize(sl.stream);
+        cudaStreamSynchronize(st);
         return fit_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
     }
     unsigned long long passes = 0;
-    if ((e = cudaMemcpyAsync(out, c->res.p, (size_t)n_tables * opt->n_cuts * sizeof(hbt_fit_result),
-                             cudaMemcpyDeviceToHost, S[0].stream)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(&passes, c->counter.p, 8, cudaMemcpyDeviceToHost, S[0].stream)) !=
+    if ((e = cudaMemcpyAsync(out, c->res.p, (size_t)n_tables * nc * sizeof(hbt_fit_result),
+                             cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&passes, c->counter.p, 8, cudaMemcpyDeviceToHost, st)) !=
             cudaSuccess ||
-        (e = cudaStreamSynchronize(S[0].stream)) != cudaSuccess)
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return fit_fail(c, HBT_ERR_CUDA, cudaGetErrorString(e));
-    for (long long f = 0; f < (long long)n_tables * opt->n_cuts; f++)
-        c->stats.points += out[f].n_points;
+    for (long long f = 0; f < (long long)n_tables * nc; f++) c->stats.points += out[f].n_points;
     c->stats.passes = (int64_t)passes;
     c->stats.upload_ms = up_ms;
     c->stats.kernel_ms = fit_ms;

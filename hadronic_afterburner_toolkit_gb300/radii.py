@@ -59,6 +59,11 @@ class HbtFitResult(ctypes.Structure):
                 ("n_points", _I32), ("iterations", _I32), ("status", _I32), ("reserved", _I32)]
 
 
+RESULT_DTYPE = np.dtype([("q_cut", "<f8"), ("p", "<f8", (6,)), ("err", "<f8", (6,)),
+                         ("chi2", "<f8"), ("n_points", "<i4"), ("iterations", "<i4"),
+                         ("status", "<i4"), ("reserved", "<i4")])
+
+
 class HbtFitStats(ctypes.Structure):
     _fields_ = [("fits", _I64), ("rows", _I64), ("points", _I64), ("passes", _I64),
                 ("upload_ms", _D), ("kernel_ms", _D)]
@@ -147,16 +152,16 @@ class Fitter:
         if rc != 0:
             raise HbtError("hbt_fit_radii: %s: %s" % (engine.STATUS.get(rc, rc),
                                                       self.L.hbt_fit_last_error(self._h).decode()))
+        res = np.frombuffer(out, dtype=RESULT_DTYPE, count=len(tables) * nc).reshape(
+            len(tables), nc)
         rows = np.empty((len(tables), nc, 13))
+        rows[..., 0] = res["q_cut"]
+        rows[..., 1::2] = res["p"]
+        rows[..., 2::2] = res["err"]
         info = np.empty((len(tables), nc), dtype=[("status", "i4"), ("chi2", "f8"),
                                                    ("n_points", "i4"), ("iterations", "i4")])
-        for t in range(len(tables)):
-            for c in range(nc):
-                r = out[t * nc + c]
-                rows[t, c, 0] = r.q_cut
-                rows[t, c, 1::2] = list(r.p)
-                rows[t, c, 2::2] = list(r.err)
-                info[t, c] = (r.status, r.chi2, r.n_points, r.iterations)
+        for k in ("status", "chi2", "n_points", "iterations"):
+            info[k] = res[k]
         self.last = info
         return rows
 

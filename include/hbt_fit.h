@@ -15,9 +15,9 @@
  * nan_to_num).  Each fit is a Levenberg-Marquardt minimisation in FP64
  * from the given start point with the analytic Jacobian; the errors are
  * the square roots of the diagonal of (J^T J)^-1 at the minimum (scipy's
- * curve_fit with absolute_sigma=True).  The fits of a call run one CTA per
- * (table, q_cut), in batches of up to 32 M input doubles with two batches
- * in flight: one copying to the device while the other fits.
+ * curve_fit with absolute_sigma=True).  The fits of a batch of tables (up
+ * to 256 M input doubles) advance together, pass by pass, with every
+ * fit's rows cut into work items spread over the GPU.
  */
 #ifndef HBT_FIT_H
 #define HBT_FIT_H
@@ -74,8 +74,8 @@ typedef struct hbt_fit_stats {
     int64_t rows;          /* table rows uploaded */
     int64_t points;        /* sum over fits of the rows fitted */
     int64_t passes;        /* sum over fits of the passes over their rows */
-    double upload_ms;      /* device time of the copies and row selection, summed over batches */
-    double kernel_ms;      /* device time of the fits, summed over batches (two overlap) */
+    double upload_ms;      /* device time of the copies and row selection */
+    double kernel_ms;      /* device time of the fits (passes, steps, errors) */
 } hbt_fit_stats;
 
 hbt_status hbt_fit_create(int device, hbt_fit_ctx **out);
