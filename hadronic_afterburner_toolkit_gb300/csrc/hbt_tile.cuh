@@ -227,8 +227,12 @@ __device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const
     } else {
         ql = dz;
     }
-    const double ph = dE * (a[7] - b[7]) - dx * (a[4] - b[4]) - dy * (a[5] - b[5]) -
-                      dz * (a[6] - b[6]);
+    // q.dx = dE dt - dx dX - dy dY - dz dZ, accumulated with fused
+    // multiply-adds (one rounding per term)
+    double ph = dE * (a[7] - b[7]);
+    ph = __fma_rn(-dx, a[4] - b[4], ph);
+    ph = __fma_rn(-dy, a[5] - b[5], ph);
+    ph = __fma_rn(-dz, a[6] - b[6], ph);
     w = table_cos(cs, g.hbarC_inv * ph);
 }
 
