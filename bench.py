@@ -77,6 +77,10 @@ def make_workload(name: str, seed: int = 1, max_groups: int | None = None):
     if name == "small":
         ev = synth.small_pions(seed=seed)
         buf, nmix = 5000, 5
+    elif name == "kaons":
+        # the precision configuration's K+ run: oversample factor 100
+        ev = synth.central_kaons(seed=seed + 1)
+        buf, nmix = 25000, 10
     elif name == "medium":
         # the central workload's events and grid, 30x oversampling (profiling)
         ev = synth.central_pions(n_events=300, seed=seed)
@@ -691,6 +695,50 @@ def fit_leg(n_tables: int = 256, cpu_seconds: float = 8.0) -> dict:
     return res
 
 
+def precision_leg(E, groups, p, local, n_kaon_groups: int = 3) -> dict:
+    """FP32-weight form against the FP64 form on the precision
+    configuration: one central pi+ group and the first K+ groups (1000 K+
+    events, Poisson(250), T = 0.30 GeV, oversample 100, 10 partners), same
+    grid and bins. Counts and denominators must be identical; for the
+    numerator (sum of cos) and the mean-q sums, per bin: the error per pair
+    |fp32w - fp64| / count, and the relative error over the bins whose sum
+    does not cancel (at least 100 pairs, |sum| at least half the count times
+    1 for cos or 0.01 GeV for q). The FP64 form is the oracle's stand-in at this size
+    (it matches the CPU oracle to 1e-12 per pair on the test cases)."""
+    def run(groups_, prec):
+        eng = E.Engine(device=local, precision=prec, **p)
+        for cols, mixed in groups_:
+            eng.bin_batch([("same", cols)] + [("mixed", l1, l2) for l1, l2 in mixed])
+        h = eng.hist()
+        eng.close()
+        return h
+
+    def errors(h64, h32):
+        out = {"counts_identical": bool(np.array_equal(h64["count"], h32["count"])),
+               "den_identical": bool(np.array_equal(h64["den"], h32["den"])),
+               "bins_with_pairs": int((h64["count"] > 0).sum())}
+        m = h64["count"] > 0
+        big = h64["count"] >= 100
+        for k, scale in (("num", 1.0), ("q_out", 0.01), ("q_side", 0.01), ("q_long", 0.01)):
+            d = np.abs(h32[k] - h64[k])
+            out[k + "_max_err_per_pair"] = float((d[m] / h64["count"][m]).max()) if m.any() else 0.0
+            # relative error where the bin's sum does not cancel: at least 100
+            # pairs and |sum| >= half the count times 1 (cos) or 0.01 GeV (q)
+            sel = big & (np.abs(h64[k]) >= 0.5 * scale * h64["count"])
+            out[k + "_max_rel_err_coherent_bins"] = (
+                float((d[sel] / np.abs(h64[k][sel])).max()) if sel.any() else 0.0)
+        return out
+
+    res = {}
+    pi = groups[:1]
+    res["pi+"] = errors(run(pi, E.PRECISION_FP64), run(pi, E.PRECISION_FP32W))
+    kg = make_workload("kaons", max_groups=n_kaon_groups)
+    res["K+"] = errors(run(kg, E.PRECISION_FP64), run(kg, E.PRECISION_FP32W))
+    res["K+"]["groups"] = len(kg)
+    res["K+"]["particles_per_group"] = int(np.mean([g[0][0].size for g in kg]))
+    return res
+
+
 def make_requests(n_jobs: int, seed: int = 5):
     """Requests of the serving workload: 10-500 events each, multiplicity
     Poisson(mu) with mu uniform in [50, 2000], pi+ or K+, qnpts in
@@ -782,6 +830,8 @@ def main() -> None:
                     help="skip the balance-function leg")
     ap.add_argument("--no-fit", action="store_true",
                     help="skip the radii-fit leg")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the FP32-weight against FP64 error report")
     ap.add_argument("--no-ingest", action="store_true",
                     help="skip the reader timing (line-by-line against block reader)")
     args = ap.parse_args()
@@ -1006,7 +1056,7 @@ def main() -> None:
         cpu = cpu_baseline(groups[0], p, nthreads=1)
 
     uneven = serving = ingest = average = None
-    balance = fits = None
+    balance = fits = precision = None
     if not args.no_ingest and rank == 0:
         ingest = ingest_leg()
         average = average_leg()
@@ -1014,6 +1064,8 @@ def main() -> None:
         balance = bf_leg()
     if not args.no_fit and rank == 0:
         fits = fit_leg()
+    if not args.no_precision and rank == 0 and args.workload == "central":
+        precision = precision_leg(E, groups, p, local)
     if not args.no_uneven:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
@@ -1054,6 +1106,7 @@ def main() -> None:
                 "average": average,
                 "balance_function": balance,
                 "radii_fit": fits,
+                "precision_fp32w_vs_fp64": precision,
                 "stats": st}
         print(json.dumps(line))
     eng.close()

@@ -36,6 +36,14 @@ struct DevBuf {
 
 }  // namespace
 
+// FP32-weight form: same-event tile pairs (at most 128 x 128 pairs each)
+// between two merges of the FP32 partials into the FP64 bins, and the
+// largest value a tuning may set.  The partials' rounding grows with the
+// pairs a bin takes between merges: on the central workload the worst
+// numerator error per pair is 6e-7 with 8192 (1e-6 to 2e-6 with 16384),
+// inside the form's 1e-6 bound.
+constexpr int kMergeChunk = 8192;
+
 struct hbt_ctx {
     hbt_params prm;
     int device = 0;
@@ -55,7 +63,7 @@ struct hbt_ctx {
     hbt::BatchRunner runner;
     int persistent_grid = 152 * 4;
     int sms = 152, max_blocks_per_sm = 5;
-    hbt_tuning tune = {0, 0.02, 0.05, 16384, 1, 0};
+    hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0};
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging
@@ -406,14 +414,14 @@ std::vector<FastJob> fast_jobs_of(int32_t n_jobs, const hbt_job *jobs) {
 
 bool tuning_valid(const hbt_tuning &t) {
     return t.blocks_per_sm >= 0 && t.cell_pt >= 0.0 && t.cell_y >= 0.0 && t.merge_chunk >= 0 &&
-           t.merge_chunk <= 16384 && (t.use_graph == 0 || t.use_graph == 1) &&
+           t.merge_chunk <= kMergeChunk && (t.use_graph == 0 || t.use_graph == 1) &&
            (t.time_kernels == 0 || t.time_kernels == 1);
 }
 
 hbt_tuning tuning_defaults(hbt_tuning t) {
     if (t.cell_pt == 0.0) t.cell_pt = 0.02;
     if (t.cell_y == 0.0) t.cell_y = 0.05;
-    if (t.merge_chunk == 0) t.merge_chunk = 16384;
+    if (t.merge_chunk == 0) t.merge_chunk = kMergeChunk;
     return t;
 }
 
@@ -583,8 +591,8 @@ hbt_status ctx_create(const hbt_params *p, int device, cudaMemPool_t pool, hbt_c
     c->cap_qinv = 50 * c->cap;
     c->n_stream = g.n_slots + g.n_KT;
     c->d.precision = p->precision;
-    // merge the FP32 partials every 16384 same-event CTAs (~2.7e8 pairs)
-    c->d.merge_chunk_blocks = 16384;
+    // merge the FP32 partials every kMergeChunk same-event CTAs
+    c->d.merge_chunk_blocks = kMergeChunk;
     c->d.block_offset = 0;
     {
         int sms = 0;
@@ -882,7 +890,7 @@ hbt_status hbt_autotune_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs, d
         }
     }
     if (c->d.precision == HBT_PRECISION_FP32W)
-        for (int chunk : {8192, 16384}) {
+        for (int chunk : {kMergeChunk / 2, kMergeChunk}) {
             if (rs != HBT_OK || chunk == cur.merge_chunk) continue;
             hbt_tuning cand = cur;
             cand.merge_chunk = chunk;
