@@ -1079,10 +1079,11 @@ def main() -> None:
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.precision == "fp64" else "f64 bins / f32 weights",
                 "data": "synthetic",
-                "config": {"workload": args.workload, "events": 1000 if args.workload == "central" else 100,
-                           "oversample": 100 if args.workload == "central" else 10,
+                "config": {"workload": args.workload,
+                           "events": {"central": 1000, "medium": 300}.get(args.workload, 100),
+                           "oversample": {"central": 100, "medium": 30}.get(args.workload, 10),
                            "particles_per_group": int(np.mean([g[0][0].size for g in groups])),
-                           "mixed_partners": 10 if args.workload == "central" else 5,
+                           "mixed_partners": 5 if args.workload == "small" else 10,
                            "qnpts": p["qnpts"], "n_KT_bins": p["n_KT"] - 1,
                            "n_Kphi": p["n_Kphi"] if p["azimuthal_flag"] else 1,
                            "precision": args.precision, "kernel": args.kernel,
