@@ -139,3 +139,21 @@ def test_dropin_writes_radii_beside_the_tables(tmp_path):
         path = tmp_path / ev / ("HBT_radii_KT_%s.dat" % kt)
         assert open(path).readline().rstrip("\n") == radii.HEADER
         _close(np.loadtxt(path), w)
+
+
+def test_empty_calls_and_tables():
+    """No tables; a table of no rows and one of five rows (too few for six
+    parameters) beside a normal one; a fit limited to two iterations
+    reports the iteration limit with the best point found."""
+    import tables
+    from hadronic_afterburner_toolkit_gb300 import radii
+    f = radii.Fitter()
+    assert f.fit([]).shape == (0, 5, 13)
+    t = tables.make_table(9, (0.5, 5.0, 4.5, 5.5, 1.0, 0.7))
+    rows = f.fit([np.zeros((0, 8)), t[:5], t])
+    assert (f.last["status"][0] == 3).all() and (f.last["status"][1] == 3).all()
+    assert np.isnan(rows[0, :, 1:]).all() and np.isnan(rows[1, :, 1:]).all()
+    assert (f.last["status"][2] == 0).all()
+    np.testing.assert_array_equal(rows[2], f.fit([t])[0])
+    f.fit([t], max_iterations=2)
+    assert (f.last["status"] == 1).all() and (f.last["iterations"] == 2).all()
