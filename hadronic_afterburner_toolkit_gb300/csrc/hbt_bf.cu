@@ -107,12 +107,27 @@ __device__ __forceinline__ float4 pack_terms(double xp, double mp, double xy, do
     return make_float4(tp, ep, ty, ey);
 }
 
-// Particle a: (phi + rot - Bphi_min) / dphi and (y - Brap_min) / drap.
+// Particle a's terms as the pair loop uses them: the azimuthal term plus
+// 19.5 and the rapidity term minus 0.5 (both shifts in FP64 before the
+// rounding to FP32, inside the bound), so that rint of a pair's difference
+// is the floor of the unshifted one (plus 20 for the azimuth: a column in
+// [0, 40) of a histogram whose columns c and c + 20 are the same bin), and
+// each bound as its distance to a half-integer, 0.5 - bound.
+__device__ __forceinline__ float4 pack_terms_a(double xp, double mp, double xy, double my) {
+    if (!(fabs(xp) < 1e9 && fabs(xy) < 1e9)) return make_float4(NAN, 0.f, NAN, 0.f);
+    const double sp = wrap20(xp) + 19.5, sy = xy - 0.5;
+    const float tp = (float)sp, ty = (float)sy;
+    const double ep = 2.0001 * kU64 * fabs((double)tp) + 0x1p-46 * (mp + 60.0) + 2e-7;
+    const double ey = 2.0001 * kU64 * fabs((double)ty) + 0x1p-46 * (my + 1.0) + 2e-7;
+    return make_float4(tp, (float)(0.5 - ep), ty, (float)(0.5 - ey));
+}
+
+// Particle a: (phi + rot - Bphi_min) / dphi and (y - Brap_min) / drap,
+// shifted (pack_terms_a).
 __device__ __forceinline__ float4 terms_a(const BfConst &c, double phi, double y, double rot) {
-    return pack_terms(((phi + rot) - c.Bphi_min) * c.inv_dphi,
-                      (fabs(phi) + fabs(rot) + fabs(c.Bphi_min)) * c.inv_dphi,
-                      (y - c.Brap_min) * c.inv_drap, (fabs(y) + fabs(c.Brap_min)) * c.inv_drap,
-                      2e-7);
+    return pack_terms_a(((phi + rot) - c.Bphi_min) * c.inv_dphi,
+                        (fabs(phi) + fabs(rot) + fabs(c.Bphi_min)) * c.inv_dphi,
+                        (y - c.Brap_min) * c.inv_drap, (fabs(y) + fabs(c.Brap_min)) * c.inv_drap);
 }
 
 // Particle b: phi / dphi and y / drap.
@@ -149,15 +164,15 @@ __global__ void __launch_bounds__(kTile, HBT_BF_MIN_BLOCKS)
     k_bf(const BfJob *jobs, const int2 *items, long long n_items, const double *phi,
          const double *y, const float4 *tb, const float2 *yb, BfConst c,
          unsigned long long *hist, unsigned long long *n_slow) {
-    extern __shared__ unsigned sh[];  // [Bnpts][kNphi]
+    extern __shared__ unsigned sh[];  // [Bnpts][2 kNphi]: columns c and c + 20 are bin c
     __shared__ float4 sb[kTile];
     __shared__ float2 sd[kTile];
     __shared__ BfJob sj;
-    const int nbins = c.Bnpts * kNphi;
+    const int nbins = c.Bnpts * kNphi, nsh = 2 * nbins;
     unsigned slow = 0;
     for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
         const int2 item = items[it];
-        for (int k = threadIdx.x; k < nbins; k += blockDim.x) sh[k] = 0u;
+        for (int k = threadIdx.x; k < nsh; k += blockDim.x) sh[k] = 0u;
         if (threadIdx.x == 0) sj = jobs[item.x];
         __syncthreads();
         const long long ia = sj.a0 + item.y + threadIdx.x;
@@ -180,30 +195,34 @@ __global__ void __launch_bounds__(kTile, HBT_BF_MIN_BLOCKS)
                 for (int j = 0; j < nb; j++) {
                     const float4 B = sb[j];
                     const float2 By = sd[j];
-                    const float t = A.x - B.x, et = A.y + B.y;
-                    const float ty = A.z - B.z, ety = A.w + B.w;
-                    const float kp = floorf(t), fp = t - kp;
-                    const float ky = floorf(ty), fy = ty - ky;
+                    // shifted differences: rint gives the floors (the azimuth
+                    // + 20); certain when their distance to the rint is
+                    // below 0.5 - bound
+                    const float tp = A.x - B.x, ty = A.z - B.z;
+                    const float kp = rintf(tp), ky = rintf(ty);
                     int k;
-                    if (fp > et && fp < 1.0f - et && fy > ety && fy < 1.0f - ety &&
+                    if (fabsf(tp - kp) < A.y - B.y && fabsf(ty - ky) < A.w - B.w &&
                         fabsf(Ay.x - By.x) > Ay.y + By.y) {
-                        // t lies in (-20, 20): kp in [-20, 19], its class mod 20
-                        // in [0, 19]; ky beyond [0, Bnpts) puts k outside the
-                        // histogram (|ty| < 2^23 here, so k fits an int)
-                        const float ipf = kp < 0.0f ? kp + 20.0f : kp;
-                        k = (int)(ky * 20.0f + ipf);
+                        // tp in (-0.5, 39.5): column kp in [0, 39]; a row ky
+                        // beyond [0, Bnpts) puts k outside the histogram
+                        // (|ty| < 2^23 here, so k fits an int)
+                        k = (int)__fmaf_rn(ky, 2.0f * kNphi, kp);
                     } else {
-                        k = bin_slow(c, phi, y, ia, b + j, sj.mixed, sj.rotation);
+                        const int k20 = bin_slow(c, phi, y, ia, b + j, sj.mixed, sj.rotation);
+                        k = k20 < 0 ? -1 : (k20 / kNphi) * (2 * kNphi) + k20 % kNphi;
                         slow++;
                     }
-                    if ((unsigned)k < (unsigned)nbins) atomicAdd(&sh[k], 1u);
+                    if ((unsigned)k < (unsigned)nsh) atomicAdd(&sh[k], 1u);
                 }
             }
             __syncthreads();
         }
         unsigned long long *h = hist + (long long)sj.hist * nbins;
-        for (int k = threadIdx.x; k < nbins; k += blockDim.x)
-            if (sh[k]) atomicAdd(h + k, (unsigned long long)sh[k]);
+        for (int k = threadIdx.x; k < nbins; k += blockDim.x) {
+            const int r = k / kNphi, col = k - r * kNphi;
+            const unsigned v = sh[r * 2 * kNphi + col] + sh[r * 2 * kNphi + col + kNphi];
+            if (v) atomicAdd(h + k, (unsigned long long)v);
+        }
         __syncthreads();
     }
     for (int o = 16; o > 0; o >>= 1) slow += __shfl_xor_sync(0xffffffffu, slow, o);
@@ -256,7 +275,7 @@ extern "C" {
 hbt_status hbt_bf_create(const hbt_bf_params *p, int device, hbt_bf_ctx **out) {
     if (!p || !out) return HBT_ERR_INVALID;
     *out = nullptr;
-    // the shared-memory histogram holds Bnpts x 20 counts (48 KB default)
+    // the shared-memory histogram holds Bnpts x 40 counts (at most 96 KB)
     if (p->Bnpts < 2 || p->Bnpts * kNphi * 4 > 48 * 1024) return HBT_ERR_INVALID;
     hbt_bf_ctx *c = new hbt_bf_ctx();
     c->p = *p;
@@ -274,7 +293,9 @@ hbt_status hbt_bf_create(const hbt_bf_params *p, int device, hbt_bf_ctx **out) {
         cudaEventCreate(&c->ev[0]) != cudaSuccess || cudaEventCreate(&c->ev[1]) != cudaSuccess ||
         cudaEventCreate(&c->ev[2]) != cudaSuccess ||
         !grow(c->hist, (size_t)8 * p->Bnpts * kNphi * sizeof(unsigned long long)) ||
-        !grow(c->counter, sizeof(unsigned long long))) {
+        !grow(c->counter, sizeof(unsigned long long)) ||
+        cudaFuncSetAttribute(k_bf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             p->Bnpts * 2 * kNphi * (int)sizeof(unsigned)) != cudaSuccess) {
         hbt_bf_destroy(c);
         return HBT_ERR_CUDA;
     }
@@ -395,7 +416,7 @@ hbt_status hbt_bf_bin(hbt_bf_ctx *c, int32_t n_lists, const hbt_bf_list *lists, 
                                   static_cast<float2 *>(c->yb.p));
     const long long n_items = (long long)items.size();
     const long long grid = std::min<long long>(n_items, 1LL << 30);
-    k_bf<<<(unsigned)grid, kTile, (size_t)c->p.Bnpts * kNphi * sizeof(unsigned), c->stream>>>(
+    k_bf<<<(unsigned)grid, kTile, (size_t)c->p.Bnpts * 2 * kNphi * sizeof(unsigned), c->stream>>>(
         static_cast<const BfJob *>(c->jobs.p), static_cast<const int2 *>(c->items.p), n_items,
         dphi_p, dy_p, static_cast<const float4 *>(c->tb.p), static_cast<const float2 *>(c->yb.p),
         c->c, static_cast<unsigned long long *>(c->hist.p),

@@ -216,3 +216,27 @@ def test_bf_fp32_screen_near_edges():
     eng.bin([A, B, A, B], [(0, 2, 0, 3, 0, 0, 0.0)])
     n_items = -(-ya.size // 128)
     assert eng.stats()["bytes_uploaded"] == 48 + 8 * n_items + 16 * (ya.size + yb.size)
+
+
+def test_bf_many_rapidity_bins():
+    """Bnpts = 600: the shared histogram (600 x 40 counts, 96 KB) needs the
+    opt-in shared-memory size; random lists against the oracle."""
+    from hadronic_afterburner_toolkit_gb300 import bf
+    Bnpts, Brap_max = 600, 3.0
+    rng = np.random.default_rng(19)
+    na, nb = 700, 500
+    A = (np.array([0, na], np.int64), rng.uniform(-np.pi, np.pi, na), rng.uniform(-2, 2, na))
+    B = (np.array([0, nb], np.int64), rng.uniform(-np.pi, np.pi, nb), rng.uniform(-2, 2, nb))
+    jobs = [(0, 0, 0, 1, 0, 0, 0.0), (5, 0, 0, 1, 0, 1, 2.1)]
+    eng = bf.BfEngine(Bnpts, Brap_max)
+    eng.bin([A, B], jobs)
+    orc = oracle_lib.BfOracle(particle_alpha=1, particle_beta=2, BpT_min=-1.0, BpT_max=10.0,
+                              Bnpts=Bnpts, Brap_max=Brap_max, rap_type=1, seed=1)
+    L = oracle_lib._bf_lib()
+    for (h, la, ea, lb, eb, mx, rot) in jobs:
+        cols = [np.ascontiguousarray(x) for x in (np.ones(na), A[1], A[2], np.ones(nb), B[1], B[2])]
+        L.orc_bf_bin(orc._h, h, na, *[oracle_lib._pd(c) for c in cols[:3]], nb,
+                     *[oracle_lib._pd(c) for c in cols[3:]], mx, rot)
+    for h in (0, 5):
+        assert np.array_equal(eng.hist(h), orc.hist(h)), h
+    assert eng.hist(0).sum() > 100000
