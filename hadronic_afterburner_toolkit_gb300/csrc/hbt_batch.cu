@@ -372,10 +372,10 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
 #undef HBT_P
         if (e != cudaSuccess) return e;
         if (prec && !b.devs) {
-            if ((e = launch_merge(d, st)) != cudaSuccess) return e;
+            if ((e = launch_merge(d, st, b.n_items, base)) != cudaSuccess) return e;
         } else if (prec) {
             for (int k = 0; k < n_host_devs; k++)
-                if ((e = launch_merge(host_devs[k], st)) != cudaSuccess) return e;
+                if ((e = launch_merge(host_devs[k], st, b.n_items, base)) != cudaSuccess) return e;
         }
     }
     if (marks && (e = cudaEventRecord(marks[1], st)) != cudaSuccess) return e;

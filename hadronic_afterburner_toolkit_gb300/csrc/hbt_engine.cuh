@@ -157,7 +157,11 @@ cudaError_t launch_export(const Device &d, int field, double *out, long long nbi
                           cudaStream_t st);
 
 // Merge of the FP32-weight partial sums into the FP64 bins (hbt_fast.cu).
-cudaError_t launch_merge(const Device &d, cudaStream_t st);
+// FP32 partials -> FP64 bins.  With n_items, the merge after a chunk of
+// the batched same-event queue starting at chunk_base returns at once when
+// the culled queue ended before it.
+cudaError_t launch_merge(const Device &d, cudaStream_t st, const unsigned *n_items = nullptr,
+                         unsigned chunk_base = 0);
 
 // Screened fast-mode kernels (hbt_fast.cu): same results as MODE_FAST of the
 // reference-chain kernels; require invariant_radius_flag == 0, n_KT <= 255

@@ -35,7 +35,11 @@ __global__ void __launch_bounds__(FT) k_mixed_screened(Device d, long long n1, C
 }  // namespace
 
 // FP32 partial sums -> FP64 bins with Kahan compensation; partials cleared.
-__global__ void __launch_bounds__(256) k_merge_partials(Device d, long long nbins) {
+__global__ void __launch_bounds__(256) k_merge_partials(Device d, long long nbins,
+                                                        const unsigned *n_items,
+                                                        unsigned chunk_base) {
+    // a chunk of the batched queue past its culled length binned nothing
+    if (n_items && chunk_base >= *n_items) return;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nbins;
          k += (long long)gridDim.x * blockDim.x) {
         const float4 p = d.part[k];
@@ -58,9 +62,11 @@ __global__ void __launch_bounds__(256) k_merge_partials(Device d, long long nbin
     }
 }
 
-cudaError_t launch_merge(const Device &d, cudaStream_t st) {
+cudaError_t launch_merge(const Device &d, cudaStream_t st, const unsigned *n_items,
+                         unsigned chunk_base) {
     const long long nbins = (long long)d.g.n_slots * d.g.q3;
-    k_merge_partials<<<(unsigned)min((nbins + 255) / 256, 152LL * 16), 256, 0, st>>>(d, nbins);
+    k_merge_partials<<<(unsigned)min((nbins + 255) / 256, 152LL * 16), 256, 0, st>>>(
+        d, nbins, n_items, chunk_base);
     return cudaGetLastError();
 }
 
