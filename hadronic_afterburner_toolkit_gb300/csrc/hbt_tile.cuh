@@ -490,7 +490,10 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
     sm.gj[tid] = make_float2(fabsf(sm.fj[tid].x) + fabsf(sm.fj[tid].y), fabsf(sm.fj[tid].z));
     __syncthreads();
     const Screen &S = d.s;
-    const int il = w * 32 + lane;
+    // warp w takes the tile's rows w, w + 4, w + 8, ...: the rows are sorted
+    // in momentum space, so interleaving spreads each warp's rows over the
+    // tile and evens out the binned pairs (the FP64 work) between warps
+    const int il = lane * (FT / 32) + w;
     const long long i = i0 + il;
     const float4 a = sm.fi[il];
     const float2 ga = sm.gi[il];
@@ -617,7 +620,7 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
     sm.gj[tid] = make_float2(fabsf(sm.fj[tid].x) + fabsf(sm.fj[tid].y), fabsf(sm.fj[tid].z));
     __syncthreads();
     const Screen &S = d.s;
-    const int il = w * 32 + lane;
+    const int il = lane * (FT / 32) + w;  // interleaved rows, as in same_tile_pair
     const bool active = i0 + il < n1;
     const float4 a = sm.fi[il];
     const float2 ga = sm.gi[il];
