@@ -1,8 +1,9 @@
-// Pipe-throughput probes used by the benchmark to measure, on the GPU it runs
-// on, the peak issue rate of the arithmetic the HBT kernels are bound by
-// (FP64 and FP32 fused multiply-add).  Each thread runs 8 independent FMA
-// chains in registers and writes one value, so the memory traffic is one
-// store per thread.
+// Throughput probes used by the benchmark to measure, on the GPU it runs
+// on, the peak rates the HBT kernels are bound by: the FP64 and FP32 fused
+// multiply-add issue rate (each thread runs 8 independent FMA chains in
+// registers and writes one value, so the memory traffic is one store per
+// thread), and the rate of FP64 atomic adds to scattered addresses of an
+// array larger than L2 (the histogram updates).
 #include <cuda_runtime.h>
 
 namespace {
@@ -45,9 +46,46 @@ int run(int blocks, int iters, float *ms, double *flops) {
     return err == cudaSuccess ? 0 : 2;
 }
 
+// FP64 atomic adds at pseudo-random positions of a 2^log2 array: each
+// thread walks its own xorshift-multiply sequence, `iters` adds.
+__global__ void __launch_bounds__(256) k_atomic(double *h, unsigned long long mask, int iters) {
+    unsigned long long x = (blockIdx.x * 256ull + threadIdx.x + 1) * 0x9E3779B97F4A7C15ull;
+    for (int k = 0; k < iters; k++) {
+        x ^= x >> 31;
+        x *= 0xBF58476D1CE4E5B9ull;
+        x ^= x >> 29;
+        atomicAdd(h + (x & mask), 1.0);
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+// Scattered FP64 atomic-add throughput over 2^log2 doubles: returns 0 and
+// the elapsed ms and the number of atomics.
+int hbt_probe_atomic(int blocks, int iters, int log2, float *ms, double *ops) {
+    if (log2 < 10 || log2 > 31) return 1;
+    double *h = nullptr;
+    const size_t n = (size_t)1 << log2;
+    if (cudaMalloc(&h, n * sizeof(double)) != cudaSuccess) return 1;
+    cudaMemset(h, 0, n * sizeof(double));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_atomic<<<blocks, 256>>>(h, n - 1, iters / 8 + 1);  // warm-up
+    cudaEventRecord(e0);
+    k_atomic<<<blocks, 256>>>(h, n - 1, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    *ops = (double)iters * blocks * 256.0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const cudaError_t err = cudaGetLastError();
+    cudaFree(h);
+    return err == cudaSuccess ? 0 : 2;
+}
 
 // FP64 FMA throughput: returns 0 and the elapsed ms and flop count.
 int hbt_probe_fp64(int blocks, int iters, float *ms, double *flops) {
