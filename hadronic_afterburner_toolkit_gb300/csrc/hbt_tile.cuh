@@ -451,6 +451,34 @@ __device__ __forceinline__ void drain(T *q, int count, int lane, F &process) {
     __syncwarp();
 }
 
+// A mixed-event pair the screens left undecided: the reference chain
+// decides.  Out of line: it runs for a few pairs per thousand, and inlined
+// its registers would crowd the screen's (the kernel spilled 420 bytes).
+static __device__ __noinline__ void undecided_mixed_pair(const Device &d, const double *const *l1,
+                                                         const double *const *l2, long long i,
+                                                         long long j, long long n1, long long n2) {
+    const Chain ch = pair_chain<true>(d.g, l1[0][i], l1[1][i], l1[2][i], l1[3][i], l2[0][j],
+                                      l2[1][j], l2[2][j], l2[3][j], nullptr, nullptr);
+    consume<true, MODE_FAST>(d, i, j, n2, n1, ch);
+}
+
+// A same-event pair of the FP32-weight form that the screens left
+// undecided: the reference chain decides; a binned pair adds its FP32
+// values to the partials.  Out of line, for the same reason.
+template <bool BOOST>
+__device__ __noinline__ void undecided_pair32(const Device &d, const double *A, const double *B,
+                                              long long i, long long j, long long n) {
+    const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2], B[3],
+                                         A + 4, B + 4);
+    if (full.ev3 != 1) {
+        consume<false, MODE_FAST>(d, i, j, n, n, full);
+    } else {
+        const long long at = (long long)full.slot * d.g.q3 + full.bin;
+        atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
+        atomicAdd(d.h.cnt + at, 1ull);
+    }
+}
+
 // Same-event pairs of the tiles starting at i0 and j0 (i0 <= j0) of one list
 // of n particles with columns c = px py pz E x y z t.  Every unordered pair
 // is visited once (position j > i); it is oriented as the reference orients
@@ -554,6 +582,10 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
             atomicAdd(d.h.cnt + at, 1ull);
             return;
         }
+        if (PREC == 1) {
+            undecided_pair32<BOOST>(d, A, B, i0 + qi, j0 + qj, n);
+            return;
+        }
         {
             // undecided somewhere: the reference chain decides (and may hand
             // a K_phi edge to the host)
@@ -645,11 +677,7 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
         if (slot >= 0) {
             atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
         } else {
-            const long long i = i0 + qi, j = j0 + qj;
-            const Chain ch = pair_chain<true>(d.g, l1[0][i], l1[1][i], l1[2][i], l1[3][i],
-                                              l2[0][j], l2[1][j], l2[2][j], l2[3][j], nullptr,
-                                              nullptr);
-            consume<true, MODE_FAST>(d, i, j, n2, n1, ch);
+            undecided_mixed_pair(d, l1, l2, i0 + qi, j0 + qj, n1, n2);
         }
     };
 
