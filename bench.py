@@ -419,6 +419,46 @@ def uneven_leg(E, torch, dev, stream, flush, local, steps=2) -> dict:
     return out
 
 
+def small_leg(E, torch, dev, stream, flush, local, steps=3) -> dict:
+    """Config 1, the reference's CPU-runnable case (100 pi+ events,
+    Poisson(500), oversample 10 -> 10 groups of ~5k particles, 5 rotated
+    partners, 41^3 grid, 4 K_T bins): every group and partner in one batched
+    FP64 launch per step, against the oracle on one host core."""
+    groups = make_workload("small")
+    p = workload_params("small")
+    dgroups = [([torch.from_numpy(c).to(dev) for c in cols],
+                [([torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in l1],
+                  [torch.from_numpy(x).to(dev) for x in l2]) for l1, l2 in mixed])
+               for cols, mixed in groups]
+    jobs = []
+    for dc, dm in dgroups:
+        jobs.append(("same", dc))
+        jobs += [("mixed", l1, l2) for l1, l2 in dm]
+    total = sum(group_pairs(g) for g in groups)
+    eng = E.Engine(device=local, precision=E.PRECISION_FP64, kernel=E.KERNEL_SCREENED, **p)
+    eng.set_stream(stream.cuda_stream)
+    ms = []
+    for k in range(3 + steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.bin_batch(jobs, device=True)
+        e1.record(stream)
+        e1.synchronize()
+        if k >= 3:
+            ms.append(e0.elapsed_time(e1))
+    eng.close()
+    value = total / (statistics.median(ms) * 1e-3)
+    cpu = cpu_baseline(groups[0], p, nthreads=1, target_s=3.0)
+    return {"events": 100, "groups": len(groups), "pairs_per_step": total,
+            "jobs_per_launch": len(jobs), "value": value, "unit": "pairs/s",
+            "ms_per_step": statistics.median(ms), "steps": steps,
+            "cpu_oracle_pairs_per_s": cpu["value"], "cpu_cores": 1,
+            "speedup_vs_cpu_core": value / cpu["value"]}
+
+
 INGEST_PARAMS = """echo_level = 0
 read_in_mode = 10
 read_in_real_mixed_events = 0
@@ -1091,6 +1131,9 @@ def main() -> None:
         fits = fit_leg()
     if not args.no_precision and rank == 0 and args.workload == "central":
         precision = precision_leg(E, groups, p, local)
+    small = None
+    if not args.no_uneven and rank == 0 and args.workload == "central":
+        small = small_leg(E, torch, dev, stream, flush, local)
     if not args.no_uneven:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
@@ -1126,6 +1169,7 @@ def main() -> None:
                                      if plain else None) for k, v in variants.items()},
                 "e2e": e2e,
                 "cpu_baseline": cpu,
+                "small_config": small,
                 "uneven": uneven,
                 "serving": serving,
                 "ingest": ingest,
