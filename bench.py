@@ -1,7 +1,7 @@
 """Benchmark of the GB300 HBT pair-binning engine.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload central|medium|small] [--precision fp64|fp32w]
+                    [--workload central|medium|small] [--precision fp64|fp32w|df64]
                     [--no-uneven] [--no-serving] [--serving-jobs J]
 
 Workload "central" (default): 1000 pi+ events, multiplicity Poisson(1500),
@@ -373,7 +373,8 @@ def uneven_leg(E, torch, dev, stream, flush, local, steps=2) -> dict:
 
     out = {"events": 4096, "groups": len(groups), "group_particles": "~50k",
            "mixed_partners": 10, "pairs_per_step": total_pairs, "qnpts": 41, "n_KT_bins": 4}
-    for label, prec in (("batched-fp64", E.PRECISION_FP64), ("batched-fp32w", E.PRECISION_FP32W)):
+    for label, prec in (("batched-fp64", E.PRECISION_FP64), ("batched-fp32w", E.PRECISION_FP32W),
+                        ("batched-df64", E.PRECISION_DF64)):
         eng = E.Engine(device=local, precision=prec, kernel=E.KERNEL_SCREENED, **UNEVEN_PARAMS)
         eng.set_stream(stream.cuda_stream)
         default_ms = statistics.median(timed(lambda: eng.bin_batch(jobs, device=True), 2))
@@ -414,7 +415,7 @@ def uneven_leg(E, torch, dev, stream, flush, local, steps=2) -> dict:
                          "sample": "%d of %d groups (%.3g pairs)" % (n_sample, len(groups), acc),
                          "kernel": "reference chain, one launch per list"}
     eng.close()
-    for k in ("batched-fp64", "batched-fp32w"):
+    for k in ("batched-fp64", "batched-fp32w", "batched-df64"):
         out[k]["speedup_vs_plain"] = out[k]["value"] / out["plain-fp64"]["value"]
     return out
 
@@ -748,8 +749,8 @@ def fit_leg(n_tables: int = 256, cpu_seconds: float = 8.0) -> dict:
     return res
 
 
-def precision_leg(E, groups, p, local, n_kaon_groups: int = 3) -> dict:
-    """FP32-weight form against the FP64 form on the precision
+def precision_leg(E, groups, p, local, other=None, n_kaon_groups: int = 3) -> dict:
+    """FP32-weight (or `other`) form against the FP64 form on the precision
     configuration: one central pi+ group and the first K+ groups (1000 K+
     events, Poisson(250), T = 0.30 GeV, oversample 100, 10 partners), same
     grid and bins. Counts and denominators must be identical; for the
@@ -782,11 +783,12 @@ def precision_leg(E, groups, p, local, n_kaon_groups: int = 3) -> dict:
                 float((d[sel] / np.abs(h64[k][sel])).max()) if sel.any() else 0.0)
         return out
 
+    other = E.PRECISION_FP32W if other is None else other
     res = {}
     pi = groups[:1]
-    res["pi+"] = errors(run(pi, E.PRECISION_FP64), run(pi, E.PRECISION_FP32W))
+    res["pi+"] = errors(run(pi, E.PRECISION_FP64), run(pi, other))
     kg = make_workload("kaons", max_groups=n_kaon_groups)
-    res["K+"] = errors(run(kg, E.PRECISION_FP64), run(kg, E.PRECISION_FP32W))
+    res["K+"] = errors(run(kg, E.PRECISION_FP64), run(kg, other))
     res["K+"]["groups"] = len(kg)
     res["K+"]["particles_per_group"] = int(np.mean([g[0][0].size for g in kg]))
     return res
@@ -821,7 +823,8 @@ def make_requests(n_jobs: int, seed: int = 5):
 def serving_leg(E, local, n_jobs=48, rate=200.0, seed=5) -> dict:
     """A Poisson request stream at `rate` jobs/s through the serving loop:
     continuous batching (FP64 and FP32 weights) against the plain per-job
-    path (reference-chain kernel, one request at a time, list by list)."""
+    path (reference-chain kernel, one request at a time, list by list);
+    the double-float form beside them."""
     from hadronic_afterburner_toolkit_gb300 import server
     reqs = make_requests(n_jobs, seed)
     rng = np.random.default_rng(seed + 1)
@@ -853,9 +856,10 @@ def serving_leg(E, local, n_jobs=48, rate=200.0, seed=5) -> dict:
            "arrival_span_s": float(arrivals[-1])}
     out["batched-fp64"] = stream_run(E.PRECISION_FP64, E.KERNEL_SCREENED)
     out["batched-fp32w"] = stream_run(E.PRECISION_FP32W, E.KERNEL_SCREENED)
+    out["batched-df64"] = stream_run(E.PRECISION_DF64, E.KERNEL_SCREENED)
     out["plain-per-job-fp64"] = stream_run(E.PRECISION_FP64, E.KERNEL_REFERENCE_CHAIN)
     out["offered_pairs_per_s"] = out["batched-fp64"]["pairs"] / float(arrivals[-1])
-    for k in ("batched-fp64", "batched-fp32w"):
+    for k in ("batched-fp64", "batched-fp32w", "batched-df64"):
         out[k]["speedup_vs_plain"] = (out[k]["pairs_per_s"] /
                                       out["plain-per-job-fp64"]["pairs_per_s"])
     return out
@@ -868,7 +872,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="central", choices=["central", "medium", "small"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32w"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32w", "df64"])
     ap.add_argument("--kernel", default="screened", choices=["screened", "reference-chain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -906,7 +910,8 @@ def main() -> None:
         dist.init_process_group("nccl")
 
     p = workload_params(args.workload)
-    prec = E.PRECISION_FP64 if args.precision == "fp64" else E.PRECISION_FP32W
+    prec = {"fp64": E.PRECISION_FP64, "fp32w": E.PRECISION_FP32W,
+            "df64": E.PRECISION_DF64}[args.precision]
     n_groups = args.warmup + args.steps
     groups = make_workload(args.workload, seed=1 + rank, max_groups=n_groups)
     dev = torch.device("cuda", local)
@@ -1011,10 +1016,13 @@ def main() -> None:
     if not args.no_plain and kern == E.KERNEL_SCREENED:
         plain = time_variant(E.KERNEL_REFERENCE_CHAIN, E.PRECISION_FP64, 1,
                              "reference-chain (FP64 reference order on every pair)", False)
-        other = E.PRECISION_FP32W if prec == E.PRECISION_FP64 else E.PRECISION_FP64
-        variants["batched-fp32w" if other == E.PRECISION_FP32W else "batched-fp64"] = \
-            time_variant(E.KERNEL_SCREENED, other, 2,
-                         "batched persistent, %s" % ("FP32 weights" if other else "FP64"), True)
+        labels = {E.PRECISION_FP64: ("batched-fp64", "FP64"),
+                  E.PRECISION_FP32W: ("batched-fp32w", "FP32 weights"),
+                  E.PRECISION_DF64: ("batched-df64", "double-float values")}
+        for other in labels:
+            if other != prec:
+                variants[labels[other][0]] = time_variant(
+                    E.KERNEL_SCREENED, other, 2, "batched persistent, " + labels[other][1], True)
         variants["grid-" + args.precision] = time_variant(
             E.KERNEL_SCREENED_GRID, prec, 1,
             "screened, one launch per list, no sorting or culling", False)
@@ -1121,7 +1129,7 @@ def main() -> None:
         cpu = cpu_baseline(groups[0], p, nthreads=1)
 
     uneven = serving = ingest = average = None
-    balance = fits = precision = None
+    balance = fits = precision = precision_df = None
     if not args.no_ingest and rank == 0:
         ingest = ingest_leg()
         average = average_leg()
@@ -1131,6 +1139,7 @@ def main() -> None:
         fits = fit_leg()
     if not args.no_precision and rank == 0 and args.workload == "central":
         precision = precision_leg(E, groups, p, local)
+        precision_df = precision_leg(E, groups, p, local, other=E.PRECISION_DF64)
     small = None
     if not args.no_uneven and rank == 0 and args.workload == "central":
         small = small_leg(E, torch, dev, stream, flush, local)
@@ -1145,7 +1154,8 @@ def main() -> None:
                 "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64" if args.precision == "fp64" else "f64 bins / f32 weights",
+                "dtype": {"fp64": "f64", "fp32w": "f64 bins / f32 weights",
+                          "df64": "f64 bins / double-float (2 x f32) values"}[args.precision],
                 "data": "synthetic",
                 "config": {"workload": args.workload,
                            "events": {"central": 1000, "medium": 300}.get(args.workload, 100),
@@ -1177,6 +1187,7 @@ def main() -> None:
                 "balance_function": balance,
                 "radii_fit": fits,
                 "precision_fp32w_vs_fp64": precision,
+                "precision_df64_vs_fp64": precision_df,
                 "stats": st}
         print(json.dumps(line))
     eng.close()

@@ -203,11 +203,13 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
 
 // Resident CTAs per SM (register budget 65536 / (128 x CTAs)): measured on
 // GB300, the FP64 form of the same-event kernel is fastest at 5 (its FP64
-// values need the registers), the FP32-weight form and the mixed-event
-// kernel at 6.
+// values need the registers), the double-float form at 4 (118 registers, no
+// spills: 167 ms per central group, against 194 ms at 5 and 234 ms at 6,
+// where its 80 registers spill in the pair loop), the FP32-weight form and
+// the mixed-event kernel at 6.
 template <int PREC>
 struct SameCtas {
-    static constexpr int value = PREC == 0 ? 5 : 6;
+    static constexpr int value = PREC == 1 ? 6 : (PREC == 2 ? 4 : 5);
 };
 constexpr int kMixedCtas = 6;
 
@@ -220,6 +222,7 @@ __global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(D
     __shared__ unsigned item;
     __shared__ double2 cs[COS_TABLE];
     if (PREC == 0) fill_cos_table(cs);
+    if (PREC == 2) fill_df_table(reinterpret_cast<float4 *>(cs));
     const unsigned stop = min(end, min(b.n_items[0], b.same_cap));
     for (;;) {
         if (threadIdx.x == 0) item = base + atomicAdd(b.item_next, 1u);
@@ -350,7 +353,7 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
     const int prec = d.precision;
     // same-event items (chunked for the FP32-weight form)
     const unsigned upper = b.same_cap;
-    if (chunk == 0 || prec == 0) chunk = upper;
+    if (chunk == 0 || prec != 1) chunk = upper;
     if (marks && (e = cudaEventRecord(marks[0], st)) != cudaSuccess) return e;
     for (unsigned base = 0; base < upper; base += chunk) {
         const unsigned end =
@@ -363,17 +366,22 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
             else if (az) HBT_P(true, false, 0);
             else if (boost) HBT_P(false, true, 0);
             else HBT_P(false, false, 0);
-        } else {
+        } else if (prec == 1) {
             if (az && boost) HBT_P(true, true, 1);
             else if (az) HBT_P(true, false, 1);
             else if (boost) HBT_P(false, true, 1);
             else HBT_P(false, false, 1);
+        } else {
+            if (az && boost) HBT_P(true, true, 2);
+            else if (az) HBT_P(true, false, 2);
+            else if (boost) HBT_P(false, true, 2);
+            else HBT_P(false, false, 2);
         }
 #undef HBT_P
         if (e != cudaSuccess) return e;
-        if (prec && !b.devs) {
+        if (prec == 1 && !b.devs) {
             if ((e = launch_merge(d, st, b.n_items, base)) != cudaSuccess) return e;
-        } else if (prec) {
+        } else if (prec == 1) {
             for (int k = 0; k < n_host_devs; k++)
                 if ((e = launch_merge(host_devs[k], st, b.n_items, base)) != cudaSuccess) return e;
         }

@@ -527,7 +527,9 @@ namespace hbt {
 
 bool params_valid(const hbt_params &p) {
     if (p.qnpts < 2 || p.n_KT < 2 || p.n_Kphi < 1 || p.qnpts > 1024) return false;
-    if (p.precision != HBT_PRECISION_FP64 && p.precision != HBT_PRECISION_FP32W) return false;
+    if (p.precision != HBT_PRECISION_FP64 && p.precision != HBT_PRECISION_FP32W &&
+        p.precision != HBT_PRECISION_DF64)
+        return false;
     if (p.kernel != HBT_KERNEL_SCREENED && p.kernel != HBT_KERNEL_REFERENCE_CHAIN &&
         p.kernel != HBT_KERNEL_SCREENED_GRID)
         return false;

@@ -19,6 +19,7 @@ __global__ void __launch_bounds__(FT) k_same_screened(Device d, long long n, Col
     __shared__ TileSmem sm;
     __shared__ double2 cs[COS_TABLE];
     if (PREC == 0) fill_cos_table(cs);
+    if (PREC == 2) fill_df_table(reinterpret_cast<float4 *>(cs));
     long long ti, tj;
     tri_tile((long long)blockIdx.x + d.block_offset, ti, tj);
     same_tile_pair<AZ, BOOST, PREC>(d, sm, cs, c.p, nullptr, n, ti * FT, tj * FT);
@@ -81,8 +82,8 @@ cudaError_t launch_same_fast(const Device &d0, long long n, const double *const 
     const int prec = d0.precision;
     // FP32 partials are merged every `chunk` CTAs to bound the number of
     // terms an FP32 partial bin accumulates
-    long long chunk = prec ? (d0.merge_chunk_blocks > 0 ? d0.merge_chunk_blocks : blocks)
-                           : blocks;
+    long long chunk = prec == 1 ? (d0.merge_chunk_blocks > 0 ? d0.merge_chunk_blocks : blocks)
+                                : blocks;
     chunk = min(chunk, 0x7fffffffLL);
     for (long long b0 = 0; b0 < blocks; b0 += chunk) {
         Device d = d0;
@@ -94,16 +95,21 @@ cudaError_t launch_same_fast(const Device &d0, long long n, const double *const 
             else if (az) HBT_SAME(true, false, 0);
             else if (boost) HBT_SAME(false, true, 0);
             else HBT_SAME(false, false, 0);
-        } else {
+        } else if (prec == 1) {
             if (az && boost) HBT_SAME(true, true, 1);
             else if (az) HBT_SAME(true, false, 1);
             else if (boost) HBT_SAME(false, true, 1);
             else HBT_SAME(false, false, 1);
+        } else {
+            if (az && boost) HBT_SAME(true, true, 2);
+            else if (az) HBT_SAME(true, false, 2);
+            else if (boost) HBT_SAME(false, true, 2);
+            else HBT_SAME(false, false, 2);
         }
 #undef HBT_SAME
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        if (prec) {
+        if (prec == 1) {
             e = launch_merge(d0, st);
             if (e != cudaSuccess) return e;
         }

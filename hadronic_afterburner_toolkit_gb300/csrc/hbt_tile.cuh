@@ -400,6 +400,148 @@ __device__ __forceinline__ float4 values32_split(const Screen &S, const float2 *
     return v;
 }
 
+// ---- Double-float form (HBT_PRECISION_DF64): the summed values of a binned
+// same-event pair to FP64-class accuracy with FP32-pipe arithmetic.  The
+// inputs are split columns; the four momentum columns are split after
+// subtracting an FP32 offset per tile (the momentum of the tile's first
+// row), so their splitting error is 2^-48 of the distance to that row (the
+// tiles are compact in momentum) instead of 2^-48 of the momentum, which
+// would be the largest term of the phase error.
+
+// a + b of two split values.
+__device__ __forceinline__ FF ff_sum(float2 a, float2 b) {
+    const FF s = two_sum(a.x, b.x);
+    return two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.y, b.y)));
+}
+
+__device__ __forceinline__ FF ff_mul_f(FF a, float b) {
+    const float p = __fmul_rn(a.h, b);
+    float e = __fmaf_rn(a.h, b, -p);
+    e = __fmaf_rn(a.l, b, e);
+    return fast_two_sum(p, e);
+}
+
+// 1 / sqrt(x): the FP32 estimate y0 and one Newton step carried in
+// double-float.  With u = x y0^2 = 1 + e (|e| ~ 2^-22, u.h - 1 exact),
+// 1 / sqrt(x) = y0 (1 - e / 2 + 3 e^2 / 8 - ...): relative error about 2^-46.
+__device__ __forceinline__ FF ff_rsqrt(FF x) {
+    const float y0 = rsqrtf(x.h);
+    const FF u = ff_mul_f(ff_mul_f(x, y0), y0);
+    const float e = __fadd_rn(__fsub_rn(u.h, 1.0f), u.l);
+    return fast_two_sum(y0, __fmul_rn(__fmul_rn(y0, e), __fmaf_rn(0.375f, e, -0.5f)));
+}
+
+// Table of cos(k / 64) and sin(k / 64), |k| <= 51, as split pairs
+// (cos hi, cos lo, sin hi, sin lo), filled by each CTA of the double-float
+// same-event kernels from the FP64 sincos.
+constexpr int DF_TABLE_HALF = 51;
+constexpr int DF_TABLE = 2 * DF_TABLE_HALF + 1;
+__device__ __forceinline__ void fill_df_table(float4 *t) {
+    for (int k = threadIdx.x; k < DF_TABLE; k += blockDim.x) {
+        double s, c;
+        sincos((k - DF_TABLE_HALF) / 64.0, &s, &c);
+        const float2 cc = split(c), ss = split(s);
+        t[k] = make_float4(cc.x, cc.y, ss.x, ss.y);
+    }
+}
+
+// cos of a double-float phase, to about 5e-15 absolute (the table's 48-bit
+// values), for |ph| < 3200 (|q.dx| / hbarC is a few hundred at most; beyond,
+// the FP64 cos).  Cody-Waite reduction by quarter periods x = ph - j pi / 2
+// with pi / 2 in four FP32 parts: the first two have 12 significant bits
+// (j times them is exact for |j| < 2^11), the third goes through an FMA
+// two-product and the fourth is below 2^-57, so x carries about 2^-48
+// absolute error; |x| <= pi / 4.  Then the table point t = k / 64 nearest x
+// (exact in FP32) and d = x - t, |d| <= 1 / 128:
+//   cos(x + j pi / 2) = A cos d + B sin d,
+// (A, B) = (C, -S), (-S, -C), (-C, S), (S, C) for j mod 4 = 0..3 with
+// C = cos t, S = sin t; cos d - 1 = -d^2 / 2 + d^4 / 24 and
+// sin d - d = d^3 (-1 / 6 + d^2 / 120) (truncations below 3.2e-16 and
+// 4e-19), the d^2 and d^3 terms in double-float.
+__device__ __forceinline__ double df_cos(const float4 *tab, FF ph) {
+    const float j = rintf(ph.h * 0.63661977f);  // 2 / pi
+    if (!(fabsf(j) < 2048.0f)) return cos((double)ph.h + (double)ph.l);
+    const float t1 = __fmaf_rn(-j, 1.57080078125f, ph.h);  // exact
+    const FF s1 = two_sum(t1, __fmul_rn(-j, -4.453584551811218e-06f));  // product exact
+    const float p3 = __fmul_rn(-j, -8.705515752716053e-10f);
+    const float e3 = __fmaf_rn(-j, -8.705515752716053e-10f, -p3);
+    const FF s2 = two_sum(s1.h, p3);
+    const FF u = two_sum(s2.h, ph.l);
+    const float rest = __fadd_rn(__fadd_rn(s1.l, s2.l),
+                                 __fadd_rn(e3, __fmul_rn(-j, 5.721188916458728e-18f)));
+    const FF x = fast_two_sum(u.h, __fadd_rn(u.l, rest));
+    const float k = rintf(x.h * 64.0f);
+    const FF dd = two_sum(__fsub_rn(x.h, k * 0.015625f), x.l);  // x.h - k / 64 exact
+    const FF d2 = ff_mul(dd, dd);
+    const float c4 = __fmul_rn(__fmul_rn(d2.h, d2.h), 1.0f / 24.0f);
+    const FF cm = {__fmul_rn(d2.h, -0.5f), __fadd_rn(__fmul_rn(d2.l, -0.5f), c4)};
+    // -1 / 6 as a split pair, plus d^2 / 120
+    const FF kq = fast_two_sum(-0.1666666716337204f,
+                               __fadd_rn(4.967053879312289e-09f, d2.h * (1.0f / 120.0f)));
+    const FF sd = ff_add(dd, ff_mul(ff_mul(d2, dd), kq));
+    const float4 e = tab[(int)k + DF_TABLE_HALF];
+    const int quad = ((int)j) & 3;
+    FF A, B;
+    if (quad == 0) {
+        A = FF{e.x, e.y};
+        B = FF{-e.z, -e.w};
+    } else if (quad == 1) {
+        A = FF{-e.z, -e.w};
+        B = FF{-e.x, -e.y};
+    } else if (quad == 2) {
+        A = FF{-e.x, -e.y};
+        B = FF{e.z, e.w};
+    } else {
+        A = FF{e.z, e.w};
+        B = FF{e.x, e.y};
+    }
+    const FF r = ff_add(A, ff_add(ff_mul(A, cm), ff_mul(B, sd)));
+    return (double)r.h + (double)r.l;
+}
+
+__device__ __forceinline__ double ff_double(FF a) { return (double)a.h + (double)a.l; }
+
+// Summed values of a binned pair in the double-float form, for the pair as
+// stored (first = a from the i-tile, second = b from the j-tile): a, b are
+// the eight split columns (momenta relative to the tiles' offsets oa, ob),
+// results as FP64, q_out, q_side, q_long negated when `neg` (the pair's
+// reference orientation is (b, a)).  The same expressions as values64, each
+// operation in double-float; q_out, q_side, q_long to about 1e-15 relative,
+// the phase to 2^-48 of its terms.
+template <bool BOOST>
+__device__ __forceinline__ void values_df(const Screen &S, const float4 *tab, const float2 *a,
+                                          const float2 *b, const float *oa, const float *ob,
+                                          bool neg, double &qo, double &qs, double &ql,
+                                          double &w) {
+    FF dp[4], sp[4];
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        dp[f] = ff_add(ff_diff(a[f], b[f]), two_sum(oa[f], -ob[f]));
+        if (f < 2 || BOOST) sp[f] = ff_add(ff_sum(a[f], b[f]), two_sum(oa[f], ob[f]));
+    }
+    const FF inv = ff_rsqrt(ff_add(ff_mul(sp[0], sp[0]), ff_mul(sp[1], sp[1])));
+    FF vo = ff_mul(ff_add(ff_mul(dp[0], sp[0]), ff_mul(dp[1], sp[1])), inv);
+    FF vs = ff_mul(ff_add(ff_mul(dp[1], sp[0]), ff_neg(ff_mul(dp[0], sp[1]))), inv);
+    FF vl = dp[2];
+    if (BOOST) {
+        const FF m2 = ff_mul(ff_add(sp[3], ff_neg(sp[2])), ff_add(sp[3], sp[2]));
+        vl = ff_mul(ff_add(ff_mul(sp[3], dp[2]), ff_neg(ff_mul(sp[2], dp[3]))), ff_rsqrt(m2));
+    }
+    if (neg) {
+        vo = ff_neg(vo);
+        vs = ff_neg(vs);
+        vl = ff_neg(vl);
+    }
+    qo = ff_double(vo);
+    qs = ff_double(vs);
+    ql = ff_double(vl);
+    FF ph = ff_mul(dp[3], ff_diff(a[7], b[7]));
+    ph = ff_add(ph, ff_neg(ff_mul(dp[0], ff_diff(a[4], b[4]))));
+    ph = ff_add(ph, ff_neg(ff_mul(dp[1], ff_diff(a[5], b[5]))));
+    ph = ff_add(ph, ff_neg(ff_mul(dp[2], ff_diff(a[6], b[6]))));
+    w = df_cos(tab, ff_mul(ph, FF{S.hc_h, S.hc_l}));
+}
+
 // Shared memory of one tile pair.
 struct TileSmem {
     // same-event tiles: FP64 columns (FP64 form) or split columns (hi, lo
@@ -415,6 +557,7 @@ struct TileSmem {
     // undecided, slot) bits, y = q bin (bin_entry)
     uint2 queue2[FT / 32][QCAP];
     unsigned oi[FT], oj[FT];  // original list positions (pair orientation)
+    float offi[4], offj[4];   // double-float form: the tiles' momentum offsets
 };
 
 // Entry of the second same-event queue.
@@ -479,6 +622,17 @@ __device__ __noinline__ void undecided_pair32(const Device &d, const double *A, 
     }
 }
 
+// A same-event pair of the double-float form that the screens left
+// undecided: the reference chain decides and bins it with FP64 values.  Out
+// of line, so that the chain's registers do not spill in the pair loop.
+static __device__ __noinline__ void undecided_pair64(const Device &d, const double *A,
+                                                     const double *B, long long i, long long j,
+                                                     long long n) {
+    const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2], B[3],
+                                         A + 4, B + 4);
+    consume<false, MODE_FAST>(d, i, j, n, n, full);
+}
+
 // Same-event pairs of the tiles starting at i0 and j0 (i0 <= j0) of one list
 // of n particles with columns c = px py pz E x y z t.  Every unordered pair
 // is visited once (position j > i); it is oriented as the reference orients
@@ -503,7 +657,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
                                  (float)sm.si[3][tid]);
         sm.fj[tid] = make_float4((float)sm.sj[0][tid], (float)sm.sj[1][tid], (float)sm.sj[2][tid],
                                  (float)sm.sj[3][tid]);
-    } else {
+    } else if (PREC == 1) {
         for (int f = 0; f < 8; f++) {
             spi[f][tid] = split((i0 + tid < n) ? c[f][i0 + tid] : 0.0);
             spj[f][tid] = split((j0 + tid < n) ? c[f][j0 + tid] : 0.0);
@@ -511,6 +665,28 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
         // the high parts are the FP32 roundings of the momenta
         sm.fi[tid] = make_float4(spi[0][tid].x, spi[1][tid].x, spi[2][tid].x, spi[3][tid].x);
         sm.fj[tid] = make_float4(spj[0][tid].x, spj[1][tid].x, spj[2][tid].x, spj[3][tid].x);
+    } else {
+        // double-float form: momenta split relative to the tile's first row
+        double vi[8], vj[8];
+        for (int f = 0; f < 8; f++) {
+            vi[f] = (i0 + tid < n) ? c[f][i0 + tid] : 0.0;
+            vj[f] = (j0 + tid < n) ? c[f][j0 + tid] : 0.0;
+        }
+        for (int f = 0; f < 4; f++) {
+            const float oi = (float)c[f][i0], oj = (float)c[f][j0];
+            if (tid == 0) {
+                sm.offi[f] = oi;
+                sm.offj[f] = oj;
+            }
+            spi[f][tid] = split(vi[f] - (double)oi);
+            spj[f][tid] = split(vj[f] - (double)oj);
+        }
+        for (int f = 4; f < 8; f++) {
+            spi[f][tid] = split(vi[f]);
+            spj[f][tid] = split(vj[f]);
+        }
+        sm.fi[tid] = make_float4((float)vi[0], (float)vi[1], (float)vi[2], (float)vi[3]);
+        sm.fj[tid] = make_float4((float)vj[0], (float)vj[1], (float)vj[2], (float)vj[3]);
     }
     sm.oi[tid] = orig ? (i0 + tid < n ? orig[i0 + tid] : 0u) : (unsigned)(i0 + tid);
     sm.oj[tid] = orig ? (j0 + tid < n ? orig[j0 + tid] : 0u) : (unsigned)(j0 + tid);
@@ -559,6 +735,25 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
             atomicAdd(d.h.cnt + at, 1ull);
             return;
         }
+        if (PREC == 2 && slot >= 0) {
+            float2 a[8], b[8];
+#pragma unroll
+            for (int f = 0; f < 8; f++) {
+                a[f] = spi[f][qi];
+                b[f] = spj[f][qj];
+            }
+            double vo, vs, vl, vw;
+            values_df<BOOST>(d.s, reinterpret_cast<const float4 *>(cs), a, b, sm.offi, sm.offj,
+                             swap, vo, vs, vl, vw);
+            const long long at = (long long)slot * d.g.q3 + bin;
+            Sums *h = d.h.sums + at;
+            atomicAdd(&h->qo, vo);
+            atomicAdd(&h->qs, vs);
+            atomicAdd(&h->ql, vl);
+            atomicAdd(&h->w, vw);
+            atomicAdd(d.h.cnt + at, 1ull);
+            return;
+        }
         // FP64 form, or a pair the window screen left undecided: the pair in
         // the reference's orientation, from the FP64 tile or (FP32-weight
         // form) the FP64 columns themselves
@@ -586,12 +781,16 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
             undecided_pair32<BOOST>(d, A, B, i0 + qi, j0 + qj, n);
             return;
         }
+        if (PREC == 2) {
+            undecided_pair64(d, A, B, i0 + qi, j0 + qj, n);
+            return;
+        }
         {
             // undecided somewhere: the reference chain decides (and may hand
             // a K_phi edge to the host)
             const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2],
                                                  B[3], A + 4, B + 4);
-            if (PREC == 0 || full.ev3 != 1) {
+            if (PREC != 1 || full.ev3 != 1) {
                 consume<false, MODE_FAST>(d, i0 + qi, j0 + qj, n, n, full);
             } else {
                 const long long at = (long long)full.slot * d.g.q3 + full.bin;

@@ -21,6 +21,7 @@ STATUS = {0: "HBT_OK", 1: "HBT_ERR_INVALID", 2: "HBT_ERR_CUDA", 3: "HBT_ERR_NOME
           4: "HBT_ERR_TIMEOUT", 5: "HBT_ERR_DEVICE", 6: "HBT_ERR_STATE"}
 PRECISION_FP64 = 0
 PRECISION_FP32W = 1
+PRECISION_DF64 = 2
 KERNEL_SCREENED = 0
 KERNEL_REFERENCE_CHAIN = 1
 KERNEL_SCREENED_GRID = 2

@@ -45,9 +45,13 @@ typedef enum hbt_status {
 /* Numerics of the weights and q sums. */
 typedef enum hbt_precision {
     HBT_PRECISION_FP64 = 0, /* plain form: everything in FP64 */
-    HBT_PRECISION_FP32W = 1 /* cos(q.dx) weight and q sums in FP32 partials,
-                               merged into FP64 bins with Kahan compensation;
-                               bins and counts stay exact */
+    HBT_PRECISION_FP32W = 1, /* cos(q.dx) weight and q sums in FP32 partials,
+                                merged into FP64 bins with Kahan compensation;
+                                bins and counts stay exact */
+    HBT_PRECISION_DF64 = 2   /* same-event weight and q sums computed in
+                                double-float arithmetic (value = hi + lo, two
+                                FP32 numbers) on the FP32 pipe and added to
+                                the FP64 bins; bins and counts stay exact */
 } hbt_precision;
 
 /* The HBT keys of parameters.dat that shape the histograms

@@ -7,7 +7,8 @@ seeded partner draws and rotations, mixed pairs).
 
 Tolerances: counts, denominators and pair counters identical; FP64 sums
 within tests/parity.py's RTOL (1e-12 per count); FP32-weight sums within
-RTOL32 = 1e-5 per count against the FP64 oracle and between runs.
+RTOL32 = 1e-5 per count against the FP64 oracle and between runs;
+double-float sums within RTOL_DF = 1e-11 per count.
 """
 import numpy as np
 import pytest
@@ -18,7 +19,9 @@ import parity
 pytestmark = pytest.mark.gpu
 
 RTOL32 = 1e-5
+RTOL_DF = 1e-11  # the double-float form's stated bound (test_precision_gpu.py)
 FP32W = 1
+DF64 = 2
 
 # name -> request: analysis parameters and the buffer's shape
 REQUESTS = {
@@ -30,6 +33,8 @@ REQUESTS = {
                  mu=150.0, partners=2, seed=13),
     "fp32w": dict(params=dict(qnpts=13, n_KT=4, precision=FP32W), n_events=6, mu=100.0,
                   partners=2, seed=14),
+    "df64": dict(params=dict(qnpts=13, n_KT=4, precision=DF64), n_events=6, mu=100.0,
+                 partners=2, seed=20),
     "cap_solo": dict(params=dict(qnpts=11, n_KT=3, needed_number_of_pairs=1500), n_events=4,
                      mu=60.0, partners=2, seed=15),
     "qinv_solo": dict(params=dict(qnpts=11, n_KT=3, invariant_radius_flag=1), n_events=3,
@@ -76,7 +81,7 @@ def _oracle_buffer(req, ev):
 
 
 def _check(res, ref, p, what):
-    rtol = RTOL32 if p["precision"] == FP32W else parity.RTOL
+    rtol = {FP32W: RTOL32, DF64: RTOL_DF}.get(p["precision"], parity.RTOL)
     try:
         return parity.compare(res, ref, _qscale(p), rtol=rtol)
     except AssertionError as e:
