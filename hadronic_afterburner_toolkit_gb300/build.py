@@ -44,7 +44,7 @@ GPU_UNITS = {
     "hbt_server.cu": ["--fmad=false"],
     "hbt_bf.cu": ["--fmad=false"],
     "hbt_fit.cu": [],
-    "hbt_check.cu": [],
+    "hbt_check.cu": ["--fmad=false"],
 }
 
 

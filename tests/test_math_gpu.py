@@ -62,3 +62,26 @@ def test_table_exp_against_libm():
     np.testing.assert_allclose(got[fin], want[fin], rtol=1e-15, atol=1e-320)
     np.testing.assert_array_equal(got[~fin], want[~fin])
     assert np.isnan(_dev(1, [np.nan])[0])
+
+
+def test_df_cos_against_libm():
+    """The double-float form's cos (csrc/hbt_tile.cuh df_cos) of x split into
+    hi = (float)x, lo = (float)(x - hi), against libm's cos of hi + lo (exact
+    in FP64): within 1e-14 absolute for |x| < 3200 (the table's 48-bit values
+    and the reduction), quarter-period and table-point edges included;
+    beyond, it calls the device's FP64 cos."""
+    rng = np.random.default_rng(3)
+    k = np.arange(-2000, 2000)
+    x = np.concatenate([rng.uniform(-3200, 3200, 200000), rng.uniform(-1, 1, 50000),
+                        k * (np.pi / 2), k * (np.pi / 2) + 1e-9, k * (np.pi / 2) + np.pi / 4,
+                        np.arange(-51, 52) / 64.0 + 1 / 128.0,
+                        [0.0, -0.0, 1e-30, -1e-30, np.pi, -np.pi, 3199.9, -3199.9]])
+    h = x.astype(np.float32)
+    xs = h.astype(np.float64) + (x - h.astype(np.float64)).astype(np.float32).astype(np.float64)
+    got = _dev(2, x)
+    assert np.max(np.abs(got - np.cos(xs))) < 1e-14
+    far = np.concatenate([rng.uniform(3300, 1e5, 2000), -rng.uniform(3300, 1e5, 2000)])
+    hf = far.astype(np.float32)
+    xf = hf.astype(np.float64) + (far - hf.astype(np.float64)).astype(np.float32).astype(np.float64)
+    assert np.max(np.abs(_dev(2, far) - np.cos(xf))) < 1e-15
+    np.testing.assert_array_equal(np.isnan(_dev(2, [np.nan, np.inf])), [True, True])
