@@ -421,7 +421,7 @@ def uneven_leg(E, torch, dev, stream, flush, local, steps=2) -> dict:
 
 
 def small_leg(E, torch, dev, stream, flush, local, steps=3) -> dict:
-    """Config 1, the reference's CPU-runnable case (100 pi+ events,
+    """The reference's CPU-runnable case (100 pi+ events,
     Poisson(500), oversample 10 -> 10 groups of ~5k particles, 5 rotated
     partners, 41^3 grid, 4 K_T bins): every group and partner in one batched
     FP64 launch per step, against the oracle on one host core."""
