@@ -98,6 +98,19 @@ def test_dropin_reference_chain_kernel(name, tmp_path):
         compare_files(open(os.path.join(res, f)).read(), want[f], f)
 
 
+@pytest.mark.parametrize("name", ["basic", "kphi"])
+def test_dropin_double_float_precision(name, tmp_path):
+    """hbt_precision=2 (same-event values in double-float arithmetic, at most
+    1e-11 per pair from the FP64 sums) gives the same files within the
+    printed precision."""
+    res, _ = run_dropin(name, str(tmp_path), ["hbt_precision=2"])
+    want = _golden(name)
+    got = sorted(f for f in os.listdir(res) if f.startswith("HBT_correlation"))
+    assert got == sorted(want)
+    for f in want:
+        compare_files(open(os.path.join(res, f)).read(), want[f], f)
+
+
 def test_dropin_missing_key_is_a_parameter_error(tmp_path):
     name = "basic"
     src = os.path.join(oracle_lib.GOLDEN, name)
