@@ -508,12 +508,24 @@ hbt_status stage(hbt_ctx *c, const double *const *src, const long long *len, int
     size_t off = 0;
     for (int f = 0; f < ncols; f++) {
         dst[f] = base + off;
-        if (len[f] > 0) {
-            if (!src[f]) return fail(c, HBT_ERR_INVALID, "null particle array");
-            CU(cudaMemcpyAsync(base + off, src[f], len[f] * sizeof(double),
-                               cudaMemcpyHostToDevice, c->stream));
-        }
+        if (len[f] > 0 && !src[f]) return fail(c, HBT_ERR_INVALID, "null particle array");
         off += (size_t)((len[f] + 31) / 32 * 32);
+    }
+    // columns laid out in host memory as they will be on the device (each a
+    // multiple of 32 doubles, back to back) go over in one copy per run
+    for (int f = 0; f < ncols;) {
+        if (len[f] <= 0) {
+            f++;
+            continue;
+        }
+        int g = f;
+        while (g + 1 < ncols && len[g + 1] > 0 &&
+               src[g] + (len[g] + 31) / 32 * 32 == src[g + 1])
+            g++;
+        const size_t n = (size_t)(dst[g] - dst[f]) + (size_t)len[g];
+        CU(cudaMemcpyAsync(const_cast<double *>(dst[f]), src[f], n * sizeof(double),
+                           cudaMemcpyHostToDevice, c->stream));
+        f = g + 1;
     }
     // the caller's arrays may be reused once the copies are done
     CU(cudaEventRecord(c->staged, c->stream));

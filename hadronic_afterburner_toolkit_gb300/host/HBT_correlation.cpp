@@ -112,7 +112,12 @@ void HBT_correlation::calculate_HBT_correlation_function(
     number_of_oversample_events_ = nev;
     std::vector<int> event_list(nev);
     for (int k = 0; k < nev; k++) event_list[k] = k;
-    combine_and_bin_particle_pairs(event_list);
+    // the buffer's same-event list and every event's mixed-event lists are
+    // gathered in the reference's order (same RNG draws) and binned in one
+    // batched launch; hbt_bin_batch keeps the reference's job order when a
+    // pair cap can bind
+    batch_begin();
+    gather_same(event_list);
 
     const int mixed_nev = particle_list->get_number_of_mixed_events();
     number_of_mixed_events_ =
@@ -126,8 +131,9 @@ void HBT_correlation::calculate_HBT_correlation_function(
             while (iev == id && mixed_nev != 1) id = ran_gen_ptr_->rand_int_uniform() % mixed_nev;
             partners[k] = id;
         }
-        combine_and_bin_particle_pairs_mixed_events(iev, partners);
+        gather_mixed(iev, partners);
     }
+    batch_flush();
 }
 
 // src/HBT_correlation.cpp:233-249
@@ -139,51 +145,103 @@ void HBT_correlation::calculate_flow_event_plane_angle(int n_order) {
     psi_ref = sums.angle(n_order);
 }
 
-// Gather of src/HBT_correlation.cpp:254-285, pair loop on the GPU.
-void HBT_correlation::combine_and_bin_particle_pairs(std::vector<int> event_list) {
+// Host lists of a batch: every column occupies a multiple of 32 doubles of
+// one packed array, the layout the engine's staging copies to the device,
+// so the whole batch goes over in one copy.
+void HBT_correlation::batch_begin() {
+    pack_.clear();
+    pending_.clear();
+}
+
+size_t HBT_correlation::pack_column(long long n) {
+    const size_t at = pack_.size();
+    pack_.resize(at + static_cast<size_t>((n + 31) / 32 * 32), 0.0);
+    return at;
+}
+
+void HBT_correlation::batch_flush() {
+    std::vector<hbt_job> jobs;
+    jobs.reserve(pending_.size());
+    const double *base = pack_.data();
+    for (const PendingJob &pj : pending_) {
+        hbt_job j = {};
+        j.kind = pj.kind;
+        j.na = pj.na;
+        j.nb = pj.nb;
+        const double **a[8] = {&j.a.px, &j.a.py, &j.a.pz, &j.a.E,
+                               &j.a.x,  &j.a.y,  &j.a.z,  &j.a.t};
+        const double **b[4] = {&j.b.px, &j.b.py, &j.b.pz, &j.b.E};
+        for (int f = 0; f < (pj.kind == 0 ? 8 : 4); f++) *a[f] = base + pj.a[f];
+        if (pj.kind == 1)
+            for (int f = 0; f < 4; f++) *b[f] = base + pj.b[f];
+        jobs.push_back(j);
+    }
+    if (!jobs.empty())
+        check(hbt_bin_batch(ctx_, static_cast<int32_t>(jobs.size()), jobs.data()),
+              "hbt_bin_batch");
+    batch_begin();
+}
+
+// Gather of src/HBT_correlation.cpp:254-285 into the batch.
+void HBT_correlation::gather_same(const std::vector<int> &event_list) {
     const double ycut_max = tanh(Krap_max_);
     const double ycut_min = tanh(Krap_min_);
-    for (auto &v : s8_) v.clear();
+    long long n = 0;
+    for (int j = 0; j < number_of_oversample_events_; j++)
+        for (const particle_info &p : particle_list->event(event_list[j])) {
+            const double ratio = p.pz / p.E;
+            if (ratio > ycut_min && ratio < ycut_max) n++;
+        }
+    PendingJob pj = {};
+    pj.kind = 0;
+    pj.na = n;
+    for (int f = 0; f < 8; f++) pj.a[f] = pack_column(n);
+    long long k = 0;
     for (int j = 0; j < number_of_oversample_events_; j++)
         for (const particle_info &p : particle_list->event(event_list[j])) {
             const double ratio = p.pz / p.E;
             if (ratio > ycut_min && ratio < ycut_max) {
-                s8_[0].push_back(p.px);
-                s8_[1].push_back(p.py);
-                s8_[2].push_back(p.pz);
-                s8_[3].push_back(p.E);
-                s8_[4].push_back(p.x);
-                s8_[5].push_back(p.y);
-                s8_[6].push_back(p.z);
-                s8_[7].push_back(p.t);
+                const double v[8] = {p.px, p.py, p.pz, p.E, p.x, p.y, p.z, p.t};
+                for (int f = 0; f < 8; f++) pack_[pj.a[f] + k] = v[f];
+                k++;
             }
         }
-    const long long n = static_cast<long long>(s8_[0].size());
     if (echo_level_ > 5)
         std::cout << "[Info] number of pairs: " << (unsigned long long)(n * (n - 1) / 2)
                   << std::endl;
-    const hbt_soa8 soa = {s8_[0].data(), s8_[1].data(), s8_[2].data(), s8_[3].data(),
-                          s8_[4].data(), s8_[5].data(), s8_[6].data(), s8_[7].data()};
-    check(hbt_bin_same(ctx_, n, &soa), "hbt_bin_same");
+    pending_.push_back(pj);
 }
 
-// Gather and random rotation of src/HBT_correlation.cpp:466-552, pair loop
-// on the GPU.
-void HBT_correlation::combine_and_bin_particle_pairs_mixed_events(
-    int event_id1, std::vector<int> mixed_event_list) {
+// Gather and random rotation of src/HBT_correlation.cpp:466-552 into the
+// batch: one rotation angle drawn per partner event, in partner order.
+void HBT_correlation::gather_mixed(int event_id1, const std::vector<int> &mixed_event_list) {
     const double ycut_max = tanh(Krap_max_);
     const double ycut_min = tanh(Krap_min_);
-    for (auto &v : l1_) v.clear();
-    for (auto &v : l2_) v.clear();
+    PendingJob pj = {};
+    pj.kind = 1;
+    for (const particle_info &p : particle_list->event(event_id1)) {
+        const double ratio = p.pz / p.E;
+        if (ratio > ycut_min && ratio < ycut_max) pj.na++;
+    }
+    for (int f = 0; f < 4; f++) pj.a[f] = pack_column(pj.na);
+    long long k = 0;
     for (const particle_info &p : particle_list->event(event_id1)) {
         const double ratio = p.pz / p.E;
         if (ratio > ycut_min && ratio < ycut_max) {
-            l1_[0].push_back(p.px);
-            l1_[1].push_back(p.py);
-            l1_[2].push_back(p.pz);
-            l1_[3].push_back(p.E);
+            pack_[pj.a[0] + k] = p.px;
+            pack_[pj.a[1] + k] = p.py;
+            pack_[pj.a[2] + k] = p.pz;
+            pack_[pj.a[3] + k] = p.E;
+            k++;
         }
     }
+    for (int iev = 0; iev < number_of_mixed_events_; iev++)
+        for (const particle_info &p : particle_list->mixed_event(mixed_event_list[iev])) {
+            const double ratio = p.pz / p.E;
+            if (ratio > ycut_min && ratio < ycut_max) pj.nb++;
+        }
+    for (int f = 0; f < 4; f++) pj.b[f] = pack_column(pj.nb);
+    k = 0;
     for (int iev = 0; iev < number_of_mixed_events_; iev++) {
         const double random_rotation = ran_gen_ptr_->rand_uniform() * 2 * M_PI;
         const double cos_phi = cos(random_rotation);
@@ -191,21 +249,33 @@ void HBT_correlation::combine_and_bin_particle_pairs_mixed_events(
         for (const particle_info &p : particle_list->mixed_event(mixed_event_list[iev])) {
             const double ratio = p.pz / p.E;
             if (ratio > ycut_min && ratio < ycut_max) {
-                l2_[0].push_back(p.px * cos_phi - p.py * sin_phi);
-                l2_[1].push_back(p.px * sin_phi + p.py * cos_phi);
-                l2_[2].push_back(p.pz);
-                l2_[3].push_back(p.E);
+                pack_[pj.b[0] + k] = p.px * cos_phi - p.py * sin_phi;
+                pack_[pj.b[1] + k] = p.px * sin_phi + p.py * cos_phi;
+                pack_[pj.b[2] + k] = p.pz;
+                pack_[pj.b[3] + k] = p.E;
+                k++;
             }
         }
     }
-    const long long n1 = static_cast<long long>(l1_[0].size());
-    const long long n2 = static_cast<long long>(l2_[0].size());
     if (echo_level_ > 5)
-        std::cout << "[Info] number of mixed pairs: " << (unsigned long long)(n1 * n2)
+        std::cout << "[Info] number of mixed pairs: " << (unsigned long long)(pj.na * pj.nb)
                   << std::endl;
-    const hbt_soa4 a = {l1_[0].data(), l1_[1].data(), l1_[2].data(), l1_[3].data()};
-    const hbt_soa4 b = {l2_[0].data(), l2_[1].data(), l2_[2].data(), l2_[3].data()};
-    check(hbt_bin_mixed(ctx_, n1, &a, n2, &b), "hbt_bin_mixed");
+    pending_.push_back(pj);
+}
+
+// Pair loop of src/HBT_correlation.cpp:282-461 on the GPU.
+void HBT_correlation::combine_and_bin_particle_pairs(std::vector<int> event_list) {
+    batch_begin();
+    gather_same(event_list);
+    batch_flush();
+}
+
+// Pair loop of src/HBT_correlation.cpp:554-689 on the GPU.
+void HBT_correlation::combine_and_bin_particle_pairs_mixed_events(
+    int event_id1, std::vector<int> mixed_event_list) {
+    batch_begin();
+    gather_mixed(event_id1, mixed_event_list);
+    batch_flush();
 }
 
 const HBT_correlation::HostHist &HBT_correlation::fetch() {

@@ -85,8 +85,21 @@ class HBT_correlation {
     int echo_level_;
 
     hbt_ctx *ctx_;
-    // host staging of the gathered lists (SoA)
-    std::vector<double> s8_[8], l1_[4], l2_[4];
+    // Gathered lists of the jobs of one batch: columns packed in one host
+    // array (each a multiple of 32 doubles, the engine's staging layout, so
+    // a batch is staged in one copy); jobs refer to columns by offset.
+    struct PendingJob {
+        int kind;          // 0 same-event (a, 8 columns), 1 mixed (a x b, 4 + 4)
+        long long na, nb;  // particles of a and b
+        size_t a[8], b[4]; // column offsets in pack_
+    };
+    std::vector<double> pack_;
+    std::vector<PendingJob> pending_;
+    void batch_begin();
+    size_t pack_column(long long n);
+    void batch_flush();
+    void gather_same(const std::vector<int> &event_list);
+    void gather_mixed(int event_id1, const std::vector<int> &mixed_event_list);
 
     // histograms copied back from the device for the writers
     struct HostHist;

@@ -50,6 +50,34 @@ double hbt_host_event_plane_angle(int64_t n, const double *px, const double *py,
     return sums.angle(n_order);
 }
 
+int64_t hbt_host_mixed_plan(int32_t seed, int32_t n_buffers, const int32_t *nev,
+                            const int32_t *mixed_nev, int32_t n_partners, int64_t cap,
+                            int32_t *partners, double *angles) {
+    if (n_buffers < 0 || cap < 0 || (n_buffers > 0 && (!nev || !mixed_nev))) return -1;
+    int64_t total = 0;
+    for (int b = 0; b < n_buffers; b++) {
+        if (nev[b] < 0 || mixed_nev[b] < 0 || (nev[b] > 0 && mixed_nev[b] == 0)) return -1;
+        const int nmix = n_partners > 0 ? n_partners : mixed_nev[b] / 2 + 1;
+        total += (int64_t)nev[b] * nmix;
+    }
+    if (total > cap || (total > 0 && (!partners || !angles))) return -1;
+    RandomUtil::Random rng(seed);
+    int64_t at = 0;
+    for (int b = 0; b < n_buffers; b++) {
+        const int nmix = n_partners > 0 ? n_partners : mixed_nev[b] / 2 + 1;
+        for (int iev = 0; iev < nev[b]; iev++) {
+            for (int k = 0; k < nmix; k++) {
+                int id = rng.rand_int_uniform() % mixed_nev[b];
+                while (iev == id && mixed_nev[b] != 1) id = rng.rand_int_uniform() % mixed_nev[b];
+                partners[at + k] = id;
+            }
+            for (int k = 0; k < nmix; k++) angles[at + k] = rng.rand_uniform() * 2 * M_PI;
+            at += nmix;
+        }
+    }
+    return at;
+}
+
 int hbt_host_scan_buffers(const char *param_file, const char *results_path, int32_t cap,
                           int32_t *nev, int64_t *n_particles, int32_t *mixed_nev,
                           int64_t *n_mixed_particles) {

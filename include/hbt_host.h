@@ -46,6 +46,25 @@ int hbt_host_write(const hbt_params *params, const char *path, int32_t eco_outpu
 double hbt_host_event_plane_angle(int64_t n, const double *px, const double *py,
                                   int32_t n_order);
 
+/* The mixed-event partner ids and rotation angles the drop-in draws for a
+ * run of n_buffers buffers from one RandomUtil::Random seeded with `seed`
+ * (HBT_correlation::calculate_HBT_correlation_function and
+ * combine_and_bin_particle_pairs_mixed_events, src/HBT_correlation.cpp
+ * :197-217 and :495-497): for buffer b and each of its nev[b] events in
+ * order, nmix partner ids (rand_int_uniform() % mixed_nev[b], redrawn while
+ * equal to the event when mixed_nev[b] != 1), then nmix angles
+ * rand_uniform() * 2 pi, with nmix = n_partners when > 0 (the optional key
+ * hbt_mixed_partners), else mixed_nev[b] / 2 + 1.  Entries are written in
+ * that order to partners[] and angles[] (sum over b of nev[b] * nmix
+ * each, at most `cap`).  The rotation of a partner's particles is
+ * px' = px cos(angle) - py sin(angle), py' = px sin(angle) + py cos(angle)
+ * with the C library's cos and sin.  For FFI callers that drive the engine
+ * themselves with the reference's partners.  Returns the number of entries,
+ * or -1 for invalid arguments or a too small `cap`. */
+int64_t hbt_host_mixed_plan(int32_t seed, int32_t n_buffers, const int32_t *nev,
+                            const int32_t *mixed_nev, int32_t n_partners, int64_t cap,
+                            int32_t *partners, double *angles);
+
 /* Reads the samples of a parameter file's HBT setup buffer by buffer with
  * the reference's reader rules (particleSamples, src/particleSamples.cpp),
  * without binning anything: for each buffer, the event count and particle

@@ -24,6 +24,9 @@ const double kHbarC = 0.197327053;  // GeV fm (src/parameters.h:4)
 struct Hist {
     // 3-D histograms, [slot][iqout][iqside][iqlong]
     std::vector<double> cnt, qo, qs, ql, num, den;
+    // sum of |cos(q.dx)| per 3-D bin: the scale of the numerator's rounding
+    // (precision comparisons); not part of the reference's output
+    std::vector<double> anum;
     // 1-D q_inv histograms, [iKT][iq]
     std::vector<double> qi_sum, qi_num, qi_cnt, qi_den;
     // pair counters per slot (3-D) and per K_T bin (q_inv)
@@ -37,6 +40,7 @@ struct Hist {
         ql.assign(nbins, 0.0);
         num.assign(nbins, 0.0);
         den.assign(nbins, 0.0);
+        anum.assign(nbins, 0.0);
         qi_sum.assign((int64_t)n_KT * qnpts, 0.0);
         qi_num.assign((int64_t)n_KT * qnpts, 0.0);
         qi_cnt.assign((int64_t)n_KT * qnpts, 0.0);
@@ -55,6 +59,7 @@ struct Hist {
             ql[i] += o.ql[i];
             num[i] += o.num[i];
             den[i] += o.den[i];
+            anum[i] += o.anum[i];
         }
         for (size_t i = 0; i < qi_sum.size(); i++) {
             qi_sum[i] += o.qi_sum[i];
@@ -227,6 +232,7 @@ inline void same_pair(const orc_ctx &c, Hist &h, const P8 &a, const P8 &b,
     h.qs[at] += q_s;
     h.ql[at] += q_l;
     h.num[at] += w;
+    h.anum[at] += fabs(w);
 }
 
 // One mixed-event pair: src/HBT_correlation.cpp:574-687.  Note the
@@ -511,6 +517,26 @@ void orc_process_buffer(orc_ctx *c, int32_t nev, const int64_t *off,
     }
 }
 
+int32_t orc_mixed_partners(const orc_ctx *c, int32_t mixed_nev) {
+    return c->p.number_of_mixed_events > 0 ? c->p.number_of_mixed_events : mixed_nev / 2 + 1;
+}
+
+int32_t orc_mixed_plan(orc_ctx *c, int32_t nev, int32_t mixed_nev, int32_t *partners,
+                       double *angles) {
+    // the draws of orc_process_buffer's mixed-event loop, in its order: per
+    // event the partner ids (:197-205), then one angle per partner (:495)
+    const int nmix = orc_mixed_partners(c, mixed_nev);
+    for (int iev = 0; iev < nev; iev++) {
+        for (int k = 0; k < nmix; k++) {
+            int id = c->uint_dist(c->gen) % mixed_nev;
+            while (iev == id && mixed_nev != 1) id = c->uint_dist(c->gen) % mixed_nev;
+            partners[(int64_t)iev * nmix + k] = id;
+        }
+        for (int k = 0; k < nmix; k++) angles[(int64_t)iev * nmix + k] = c->u01(c->gen) * 2 * M_PI;
+    }
+    return nmix;
+}
+
 int64_t orc_n_bins(const orc_ctx *c) { return c->n_slots * c->q3; }
 
 void orc_get_hist(const orc_ctx *c, double *num_count, double *q_out_sum,
@@ -523,6 +549,11 @@ void orc_get_hist(const orc_ctx *c, double *num_count, double *q_out_sum,
     if (q_long_sum) memcpy(q_long_sum, c->h.ql.data(), n);
     if (num) memcpy(num, c->h.num.data(), n);
     if (den) memcpy(den, c->h.den.data(), n);
+}
+
+void orc_get_abs_num(const orc_ctx *c, double *abs_num) {
+    flush_parts(c);
+    memcpy(abs_num, c->h.anum.data(), c->h.anum.size() * sizeof(double));
 }
 
 void orc_get_qinv(const orc_ctx *c, double *qinv_sum, double *num, double *num_count,

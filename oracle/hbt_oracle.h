@@ -73,12 +73,26 @@ double orc_get_psi_ref(const orc_ctx *c);
 double orc_event_plane_angle(int64_t n, const double *px, const double *py,
                              int32_t n_order);
 
+/* Mixed-event partners per event for a pool of mixed_nev events
+ * (number_of_mixed_events, or the reference's mixed_nev / 2 + 1). */
+int32_t orc_mixed_partners(const orc_ctx *c, int32_t mixed_nev);
+
+/* Draws what orc_process_buffer's mixed-event loop draws for a buffer of
+ * nev events and a pool of mixed_nev events (src/HBT_correlation.cpp:197-217,
+ * :495-497), advancing the same generator: partners[iev * nmix + k] and the
+ * rotation angles[iev * nmix + k] = rand_uniform() * 2 pi.  Returns nmix. */
+int32_t orc_mixed_plan(orc_ctx *c, int32_t nev, int32_t mixed_nev, int32_t *partners,
+                       double *angles);
+
 /* Histogram geometry: n_slots = n_KT (azimuthal 0) or n_KT * n_Kphi;
  * per slot qnpts^3 bins in [iqout][iqside][iqlong] order. */
 int64_t orc_n_bins(const orc_ctx *c);
 void orc_get_hist(const orc_ctx *c, double *num_count, double *q_out_sum,
                   double *q_side_sum, double *q_long_sum, double *num,
                   double *den);
+/* Sum of |cos(q.dx)| per 3-D bin (the scale against which the numerator's
+ * rounding is stated; no counterpart in the reference's output). */
+void orc_get_abs_num(const orc_ctx *c, double *abs_num);
 /* q_inv histograms, [n_KT][qnpts] each. */
 void orc_get_qinv(const orc_ctx *c, double *qinv_sum, double *num,
                   double *num_count, double *den);

@@ -283,3 +283,72 @@ def test_host_library_exports_every_declared_symbol(host):
     assert "hbt_host_run" in names and "hbt_host_event_plane_angle" in names
     for name in names:
         assert hasattr(host, name), name
+
+
+def _bind_plan(host):
+    host.hbt_host_mixed_plan.restype = ctypes.c_int64
+    host.hbt_host_mixed_plan.argtypes = [ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                         ctypes.c_int64, ctypes.POINTER(ctypes.c_int32), _PD]
+
+
+def host_mixed_plan(host, seed, nev, mixed_nev, n_partners):
+    """(partners, angles) the drop-in draws for buffers of nev[b] events and
+    pools of mixed_nev[b] events."""
+    _bind_plan(host)
+    nev = np.ascontiguousarray(nev, dtype=np.int32)
+    mixed_nev = np.ascontiguousarray(mixed_nev, dtype=np.int32)
+    nmix = [n_partners if n_partners > 0 else m // 2 + 1 for m in mixed_nev]
+    total = int(sum(int(a) * b for a, b in zip(nev, nmix)))
+    partners = np.zeros(max(total, 1), dtype=np.int32)
+    angles = np.zeros(max(total, 1))
+    _pi = ctypes.POINTER(ctypes.c_int32)
+    got = host.hbt_host_mixed_plan(seed, nev.size, nev.ctypes.data_as(_pi),
+                                   mixed_nev.ctypes.data_as(_pi), n_partners, total,
+                                   partners.ctypes.data_as(_pi), angles.ctypes.data_as(_PD))
+    assert got == total
+    return partners[:total], angles[:total]
+
+
+@pytest.mark.parametrize("n_partners", [0, 5])
+def test_host_mixed_plan_draws_what_the_oracle_draws(host, n_partners):
+    """hbt_host_mixed_plan replays the drop-in's partner and angle draws
+    (src/HBT_correlation.cpp:197-217, :495-497); the oracle, pinned to the
+    reference's files, draws the same, buffer after buffer, including a
+    one-event pool (the reference keeps the event as its own partner)."""
+    nev = [11, 10, 1, 7]
+    mixed_nev = [11, 10, 1, 9]
+    partners, angles = host_mixed_plan(host, 17, nev, mixed_nev, n_partners)
+    orc = oracle_lib.Oracle(seed=17, number_of_mixed_events=n_partners)
+    L = oracle_lib.lib()
+    L.orc_mixed_plan.restype = ctypes.c_int32
+    L.orc_mixed_plan.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                 ctypes.POINTER(ctypes.c_int32), _PD]
+    at = 0
+    for ne, mn in zip(nev, mixed_nev):
+        nmix = n_partners if n_partners > 0 else mn // 2 + 1
+        p = np.zeros(ne * nmix, dtype=np.int32)
+        a = np.zeros(ne * nmix)
+        assert L.orc_mixed_plan(orc._h, ne, mn, p.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                a.ctypes.data_as(_PD)) == nmix
+        assert np.array_equal(partners[at:at + p.size], p)
+        assert np.array_equal(angles[at:at + a.size], a)
+        at += p.size
+    assert at == partners.size
+    # a partner is never the event itself unless the pool has one event
+    assert partners[sum(n * (n_partners or m // 2 + 1) for n, m in zip(nev[:2], mixed_nev[:2]))] == 0
+
+
+def test_host_mixed_plan_rejects_bad_arguments(host):
+    _bind_plan(host)
+    _pi = ctypes.POINTER(ctypes.c_int32)
+    nev = (ctypes.c_int32 * 1)(3)
+    empty = (ctypes.c_int32 * 1)(0)
+    out = (ctypes.c_int32 * 8)()
+    ang = (ctypes.c_double * 8)()
+    # an empty pool for a non-empty buffer, a too small cap, negative counts
+    assert host.hbt_host_mixed_plan(1, 1, nev, empty, 2, 8, out, ang) == -1
+    assert host.hbt_host_mixed_plan(1, 1, nev, nev, 5, 8, out, ang) == -1
+    assert host.hbt_host_mixed_plan(1, -1, nev, nev, 2, 8, out, ang) == -1
+    assert host.hbt_host_mixed_plan(1, 0, None, None, 2, 0, None, None) == 0
