@@ -309,6 +309,42 @@ UNEVEN_PARAMS = dict(qnpts=41, q_min=-0.15, q_max=0.15, n_KT=5, KT_min=0.0, KT_m
                      long_comoving_boost=1, needed_number_of_pairs=1e18)
 
 
+def allreduce_hist(h: dict, device=None) -> dict:
+    """Sums a histogram dict (Engine.hist()) over the ranks of the default
+    process group: the replicas' one reduction when bench.py runs under
+    torchrun.  Counts travel as int64 (exact), sums as float64."""
+    import torch
+    import torch.distributed as dist
+    from hadronic_afterburner_toolkit_gb300 import replicas
+    out = dict(h)
+    for keys, dtype in ((replicas.COUNT_KEYS, torch.int64), (replicas.SUM_KEYS, torch.float64)):
+        present = [k for k in keys if k in h]
+        if not present:
+            continue
+        flat = np.concatenate([np.asarray(h[k]).ravel().astype(
+            np.int64 if dtype == torch.int64 else np.float64) for k in present])
+        t = torch.from_numpy(flat)
+        if device is not None:
+            t = t.to(device)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        flat = t.cpu().numpy()
+        at = 0
+        for k in present:
+            n = np.asarray(h[k]).size
+            part = flat[at:at + n].reshape(np.asarray(h[k]).shape)
+            out[k] = part.astype(np.asarray(h[k]).dtype) if dtype == torch.int64 else part
+            at += n
+    sc = [k for k in replicas.SCALAR_KEYS if k in h]
+    if sc:
+        t = torch.tensor([int(h[k]) for k in sc], dtype=torch.int64)
+        if device is not None:
+            t = t.to(device)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        for k, v in zip(sc, t.cpu().tolist()):
+            out[k] = int(v)
+    return out
+
+
 def make_uneven(seed: int = 3, group_particles: int = 50_000, nmix: int = 10):
     """The uneven-multiplicity workload: 4096 pi+ events with log-uniform
     multiplicities in [20, 3000] (sigma_xy = 1.2 N^(1/3) fm), oversample
@@ -975,8 +1011,7 @@ def main() -> None:
     reduced_bins = None
     if world > 1:
         # replicas: one histogram sum at the end (outside the timed region)
-        from hadronic_afterburner_toolkit_gb300 import replicas
-        reduced_bins = int(replicas.allreduce_hist(eng.hist(), device=dev)["count"].sum())
+        reduced_bins = int(allreduce_hist(eng.hist(), device=dev)["count"].sum())
         t = torch.tensor([t_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_ms = float(t.item())

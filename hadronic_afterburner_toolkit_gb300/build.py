@@ -158,10 +158,12 @@ def build_oracle() -> str:
     return os.path.join(REPO, "oracle", "liboracle.so")
 
 
-def build_reference(ref_root: str = "/root/reference") -> str | None:
-    """Compile the unmodified reference into oracle/_ref when its sources
-    are present on this machine."""
-    if not os.path.isdir(os.path.join(ref_root, "src")):
+def build_reference(ref_root: str | None = None) -> str | None:
+    """Compile the unmodified reference into oracle/_ref when a checkout of
+    it is named (``ref_root``, else the environment variable
+    HBT_REFERENCE_ROOT) and its sources are there."""
+    ref_root = ref_root or os.environ.get("HBT_REFERENCE_ROOT")
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src")):
         return None
     try:
         _run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + ref_root])

@@ -83,6 +83,9 @@ struct hbt_ctx {
     u64 ub[4] = {0, 0, 0, 0};
     hbt_stats st;
     std::string err;
+    // allocation-failure injection (hbt_inject_alloc_failure): allocations
+    // left to succeed before one fails; -1 = off
+    int fail_after = -1;
 };
 
 namespace {
@@ -120,6 +123,8 @@ hbt_status dalloc(hbt_ctx *c, DevBuf &b, size_t bytes) {
     if (b.bytes >= bytes && b.p) return HBT_OK;
     dfree(c, b);
     if (bytes == 0) return HBT_OK;
+    if (c->fail_after >= 0 && c->fail_after-- == 0)
+        return fail(c, HBT_ERR_NOMEM, "device allocation failed (injected)");
     cudaError_t e = c->pool ? cudaMallocFromPoolAsync(&b.p, bytes, c->pool, c->own)
                             : cudaMalloc(&b.p, bytes);
     if (e != cudaSuccess) {
@@ -325,33 +330,7 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
 }
 
 // FP32 copies of the screen constants with their rounding slack.
-void fill_screen(hbt_ctx *c) {
-    const hbt::Grid &g = c->d.g;
-    hbt::Screen &s = c->d.s;
-    auto f = [](double v) { return static_cast<float>(v); };
-    auto slack = [](double v, float v32) { return std::fabs(v - static_cast<double>(v32)); };
-    const double lo4 = 4.0 * g.KT_min_sq, hi4 = 4.0 * g.KT_max_sq;
-    s.kt_lo4 = f(lo4);
-    s.kt_hi4 = f(hi4);
-    s.kt_slack = f(std::max(slack(lo4, s.kt_lo4), slack(hi4, s.kt_hi4)) + 1e-7 * hi4);
-    s.lo = f(g.q_lo);
-    s.hi = f(g.q_hi);
-    s.win_slack = f(std::max(slack(g.q_lo, s.lo), slack(g.q_hi, s.hi)) + 1e-12);
-    s.base = f(g.q_base);
-    s.inv_dq = f(1.0 / g.delta_q);
-    s.t_slack = f(slack(g.q_base, s.base) / g.delta_q + 4.0 * 5.96e-8 * g.qnpts + 1e-9);
-    s.KT_min = f(g.KT_min);
-    s.inv_dKT = f(1.0 / g.dKT);
-    s.kt_t_slack = f(slack(g.KT_min, s.KT_min) / g.dKT + 4.0 * 5.96e-8 * g.n_KT + 1e-9);
-    s.psi = f(g.psi_ref);
-    s.psi_slack = f(slack(g.psi_ref, s.psi));
-    s.two_pi = f(g.two_pi);
-    s.inv_dKphi = f(1.0 / g.dKphi);
-    s.qnpts = g.qnpts;
-    s.n_KT = g.n_KT;
-    s.n_Kphi = g.n_Kphi;
-    hbt::fill_prefilter(s);
-}
+void fill_screen(hbt_ctx *c) { hbt::screen_from_grid(c->d.g, c->d.s); }
 
 bool screened_ok(const hbt_ctx *c) {
     return (c->prm.kernel == HBT_KERNEL_SCREENED || c->prm.kernel == HBT_KERNEL_SCREENED_GRID) &&
@@ -537,6 +516,58 @@ hbt_status stage(hbt_ctx *c, const double *const *src, const long long *len, int
 
 namespace hbt {
 
+void grid_from_params(const hbt_params &p, Grid &g) {
+    // constants with the reference's expressions (src/HBT_correlation.cpp:25-61)
+    g = Grid{};
+    g.qnpts = p.qnpts;
+    g.n_KT = p.n_KT;
+    g.n_Kphi = p.n_Kphi;
+    g.azimuthal = p.azimuthal_flag == 1;
+    g.qinv = p.invariant_radius_flag == 1;
+    g.boost = p.long_comoving_boost == 1;
+    g.n_slots = g.azimuthal ? p.n_KT * p.n_Kphi : p.n_KT;
+    g.q3 = (long long)p.qnpts * p.qnpts * p.qnpts;
+    g.delta_q = (p.q_max - p.q_min) / (p.qnpts - 1);
+    g.q_lo = p.q_min - g.delta_q / 2. + 1e-8;
+    g.q_hi = p.q_max + g.delta_q / 2. - 1e-8;
+    g.q_base = p.q_min - g.delta_q / 2.;
+    g.KT_min = p.KT_min;
+    g.dKT = (p.KT_max - p.KT_min) / (p.n_KT - 1);
+    g.KT_min_sq = p.KT_min * p.KT_min;
+    g.KT_max_sq = p.KT_max * p.KT_max;
+    g.dKphi = 2 * M_PI / p.n_Kphi;
+    g.two_pi = 2. * M_PI;
+    g.psi_ref = 0.0;
+    g.kphi_tol = p.kphi_defer_tol > 0 ? p.kphi_defer_tol : 1e-13;
+    g.hbarC_inv = 1. / kHbarC;
+}
+
+void screen_from_grid(const Grid &g, Screen &s) {
+    auto f = [](double v) { return static_cast<float>(v); };
+    auto slack = [](double v, float v32) { return std::fabs(v - static_cast<double>(v32)); };
+    const double lo4 = 4.0 * g.KT_min_sq, hi4 = 4.0 * g.KT_max_sq;
+    s.kt_lo4 = f(lo4);
+    s.kt_hi4 = f(hi4);
+    s.kt_slack = f(std::max(slack(lo4, s.kt_lo4), slack(hi4, s.kt_hi4)) + 1e-7 * hi4);
+    s.lo = f(g.q_lo);
+    s.hi = f(g.q_hi);
+    s.win_slack = f(std::max(slack(g.q_lo, s.lo), slack(g.q_hi, s.hi)) + 1e-12);
+    s.base = f(g.q_base);
+    s.inv_dq = f(1.0 / g.delta_q);
+    s.t_slack = f(slack(g.q_base, s.base) / g.delta_q + 4.0 * 5.96e-8 * g.qnpts + 1e-9);
+    s.KT_min = f(g.KT_min);
+    s.inv_dKT = f(1.0 / g.dKT);
+    s.kt_t_slack = f(slack(g.KT_min, s.KT_min) / g.dKT + 4.0 * 5.96e-8 * g.n_KT + 1e-9);
+    s.psi = f(g.psi_ref);
+    s.psi_slack = f(slack(g.psi_ref, s.psi));
+    s.two_pi = f(g.two_pi);
+    s.inv_dKphi = f(1.0 / g.dKphi);
+    s.qnpts = g.qnpts;
+    s.n_KT = g.n_KT;
+    s.n_Kphi = g.n_Kphi;
+    fill_prefilter(s);
+}
+
 bool params_valid(const hbt_params &p) {
     if (p.qnpts < 2 || p.n_KT < 2 || p.n_Kphi < 1 || p.qnpts > 1024) return false;
     if (p.precision != HBT_PRECISION_FP64 && p.precision != HBT_PRECISION_FP32W &&
@@ -577,29 +608,8 @@ hbt_status ctx_create(const hbt_params *p, int device, cudaMemPool_t pool, hbt_c
     c->stream = c->own;
     CU(cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming));
 
-    // constants with the reference's expressions (src/HBT_correlation.cpp:25-61)
     hbt::Grid &g = c->d.g;
-    g.qnpts = p->qnpts;
-    g.n_KT = p->n_KT;
-    g.n_Kphi = p->n_Kphi;
-    g.azimuthal = p->azimuthal_flag == 1;
-    g.qinv = p->invariant_radius_flag == 1;
-    g.boost = p->long_comoving_boost == 1;
-    g.n_slots = g.azimuthal ? p->n_KT * p->n_Kphi : p->n_KT;
-    g.q3 = (long long)p->qnpts * p->qnpts * p->qnpts;
-    g.delta_q = (p->q_max - p->q_min) / (p->qnpts - 1);
-    g.q_lo = p->q_min - g.delta_q / 2. + 1e-8;
-    g.q_hi = p->q_max + g.delta_q / 2. - 1e-8;
-    g.q_base = p->q_min - g.delta_q / 2.;
-    g.KT_min = p->KT_min;
-    g.dKT = (p->KT_max - p->KT_min) / (p->n_KT - 1);
-    g.KT_min_sq = p->KT_min * p->KT_min;
-    g.KT_max_sq = p->KT_max * p->KT_max;
-    g.dKphi = 2 * M_PI / p->n_Kphi;
-    g.two_pi = 2. * M_PI;
-    g.psi_ref = 0.0;
-    g.kphi_tol = p->kphi_defer_tol > 0 ? p->kphi_defer_tol : 1e-13;
-    g.hbarC_inv = 1. / kHbarC;
+    hbt::grid_from_params(*p, g);
     fill_screen(c);
     c->cap = static_cast<u64>(p->needed_number_of_pairs);
     c->cap_qinv = 50 * c->cap;
@@ -1063,6 +1073,12 @@ hbt_status hbt_read_counters(hbt_ctx *c, uint64_t *num, uint64_t *den, uint64_t 
         if (num_qinv) num_qinv[k] = ctr[2 * ns + k];
         if (den_qinv) den_qinv[k] = ctr[2 * ns + nk + k];
     }
+    return HBT_OK;
+}
+
+hbt_status hbt_inject_alloc_failure(hbt_ctx *c, int32_t n_ok) {
+    if (!c || n_ok < -1) return HBT_ERR_INVALID;
+    c->fail_after = n_ok;
     return HBT_OK;
 }
 

@@ -10,6 +10,12 @@ namespace hbt {
 
 // hbt_create's parameter checks.
 bool params_valid(const hbt_params &p);
+// The histogram geometry and the constants the reference derives from the
+// parameters (src/HBT_correlation.cpp:25-61), psi_ref = 0.
+void grid_from_params(const hbt_params &p, Grid &g);
+// FP32 copies of a grid's constants for the pair screen, with the bound on
+// each one's rounding.
+void screen_from_grid(const Grid &g, Screen &s);
 // hbt_create with the context's device memory taken, stream-ordered on its
 // own stream, from `pool` (nullptr: cudaMalloc), so that creating and
 // destroying contexts does not synchronise the device.

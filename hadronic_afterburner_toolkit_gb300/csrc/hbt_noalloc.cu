@@ -27,13 +27,24 @@
 //    threads on the same device) race on it; order them on one stream.
 //  - The first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    before any stream capture.  The address is kept per device together
+//    with the CUDA context it was looked up in, and looked up again when the
+//    device's current context changes (after cudaDeviceReset, or when the
+//    host framework tears down and re-creates the primary context).
+//  - The pool must already carry the rapidity cut the reference applies to
+//    partner particles before rotating them (src/HBT_correlation.cpp:
+//    509-511); list1 likewise (:474-476).  Pairs the reference would index
+//    out of bounds (an LCMS component NaN because K_perp == 0) are skipped
+//    and not reported here; hbt_get_stats of a context counts them.
+#include <cuda.h>
+
 #include <cmath>
 #include <cstdio>
 #include <mutex>
 
 #include "../../include/hbt_gpu.h"
 #include "hbt_engine.cuh"
+#include "hbt_internal.h"
 
 namespace hbt {
 namespace {
@@ -44,10 +55,43 @@ constexpr size_t kScratchBytes = (size_t)4 * kPool * sizeof(double) + STAT_N * s
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Device address of the scratch array, per device (looked up once).
+// Device address of the scratch array, per device, with the unique id of
+// the CUDA context it was looked up in (0: unknown).
 constexpr int kMaxDevices = 64;
 unsigned char *g_scratch_addr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};
 std::mutex g_scratch_mutex;
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId, which
+// never repeats within a process, unlike a context handle), through the
+// driver entry points the runtime hands out; 0 when it cannot be had, in
+// which case the address is looked up on every call.
+unsigned long long current_context_id() {
+    typedef CUresult (*GetCurrent)(CUcontext *);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long *);
+    static GetCurrent cur = nullptr;
+    static GetId id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr, *q = nullptr;
+        cudaDriverEntryPointQueryResult r1, r2;
+        if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &p, cudaEnableDefault, &r1) ==
+                cudaSuccess &&
+            r1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPoint("cuCtxGetId", &q, cudaEnableDefault, &r2) == cudaSuccess &&
+            r2 == cudaDriverEntryPointSuccess) {
+            cur = reinterpret_cast<GetCurrent>(p);
+            id = reinterpret_cast<GetId>(q);
+        } else {
+            cudaGetLastError();
+        }
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long v = 0;
+    if (!cur || !id || cur(&ctx) != CUDA_SUCCESS || !ctx || id(ctx, &v) != CUDA_SUCCESS)
+        return 0;
+    return v;
+}
 
 __global__ void k_rotate(long long n, const double *px, const double *py, const double *pz,
                          const double *E, double cph, double sph, double *out) {
@@ -89,19 +133,31 @@ extern "C" hbt_status hbt_bin_mixed_rotated_noalloc(const hbt_params *p, int64_t
                                 "azimuthal_flag and invariant_radius_flag must be 0");
     if (p->qnpts < 2 || p->qnpts > 1024 || p->n_KT < 2 || p->n_KT > 255)
         return (hbt_status)fail(errbuf, errlen, HBT_ERR_INVALID, "qnpts or n_KT out of range");
+    // an error left by earlier work on this thread is reported as such, not
+    // as a failure of this call's launches
+    const cudaError_t prior = cudaGetLastError();
+    if (prior != cudaSuccess) {
+        char msg[200];
+        snprintf(msg, sizeof(msg), "a CUDA error from earlier work was pending: %s",
+                 cudaGetErrorString(prior));
+        return (hbt_status)fail(errbuf, errlen, HBT_ERR_CUDA, msg);
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return (hbt_status)fail(errbuf, errlen, HBT_ERR_CUDA, "cudaGetDevice failed");
     unsigned char *scratch = nullptr;
     {
+        // once per device (and again if the device's context was re-created)
+        const unsigned long long ctx = current_context_id();
         std::lock_guard<std::mutex> lock(g_scratch_mutex);
-        if (!g_scratch_addr[dev]) {
+        if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
             void *addr = nullptr;
             const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
             if (e != cudaSuccess)
                 return (hbt_status)fail(errbuf, errlen, HBT_ERR_CUDA,
                                         "cudaGetSymbolAddress of the scratch array failed");
             g_scratch_addr[dev] = static_cast<unsigned char *>(addr);
+            g_scratch_ctx[dev] = ctx;
         }
         scratch = g_scratch_addr[dev];
     }
@@ -112,51 +168,13 @@ extern "C" hbt_status hbt_bin_mixed_rotated_noalloc(const hbt_params *p, int64_t
         return (hbt_status)fail(errbuf, errlen, HBT_ERR_CUDA, "clearing the scratch counters failed");
     if (n1 == 0 || n2 == 0) return HBT_OK;
 
-    // constants with the reference's expressions (src/HBT_correlation.cpp:25-61)
+    // the engine's constants and FP32 screen for these parameters, as
+    // hbt_create derives them
+    hbt_params prm = *p;
+    if (prm.n_Kphi < 1) prm.n_Kphi = 1;  // unused without K_phi bins
     Device d = {};
-    Grid &g = d.g;
-    g.qnpts = p->qnpts;
-    g.n_KT = p->n_KT;
-    g.n_Kphi = p->n_Kphi > 0 ? p->n_Kphi : 1;
-    g.n_slots = p->n_KT;
-    g.azimuthal = 0;
-    g.qinv = 0;
-    g.boost = p->long_comoving_boost == 1;
-    g.q3 = (long long)p->qnpts * p->qnpts * p->qnpts;
-    g.delta_q = (p->q_max - p->q_min) / (p->qnpts - 1);
-    g.q_lo = p->q_min - g.delta_q / 2. + 1e-8;
-    g.q_hi = p->q_max + g.delta_q / 2. - 1e-8;
-    g.q_base = p->q_min - g.delta_q / 2.;
-    g.KT_min = p->KT_min;
-    g.dKT = (p->KT_max - p->KT_min) / (p->n_KT - 1);
-    g.KT_min_sq = p->KT_min * p->KT_min;
-    g.KT_max_sq = p->KT_max * p->KT_max;
-    g.dKphi = 2 * M_PI / g.n_Kphi;
-    g.two_pi = 2. * M_PI;
-    g.hbarC_inv = 1. / 0.197327053;
-    // FP32 screen constants and the bounds on their rounding
-    Screen &s = d.s;
-    auto f = [](double v) { return static_cast<float>(v); };
-    auto slack = [](double v, float v32) { return std::fabs(v - static_cast<double>(v32)); };
-    const double lo4 = 4.0 * g.KT_min_sq, hi4 = 4.0 * g.KT_max_sq;
-    s.kt_lo4 = f(lo4);
-    s.kt_hi4 = f(hi4);
-    s.kt_slack = f(std::fmax(slack(lo4, s.kt_lo4), slack(hi4, s.kt_hi4)) + 1e-7 * hi4);
-    s.lo = f(g.q_lo);
-    s.hi = f(g.q_hi);
-    s.win_slack = f(std::fmax(slack(g.q_lo, s.lo), slack(g.q_hi, s.hi)) + 1e-12);
-    s.base = f(g.q_base);
-    s.inv_dq = f(1.0 / g.delta_q);
-    s.t_slack = f(slack(g.q_base, s.base) / g.delta_q + 4.0 * 5.96e-8 * g.qnpts + 1e-9);
-    s.KT_min = f(g.KT_min);
-    s.inv_dKT = f(1.0 / g.dKT);
-    s.kt_t_slack = f(slack(g.KT_min, s.KT_min) / g.dKT + 4.0 * 5.96e-8 * g.n_KT + 1e-9);
-    s.two_pi = f(g.two_pi);
-    s.inv_dKphi = f(1.0 / g.dKphi);
-    s.qnpts = g.qnpts;
-    s.n_KT = g.n_KT;
-    s.n_Kphi = g.n_Kphi;
-    fill_prefilter(s);
+    grid_from_params(prm, d.g);
+    screen_from_grid(d.g, d.s);
     d.h.den = reinterpret_cast<u64 *>(den);
     d.stats = stats;
 

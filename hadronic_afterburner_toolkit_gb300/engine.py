@@ -98,6 +98,7 @@ _SIGNATURES = {
     "hbt_read_qinv": (_I32, [ctypes.c_void_p] + [_PD] * 4),
     "hbt_read_counters": (_I32, [ctypes.c_void_p] + [_PU64] * 4),
     "hbt_get_stats": (_I32, [ctypes.c_void_p, ctypes.POINTER(HbtStats)]),
+    "hbt_inject_alloc_failure": (_I32, [ctypes.c_void_p, _I32]),
     "hbt_bin_mixed_rotated_noalloc": (_I32, [ctypes.POINTER(HbtParams), _I64,
                                              ctypes.POINTER(HbtSoa4), _I64,
                                              ctypes.POINTER(HbtSoa4), _D, _D,

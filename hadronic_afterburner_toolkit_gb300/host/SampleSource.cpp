@@ -27,6 +27,18 @@ namespace {
 
 const char *kBadParticle = "particleSamples: truncated or malformed particle line";
 const char *kBadOscar = "particleSamples: truncated or malformed OSCAR line";
+// zlib reports a gzip stream that ends before its trailer as Z_BUF_ERROR once
+// the data it could inflate is used up; the reference reads on as if the
+// file ended there.  Here that is an error.
+const char *kTruncatedGz = "particleSamples: gzip stream ends early (truncated file)";
+
+#ifdef HBT_HAVE_ZLIB
+void check_gz_end(void *gzf) {
+    int errnum = Z_OK;
+    gzerror(static_cast<gzFile>(gzf), &errnum);
+    if (errnum == Z_BUF_ERROR) throw std::runtime_error(kTruncatedGz);
+}
+#endif
 
 // Parses `count` numbers separated by blanks from a NUL-terminated line;
 // returns how many were read (the reference's readers parse line by line).
@@ -168,6 +180,9 @@ class LineSampleSource : public SampleSource {
             got = fgets(&buf_[0], static_cast<int>(buf_.size()), pipe_);
 #endif
             if (!got) {
+#ifdef HBT_HAVE_ZLIB
+                check_gz_end(gzf_);
+#endif
                 eof_ = true;
                 return line;
             }
@@ -178,6 +193,9 @@ class LineSampleSource : public SampleSource {
             }
             line.append(got, len);
             if (len + 1 < buf_.size()) {  // short read without newline: end of file
+#ifdef HBT_HAVE_ZLIB
+                check_gz_end(gzf_);
+#endif
                 eof_ = true;
                 return line;
             }
@@ -236,6 +254,7 @@ class ByteSource {
         if (gzf_) {
             const int got = gzread(static_cast<gzFile>(gzf_), dst, static_cast<unsigned>(n));
             if (got < 0) throw std::runtime_error("particleSamples: gzip read error");
+            if (got == 0) check_gz_end(gzf_);
             return static_cast<size_t>(got);
         }
 #endif

@@ -6,8 +6,10 @@ run over the whole job in the reference's order.  With no cap that can
 bind, ranks bin disjoint shards of the groups into their own histograms and
 one sum at the end gives the single-process histograms: counts, denominators
 and pair counters exactly (integer sums), the FP64 sums up to summation
-order.  No collective runs on the data path; the one reduction uses
-torch.distributed (gloo on CPU tensors, NCCL on GPU tensors).
+order.  No collective runs on the data path.  Each replica (one process per
+GPU, on one box or many) saves its histograms with save_hist; one host
+process adds the files with sum_hists and writes the reference's output
+files from the sum (hbt_host_write).
 """
 from __future__ import annotations
 
@@ -40,38 +42,42 @@ def caps_allow_sharding(params: dict, total_same_pairs: int, total_mixed_pairs: 
     return ok
 
 
-def allreduce_hist(h: Dict[str, np.ndarray], device=None) -> Dict[str, np.ndarray]:
-    """Sums a histogram dict over all ranks of the default process group.
-    Counts travel as int64 (exact), sums as float64."""
-    import torch
-    import torch.distributed as dist
-    out = dict(h)
-    for keys, dtype in ((COUNT_KEYS, torch.int64), (SUM_KEYS, torch.float64)):
-        present = [k for k in keys if k in h]
-        if not present:
-            continue
-        flat = np.concatenate([np.asarray(h[k]).ravel().astype(
-            np.int64 if dtype == torch.int64 else np.float64) for k in present])
-        t = torch.from_numpy(flat)
-        if device is not None:
-            t = t.to(device)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        flat = t.cpu().numpy()
-        at = 0
-        for k in present:
-            n = np.asarray(h[k]).size
-            part = flat[at:at + n].reshape(np.asarray(h[k]).shape)
-            out[k] = part.astype(np.asarray(h[k]).dtype) if dtype == torch.int64 else part
-            at += n
-    sc = [k for k in SCALAR_KEYS if k in h]
-    if sc:
-        t = torch.tensor([int(h[k]) for k in sc], dtype=torch.int64)
-        if device is not None:
-            t = t.to(device)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        for k, v in zip(sc, t.cpu().tolist()):
-            out[k] = int(v)
+def sum_hists(hists: Sequence[Dict[str, np.ndarray]]) -> Dict[str, np.ndarray]:
+    """Host-side sum of the histograms of several replicas, in the order
+    given: counts and pair counters as exact int64 sums (returned in their
+    own dtype), the FP64 sums added in float64, the scalar totals as ints."""
+    if not hists:
+        raise ValueError("no histograms to sum")
+    out: Dict[str, np.ndarray] = {}
+    for k in COUNT_KEYS:
+        if k in hists[0]:
+            acc = np.zeros(np.asarray(hists[0][k]).shape, dtype=np.int64)
+            for h in hists:
+                acc += np.asarray(h[k]).astype(np.int64)
+            out[k] = acc.astype(np.asarray(hists[0][k]).dtype)
+    for k in SUM_KEYS:
+        if k in hists[0]:
+            acc = np.zeros(np.asarray(hists[0][k]).shape, dtype=np.float64)
+            for h in hists:
+                acc += np.asarray(h[k], dtype=np.float64)
+            out[k] = acc
+    for k in SCALAR_KEYS:
+        if k in hists[0]:
+            out[k] = int(sum(int(h[k]) for h in hists))
     return out
+
+
+def save_hist(path: str, h: Dict[str, np.ndarray]) -> None:
+    """One replica's histograms (Engine.hist()) as an .npz file."""
+    np.savez(path, **{k: np.asarray(v) for k, v in h.items()})
+
+
+def load_hist(path: str) -> Dict[str, np.ndarray]:
+    d = dict(np.load(path))
+    for k in SCALAR_KEYS:
+        if k in d:
+            d[k] = int(d[k])
+    return d
 
 
 def bin_shard(binner, groups: Sequence, rank: int, world: int) -> List[int]:

@@ -246,6 +246,14 @@ hbt_status hbt_read_counters(hbt_ctx *ctx, uint64_t *num, uint64_t *den,
 
 hbt_status hbt_get_stats(hbt_ctx *ctx, hbt_stats *out);
 
+/* Fault injection for tests of the error paths; no counterpart in the
+ * reference.  After n_ok more device allocations of this context succeed,
+ * the next one fails as an out-of-memory would (the call returns
+ * HBT_ERR_NOMEM, the histograms are unchanged and the context stays
+ * usable); the injection then switches itself off.  n_ok = -1 switches it
+ * off. */
+hbt_status hbt_inject_alloc_failure(hbt_ctx *ctx, int32_t n_ok);
+
 /* Largest partner pool hbt_bin_mixed_rotated_noalloc accepts (particles). */
 #define HBT_NOALLOC_MAX_POOL 65536
 
@@ -260,10 +268,17 @@ hbt_status hbt_get_stats(hbt_ctx *ctx, hbt_stats *out);
  * rotates a mixed event and binned against list1 on `stream`; the rotated
  * copy lives in a fixed 2 MB __device__ scratch array that every GPU loading
  * the library holds until exit.  Requires azimuthal_flag == 0 and
- * invariant_radius_flag == 0; applies no needed_number_of_pairs cap.  Calls
- * share the scratch and race if they overlap on the GPU.  The first call on
- * a device looks up the scratch address and should come before any stream
- * capture.  On error a message is written to errbuf (may be NULL). */
+ * invariant_radius_flag == 0; applies no needed_number_of_pairs cap.  list1
+ * and the pool must already carry the rapidity cut the reference applies
+ * before rotating (src/HBT_correlation.cpp:474-476, :509-511).  Pairs the
+ * reference would index out of bounds (a NaN LCMS component, K_perp == 0)
+ * are skipped and not reported by this entry point.  Calls share the
+ * scratch and race if they overlap on the GPU.  The first call on a device
+ * looks up the scratch address (again after the device's CUDA context is
+ * re-created) and should come before any stream capture.  A CUDA error left
+ * pending by earlier work is reported as such (HBT_ERR_CUDA) before
+ * anything is launched.  On error a message is written to errbuf (may be
+ * NULL). */
 hbt_status hbt_bin_mixed_rotated_noalloc(const hbt_params *params, int64_t n1,
                                          const hbt_soa4 *list1, int64_t n2,
                                          const hbt_soa4 *pool, double cos_phi,

@@ -197,7 +197,9 @@ def run_case(name: str, case: dict, ref_root: str) -> None:
 
 
 def main(argv):
-    ref_root = argv[1] if len(argv) > 1 else "/root/reference"
+    ref_root = argv[1] if len(argv) > 1 else os.environ.get("HBT_REFERENCE_ROOT")
+    if not ref_root:
+        raise SystemExit("usage: %s <reference checkout> (or set HBT_REFERENCE_ROOT)" % argv[0])
     if not os.path.exists(REF_BIN):
         raise SystemExit("build the reference first: make -C oracle ref")
     for name, case in CASES.items():

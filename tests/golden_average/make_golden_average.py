@@ -3,7 +3,7 @@ folders holding HBT correlation files in the writer's format, and the
 averages the reference's ebe_scripts/average_event_HBT_correlation_function.py
 writes for them (run from the reference checkout given as argv[1]).
 
-    python tests/golden_average/make_golden_average.py /root/reference
+    python tests/golden_average/make_golden_average.py <reference checkout>
 
 Writes tests/golden_average/case.tar.gz with work/ (inputs) and avg/
 (the reference script's outputs).
@@ -68,4 +68,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HBT_REFERENCE_ROOT")
+    if not ref:
+        raise SystemExit("usage: %s <reference checkout> (or set HBT_REFERENCE_ROOT)" % sys.argv[0])
+    main(ref)

@@ -76,7 +76,9 @@ def _stub_h5py(db):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HBT_REFERENCE_ROOT")
+    if not ref:
+        raise SystemExit("usage: %s <reference checkout> (or set HBT_REFERENCE_ROOT)" % sys.argv[0])
     script = os.path.join(ref, "ebe_scripts", "fit_HBT_radii.py")
     db = tables.database()
     h5 = _stub_h5py(db)

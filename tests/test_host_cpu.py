@@ -352,3 +352,30 @@ def test_host_mixed_plan_rejects_bad_arguments(host):
     assert host.hbt_host_mixed_plan(1, 1, nev, nev, 5, 8, out, ang) == -1
     assert host.hbt_host_mixed_plan(1, -1, nev, nev, 2, 8, out, ang) == -1
     assert host.hbt_host_mixed_plan(1, 0, None, None, 2, 0, None, None) == 0
+
+
+@pytest.mark.parametrize("fast", [1, 0])
+def test_readers_reject_a_truncated_gzip_file(host, fast, tmp_path):
+    """A particle_samples.gz cut short anywhere - inside the data, or only
+    its 8-byte trailer - is an error for both readers (the line reader and
+    the block reader), reported as -1 instead of buffers read from a partial
+    stream; the intact file reads as before.  (The reference reads what
+    inflates and takes the early end for the end of the file.)"""
+    src = os.path.join(oracle_lib.GOLDEN, "basic")
+    data = open(os.path.join(src, "particle_samples.gz"), "rb").read()
+    res = tmp_path / "results"
+    res.mkdir()
+    host.hbt_host_digest_buffers.restype = ctypes.c_int
+    host.hbt_host_digest_buffers.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
+                                             ctypes.POINTER(ctypes.c_char_p), ctypes.c_int32,
+                                             ctypes.POINTER(ctypes.c_uint64)]
+    args = (ctypes.c_char_p * 1)(b"hbt_fast_reader=%d" % fast)
+    pfile = os.path.join(src, "parameters.dat").encode()
+    for cut in (len(data), len(data) - 4, len(data) - 8, len(data) - 20, len(data) // 2, 10):
+        (res / "particle_samples.gz").write_bytes(data[:cut])
+        dig = (ctypes.c_uint64 * 256)()
+        nb = host.hbt_host_digest_buffers(pfile, str(res).encode(), 1, args, 256, dig)
+        if cut == len(data):
+            assert nb > 0
+        else:
+            assert nb == -1, cut

@@ -24,10 +24,11 @@ import pytest
 
 from hadronic_afterburner_toolkit_gb300 import build
 
-REF = os.environ.get("HBT_REFERENCE_ROOT", "/root/reference")
-UNIT = os.path.join(REF, "unit_tests")
-pytestmark = pytest.mark.skipif(not os.path.isdir(UNIT),
-                                reason="the reference's unit-test fixtures are not here")
+# the reference checkout whose unit-test fixtures are read in place
+REF = os.environ.get("HBT_REFERENCE_ROOT", "")
+UNIT = os.path.join(REF, "unit_tests") if REF else ""
+pytestmark = pytest.mark.skipif(not UNIT or not os.path.isdir(UNIT),
+                                reason="set HBT_REFERENCE_ROOT to a reference checkout")
 
 
 @pytest.fixture(scope="module")

@@ -1,9 +1,10 @@
 """Replicas over oversample groups (hadronic_afterburner_toolkit_gb300/
 replicas.py) with world_size 2 over gloo on the CPU: each rank bins its
-shard of the groups, one all-reduce sums the histograms, and the result is
-the single-process binning of every group (counts exact, FP64 sums within
-1e-12 relative).  The CPU oracle stands in for the GPU engine here; the
-engine exposes the same bin_same / bin_mixed / hist interface."""
+shard of the groups; the benchmark's one all-reduce (bench.allreduce_hist)
+and the host-side sum of the ranks' saved histograms (replicas.sum_hists)
+both give the single-process binning of every group (counts exact, FP64
+sums within 1e-12 relative).  The CPU oracle stands in for the GPU engine
+here; the engine exposes the same bin_same / bin_mixed / hist interface."""
 import os
 import socket
 
@@ -52,7 +53,9 @@ def _rank_main(rank, world, port, out_dir):
         groups = _groups()
         orc = oracle_lib.Oracle(**P)
         mine = replicas.bin_shard(orc, groups, rank, world)
-        h = replicas.allreduce_hist(orc.hist())
+        replicas.save_hist(os.path.join(out_dir, "rank%d.npz" % rank), orc.hist())
+        import bench
+        h = bench.allreduce_hist(orc.hist())
         if rank == 0:
             np.savez(os.path.join(out_dir, "reduced.npz"), mine=np.array(mine),
                      **{k: np.asarray(v) for k, v in h.items()})
@@ -100,3 +103,8 @@ def test_two_gloo_ranks_equal_one_process(tmp_path):
     assert ref["count"].sum() > 100 and ref["den"].sum() > 100
     scale = 0.15 + 0.3 / 10
     parity.compare(red, ref, scale)
+    # the same sum on the host from the ranks' saved histograms
+    from hadronic_afterburner_toolkit_gb300 import replicas
+    summed = replicas.sum_hists([replicas.load_hist(str(tmp_path / ("rank%d.npz" % r)))
+                                 for r in range(2)])
+    parity.compare(summed, ref, scale)
