@@ -55,10 +55,26 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-# FP64 operations per pair and stage, counted from the reference's code
-# (src/HBT_correlation.cpp): add/mul + div + sqrt + cos, each counted once.
-STAGE_OPS_SAME = (11, 12, 5, 11, 15)
-STAGE_OPS_MIXED = (11, 12, 5, 11, 2)
+# The reference's per-pair chain (src/HBT_correlation.cpp:311-458), counted
+# from its code, per stage: FP64 add/mul, divide, square root, cos, FP64
+# atomics (histogram adds).  Stages: all pairs; K_T passed; q_out passed;
+# q_side passed; binned.
+STAGE_COUNTS_SAME = ((11, 0, 0, 0, 0), (8, 3, 1, 0, 0), (4, 1, 0, 0, 0), (7, 3, 1, 0, 0),
+                     (13, 1, 0, 1, 5))
+STAGE_COUNTS_MIXED = ((11, 0, 0, 0, 0), (8, 3, 1, 0, 0), (4, 1, 0, 0, 0), (7, 3, 1, 0, 0),
+                      (1, 1, 0, 0, 1))
+STAGE_OPS_SAME = tuple(sum(c[:4]) for c in STAGE_COUNTS_SAME)
+STAGE_OPS_MIXED = tuple(sum(c[:4]) for c in STAGE_COUNTS_MIXED)
+
+# FP64-pipe instructions (warp-level, ncu smsp__inst_executed_pipe_fp64.sum)
+# that k_persistent_same executes per binned same-event pair in the FP64
+# form, all of the kernel's FP64 work (values, undecided pairs, tile loads)
+# divided by the pairs it bins: measured on one central group launch,
+# profiles/k_persistent_same_fp64_central.md.
+FP64_WARP_INST_PER_BINNED_PAIR = None
+# DRAM bytes (read + write) of one k_persistent_same launch on a central
+# group, FP64 form: same capture.
+CENTRAL_SAME_DRAM_BYTES = None
 
 
 def workload_params(name: str) -> dict:
@@ -226,6 +242,20 @@ def measure_fp64_peak() -> dict:
                 raise RuntimeError("probe failed")
             best = max(best, fl.value / (ms.value * 1e-3))
         out[name + "_tflops"] = best / 1e12
+    # FP64 divide, square root and cos, each with one add (the reference
+    # chain's other operations)
+    fn = L.hbt_probe_op64
+    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                   ctypes.POINTER(ctypes.c_double)]
+    for key, op, iters in (("div_gops", 0, 1 << 11), ("sqrt_gops", 1, 1 << 11),
+                           ("cos_gops", 2, 1 << 10)):
+        ms, ops = ctypes.c_float(), ctypes.c_double()
+        best = 0.0
+        for _ in range(3):
+            if fn(op, 152 * 8, iters, ctypes.byref(ms), ctypes.byref(ops)) != 0:
+                raise RuntimeError("probe failed")
+            best = max(best, ops.value / (ms.value * 1e-3))
+        out[key] = best / 1e9
     # scattered FP64 atomic adds: over 32 MB (L2-resident, the atomic units'
     # rate) and over 256 MB (beyond L2, like the whole histogram)
     fn = L.hbt_probe_atomic
@@ -987,6 +1017,7 @@ def main() -> None:
     if world > 1:
         torch.distributed.barrier()
     launches0 = eng.stats()["launches"]
+    ctr0 = eng.counters()
     ms_steps, pairs, same_ms, mixed_ms = [], 0, [], []
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -1007,6 +1038,10 @@ def main() -> None:
                 mixed_ms.append(kst["mixed_kernel_ms"])
     torch.cuda.synchronize()
     launches = eng.stats()["launches"] - launches0
+    ctr1 = eng.counters()
+    # binned pairs of the timed steps (the pair counters are exact)
+    binned_same = int(ctr1["num"].sum()) - int(ctr0["num"].sum())
+    binned_mixed = int(ctr1["den"].sum()) - int(ctr0["den"].sum())
     t_ms = sum(ms_steps)
     reduced_bins = None
     if world > 1:
@@ -1062,57 +1097,81 @@ def main() -> None:
             E.KERNEL_SCREENED_GRID, prec, 1,
             "screened, one launch per list, no sorting or culling", False)
 
-    # roofline of the step's pair binning against the live FP64 peak
+    # roofline of the dominant kernel, k_persistent_same: the FP64-pipe
+    # instructions it executes (ncu count per binned pair, see
+    # FP64_WARP_INST_PER_BINNED_PAIR) over its own time (CUDA events around
+    # its launches), against the FP64 FMA instruction rate measured live on
+    # this GPU (one FMA = one instruction on both sides)
     peaks = measure_fp64_peak()
     g0 = groups[args.warmup % len(groups)]
     fr = survival_fractions(g0, p)
+    t_step = statistics.median(ms_steps) * 1e-3
+    t_same_all = sum(same_ms) * 1e-3 if same_ms and min(same_ms) > 0 else t_ms * 1e-3
+    t_same = t_same_all / max(1, len(same_ms) or args.steps)
+    inst_peak = peaks["fp64_tflops"] * 1e12 / 2.0          # FP64 FMA instructions / s
+    per_binned = FP64_WARP_INST_PER_BINNED_PAIR if (
+        batched and args.precision == "fp64") else None
+    achieved = (per_binned * 32.0 * binned_same / t_same_all) if per_binned else None
+    # the reference's chain at the measured rates of its operations
+    # (the bound for an implementation that evaluates it on every pair)
     n = g0[0][0].size
     P_same = n * (n - 1) / 2
     P_mixed = sum(l1[0].size * l2[0].size for l1, l2 in g0[1])
-    ops = (sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)) * P_same +
-           sum(o * f for o, f in zip(STAGE_OPS_MIXED, fr)) * P_mixed)
-    t_step = statistics.median(ms_steps) * 1e-3
-    step_achieved = ops / t_step / 1e12
-    # the dominant kernel: same-event pairs' FP64 work over its own time
-    ops_same = sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)) * P_same
-    t_same = statistics.median(same_ms) * 1e-3 if same_ms and min(same_ms) > 0 else t_step
-    achieved = ops_same / t_same / 1e12
+    rates = (inst_peak, peaks["div_gops"] * 1e9, peaks["sqrt_gops"] * 1e9,
+             peaks["cos_gops"] * 1e9, peaks["atomic_gops_l2"] * 1e9)
+
+    def chain_seconds(counts, P):
+        return sum(P * f * sum(c / r for c, r in zip(stage, rates))
+                   for stage, f in zip(counts, fr))
+    chain_s = chain_seconds(STAGE_COUNTS_SAME, P_same) + chain_seconds(STAGE_COUNTS_MIXED, P_mixed)
     # DRAM bytes per launch of k_persistent_same on this workload (ncu,
-    # profiles/k_persistent_central_dram.md; not measured in this run)
-    traffic = 1.44e9 if (args.workload == "central" and args.precision == "fp64" and batched) \
-        else None
+    # profiles/k_persistent_same_fp64_central.md; not measured in this run)
+    traffic = CENTRAL_SAME_DRAM_BYTES if (args.workload == "central" and
+                                          args.precision == "fp64" and batched) else None
     try:
         hbm_peak = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]
     except (OSError, ValueError, KeyError):
         hbm_peak = 6800.0
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"], "traffic": traffic,
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": inst_peak,
+                "unit": "FP64 inst/s (warp instructions x 32)",
+                "frac": achieved / inst_peak if achieved else None, "traffic": traffic,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                                  "k_persistent_same, one central launch" if traffic else None,
+                                  "k_persistent_same, one central launch "
+                                  "(profiles/k_persistent_same_fp64_central.md)" if traffic else None,
                 "kernel": "k_persistent_same (same-event pairs; CUDA events around its "
                           "launch)" if batched and same_ms else "pair-binning kernels",
                 "kernel_ms": t_same * 1e3,
                 "mixed_kernel_ms": statistics.median(mixed_ms) if mixed_ms else None,
-                "algorithmic_work": "FP64 ops of the reference chain per same-event pair "
-                                    "(stage counts 11, 12, 5, 11, 15 of the reference loop x measured survival) x pairs",
+                "algorithmic_work": "FP64-pipe instructions per binned same-event pair "
+                                    "(ncu, one central launch) x binned pairs of the timed "
+                                    "launches; peak = live FP64 FMA probe / 2 (instructions)",
+                "fp64_warp_inst_per_binned_pair": per_binned,
+                "binned_same_pairs_per_launch": binned_same / max(1, args.steps),
                 "hbm": {"achieved_gbs": traffic / t_same / 1e9 if traffic else None,
                         "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json",
                         "frac": (traffic / t_same / 1e9 / hbm_peak) if traffic else None},
-                "step_achieved": step_achieved,
                 "peak_source": "measured live: FP64 FMA probe (lib/libhbt_probe.so)",
-                "ops_per_pair_same": round(sum(o * f for o, f in zip(STAGE_OPS_SAME, fr)), 2),
-                "ops_per_pair_mixed": round(sum(o * f for o, f in zip(STAGE_OPS_MIXED, fr)), 2),
-                "survival": [round(x, 4) for x in fr],
-                "fp32_tflops_measured": peaks["fp32_tflops"],
+                "probes": {k: peaks[k] for k in ("fp64_tflops", "fp32_tflops", "div_gops",
+                                                 "sqrt_gops", "cos_gops", "atomic_gops_l2",
+                                                 "atomic_gops_256mb")},
+                # the reference's per-pair chain on every pair at these rates
+                # (SURVEY-style stage counts x measured survival): the time an
+                # implementation of the plain chain cannot beat
+                "reference_chain": {
+                    "stage_counts_same": STAGE_COUNTS_SAME,
+                    "stage_counts_mixed": STAGE_COUNTS_MIXED,
+                    "survival": [round(x, 4) for x in fr],
+                    "bound_ms_per_step": chain_s * 1e3,
+                    "step_ms": t_step * 1e3,
+                    "step_vs_bound": chain_s / t_step},
                 # histogram updates of the same-event kernel: per binned pair
                 # four FP64 sums (one 32-byte bin) and one u64 count, against
                 # scattered FP64 atomic adds measured live on L2-resident data
-                # (the atomic units) and on 256 MB (beyond L2; the histogram
-                # is 238 MB with a 70 % L2 hit rate, ncu)
+                # (the atomic units) and on 256 MB (beyond L2)
                 "l2_atomics": {
-                    "achieved_gops": 5 * fr[4] * P_same / t_same / 1e9,
+                    "achieved_gops": 5 * binned_same / t_same_all / 1e9,
                     "peak_gops": peaks["atomic_gops_l2"],
-                    "frac": 5 * fr[4] * P_same / t_same / 1e9 / peaks["atomic_gops_l2"],
+                    "frac": 5 * binned_same / t_same_all / 1e9 / peaks["atomic_gops_l2"],
                     "scattered_256mb_gops": peaks["atomic_gops_256mb"],
                     "peak_source": "measured live: scattered FP64 atomicAdd probe over 32 MB "
                                    "and 256 MB (lib/libhbt_probe.so)"}}
@@ -1208,10 +1267,16 @@ def main() -> None:
                 "replica_reduction_binned_pairs": reduced_bins,
                 "clocks": clk.summary(),
                 "roofline": roofline,
-                "plain_kernel": plain,
+                "plain_kernel": dict(plain, frac_of_reference_chain_bound=(
+                    roofline["reference_chain"]["bound_ms_per_step"] / plain["ms_per_step"]))
+                if plain else None,
                 "speedup_vs_plain": (value / plain["value"]) if plain else None,
+                # each form against the plain kernel and against the best
+                # batched FP64 form (the headline) on the same GPU
                 "variants": {k: dict(v, speedup_vs_plain=(v["value"] / plain["value"])
-                                     if plain else None) for k, v in variants.items()},
+                                     if plain else None,
+                                     speedup_vs_batched_fp64=v["value"] / value)
+                             for k, v in variants.items()},
                 "e2e": e2e,
                 "cpu_baseline": cpu,
                 "small_config": small,

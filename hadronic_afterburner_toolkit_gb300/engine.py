@@ -304,6 +304,15 @@ class Engine:
         out["pairs_mixed"] = st["pairs_mixed"]
         return out
 
+    def counters(self) -> dict:
+        """The pair counters alone (hbt_read_counters): binned numerator and
+        denominator pairs per slot and per K_T bin of the q_inv histograms."""
+        ns, nk = self.n_slots, self.params["n_KT"]
+        ctr = [np.zeros(ns, np.uint64), np.zeros(ns, np.uint64),
+               np.zeros(nk, np.uint64), np.zeros(nk, np.uint64)]
+        self._check(self.L.hbt_read_counters(self._h, *[c.ctypes.data_as(_PU64) for c in ctr]))
+        return dict(num=ctr[0], den=ctr[1], num_qinv=ctr[2], den_qinv=ctr[3])
+
     def stats(self) -> dict:
         s = HbtStats()
         self._check(self.L.hbt_get_stats(self._h, ctypes.byref(s)))
