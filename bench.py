@@ -71,10 +71,10 @@ STAGE_OPS_MIXED = tuple(sum(c[:4]) for c in STAGE_COUNTS_MIXED)
 # form, all of the kernel's FP64 work (values, undecided pairs, tile loads)
 # divided by the pairs it bins: measured on one central group launch,
 # profiles/k_persistent_same_fp64_central.md.
-FP64_WARP_INST_PER_BINNED_PAIR = None
+FP64_WARP_INST_PER_BINNED_PAIR = 3549259087 / 1942004247
 # DRAM bytes (read + write) of one k_persistent_same launch on a central
 # group, FP64 form: same capture.
-CENTRAL_SAME_DRAM_BYTES = None
+CENTRAL_SAME_DRAM_BYTES = 290474240 + 1157159424
 
 
 def workload_params(name: str) -> dict:

@@ -214,7 +214,8 @@ struct SameCtas {
 constexpr int kMixedCtas = 6;
 
 // Same-event items [base, min(end, queued)) pulled by persistent CTAs.
-template <bool AZ, bool BOOST, int PREC>
+// MODE: fast binning, or one pass of ordered cap admission.
+template <bool AZ, bool BOOST, int PREC, int MODE>
 __global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(Device d, BatchDev b, unsigned base,
                                                            unsigned end) {
     __shared__ TileSmem sm;
@@ -236,14 +237,14 @@ __global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(D
         const double *c[8];
 #pragma unroll
         for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
-        same_tile_pair<AZ, BOOST, PREC>(dd, sm, cs, c, b.orig + la.off, la.n, (long long)it.ti * FT,
-                                        (long long)it.tj * FT);
+        same_tile_pair<AZ, BOOST, PREC, MODE>(dd, sm, cs, c, b.orig + la.off, la.n,
+                                              (long long)it.ti * FT, (long long)it.tj * FT);
         __syncthreads();
     }
 }
 
 // Mixed-event items, all in one launch.
-template <bool AZ, bool BOOST>
+template <bool AZ, bool BOOST, int MODE>
 __global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, BatchDev b) {
     __shared__ TileSmem sm;
     __shared__ Device dsm;
@@ -264,8 +265,9 @@ __global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, B
             c1[f] = b.table + (long long)f * b.cap + la.off;
             c2[f] = b.table + (long long)f * b.cap + lb.off;
         }
-        mixed_tile_pair<AZ, BOOST>(dd, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
-                                   (long long)it.tj * FT);
+        mixed_tile_pair<AZ, BOOST, MODE>(dd, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
+                                         (long long)it.tj * FT, b.orig + la.off,
+                                         b.orig + lb.off);
         __syncthreads();
     }
 }
@@ -291,26 +293,65 @@ int persistent_grid(K kernel, int grid) {
     return sm_count() * nb;
 }
 
-template <bool AZ, bool BOOST, int PREC>
+template <bool AZ, bool BOOST, int PREC, int MODE>
 cudaError_t launch_same_items(const Device &d, const BatchDev &b, unsigned base, unsigned end,
                               int grid, cudaStream_t st) {
-    grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC>, grid);
-    k_persistent_same<AZ, BOOST, PREC><<<grid, FT, 0, st>>>(d, b, base, end);
+    grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC, MODE>, grid);
+    k_persistent_same<AZ, BOOST, PREC, MODE><<<grid, FT, 0, st>>>(d, b, base, end);
     return cudaGetLastError();
 }
 
-template <bool AZ, bool BOOST>
+template <bool AZ, bool BOOST, int MODE>
 cudaError_t launch_mixed_items(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
-    grid = persistent_grid(k_persistent_mixed<AZ, BOOST>, grid);
-    k_persistent_mixed<AZ, BOOST><<<grid, FT, 0, st>>>(d, b);
+    grid = persistent_grid(k_persistent_mixed<AZ, BOOST, MODE>, grid);
+    k_persistent_mixed<AZ, BOOST, MODE><<<grid, FT, 0, st>>>(d, b);
     return cudaGetLastError();
+}
+
+// The same-event kernel for a precision form and admission mode.  The
+// COUNT pass only counts decided pairs per row, the same in every form, so
+// it runs the FP64 form's kernel.
+template <int MODE>
+cudaError_t launch_same_mode(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+                             int grid, cudaStream_t st) {
+    const bool az = d.g.azimuthal, boost = d.g.boost;
+    // the forms this mode instantiates: FP64 only for COUNT
+    constexpr int P1 = MODE == MODE_COUNT ? 0 : 1, P2 = MODE == MODE_COUNT ? 0 : 2;
+    const int prec = MODE == MODE_COUNT ? 0 : d.precision;
+#define HBT_P(AZ_, BO_, PR_) return launch_same_items<AZ_, BO_, PR_, MODE>(d, b, base, end, grid, st)
+    if (prec == 0) {
+        if (az && boost) HBT_P(true, true, 0);
+        if (az) HBT_P(true, false, 0);
+        if (boost) HBT_P(false, true, 0);
+        HBT_P(false, false, 0);
+    }
+    if (prec == 1) {
+        if (az && boost) HBT_P(true, true, P1);
+        if (az) HBT_P(true, false, P1);
+        if (boost) HBT_P(false, true, P1);
+        HBT_P(false, false, P1);
+    }
+    if (az && boost) HBT_P(true, true, P2);
+    if (az) HBT_P(true, false, P2);
+    if (boost) HBT_P(false, true, P2);
+    HBT_P(false, false, P2);
+#undef HBT_P
+}
+
+template <int MODE>
+cudaError_t launch_mixed_mode(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
+    const bool az = d.g.azimuthal, boost = d.g.boost;
+    if (az && boost) return launch_mixed_items<true, true, MODE>(d, b, grid, st);
+    if (az) return launch_mixed_items<true, false, MODE>(d, b, grid, st);
+    if (boost) return launch_mixed_items<false, true, MODE>(d, b, grid, st);
+    return launch_mixed_items<false, false, MODE>(d, b, grid, st);
 }
 
 }  // namespace
 
 int persistent_blocks_per_sm() {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_persistent_same<true, true, 0>, FT,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_persistent_same<true, true, 0, MODE_FAST>, FT,
                                                       0) != cudaSuccess)
         return 4;
     return nb > 0 ? nb : 1;
@@ -326,7 +367,7 @@ size_t batch_sort_temp_bytes(long long cap) {
 
 cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
                       const Device *host_devs, int n_host_devs, cudaStream_t st,
-                      cudaEvent_t *marks) {
+                      cudaEvent_t *marks, int mode) {
     cudaError_t e;
     const int gs = 152 * 8;
     if (b.total > 0) {
@@ -349,8 +390,8 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
         k_cull<<<gs, 256, 0, st>>>(b);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    const bool az = d.g.azimuthal, boost = d.g.boost;
-    const int prec = d.precision;
+    // the COUNT pass bins nothing: no FP32 partials to merge
+    const int prec = mode == MODE_COUNT ? 0 : d.precision;
     // same-event items (chunked for the FP32-weight form)
     const unsigned upper = b.same_cap;
     if (chunk == 0 || prec != 1) chunk = upper;
@@ -360,24 +401,12 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
             (unsigned)min((unsigned long long)base + chunk, (unsigned long long)upper);
         if (base > 0 && (e = cudaMemsetAsync(b.item_next, 0, sizeof(unsigned), st)) != cudaSuccess)
             return e;
-#define HBT_P(AZ_, BO_, PR_) e = launch_same_items<AZ_, BO_, PR_>(d, b, base, end, grid, st)
-        if (prec == 0) {
-            if (az && boost) HBT_P(true, true, 0);
-            else if (az) HBT_P(true, false, 0);
-            else if (boost) HBT_P(false, true, 0);
-            else HBT_P(false, false, 0);
-        } else if (prec == 1) {
-            if (az && boost) HBT_P(true, true, 1);
-            else if (az) HBT_P(true, false, 1);
-            else if (boost) HBT_P(false, true, 1);
-            else HBT_P(false, false, 1);
-        } else {
-            if (az && boost) HBT_P(true, true, 2);
-            else if (az) HBT_P(true, false, 2);
-            else if (boost) HBT_P(false, true, 2);
-            else HBT_P(false, false, 2);
-        }
-#undef HBT_P
+        if (mode == MODE_COUNT)
+            e = launch_same_mode<MODE_COUNT>(d, b, base, end, grid, st);
+        else if (mode == MODE_ORDER)
+            e = launch_same_mode<MODE_ORDER>(d, b, base, end, grid, st);
+        else
+            e = launch_same_mode<MODE_FAST>(d, b, base, end, grid, st);
         if (e != cudaSuccess) return e;
         if (prec == 1 && !b.devs) {
             if ((e = launch_merge(d, st, b.n_items, base)) != cudaSuccess) return e;
@@ -390,10 +419,12 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
     if (marks && (e = cudaEventRecord(marks[2], st)) != cudaSuccess) return e;
     // mixed-event items
     if (b.mixed_cap > 0) {
-        if (az && boost) e = launch_mixed_items<true, true>(d, b, grid, st);
-        else if (az) e = launch_mixed_items<true, false>(d, b, grid, st);
-        else if (boost) e = launch_mixed_items<false, true>(d, b, grid, st);
-        else e = launch_mixed_items<false, false>(d, b, grid, st);
+        if (mode == MODE_COUNT)
+            e = launch_mixed_mode<MODE_COUNT>(d, b, grid, st);
+        else if (mode == MODE_ORDER)
+            e = launch_mixed_mode<MODE_ORDER>(d, b, grid, st);
+        else
+            e = launch_mixed_mode<MODE_FAST>(d, b, grid, st);
         if (e != cudaSuccess) return e;
     }
     if (marks && (e = cudaEventRecord(marks[3], st)) != cudaSuccess) return e;

@@ -83,8 +83,11 @@ size_t batch_sort_temp_bytes(long long cap);
 // host_devs[k] (the host copies of b.devs) for a batch of many analyses.
 // marks (optional, 4 events): recorded before and after the same-event
 // kernels (with their merges) and before and after the mixed-event kernel.
+// mode: MODE_FAST bins every pair; MODE_COUNT / MODE_ORDER run one pass of
+// ordered cap admission over the batch (d.caps; rows are positions in the
+// callers' lists).
 cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chunk,
                       const Device *host_devs, int n_host_devs, cudaStream_t st,
-                      cudaEvent_t *marks = nullptr);
+                      cudaEvent_t *marks = nullptr, int mode = MODE_FAST);
 
 }  // namespace hbt

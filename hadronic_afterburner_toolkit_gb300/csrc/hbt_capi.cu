@@ -247,9 +247,25 @@ bool caps_may_bind(const hbt_ctx *c, int mixed, u64 P) {
     return false;
 }
 
-// Ordered admission for one launch (same-event: mixed = 0).
+hbt_status run_fast_jobs(hbt_ctx *c, std::vector<hbt::FastJob> jobs, int mode = hbt::MODE_FAST);
+bool batched_ok(const hbt_ctx *c);
+
+// Ordered admission for one launch (same-event: mixed = 0).  The two
+// passes over every pair (COUNT: survivors per stream bin and row; ORDER:
+// the rows before each bin's cut) run on the batched screened kernels when
+// the context uses them, else on the reference-chain kernels; the cut row
+// of each bin is admitted pair by pair in the reference's order
+// (k_straddle).
 hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
                           const double *const *a, const double *const *b) {
+    const bool batched = batched_ok(c);
+    hbt::FastJob job = {};
+    job.kind = mixed;
+    job.na = rows;
+    job.nb = mixed ? cols : 0;
+    for (int f = 0; f < (mixed ? 4 : 8); f++) job.a[f] = a[f];
+    if (mixed)
+        for (int f = 0; f < 4; f++) job.b[f] = b[f];
     TRY(drain_deferrals(c));
     std::vector<u64> ctr;
     TRY(read_counters(c, ctr));
@@ -276,11 +292,15 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
     CU(cudaMemsetAsync(c->rowcnt.p, 0, (size_t)nst * rows * sizeof(unsigned), c->stream));
     CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
     // pass A: survivors per (stream bin, row)
-    if (mixed)
-        CU(hbt::launch_mixed(c->d, hbt::MODE_COUNT, rows, a, cols, b, c->stream));
-    else
-        CU(hbt::launch_same(c->d, hbt::MODE_COUNT, rows, a, c->stream));
-    c->st.launches++;
+    if (batched) {
+        TRY(run_fast_jobs(c, std::vector<hbt::FastJob>{job}, hbt::MODE_COUNT));
+    } else {
+        if (mixed)
+            CU(hbt::launch_mixed(c->d, hbt::MODE_COUNT, rows, a, cols, b, c->stream));
+        else
+            CU(hbt::launch_same(c->d, hbt::MODE_COUNT, rows, a, c->stream));
+        c->st.launches++;
+    }
     // deferred K_phi bins: decided here, added to the row counts, and looked
     // up by the admission passes
     if (c->prm.azimuthal_flag) {
@@ -315,15 +335,21 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
                        c->stream));
     CU(hbt::launch_cut(c->d, rows, nst, ptr<unsigned long long>(c->remaining), c->stream));
     // pass B: rows before each cut, then the cut rows in pair order
-    if (mixed) {
-        CU(hbt::launch_mixed(c->d, hbt::MODE_ORDER, rows, a, cols, b, c->stream));
-        CU(hbt::launch_mixed_straddle(c->d, rows, a, cols, b, nst, c->stream));
+    if (batched) {
+        TRY(run_fast_jobs(c, std::vector<hbt::FastJob>{job}, hbt::MODE_ORDER));
     } else {
-        CU(hbt::launch_same(c->d, hbt::MODE_ORDER, rows, a, c->stream));
-        CU(hbt::launch_same_straddle(c->d, rows, a, nst, c->stream));
+        if (mixed)
+            CU(hbt::launch_mixed(c->d, hbt::MODE_ORDER, rows, a, cols, b, c->stream));
+        else
+            CU(hbt::launch_same(c->d, hbt::MODE_ORDER, rows, a, c->stream));
+        c->st.launches++;
     }
+    if (mixed)
+        CU(hbt::launch_mixed_straddle(c->d, rows, a, cols, b, nst, c->stream));
+    else
+        CU(hbt::launch_same_straddle(c->d, rows, a, nst, c->stream));
     CU(cudaStreamSynchronize(c->stream));
-    c->st.launches += 4;
+    c->st.launches += 2;
     c->st.ordered_passes++;
     c->d.caps.n_resolved = 0;
     return HBT_OK;
@@ -356,8 +382,9 @@ hbt::Tuning runner_tuning(const hbt_ctx *c, const hbt_tuning &t) {
     return r;
 }
 
-// Sort, cull and bin fast jobs of this analysis in one persistent launch.
-hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs) {
+// Sort, cull and bin fast jobs of this analysis in one persistent launch
+// (mode: MODE_FAST, or a pass of ordered cap admission).
+hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs, int mode) {
     const double Q = std::max(std::fabs(c->d.g.q_lo), std::fabs(c->d.g.q_hi));
     for (FastJob &j : jobs) {
         j.dev = 0;
@@ -365,7 +392,7 @@ hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs) {
         j.boost = c->d.g.boost;
     }
     std::string err;
-    if (!c->runner.run(jobs, c->d, runner_tuning(c, c->tune), c->stream, err))
+    if (!c->runner.run(jobs, c->d, runner_tuning(c, c->tune), c->stream, err, mode))
         return fail(c, HBT_ERR_CUDA, err);
     c->st.launches += 6;
     if (c->runner.last_graph_reuse() == 0) c->st.graph_captures++;

@@ -38,8 +38,8 @@ bool BatchRunner::grow(Buf &b, size_t bytes, std::string &err) {
 }
 
 bool BatchRunner::run(const std::vector<FastJob> &jobs, const Device &d, const Tuning &t,
-                      cudaStream_t st, std::string &err) {
-    return run_impl(jobs, d, nullptr, nullptr, 0, t, st, err);
+                      cudaStream_t st, std::string &err, int mode) {
+    return run_impl(jobs, d, nullptr, nullptr, 0, t, st, err, mode);
 }
 
 bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<Device> &devs,
@@ -66,7 +66,7 @@ bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<
         return false;
     }
     return run_impl(jobs, devs[0], static_cast<const Device *>(devs_.p), devs.data(),
-                    (int)devs.size(), t, st, err);
+                    (int)devs.size(), t, st, err, MODE_FAST);
 }
 
 // The graph captured for one set of launch arguments stays valid while they
@@ -96,7 +96,7 @@ bool BatchRunner::kernel_times(float &same_ms, float &mixed_ms) {
 }
 
 cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device *devs_host,
-                                int n_devs, const Tuning &t, cudaStream_t st) {
+                                int n_devs, const Tuning &t, cudaStream_t st, int mode) {
     cudaEvent_t *marks = nullptr;
     if (t.time_kernels) {
         for (cudaEvent_t &e : marks_)
@@ -108,7 +108,7 @@ cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device
     if (!t.graph || st == nullptr || cudaStreamIsCapturing(st, &cap) != cudaSuccess ||
         cap != cudaStreamCaptureStatusNone) {
         last_reuse_ = -1;
-        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks);
+        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks, mode);
     }
     std::vector<unsigned char> key;
     auto put = [&](const void *p, size_t n) {
@@ -121,6 +121,7 @@ cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device
     put(&t.chunk, sizeof(t.chunk));
     put(&n_devs, sizeof(n_devs));
     put(&timed_, sizeof(timed_));
+    put(&mode, sizeof(mode));
     if (n_devs > 0) put(devs_host, sizeof(Device) * n_devs);
     if (exec_ && key == key_) {
         last_reuse_ = 1;
@@ -130,11 +131,11 @@ cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device
         // a new shape: run directly; capture if it comes again
         last_key_.swap(key);
         last_reuse_ = -1;
-        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks);
+        return run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks, mode);
     }
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    const cudaError_t run_e = run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks);
+    const cudaError_t run_e = run_batch(d, b, t.grid, t.chunk, devs_host, n_devs, st, marks, mode);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(st, &g);
     if (run_e != cudaSuccess || e != cudaSuccess) {
@@ -166,7 +167,7 @@ cudaError_t BatchRunner::launch(const Device &d, const BatchDev &b, const Device
 
 bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
                            const Device *devs_dev, const Device *devs_host, int n_devs,
-                           const Tuning &t, cudaStream_t st, std::string &err) {
+                           const Tuning &t, cudaStream_t st, std::string &err, int mode) {
     std::vector<BatchList> lists;
     std::vector<BatchJob> bj;
     std::vector<long long> list_off, tile_off, pair_off;
@@ -277,7 +278,7 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
     b.inv_cell_y = 1.0 / t.cell_y;
     b.devs = devs_dev;
     b.n_devs = n_devs;
-    const cudaError_t e = launch(d, b, devs_host, n_devs, t, st);
+    const cudaError_t e = launch(d, b, devs_host, n_devs, t, st, mode);
     if (e != cudaSuccess) {
         err = std::string("batch launch failed: ") + cudaGetErrorString(e);
         return false;

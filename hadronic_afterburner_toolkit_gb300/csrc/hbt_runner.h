@@ -43,9 +43,10 @@ class BatchRunner {
 
     // Runs the jobs of one analysis: every job bins into `d`.  Returns
     // false and sets `err` on failure.  Allocates scratch on first use and
-    // when a batch outgrows it.
+    // when a batch outgrows it.  mode: MODE_FAST, or one pass (MODE_COUNT,
+    // MODE_ORDER) of ordered cap admission with d.caps.
     bool run(const std::vector<FastJob> &jobs, const Device &d, const Tuning &t, cudaStream_t st,
-             std::string &err);
+             std::string &err, int mode = MODE_FAST);
 
     // Runs jobs of several analyses in one launch: job.dev indexes `devs`,
     // whose entries must share azimuthal_flag, long_comoving_boost and
@@ -77,10 +78,10 @@ class BatchRunner {
     bool grow(Buf &b, size_t bytes, std::string &err);
     bool run_impl(const std::vector<FastJob> &jobs, const Device &d, const Device *devs_dev,
                   const Device *devs_host, int n_devs, const Tuning &t, cudaStream_t st,
-                  std::string &err);
+                  std::string &err, int mode);
     // Runs the device pipeline, through a cached CUDA graph when possible.
     cudaError_t launch(const Device &d, const BatchDev &b, const Device *devs_host, int n_devs,
-                       const Tuning &t, cudaStream_t st);
+                       const Tuning &t, cudaStream_t st, int mode);
     Buf lists_, jobs_, offs_, table_, keys_, vals_, sort_temp_, boxes_, items_, counters_, devs_;
     long long last_pairs_ = 0, last_same_ = 0, last_mixed_ = 0;
     cudaStream_t last_stream_ = nullptr;

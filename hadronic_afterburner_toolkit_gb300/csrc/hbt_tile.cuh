@@ -633,14 +633,45 @@ static __device__ __noinline__ void undecided_pair64(const Device &d, const doub
     consume<false, MODE_FAST>(d, i, j, n, n, full);
 }
 
+// A pair the screens left undecided, under ordered cap admission (COUNT
+// or ORDER mode): the reference chain decides; the pair is counted or
+// admitted at its position in the caller's lists (row, col).  Out of line,
+// like the fast-mode helpers above.
+template <bool MIXED, int MODE>
+__device__ __noinline__ void undecided_pair_ordered(const Device &d, const double *A,
+                                                    const double *B, long long row,
+                                                    long long col, long long rows,
+                                                    long long cols) {
+    const Chain full = pair_chain<MIXED>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2], B[3],
+                                         MIXED ? nullptr : A + 4, MIXED ? nullptr : B + 4);
+    consume<MIXED, MODE>(d, row, col, cols, rows, full);
+}
+
+// Ordered cap admission of a pair the screen decided (slot, row in the
+// caller's order): COUNT adds it to its row's survivor count and returns
+// false; ORDER returns true when its row lies before the slot's cut row
+// (the cut row itself is admitted pair by pair by k_straddle).
+template <int MODE>
+__device__ __forceinline__ bool admit(const Device &d, int slot, long long row, long long rows) {
+    if (MODE == MODE_FAST) return true;
+    if (MODE == MODE_COUNT) {
+        atomicAdd(d.caps.rowcnt + (long long)slot * rows + row, 1u);
+        return false;
+    }
+    return row < d.caps.row_cut[slot];
+}
+
 // Same-event pairs of the tiles starting at i0 and j0 (i0 <= j0) of one list
 // of n particles with columns c = px py pz E x y z t.  Every unordered pair
 // is visited once (position j > i); it is oriented as the reference orients
 // it, q = p_first - p_second with `first` the particle earlier in the
 // caller's list: orig[k] is that original index of row k, or nullptr when
-// the rows are in the caller's order.  Called by all FT threads of the CTA;
-// the caller syncs before reusing `sm`.
-template <bool AZ, bool BOOST, int PREC>
+// the rows are in the caller's order.  MODE selects the admission: FAST bins
+// every pair; COUNT and ORDER are the two passes of ordered cap admission,
+// which see each pair at its row (the earlier of its two positions in the
+// caller's list).  Called by all FT threads of the CTA; the caller syncs
+// before reusing `sm`.
+template <bool AZ, bool BOOST, int PREC, int MODE = MODE_FAST>
 __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, const double2 *cs,
                                                const double *const *c, const unsigned *orig,
                                                long long n, long long i0, long long j0) {
@@ -715,6 +746,23 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
         const bool swap = (e >> 16) & 1u;
         const int slot = (e >> 17) & 1u ? -1 : (int)(e >> 18);
         const int bin = (int)e2.y;
+        if (MODE != MODE_FAST) {
+            const long long oa = sm.oi[qi], ob = sm.oj[qj];
+            const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
+            if (slot < 0) {
+                double A[8], B[8];
+#pragma unroll
+                for (int f = 0; f < 8; f++) {
+                    const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+                    const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+                    A[f] = swap ? v : u;
+                    B[f] = swap ? u : v;
+                }
+                undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
+                return;
+            }
+            if (!admit<MODE>(d, slot, row, n)) return;
+        }
         if (PREC == 1 && slot >= 0) {
             // the pair as stored (i, j); swapping first and second negates
             // q_out, q_side, q_long exactly and leaves the phase unchanged
@@ -834,12 +882,17 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
 }
 
 // Mixed-event pairs of the list-1 tile at i0 (n1 particles, columns l1 =
-// px py pz E) and the list-2 tile at j0 (n2 particles, columns l2).
-template <bool AZ, bool BOOST>
+// px py pz E) and the list-2 tile at j0 (n2 particles, columns l2).  Under
+// ordered cap admission (MODE COUNT / ORDER) a pair's row and column are
+// its positions in the caller's lists, orig1 / orig2 (nullptr: the rows are
+// in the caller's order).
+template <bool AZ, bool BOOST, int MODE = MODE_FAST>
 __device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
                                                 const double *const *l1, long long n1,
                                                 const double *const *l2, long long n2,
-                                                long long i0, long long j0) {
+                                                long long i0, long long j0,
+                                                const unsigned *orig1 = nullptr,
+                                                const unsigned *orig2 = nullptr) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     sm.fi[tid] = (i0 + tid < n1) ? make_float4((float)l1[0][i0 + tid], (float)l1[1][i0 + tid],
                                                (float)l1[2][i0 + tid], (float)l1[3][i0 + tid])
@@ -872,6 +925,19 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
                 const int ip = kphi_screen(S, s);
                 slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
             }
+        }
+        if (MODE != MODE_FAST) {
+            const long long row = orig1 ? (long long)orig1[i0 + qi] : i0 + qi;
+            const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
+            if (slot < 0) {
+                const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi],
+                                     l1[3][i0 + qi]};
+                const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
+                                     l2[3][j0 + qj]};
+                undecided_pair_ordered<true, MODE>(d, A, B, row, col, n1, n2);
+                return;
+            }
+            if (!admit<MODE>(d, slot, row, n1)) return;
         }
         if (slot >= 0) {
             atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);

@@ -290,3 +290,37 @@ def test_kaon_groups_precision_forms_against_the_oracle(host):
         assert np.array_equal(h["count"], o["count"]) and np.array_equal(h["den"], o["den"])
         e = _precision_errors(h, o)
         assert e["num_per_pair"] <= b_num and e["q_per_pair"] <= b_q * 0.15, (precision, e)
+
+
+@pytest.mark.parametrize("azimuthal", [0, 1])
+def test_small_configuration_with_a_binding_cap(small_run, azimuthal):
+    """The small configuration in full with needed_number_of_pairs = 1e6,
+    which binds in the busiest K_T (x K_phi) slots within the first buffers:
+    pairs are admitted in the reference's order (src/HBT_correlation.cpp
+    :400-406, :651-655) through the batched kernels' count and order passes
+    plus the pair-by-pair cut row, one job at a time.  Counts, denominators
+    and counters identical to the oracle's buffer loop; K_phi edges decided
+    on the host take part in the order."""
+    ev, bufs, _, jobs = small_run
+    p = dict(SMALL, needed_number_of_pairs=1e6, azimuthal_flag=azimuthal, n_Kphi=4)
+    orc = oracle_lib.Oracle(number_of_mixed_events=5, seed=1, **p)
+    psis = []
+    for a, b in bufs:
+        g = synth.subset(ev, a, b)
+        orc.process_buffer(g)
+        psis.append(oracle_lib.event_plane_angle(g.px, g.py, 2) if azimuthal else None)
+    o = orc.hist()
+    eng = engine.Engine(device=0, **p)
+    at = 0
+    for (a, b), psi in zip(bufs, psis):
+        nj = 1 + (b - a)
+        if psi is not None:
+            eng.set_psi_ref(psi)
+        eng.bin_batch(jobs[at:at + nj])
+        at += nj
+    h = eng.hist()
+    st = eng.stats()
+    eng.close()
+    assert st["ordered_passes"] > 0
+    assert (o["ctr_num"] > 1e6).any() and (o["ctr_den"] > 1e6).any()
+    parity.compare(h, o, q_scale=0.15)
