@@ -537,6 +537,42 @@ rapidity_shift = 0.0
 """
 
 
+def capped_leg(E, torch, dev, dgroups, groups, p, local, uncapped_ms, cap=3e7, n_groups=3):
+    """The central workload at the reference's default pair cap,
+    needed_number_of_pairs = 3e7 (parameters.dat), which binds in the first
+    group: every job runs the two passes of ordered cap admission (count
+    survivors per row, admit the rows before each slot's cut) on the batched
+    kernels, and the cut rows pair by pair, one job at a time in the
+    reference's order.  Later groups find most slots full.  Device-resident
+    inputs, CUDA events around each group."""
+    eng = E.Engine(device=local, **dict(p, needed_number_of_pairs=cap))
+    stream = torch.cuda.Stream(device=dev)
+    eng.set_stream(stream.cuda_stream)
+    ms, prs = [], 0
+    for g in range(min(n_groups, len(dgroups))):
+        dc, dm = dgroups[g]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        eng.bin_batch([("same", dc)] + [("mixed", l1, l2) for l1, l2 in dm], device=True)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        prs += group_pairs(groups[g])
+    ctr = eng.counters()
+    st = eng.stats()
+    eng.close()
+    return {"needed_number_of_pairs": cap, "groups": len(ms), "ms_per_group": ms,
+            "pairs_per_s": prs / (sum(ms) * 1e-3),
+            "uncapped_ms_per_group": uncapped_ms,
+            "first_group_vs_uncapped": ms[0] / uncapped_ms,
+            "slots_at_cap": int((ctr["num"] > cap).sum()),
+            "ordered_passes": st["ordered_passes"],
+            "path": "count and order passes on the batched screened kernels, cut rows "
+                    "by the pair-order kernel, jobs one at a time"}
+
+
 def ingest_leg(n_events: int = 200, seed: int = 3) -> dict:
     """The reader (read_in_mode 10: gzip text, ~100 oversampled events per
     150k-particle buffer as on the central workload): the line-by-line
@@ -955,6 +991,8 @@ def main() -> None:
                     help="skip the radii-fit leg")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the FP32-weight against FP64 error report")
+    ap.add_argument("--no-capped", action="store_true",
+                    help="skip the central workload at the default pair cap (3e7)")
     ap.add_argument("--no-ingest", action="store_true",
                     help="skip the reader timing (line-by-line against block reader)")
     args = ap.parse_args()
@@ -1237,6 +1275,9 @@ def main() -> None:
     small = None
     if not args.no_uneven and rank == 0 and args.workload == "central":
         small = small_leg(E, torch, dev, stream, flush, local)
+    capped = None
+    if not args.no_capped and rank == 0 and args.workload == "central" and batched:
+        capped = capped_leg(E, torch, dev, dgroups, groups, p, local, t_ms / args.steps)
     if not args.no_uneven:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
@@ -1280,6 +1321,7 @@ def main() -> None:
                 "e2e": e2e,
                 "cpu_baseline": cpu,
                 "small_config": small,
+                "capped": capped,
                 "uneven": uneven,
                 "serving": serving,
                 "ingest": ingest,

@@ -40,6 +40,9 @@ GPU_UNITS = {
     "hbt_fast.cu": ["--fmad=false"],
     "hbt_noalloc.cu": ["--fmad=false"],
     "hbt_batch.cu": ["--fmad=false"],
+    "hbt_persist_fast.cu": ["--fmad=false"],
+    "hbt_persist_caps.cu": ["--fmad=false"],
+    "hbt_persist_qinv.cu": ["--fmad=false"],
     "hbt_runner.cu": [],
     "hbt_server.cu": ["--fmad=false"],
     "hbt_bf.cu": ["--fmad=false"],

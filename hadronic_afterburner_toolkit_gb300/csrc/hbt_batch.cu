@@ -19,14 +19,15 @@
 //     which grows with m_T1, m_T2 and |y1 - y2|, so its smallest value over
 //     two tiles bounds |q_long| from below; without the boost q_long = q_z.
 //     Each bound carries a 1e-6 relative margin for rounding;
-//  4. k_persistent_same / k_persistent_mixed: persistent CTAs (5 per SM)
-//     pull (job, i-tile, j-tile) items from the culled same-event and
-//     mixed-event queues and run the screened tile-pair bodies of
-//     hbt_tile.cuh.  The FP32-weight form runs the same-event queue in
-//     chunks and merges the FP32 partials between them.
+//  4. k_persistent_same / k_persistent_mixed (hbt_persist.cuh): persistent
+//     CTAs (5 per SM) pull (job, i-tile, j-tile) items from the culled
+//     same-event and mixed-event queues and run the screened tile-pair
+//     bodies of hbt_tile.cuh.  The FP32-weight form runs the same-event
+//     queue in chunks and merges the FP32 partials between them.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "hbt_batch.cuh"
+#include "hbt_persist.cuh"
 #include "hbt_tile.cuh"
 
 namespace hbt {
@@ -138,6 +139,7 @@ __global__ void k_boxes(BatchDev b) {
 
 // Can a pair with one particle in box a and one in box b pass the windows?
 __device__ __forceinline__ bool boxes_may_pair(const BatchJob &b, const Box &a, const Box &c) {
+    if (b.qinv) return true;
     const double gx = fmax(0.0, fmax(a.x0 - c.x1, c.x0 - a.x1));
     const double gy = fmax(0.0, fmax(a.y0 - c.y1, c.y0 - a.y1));
     if (gx * gx + gy * gy > b.qt2_max) return false;
@@ -188,173 +190,23 @@ __global__ void k_cull(BatchDev b) {
     }
 }
 
-// Engine descriptor of an item: the launch's own, or (serving many
-// analyses) the job's entry of b.devs copied into shared memory.
-__device__ __forceinline__ const Device &item_device(const Device &d, const BatchDev &b,
-                                                    const BatchJob &job, Device &dsm) {
-    if (!b.devs) return d;
-    const int *src = reinterpret_cast<const int *>(b.devs + job.dev);
-    int *dst = reinterpret_cast<int *>(&dsm);
-    for (int k = threadIdx.x; k < (int)(sizeof(Device) / sizeof(int)); k += blockDim.x)
-        dst[k] = src[k];
-    __syncthreads();
-    return dsm;
-}
-
-// Resident CTAs per SM (register budget 65536 / (128 x CTAs)): measured on
-// GB300, the FP64 form of the same-event kernel is fastest at 5 (its FP64
-// values need the registers), the double-float form at 4 (118 registers, no
-// spills: 167 ms per central group, against 194 ms at 5 and 234 ms at 6,
-// where its 80 registers spill in the pair loop), the FP32-weight form and
-// the mixed-event kernel at 6.
-template <int PREC>
-struct SameCtas {
-    static constexpr int value = PREC == 1 ? 6 : (PREC == 2 ? 4 : 5);
-};
-constexpr int kMixedCtas = 6;
-
-// Same-event items [base, min(end, queued)) pulled by persistent CTAs.
-// MODE: fast binning, or one pass of ordered cap admission.
-template <bool AZ, bool BOOST, int PREC, int MODE>
-__global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(Device d, BatchDev b, unsigned base,
-                                                           unsigned end) {
-    __shared__ TileSmem sm;
-    __shared__ Device dsm;
-    __shared__ unsigned item;
-    __shared__ double2 cs[COS_TABLE];
-    if (PREC == 0) fill_cos_table(cs);
-    if (PREC == 2) fill_df_table(reinterpret_cast<float4 *>(cs));
-    const unsigned stop = min(end, min(b.n_items[0], b.same_cap));
-    for (;;) {
-        if (threadIdx.x == 0) item = base + atomicAdd(b.item_next, 1u);
-        __syncthreads();
-        const unsigned k = item;
-        if (k >= stop) break;
-        const Item it = b.items[k];
-        const BatchJob &job = b.jobs[it.job];
-        const Device &dd = item_device(d, b, job, dsm);
-        const BatchList &la = b.lists[job.la];
-        const double *c[8];
-#pragma unroll
-        for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
-        same_tile_pair<AZ, BOOST, PREC, MODE>(dd, sm, cs, c, b.orig + la.off, la.n,
-                                              (long long)it.ti * FT, (long long)it.tj * FT);
-        __syncthreads();
-    }
-}
-
-// Mixed-event items, all in one launch.
-template <bool AZ, bool BOOST, int MODE>
-__global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, BatchDev b) {
-    __shared__ TileSmem sm;
-    __shared__ Device dsm;
-    __shared__ unsigned item;
-    const unsigned stop = min(b.n_items[1], b.mixed_cap);
-    for (;;) {
-        if (threadIdx.x == 0) item = atomicAdd(b.item_next + 1, 1u);
-        __syncthreads();
-        const unsigned k = item;
-        if (k >= stop) break;
-        const Item it = b.items[b.same_cap + k];
-        const BatchJob &job = b.jobs[it.job];
-        const Device &dd = item_device(d, b, job, dsm);
-        const BatchList &la = b.lists[job.la], &lb = b.lists[job.lb];
-        const double *c1[4], *c2[4];
-#pragma unroll
-        for (int f = 0; f < 4; f++) {
-            c1[f] = b.table + (long long)f * b.cap + la.off;
-            c2[f] = b.table + (long long)f * b.cap + lb.off;
-        }
-        mixed_tile_pair<AZ, BOOST, MODE>(dd, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
-                                         (long long)it.tj * FT, b.orig + la.off,
-                                         b.orig + lb.off);
-        __syncthreads();
-    }
-}
-
-int sm_count() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            sms = 152;
-    }
-    return sms;
-}
-
-// grid > 0: that many CTAs; otherwise one CTA per resident slot.
-template <class K>
-int persistent_grid(K kernel, int grid) {
-    if (grid > 0) return grid;
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, FT, 0) != cudaSuccess || nb < 1)
-        nb = 4;
-    return sm_count() * nb;
-}
-
-template <bool AZ, bool BOOST, int PREC, int MODE>
-cudaError_t launch_same_items(const Device &d, const BatchDev &b, unsigned base, unsigned end,
-                              int grid, cudaStream_t st) {
-    grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC, MODE>, grid);
-    k_persistent_same<AZ, BOOST, PREC, MODE><<<grid, FT, 0, st>>>(d, b, base, end);
-    return cudaGetLastError();
-}
-
-template <bool AZ, bool BOOST, int MODE>
-cudaError_t launch_mixed_items(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
-    grid = persistent_grid(k_persistent_mixed<AZ, BOOST, MODE>, grid);
-    k_persistent_mixed<AZ, BOOST, MODE><<<grid, FT, 0, st>>>(d, b);
-    return cudaGetLastError();
-}
-
-// The same-event kernel for a precision form and admission mode.  The
-// COUNT pass only counts decided pairs per row, the same in every form, so
-// it runs the FP64 form's kernel.
-template <int MODE>
-cudaError_t launch_same_mode(const Device &d, const BatchDev &b, unsigned base, unsigned end,
-                             int grid, cudaStream_t st) {
-    const bool az = d.g.azimuthal, boost = d.g.boost;
-    // the forms this mode instantiates: FP64 only for COUNT
-    constexpr int P1 = MODE == MODE_COUNT ? 0 : 1, P2 = MODE == MODE_COUNT ? 0 : 2;
-    const int prec = MODE == MODE_COUNT ? 0 : d.precision;
-#define HBT_P(AZ_, BO_, PR_) return launch_same_items<AZ_, BO_, PR_, MODE>(d, b, base, end, grid, st)
-    if (prec == 0) {
-        if (az && boost) HBT_P(true, true, 0);
-        if (az) HBT_P(true, false, 0);
-        if (boost) HBT_P(false, true, 0);
-        HBT_P(false, false, 0);
-    }
-    if (prec == 1) {
-        if (az && boost) HBT_P(true, true, P1);
-        if (az) HBT_P(true, false, P1);
-        if (boost) HBT_P(false, true, P1);
-        HBT_P(false, false, P1);
-    }
-    if (az && boost) HBT_P(true, true, P2);
-    if (az) HBT_P(true, false, P2);
-    if (boost) HBT_P(false, true, P2);
-    HBT_P(false, false, P2);
-#undef HBT_P
-}
-
-template <int MODE>
-cudaError_t launch_mixed_mode(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
-    const bool az = d.g.azimuthal, boost = d.g.boost;
-    if (az && boost) return launch_mixed_items<true, true, MODE>(d, b, grid, st);
-    if (az) return launch_mixed_items<true, false, MODE>(d, b, grid, st);
-    if (boost) return launch_mixed_items<false, true, MODE>(d, b, grid, st);
-    return launch_mixed_items<false, false, MODE>(d, b, grid, st);
-}
-
 }  // namespace
 
-int persistent_blocks_per_sm() {
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_persistent_same<true, true, 0, MODE_FAST>, FT,
-                                                      0) != cudaSuccess)
-        return 4;
-    return nb > 0 ? nb : 1;
+cudaError_t persistent_same(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+                            int grid, cudaStream_t st, int mode) {
+    if (d.g.qinv)
+        return mode == MODE_FAST ? persistent_same_qinv(d, b, base, end, grid, st)
+                                 : cudaErrorNotSupported;
+    if (mode == MODE_FAST) return persistent_same_fast(d, b, base, end, grid, st);
+    return persistent_same_ordered(d, b, base, end, grid, st, mode);
+}
+
+cudaError_t persistent_mixed(const Device &d, const BatchDev &b, int grid, cudaStream_t st,
+                             int mode) {
+    if (d.g.qinv)
+        return mode == MODE_FAST ? persistent_mixed_qinv(d, b, grid, st) : cudaErrorNotSupported;
+    if (mode == MODE_FAST) return persistent_mixed_fast(d, b, grid, st);
+    return persistent_mixed_ordered(d, b, grid, st, mode);
 }
 
 size_t batch_sort_temp_bytes(long long cap) {
@@ -401,12 +253,7 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
             (unsigned)min((unsigned long long)base + chunk, (unsigned long long)upper);
         if (base > 0 && (e = cudaMemsetAsync(b.item_next, 0, sizeof(unsigned), st)) != cudaSuccess)
             return e;
-        if (mode == MODE_COUNT)
-            e = launch_same_mode<MODE_COUNT>(d, b, base, end, grid, st);
-        else if (mode == MODE_ORDER)
-            e = launch_same_mode<MODE_ORDER>(d, b, base, end, grid, st);
-        else
-            e = launch_same_mode<MODE_FAST>(d, b, base, end, grid, st);
+        e = persistent_same(d, b, base, end, grid, st, mode);
         if (e != cudaSuccess) return e;
         if (prec == 1 && !b.devs) {
             if ((e = launch_merge(d, st, b.n_items, base)) != cudaSuccess) return e;
@@ -419,12 +266,7 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
     if (marks && (e = cudaEventRecord(marks[2], st)) != cudaSuccess) return e;
     // mixed-event items
     if (b.mixed_cap > 0) {
-        if (mode == MODE_COUNT)
-            e = launch_mixed_mode<MODE_COUNT>(d, b, grid, st);
-        else if (mode == MODE_ORDER)
-            e = launch_mixed_mode<MODE_ORDER>(d, b, grid, st);
-        else
-            e = launch_mixed_mode<MODE_FAST>(d, b, grid, st);
+        e = persistent_mixed(d, b, grid, st, mode);
         if (e != cudaSuccess) return e;
     }
     if (marks && (e = cudaEventRecord(marks[3], st)) != cudaSuccess) return e;

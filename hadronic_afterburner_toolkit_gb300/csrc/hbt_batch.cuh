@@ -28,7 +28,10 @@ struct BatchJob {
     // |q_long| of any pair that can be binned
     double qt2_max;
     double ql_max;
-    int boost, pad;
+    int boost;
+    // 1: the job's analysis bins q_inv histograms, whose window the 3-D
+    // bounds do not cover: every tile pair is kept
+    int qinv;
 };
 
 // Momentum-space box of a 128-particle tile.

@@ -258,7 +258,9 @@ bool batched_ok(const hbt_ctx *c);
 // (k_straddle).
 hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
                           const double *const *a, const double *const *b) {
-    const bool batched = batched_ok(c);
+    // (the batched kernels' admission passes cover the 3-D histograms; with
+    // the q_inv histograms the reference-chain kernels run both passes)
+    const bool batched = batched_ok(c) && !c->d.g.qinv;
     hbt::FastJob job = {};
     job.kind = mixed;
     job.na = rows;
@@ -358,9 +360,12 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
 // FP32 copies of the screen constants with their rounding slack.
 void fill_screen(hbt_ctx *c) { hbt::screen_from_grid(c->d.g, c->d.s); }
 
+// The screened kernels decide bins in FP32 with error bounds; the q_inv
+// histograms are screened on the batched path only.
 bool screened_ok(const hbt_ctx *c) {
-    return (c->prm.kernel == HBT_KERNEL_SCREENED || c->prm.kernel == HBT_KERNEL_SCREENED_GRID) &&
-           !c->d.g.qinv && c->d.g.n_KT <= 255 && c->d.g.qnpts <= 1024 && c->d.g.n_slots < 16384;
+    return (c->prm.kernel == HBT_KERNEL_SCREENED ||
+            (c->prm.kernel == HBT_KERNEL_SCREENED_GRID && !c->d.g.qinv)) &&
+           c->d.g.n_KT <= 255 && c->d.g.qnpts <= 1024 && c->d.g.n_slots < 16384;
 }
 
 bool batched_ok(const hbt_ctx *c) {
@@ -390,6 +395,7 @@ hbt_status run_fast_jobs(hbt_ctx *c, std::vector<FastJob> jobs, int mode) {
         j.dev = 0;
         j.q_window = Q;
         j.boost = c->d.g.boost;
+        j.qinv = c->d.g.qinv;
     }
     std::string err;
     if (!c->runner.run(jobs, c->d, runner_tuning(c, c->tune), c->stream, err, mode))
@@ -1165,7 +1171,7 @@ size_t ctx_device_bytes(const hbt_params &p) {
     return bytes;
 }
 
-bool ctx_batchable(const hbt_ctx *c) { return batched_ok(c); }
+bool ctx_batchable(const hbt_ctx *c) { return batched_ok(c) && !c->d.g.qinv; }
 
 bool ctx_caps_may_bind(const hbt_ctx *c, int mixed, u64 P) { return caps_may_bind(c, mixed, P); }
 

@@ -96,6 +96,9 @@ struct Screen {
     float pq, pq2, pqt2, pqt_c;
     // 1 / hbarC as a double-float pair (FP32-weight phase)
     float hc_h, hc_l;
+    // q_inv prefilter (invariant_radius_flag): square of the upper window
+    // bound with its slack and a margin; -1 when no q_inv >= 0 can pass
+    float qi_hi2;
 };
 
 // Host: the prefilter constants of a screen whose window is filled in.
@@ -110,6 +113,8 @@ inline void fill_prefilter(Screen &s) {
     const double hc = 1.0 / 0.197327053;  // 1 / hbarC [1 / (GeV fm)]
     s.hc_h = (float)hc;
     s.hc_l = (float)(hc - (double)s.hc_h);
+    const double qh = ((double)s.hi + (double)s.win_slack) * (1.0 + 1e-6);
+    s.qi_hi2 = qh > 0.0 ? (float)(qh * qh * (1.0 + 2e-4)) : -1.0f;
 }
 
 struct Device {

@@ -1,0 +1,198 @@
+// Persistent pair-binning kernels of the batched path: CTAs pull
+// (job, i-tile, j-tile) items from the culled queues that hbt_batch.cu
+// builds and run the screened tile-pair bodies of hbt_tile.cuh on them.
+// The kernel templates are instantiated in three translation units,
+// compiled in parallel: hbt_persist_fast.cu (fast binning),
+// hbt_persist_caps.cu (the two passes of ordered cap admission) and
+// hbt_persist_qinv.cu (fast binning with the q_inv histograms).
+#pragma once
+
+#include "hbt_batch.cuh"
+#include "hbt_tile.cuh"
+
+namespace hbt {
+
+// Launchers, one family per translation unit (same-event items
+// [base, end) of the queue; mixed-event items all at once).
+cudaError_t persistent_same_fast(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+                                 int grid, cudaStream_t st);
+cudaError_t persistent_mixed_fast(const Device &d, const BatchDev &b, int grid, cudaStream_t st);
+cudaError_t persistent_same_ordered(const Device &d, const BatchDev &b, unsigned base,
+                                    unsigned end, int grid, cudaStream_t st, int mode);
+cudaError_t persistent_mixed_ordered(const Device &d, const BatchDev &b, int grid,
+                                     cudaStream_t st, int mode);
+cudaError_t persistent_same_qinv(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+                                 int grid, cudaStream_t st);
+cudaError_t persistent_mixed_qinv(const Device &d, const BatchDev &b, int grid, cudaStream_t st);
+// Dispatch on the admission mode and the q_inv histograms.
+cudaError_t persistent_same(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+                            int grid, cudaStream_t st, int mode);
+cudaError_t persistent_mixed(const Device &d, const BatchDev &b, int grid, cudaStream_t st,
+                             int mode);
+
+namespace persist {
+
+using namespace tile;
+
+// Engine descriptor of an item: the launch's own, or (serving many
+// analyses) the job's entry of b.devs copied into shared memory.
+__device__ __forceinline__ const Device &item_device(const Device &d, const BatchDev &b,
+                                                    const BatchJob &job, Device &dsm) {
+    if (!b.devs) return d;
+    const int *src = reinterpret_cast<const int *>(b.devs + job.dev);
+    int *dst = reinterpret_cast<int *>(&dsm);
+    for (int k = threadIdx.x; k < (int)(sizeof(Device) / sizeof(int)); k += blockDim.x)
+        dst[k] = src[k];
+    __syncthreads();
+    return dsm;
+}
+
+// Resident CTAs per SM (register budget 65536 / (128 x CTAs)): measured on
+// GB300, the FP64 form of the same-event kernel is fastest at 5 (its FP64
+// values need the registers), the double-float form at 4 (118 registers, no
+// spills: 167 ms per central group, against 194 ms at 5 and 234 ms at 6,
+// where its 80 registers spill in the pair loop), the FP32-weight form and
+// the mixed-event kernel at 6.
+template <int PREC>
+struct SameCtas {
+    static constexpr int value = PREC == 1 ? 6 : (PREC == 2 ? 4 : 5);
+};
+constexpr int kMixedCtas = 6;
+
+// Same-event items [base, min(end, queued)) pulled by persistent CTAs.
+// MODE: fast binning, or one pass of ordered cap admission.
+template <bool AZ, bool BOOST, int PREC, int MODE, bool QINV>
+__global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(Device d, BatchDev b, unsigned base,
+                                                           unsigned end) {
+    __shared__ SmemFor<QINV> sm;
+    __shared__ Device dsm;
+    __shared__ unsigned item;
+    __shared__ double2 cs[COS_TABLE];
+    if (PREC == 0) fill_cos_table(cs);
+    if (PREC == 2) fill_df_table(reinterpret_cast<float4 *>(cs));
+    const unsigned stop = min(end, min(b.n_items[0], b.same_cap));
+    for (;;) {
+        if (threadIdx.x == 0) item = base + atomicAdd(b.item_next, 1u);
+        __syncthreads();
+        const unsigned k = item;
+        if (k >= stop) break;
+        const Item it = b.items[k];
+        const BatchJob &job = b.jobs[it.job];
+        const Device &dd = item_device(d, b, job, dsm);
+        const BatchList &la = b.lists[job.la];
+        const double *c[8];
+#pragma unroll
+        for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
+        same_tile_pair<AZ, BOOST, PREC, MODE, QINV>(dd, sm, cs, c, b.orig + la.off, la.n,
+                                              (long long)it.ti * FT, (long long)it.tj * FT);
+        __syncthreads();
+    }
+}
+
+// Mixed-event items, all in one launch.
+template <bool AZ, bool BOOST, int MODE, bool QINV>
+__global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, BatchDev b) {
+    __shared__ TileSmem sm;
+    __shared__ Device dsm;
+    __shared__ unsigned item;
+    const unsigned stop = min(b.n_items[1], b.mixed_cap);
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(b.item_next + 1, 1u);
+        __syncthreads();
+        const unsigned k = item;
+        if (k >= stop) break;
+        const Item it = b.items[b.same_cap + k];
+        const BatchJob &job = b.jobs[it.job];
+        const Device &dd = item_device(d, b, job, dsm);
+        const BatchList &la = b.lists[job.la], &lb = b.lists[job.lb];
+        const double *c1[4], *c2[4];
+#pragma unroll
+        for (int f = 0; f < 4; f++) {
+            c1[f] = b.table + (long long)f * b.cap + la.off;
+            c2[f] = b.table + (long long)f * b.cap + lb.off;
+        }
+        mixed_tile_pair<AZ, BOOST, MODE, QINV>(dd, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
+                                         (long long)it.tj * FT, b.orig + la.off,
+                                         b.orig + lb.off);
+        __syncthreads();
+    }
+}
+
+inline int sm_count() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+    }
+    return sms;
+}
+
+// grid > 0: that many CTAs; otherwise one CTA per resident slot.
+template <class K>
+int persistent_grid(K kernel, int grid) {
+    if (grid > 0) return grid;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, FT, 0) != cudaSuccess || nb < 1)
+        nb = 4;
+    return sm_count() * nb;
+}
+
+template <bool AZ, bool BOOST, int PREC, int MODE, bool QINV>
+cudaError_t launch_same_items(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+                              int grid, cudaStream_t st) {
+    grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC, MODE, QINV>, grid);
+    k_persistent_same<AZ, BOOST, PREC, MODE, QINV><<<grid, FT, 0, st>>>(d, b, base, end);
+    return cudaGetLastError();
+}
+
+template <bool AZ, bool BOOST, int MODE, bool QINV>
+cudaError_t launch_mixed_items(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
+    grid = persistent_grid(k_persistent_mixed<AZ, BOOST, MODE, QINV>, grid);
+    k_persistent_mixed<AZ, BOOST, MODE, QINV><<<grid, FT, 0, st>>>(d, b);
+    return cudaGetLastError();
+}
+
+// The same-event kernel of the context's flags and precision form for one
+// admission mode.  The COUNT pass only counts decided pairs per row, the
+// same in every form, so it runs the FP64 form's kernel.
+template <int MODE, bool QINV>
+cudaError_t launch_same_mode(const Device &d, const BatchDev &b, unsigned base, unsigned end,
+                             int grid, cudaStream_t st) {
+    const bool az = d.g.azimuthal, boost = d.g.boost;
+    // the forms this mode instantiates: FP64 only for COUNT
+    constexpr int P1 = MODE == MODE_COUNT ? 0 : 1, P2 = MODE == MODE_COUNT ? 0 : 2;
+    const int prec = MODE == MODE_COUNT ? 0 : d.precision;
+#define HBT_P(AZ_, BO_, PR_) \
+    return launch_same_items<AZ_, BO_, PR_, MODE, QINV>(d, b, base, end, grid, st)
+    if (prec == 0) {
+        if (az && boost) HBT_P(true, true, 0);
+        if (az) HBT_P(true, false, 0);
+        if (boost) HBT_P(false, true, 0);
+        HBT_P(false, false, 0);
+    }
+    if (prec == 1) {
+        if (az && boost) HBT_P(true, true, P1);
+        if (az) HBT_P(true, false, P1);
+        if (boost) HBT_P(false, true, P1);
+        HBT_P(false, false, P1);
+    }
+    if (az && boost) HBT_P(true, true, P2);
+    if (az) HBT_P(true, false, P2);
+    if (boost) HBT_P(false, true, P2);
+    HBT_P(false, false, P2);
+#undef HBT_P
+}
+
+template <int MODE, bool QINV>
+cudaError_t launch_mixed_mode(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
+    const bool az = d.g.azimuthal, boost = d.g.boost;
+    if (az && boost) return launch_mixed_items<true, true, MODE, QINV>(d, b, grid, st);
+    if (az) return launch_mixed_items<true, false, MODE, QINV>(d, b, grid, st);
+    if (boost) return launch_mixed_items<false, true, MODE, QINV>(d, b, grid, st);
+    return launch_mixed_items<false, false, MODE, QINV>(d, b, grid, st);
+}
+
+}  // namespace persist
+}  // namespace hbt

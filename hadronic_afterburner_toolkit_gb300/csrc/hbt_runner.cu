@@ -55,8 +55,9 @@ bool BatchRunner::run_multi(const std::vector<FastJob> &jobs, const std::vector<
         }
     for (const Device &x : devs)
         if (x.g.azimuthal != devs[0].g.azimuthal || x.g.boost != devs[0].g.boost ||
-            x.precision != devs[0].precision) {
-            err = "analyses of one batch must share azimuthal_flag, boost and precision";
+            x.precision != devs[0].precision || x.g.qinv != devs[0].g.qinv) {
+            err = "analyses of one batch must share azimuthal_flag, boost, precision and "
+                  "invariant_radius_flag";
             return false;
         }
     if (!grow(devs_, devs.size() * sizeof(Device), err)) return false;
@@ -208,6 +209,7 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
         b.qt2_max = 2.0 * j.q_window * j.q_window * (1.0 + 1e-6) + 1e-300;
         b.ql_max = j.q_window * (1.0 + 1e-6) + 1e-300;
         b.boost = j.boost;
+        b.qinv = j.qinv;
         pair_off.push_back(pairs);
         pairs += b.n_pairs;
         bj.push_back(b);

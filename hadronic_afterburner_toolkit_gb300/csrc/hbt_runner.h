@@ -22,6 +22,7 @@ struct FastJob {
     int dev;             // index of the analysis (serving), 0 otherwise
     double q_window;     // Q = max(|lo|, |hi|) of the analysis' q window
     int boost;           // long_comoving_boost of the analysis
+    int qinv;            // 1: the analysis bins q_inv histograms (no cull)
 };
 
 // Launch shape of a batch, chosen by hbt_set_tuning / hbt_autotune_batch.
@@ -49,8 +50,8 @@ class BatchRunner {
              std::string &err, int mode = MODE_FAST);
 
     // Runs jobs of several analyses in one launch: job.dev indexes `devs`,
-    // whose entries must share azimuthal_flag, long_comoving_boost and
-    // precision (they select the kernel).  The FP32-weight partials of
+    // whose entries must share azimuthal_flag, long_comoving_boost,
+    // precision and invariant_radius_flag (they select the kernel).  The FP32-weight partials of
     // every analysis are merged after each chunk of `chunk` same-event
     // items and at the end.
     bool run_multi(const std::vector<FastJob> &jobs, const std::vector<Device> &devs,

@@ -51,6 +51,8 @@
 // FP64 reference's own rounding (2^-29 times smaller).
 #pragma once
 
+#include <type_traits>
+
 #include "hbt_chain.cuh"
 #include "hbt_math.cuh"
 
@@ -104,24 +106,29 @@ __device__ __forceinline__ bool prefilter(const Screen &S, float4 a, float2 ga, 
     return true;
 }
 
-// Stage B: window checks.  Returns 0 (reject), 1 (all windows certainly
-// passed), 2 (undecided).
-template <bool BOOST>
-__device__ __forceinline__ int screen_windows(const Screen &S, float4 a, float4 b, Q &q) {
+// Stage B, K_T part: fills q's transverse sums and K_perp^2 with its bound;
+// 0 the K_T cut certainly fails, 1 certainly passes, 2 undecided.
+__device__ __forceinline__ int screen_kt(const Screen &S, float4 a, float4 b, Q &q) {
     q.sx = a.x + b.x;
     q.sy = a.y + b.y;
-    const float dx = a.x - b.x, dy = a.y - b.y;
     q.Ax = fabsf(a.x) + fabsf(b.x);
     q.Ay = fabsf(a.y) + fabsf(b.y);
     q.k2 = __fmaf_rn(q.sx, q.sx, q.sy * q.sy);
-    const float AA = __fmaf_rn(q.Ax, q.Ax, q.Ay * q.Ay);
     // |k2 - (S_x^2 + S_y^2)|
     q.ek2 = 6.1f * U * __fmaf_rn(q.Ax, fabsf(q.sx), q.Ay * fabsf(q.sy)) + 3.1f * U * q.k2 +
-            1e-13f * AA;
+            1e-13f * __fmaf_rn(q.Ax, q.Ax, q.Ay * q.Ay);
     // K_T window (reference rejects Kp2 < KT_min^2 or Kp2 > KT_max^2)
     const float ekt = 2.0f * q.ek2 + S.kt_slack;
     if ((S.kt_lo4 > 0.0f && q.k2 + ekt < S.kt_lo4) || q.k2 - ekt > S.kt_hi4) return 0;
-    int cls = ((S.kt_lo4 == 0.0f || q.k2 - ekt > S.kt_lo4) && q.k2 + ekt < S.kt_hi4) ? 1 : 2;
+    return ((S.kt_lo4 == 0.0f || q.k2 - ekt > S.kt_lo4) && q.k2 + ekt < S.kt_hi4) ? 1 : 2;
+}
+
+// Stage B, LCMS part (after screen_kt): q_out, q_side, q_long and their
+// bounds; 0 a window certainly fails, 1 all certainly pass, 2 undecided.
+template <bool BOOST>
+__device__ __forceinline__ int screen_lcms(const Screen &S, float4 a, float4 b, Q &q) {
+    const float dx = a.x - b.x, dy = a.y - b.y;
+    const float AA = __fmaf_rn(q.Ax, q.Ax, q.Ay * q.Ay);
     const float rel_k2 = __fdividef(q.ek2, q.k2) * 1.0001f;
     if (!(q.k2 > 0.0f) || !(rel_k2 <= 0.05f)) return 2;  // |S| too small for the bounds
     const float inv = rsqrtf(q.k2);
@@ -157,7 +164,17 @@ __device__ __forceinline__ int screen_windows(const Screen &S, float4 a, float4 
               wl = window_class(S, q.ql, q.eql);
     if (wo == 0 || ws == 0 || wl == 0) return 0;
     if (wo == 2 || ws == 2 || wl == 2) return 2;
-    return cls;
+    return 1;
+}
+
+// Stage B: window checks.  Returns 0 (reject), 1 (all windows certainly
+// passed), 2 (undecided).
+template <bool BOOST>
+__device__ __forceinline__ int screen_windows(const Screen &S, float4 a, float4 b, Q &q) {
+    const int cls = screen_kt(S, a, b, q);
+    if (cls == 0) return 0;
+    const int w = screen_lcms<BOOST>(S, a, b, q);
+    return w == 1 ? cls : w;
 }
 
 // floor((v - base) / delta_q) when certain, else -1.
@@ -189,6 +206,66 @@ __device__ __forceinline__ bool decide_bins(const Screen &S, const Q &q, int &iK
     if (io < 0 || is < 0 || il < 0) return false;
     bin = (io * S.qnpts + is) * S.qnpts + il;
     return true;
+}
+
+// q_inv^2 = q_x^2 + q_y^2 + q_z^2 - q_E^2 of a pair in FP32 (a, b: FP32
+// momenta) and a bound on its distance from the reference's FP64 value
+// -(q_E q_E - q_x q_x - q_y q_y - q_z q_z): each difference lies within
+// e = 2.01 u (|a| + |b|) of the exact difference of the FP64 inputs, so its
+// square within e (2 |d| + e); the FMA chain rounds four times, each below
+// u times the sum of squares; the reference's own FP64 rounding is 2^-29
+// times smaller and covered by a fifth u.
+__device__ __forceinline__ void qinv2_bound(float4 a, float4 b, float &t, float &et) {
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z, dE = a.w - b.w;
+    const float ex = 2.01f * U * (fabsf(a.x) + fabsf(b.x));
+    const float ey = 2.01f * U * (fabsf(a.y) + fabsf(b.y));
+    const float ez = 2.01f * U * (fabsf(a.z) + fabsf(b.z));
+    const float eE = 2.01f * U * (fabsf(a.w) + fabsf(b.w));
+    t = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, -(dE * dE))));
+    const float s2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, dE * dE)));
+    et = (ex * (2.0f * fabsf(dx) + ex) + ey * (2.0f * fabsf(dy) + ey) +
+          ez * (2.0f * fabsf(dz) + ez) + eE * (2.0f * fabsf(dE) + eE)) * 1.0001f +
+         5.0f * U * s2 + 1e-30f;
+}
+
+// Stage A for q_inv: false only when q_inv is certainly above the window
+// (q_inv^2 lower bound above the square of the upper bound).
+__device__ __forceinline__ bool prefilter_qinv(const Screen &S, float4 a, float4 b) {
+    float t, et;
+    qinv2_bound(a, b, t, et);
+    return !(t - et > S.qi_hi2);
+}
+
+// Stage B for q_inv: 0 no q_inv event (q_inv outside the window or NaN),
+// 1 event in q_inv bin k (certain), 2 undecided.
+__device__ __forceinline__ int qinv_class(const Screen &S, float4 a, float4 b, int &k) {
+    float t, et;
+    qinv2_bound(a, b, t, et);
+    if (t + et < 0.0f) return 0;  // the reference's q_inv is NaN: fails both bounds
+    if (!(t - et > 0.0f)) return 2;
+    const float qf = __fsqrt_rn(t);
+    // |sqrt(t) - sqrt(T)| = |t - T| / (sqrt(t) + sqrt(T)) <= et / (sqrt(t) + sqrt(t - et))
+    const float err = __fdividef(et, qf + __fsqrt_rn(t - et)) * 1.0001f + U * qf;
+    const int w = window_class(S, qf, err);
+    if (w != 1) return w;
+    k = q_index(S, qf, err);
+    return k < 0 ? 2 : 1;
+}
+
+// K_T bin from the FP32 screen values (after screen_kt): >= 0 certain,
+// -1 undecided.
+__device__ __forceinline__ int kt_index(const Screen &S, const Q &q) {
+    const float inv = rsqrtf(q.k2);
+    const float kp = 0.5f * q.k2 * inv;  // |S|/2 = K_perp
+    const float ekp = 0.5f * q.ek2 * inv * 1.1f + 8.0f * U * kp;
+    const float t = (kp - S.KT_min) * S.inv_dKT;
+    const float et = 2.0f * ekp * S.inv_dKT + 4.0f * U * (fabsf(t) + S.KT_min * S.inv_dKT) +
+                     S.kt_t_slack;
+    const float k = floorf(t);
+    const float fr = t - k;
+    if (!(q.k2 > 0.0f) || !(__fdividef(q.ek2, q.k2) <= 0.05f)) return -1;
+    if (!(fr > et) || !(fr < 1.0f - et) || k < 0.0f || k >= (float)S.n_KT) return -1;
+    return (int)k;
 }
 
 // K_phi bin from the FP32 screen values: >= 0 certain, -2 undecided.
@@ -542,8 +619,10 @@ __device__ __forceinline__ void values_df(const Screen &S, const float4 *tab, co
     w = df_cos(tab, ff_mul(ph, FF{S.hc_h, S.hc_l}));
 }
 
-// Shared memory of one tile pair.
-struct TileSmem {
+// Shared memory of one tile pair; E2 is the entry of the second same-event
+// queue (uint2, or uint4 when q_inv histograms are binned too).
+template <class E2>
+struct TileSmemT {
     // same-event tiles: FP64 columns (FP64 form) or split columns (hi, lo
     // FP32 pairs, FP32-weight form), px py pz E x y z t
     double si[8][FT];
@@ -554,11 +633,16 @@ struct TileSmem {
     float2 gj[FT];
     unsigned queue[FT / 32][QCAP];
     // same-event pairs that passed the window screen: x = (i, j, swap,
-    // undecided, slot) bits, y = q bin (bin_entry)
-    uint2 queue2[FT / 32][QCAP];
+    // undecided, slot) bits, y = q bin (bin_entry); with q_inv, x = (i, j,
+    // swap, undecided, 3-D event, q_inv event) bits, y = q bin, z = slot |
+    // K_T bin << 16, w = q_inv bin
+    E2 queue2[FT / 32][QCAP];
     unsigned oi[FT], oj[FT];  // original list positions (pair orientation)
     float offi[4], offj[4];   // double-float form: the tiles' momentum offsets
 };
+using TileSmem = TileSmemT<uint2>;
+template <bool QINV>
+using SmemFor = TileSmemT<typename std::conditional<QINV, uint4, uint2>::type>;
 
 // Entry of the second same-event queue.
 __device__ __forceinline__ uint2 bin_entry(unsigned e, bool undecided, int slot, int bin) {
@@ -669,10 +753,14 @@ __device__ __forceinline__ bool admit(const Device &d, int slot, long long row, 
 // the rows are in the caller's order.  MODE selects the admission: FAST bins
 // every pair; COUNT and ORDER are the two passes of ordered cap admission,
 // which see each pair at its row (the earlier of its two positions in the
-// caller's list).  Called by all FT threads of the CTA; the caller syncs
-// before reusing `sm`.
-template <bool AZ, bool BOOST, int PREC, int MODE = MODE_FAST>
-__device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, const double2 *cs,
+// caller's list).  QINV: the pairs also go to the q_inv histograms
+// (invariant_radius_flag, src/HBT_correlation.cpp:331-356): a pair is kept
+// when its 3-D window or its q_inv window can pass, and its q_inv bin is
+// decided in FP32 with an error bound like the 3-D bins (qinv_class).
+// Called by all FT threads of the CTA; the caller syncs before reusing `sm`.
+template <bool AZ, bool BOOST, int PREC, int MODE = MODE_FAST, bool QINV = false>
+__device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &sm,
+                                               const double2 *cs,
                                                const double *const *c, const unsigned *orig,
                                                long long n, long long i0, long long j0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -735,8 +823,140 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
     const unsigned oa = sm.oi[il];
     const int jend = (int)min((long long)FT, n - j0);
     unsigned *q = sm.queue[w];
-    uint2 *q2 = sm.queue2[w];
+    auto *q2 = sm.queue2[w];
     int count = 0, count2 = 0;
+
+    // stage C with q_inv histograms, for 32 screened pairs: the 3-D event
+    // and the q_inv event of each pair (cos(q.dx) computed once for both)
+    auto values_q = [&](uint4 e4, bool valid) {
+        if (!valid) return;
+        const unsigned e = e4.x;
+        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        const bool swap = (e >> 16) & 1u;
+        bool has3 = (e >> 18) & 1u, hasq = (e >> 19) & 1u;
+        const int bin = (int)e4.y, slot = (int)(e4.z & 0xffffu), iK = (int)(e4.z >> 16);
+        const int kq = (int)e4.w;
+        double A[8], B[8];  // first and second particle of the pair
+#pragma unroll
+        for (int f = 0; f < 8; f++) {
+            const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+            const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+            A[f] = swap ? v : u;
+            B[f] = swap ? u : v;
+        }
+        const long long oa = sm.oi[qi], ob = sm.oj[qj];
+        const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
+        if ((e >> 17) & 1u) {
+            // undecided: the reference chain decides both events
+            if (MODE == MODE_FAST)
+                undecided_pair_ordered<false, MODE_FAST>(d, A, B, i0 + qi, j0 + qj, n, n);
+            else
+                undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
+            return;
+        }
+        if (MODE != MODE_FAST) {
+            has3 = has3 && admit<MODE>(d, slot, row, n);
+            hasq = hasq && admit<MODE>(d, d.g.n_slots + iK, row, n);
+            if (!has3 && !hasq) return;
+        }
+        const long long at = (long long)slot * d.g.q3 + bin;
+        double wq;
+        if (PREC == 1) {
+            float2 a[8], b[8];
+#pragma unroll
+            for (int f = 0; f < 8; f++) {
+                a[f] = spi[f][qi];
+                b[f] = spj[f][qj];
+            }
+            float4 v = values32_split<BOOST>(d.s, a, b);
+            if (swap) {
+                v.x = -v.x;
+                v.y = -v.y;
+                v.z = -v.z;
+            }
+            if (has3) {
+                atomicAdd(d.part + at, v);
+                atomicAdd(d.h.cnt + at, 1ull);
+            }
+            wq = v.w;
+        } else {
+            double vo, vs, vl;
+            if (PREC == 0) {
+                values64<BOOST>(d.g, cs, A, B, vo, vs, vl, wq);
+            } else {
+                float2 a[8], b[8];
+#pragma unroll
+                for (int f = 0; f < 8; f++) {
+                    a[f] = spi[f][qi];
+                    b[f] = spj[f][qj];
+                }
+                values_df<BOOST>(d.s, reinterpret_cast<const float4 *>(cs), a, b, sm.offi,
+                                 sm.offj, swap, vo, vs, vl, wq);
+            }
+            if (has3) {
+                Sums *h = d.h.sums + at;
+                atomicAdd(&h->qo, vo);
+                atomicAdd(&h->qs, vs);
+                atomicAdd(&h->ql, vl);
+                atomicAdd(&h->w, wq);
+                atomicAdd(d.h.cnt + at, 1ull);
+            }
+        }
+        if (hasq) {
+            // the reference's q_inv expression (FP64, same order, no
+            // contraction): the summed value equals the oracle's exactly
+            const double q_x = A[0] - B[0], q_y = A[1] - B[1], q_z = A[2] - B[2];
+            const double q_E = A[3] - B[3];
+            const double qinv = sqrt(-(q_E * q_E - q_x * q_x - q_y * q_y - q_z * q_z));
+            const int aq = iK * d.g.qnpts + kq;
+            atomicAdd(&d.h.qi_sums[aq].q, qinv);
+            atomicAdd(&d.h.qi_sums[aq].w, wq);
+            atomicAdd(d.h.qi_cnt + aq, 1ull);
+        }
+    };
+
+    // stage B with q_inv histograms: the K_T window and bin, the 3-D
+    // windows and bins, and the q_inv window and bin of each pair; a pair
+    // with any of them undecided goes to the reference chain as a whole
+    auto screen_q = [&](unsigned e, bool valid) {
+        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        const bool swap = (e >> 16) & 1u;
+        const float4 fa = swap ? sm.fj[qj] : sm.fi[qi], fb = swap ? sm.fi[qi] : sm.fj[qj];
+        Q s;
+        int c3 = 0, cq = 0, iK = -1, bin = 0, slot = -1, kq = 0;
+        bool und = false;
+        if (valid) {
+            const int kt = screen_kt(S, fa, fb, s);
+            if (kt != 0) {
+                c3 = screen_lcms<BOOST>(S, fa, fb, s);
+                cq = qinv_class(S, fa, fb, kq);
+                if (c3 == 1 || cq == 1) {
+                    iK = kt == 1 ? kt_index(S, s) : -1;
+                    und = iK < 0;
+                }
+                if (c3 == 1 && !und) {
+                    int iK2 = 0;
+                    if (decide_bins(S, s, iK2, bin)) {
+                        slot = iK2;
+                        if (AZ) {
+                            const int ip = kphi_screen(S, s);
+                            slot = ip < 0 ? -1 : iK2 * d.g.n_Kphi + ip;
+                        }
+                    }
+                    und = slot < 0;
+                }
+                und = und || c3 == 2 || cq == 2;
+            }
+        }
+        const bool take = valid && (und || c3 == 1 || cq == 1);
+        const unsigned x = e | (und ? 1u << 17 : 0u) | (!und && c3 == 1 ? 1u << 18 : 0u) |
+                           (!und && cq == 1 ? 1u << 19 : 0u);
+        const uint4 ent = make_uint4(x, (unsigned)bin,
+                                     (unsigned)(slot < 0 ? 0 : slot) |
+                                         ((unsigned)(iK < 0 ? 0 : iK) << 16),
+                                     (unsigned)kq);
+        if constexpr (QINV) enqueue(q2, count2, take, ent, lane, values_q);
+    };
 
     // stage C for 32 screened pairs (all lanes of the warp in step)
     auto values = [&](uint2 e2, bool valid) {
@@ -866,19 +1086,29 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
                 slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
             }
         }
-        enqueue(q2, count2, wcls != 0, bin_entry(e, slot < 0, slot < 0 ? 0 : slot, bin), lane,
-                values);
+        if constexpr (!QINV)
+            enqueue(q2, count2, wcls != 0, bin_entry(e, slot < 0, slot < 0 ? 0 : slot, bin),
+                    lane, values);
     };
 
     for (int jj = 0; jj < jend; jj++) {
         const long long j = j0 + jj;
         const bool swap = oa > sm.oj[jj];
-        const bool take = i < n && j > i && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
-        enqueue(q, count, take,
-                (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16), lane, screen);
+        bool take = i < n && j > i && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
+        if (QINV) take = take || (i < n && j > i && prefilter_qinv(S, a, sm.fj[jj]));
+        const unsigned e = (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16);
+        if constexpr (QINV)
+            enqueue(q, count, take, e, lane, screen_q);
+        else
+            enqueue(q, count, take, e, lane, screen);
     }
-    drain(q, count, lane, screen);
-    drain(q2, count2, lane, values);
+    if constexpr (QINV) {
+        drain(q, count, lane, screen_q);
+        drain(q2, count2, lane, values_q);
+    } else {
+        drain(q, count, lane, screen);
+        drain(q2, count2, lane, values);
+    }
 }
 
 // Mixed-event pairs of the list-1 tile at i0 (n1 particles, columns l1 =
@@ -886,8 +1116,8 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, TileSmem &sm, co
 // ordered cap admission (MODE COUNT / ORDER) a pair's row and column are
 // its positions in the caller's lists, orig1 / orig2 (nullptr: the rows are
 // in the caller's order).
-template <bool AZ, bool BOOST, int MODE = MODE_FAST>
-__device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
+template <bool AZ, bool BOOST, int MODE = MODE_FAST, bool QINV = false, class SM = TileSmem>
+__device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
                                                 const double *const *l1, long long n1,
                                                 const double *const *l2, long long n2,
                                                 long long i0, long long j0,
@@ -946,11 +1176,69 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, TileSmem &sm,
         }
     };
 
+    // with q_inv histograms: the 3-D and the q_inv denominator events
+    auto process_q = [&](unsigned e, bool valid) {
+        if (!valid) return;
+        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        Q s;
+        const int kt = screen_kt(S, sm.fi[qi], sm.fj[qj], s);
+        if (kt == 0) return;
+        const int c3 = screen_lcms<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+        int kq = 0, iK = -1, bin = 0, slot = -1;
+        const int cq = qinv_class(S, sm.fi[qi], sm.fj[qj], kq);
+        bool und = false;
+        if (c3 == 1 || cq == 1) {
+            iK = kt == 1 ? kt_index(S, s) : -1;
+            und = iK < 0;
+        }
+        if (c3 == 1 && !und) {
+            int iK2 = 0;
+            if (decide_bins(S, s, iK2, bin)) {
+                slot = iK2;
+                if (AZ) {
+                    const int ip = kphi_screen(S, s);
+                    slot = ip < 0 ? -1 : iK2 * d.g.n_Kphi + ip;
+                }
+            }
+            und = slot < 0;
+        }
+        und = und || c3 == 2 || cq == 2;
+        if (!und && c3 != 1 && cq != 1) return;
+        const long long row = orig1 ? (long long)orig1[i0 + qi] : i0 + qi;
+        const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
+        if (und) {
+            if (MODE == MODE_FAST) {
+                undecided_mixed_pair(d, l1, l2, i0 + qi, j0 + qj, n1, n2);
+            } else {
+                const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi],
+                                     l1[3][i0 + qi]};
+                const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
+                                     l2[3][j0 + qj]};
+                undecided_pair_ordered<true, MODE>(d, A, B, row, col, n1, n2);
+            }
+            return;
+        }
+        bool h3 = c3 == 1, hq = cq == 1;
+        if (MODE != MODE_FAST) {
+            h3 = h3 && admit<MODE>(d, slot, row, n1);
+            hq = hq && admit<MODE>(d, d.g.n_slots + iK, row, n1);
+        }
+        if (h3) atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
+        if (hq) atomicAdd(d.h.qi_den + iK * d.g.qnpts + kq, 1ull);
+    };
+
     for (int jj = 0; jj < jend; jj++) {
-        const bool take = active && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
-        enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process);
+        bool take = active && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
+        if (QINV) take = take || (active && prefilter_qinv(S, a, sm.fj[jj]));
+        if constexpr (QINV)
+            enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process_q);
+        else
+            enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process);
     }
-    drain(q, count, lane, process);
+    if constexpr (QINV)
+        drain(q, count, lane, process_q);
+    else
+        drain(q, count, lane, process);
 }
 
 }  // namespace tile

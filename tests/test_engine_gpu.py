@@ -337,3 +337,64 @@ def test_screen_kphi_edges():
     h = orc.hist()
     assert h["count"].sum() > 50
     parity.compare(eng.hist(), h, _qscale(p))
+
+
+def _qinv_edge_pairs(p, seed=13, per_edge=20):
+    """Pairs whose q_inv, computed with the reference's FP64 expression
+    sqrt(-(qE*qE - qx*qx - qy*qy - qz*qz)), lies within a few ulps of every
+    q bin edge and window bound above 0: p1 = p2 + s v with s found by
+    bisection, then s stepped by single ulps around it."""
+    rng = np.random.default_rng(seed)
+    m = 0.13957
+    dq = (p["q_max"] - p["q_min"]) / (p["qnpts"] - 1)
+    base = p["q_min"] - dq / 2.0
+    edges = [base + k * dq for k in range(p["qnpts"] + 1)]
+    edges += [p["q_min"] - dq / 2.0 + 1e-8, p["q_max"] + dq / 2.0 - 1e-8]
+    edges = [e for e in edges if e > 1e-4]
+
+    def qinv(p1, p2):
+        e1 = np.sqrt(p1 @ p1 + m * m)
+        e2 = np.sqrt(p2 @ p2 + m * m)
+        qx, qy, qz, qE = p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2], e1 - e2
+        return np.sqrt(-(qE * qE - qx * qx - qy * qy - qz * qz))
+
+    rows = []
+    for e in edges:
+        p2 = np.array([rng.uniform(0.2, 0.5), rng.uniform(-0.2, 0.2), rng.uniform(-0.3, 0.3)])
+        v = rng.normal(size=3)
+        v /= np.sqrt(v @ v)
+        lo, hi = 0.0, 1.0
+        for _ in range(80):
+            mid = 0.5 * (lo + hi)
+            if qinv(p2 + mid * v, p2) < e:
+                lo = mid
+            else:
+                hi = mid
+        for k in range(-per_edge, per_edge + 1):
+            s = np.nextafter(lo, np.inf if k > 0 else -np.inf) if k else lo
+            for _ in range(abs(k) - 1):
+                s = np.nextafter(s, np.inf if k > 0 else -np.inf)
+            p1 = p2 + s * v
+            for q in (p1, p2):
+                rows.append((q[0], q[1], q[2], np.sqrt(q @ q + m * m)))
+    a = np.array(rows)
+    pos = rng.normal(0, 1, size=(a.shape[0], 4))
+    return [np.ascontiguousarray(a[:, k]) for k in range(4)] + \
+        [np.ascontiguousarray(pos[:, k]) for k in range(4)]
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_qinv_edge_pairs_bit_exact(kernel):
+    """q_inv histograms on pairs at every q_inv bin edge (same-event and
+    mixed-event): the batched kernels' FP32 q_inv screen hands every pair it
+    cannot decide to the reference chain, so counts equal the oracle's."""
+    p = dict(BASIC, invariant_radius_flag=1, qnpts=11, q_min=0.0, q_max=0.2, KT_min=0.0)
+    c = _qinv_edge_pairs(p)
+    eng, orc = _engine(kernel=kernel, **p), _oracle(**p)
+    eng.bin_same(c)
+    orc.bin_same(c)
+    eng.bin_mixed(c[:4], c[:4])
+    orc.bin_mixed(c[:4], c[:4])
+    h = orc.hist()
+    assert h["qinv_count"].sum() > 1000 and h["qinv_den"].sum() > 1000
+    parity.compare(eng.hist(), h, _qscale(p))

@@ -324,3 +324,32 @@ def test_small_configuration_with_a_binding_cap(small_run, azimuthal):
     assert st["ordered_passes"] > 0
     assert (o["ctr_num"] > 1e6).any() and (o["ctr_den"] > 1e6).any()
     parity.compare(h, o, q_scale=0.15)
+
+
+def test_small_configuration_with_qinv_histograms(small_run):
+    """invariant_radius_flag = 1 on the small configuration in one batched
+    call: the q_inv bins are decided in FP32 with an error bound on the
+    batched kernels (src/HBT_correlation.cpp:331-356, :595-607), pairs near a
+    q_inv edge by the reference chain; q_inv counts and denominators and the
+    3-D histograms identical to the oracle's, sums within parity.RTOL."""
+    ev, bufs, _, jobs = small_run
+    p = dict(SMALL, invariant_radius_flag=1)
+    orc = oracle_lib.Oracle(number_of_mixed_events=5, seed=1, **p)
+    for a, b in bufs:
+        orc.process_buffer(synth.subset(ev, a, b))
+    o = orc.hist()
+    h, st = engine_hist(p, jobs)
+    assert o["qinv_count"].sum() > 1e6 and o["qinv_den"].sum() > 1e6
+    parity.compare(h, o, q_scale=0.15)
+
+
+def test_central_group_with_qinv_and_kphi(central_group):
+    """One central group with the q_inv histograms and 8 K_phi bins on the
+    batched kernels (kernel 0): every count identical to the oracle's,
+    sums within parity.RTOL."""
+    g, psi, jobs, _ = central_group
+    p = dict(CENTRAL, invariant_radius_flag=1)
+    o = oracle_mt(p, jobs, psi)
+    h, st = engine_hist(p, jobs, psi)
+    assert o["qinv_count"].sum() > 1e9
+    parity.compare(h, o, q_scale=0.15)
