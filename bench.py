@@ -272,63 +272,126 @@ def measure_fp64_peak() -> dict:
     return out
 
 
-def cpu_baseline(group, p, nthreads=1, target_s=12.0) -> dict:
-    """Oracle (sequential restatement of the reference loops) on a bounded
-    sample: the first rows of the group's same-event list and the first
-    events' mixed lists."""
+def step_mix(group) -> float:
+    """Share of same-event pairs among a group's candidate pairs."""
+    cols, mixed = group
+    n = cols[0].size
+    same = n * (n - 1) / 2
+    return same / (same + sum(l1[0].size * l2[0].size for l1, l2 in mixed))
+
+
+def oracle_sample(orc, group, same_pairs, mixed_pairs, first_row=0, first_event=0):
+    """Times the oracle (one host thread) on a bounded sample of one group:
+    the same-event pairs of a contiguous slice of its list, then mixed
+    pairs of its events from `first_event` on (the last event's list 1 cut
+    short to fit).  Returns (pairs, seconds)."""
+    cols, mixed = group
+    n = cols[0].size
+    ns = int(min(n - first_row, max(2, round(np.sqrt(2.0 * same_pairs)))))
+    pieces, acc = [], 0
+    e = first_event % len(mixed)
+    while acc < mixed_pairs and len(pieces) < len(mixed):
+        l1, l2 = mixed[e]
+        n1 = int(min(l1[0].size, max(1, round((mixed_pairs - acc) / l2[0].size))))
+        pieces.append(([c[:n1] for c in l1], l2))
+        acc += n1 * l2[0].size
+        e = (e + 1) % len(mixed)
+    t0 = time.perf_counter()
+    orc.bin_same([c[first_row:first_row + ns] for c in cols])
+    for l1, l2 in pieces:
+        orc.bin_mixed(l1, l2)
+    dt = time.perf_counter() - t0
+    return ns * (ns - 1) // 2 + acc, dt
+
+
+def cpu_baseline(group, p, target_s=12.0) -> dict:
+    """The oracle (sequential restatement of the reference loops) on one
+    host core, on a bounded sample of the group with the step's mix of
+    same-event and mixed-event pairs."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
     import oracle_lib
-    cols, mixed = group
-    orc = oracle_lib.Oracle(**{k: v for k, v in p.items()})
-    # calibrate on a small slice, then scale to ~target_s
-    n0 = min(3000, cols[0].size)
-    t0 = time.perf_counter()
-    orc.bin_same([c[:n0] for c in cols], nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    rate = (n0 * (n0 - 1) / 2) / max(dt, 1e-6)
-    n_same = int(min(cols[0].size, np.sqrt(2 * rate * target_s / 2)))
-    n_ev = 0
-    budget_mixed = rate * target_s / 2
-    acc = 0
-    for l1, l2 in mixed:
-        if acc >= budget_mixed:
-            break
-        acc += l1[0].size * l2[0].size
-        n_ev += 1
     orc = oracle_lib.Oracle(**p)
-    t0 = time.perf_counter()
-    orc.bin_same([c[:n_same] for c in cols], nthreads=nthreads)
-    for l1, l2 in mixed[:n_ev]:
-        orc.bin_mixed(l1, l2, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    pairs = n_same * (n_same - 1) // 2 + sum(l1[0].size * l2[0].size for l1, l2 in mixed[:n_ev])
-    return {"value": pairs / dt, "unit": "pairs/s", "cores": nthreads, "kind": "port",
-            "sample": "same-event pairs of the first %d particles of one ~%dk-particle group + "
-                      "mixed pairs of its first %d events (%.3g pairs, %.1f s)"
-                      % (n_same, cols[0].size // 1000, n_ev, pairs, dt)}
+    f = step_mix(group)
+    pairs, dt = oracle_sample(orc, group, 2e6 * f, 2e6 * (1 - f))  # calibration
+    rate = pairs / max(dt, 1e-6)
+    pairs, dt = oracle_sample(orc, group, rate * target_s * f, rate * target_s * (1 - f))
+    return {"value": pairs / dt, "unit": "pairs/s", "cores": 1, "kind": "port",
+            "sample": "one host core: same-event pairs of a %.3g-pair slice of one ~%dk-particle "
+                      "group and mixed pairs of its events, %.1f%% same-event as in the step "
+                      "(%.3g pairs, %.1f s)" % (pairs * f, group[0][0].size // 1000, 100 * f,
+                                                pairs, dt)}
+
+
+_REF = {}
+
+
+def _ref_init(workload):
+    """Worker of the reference arm: the workload's first group and one
+    oracle context, built once per process."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    _REF["group"] = make_workload(workload, max_groups=1)[0]
+    _REF["orc"] = oracle_lib.Oracle(**workload_params(workload))
+
+
+def _ref_task(args):
+    w, nproc, same_pairs, mixed_pairs = args
+    cols, mixed = _REF["group"]
+    n = cols[0].size
+    row = (w * n) // nproc
+    row = min(row, max(0, n - int(np.sqrt(2.0 * same_pairs)) - 1))
+    return oracle_sample(_REF["orc"], _REF["group"], same_pairs, mixed_pairs, row,
+                         (w * len(mixed)) // nproc)
 
 
 def run_reference(args) -> None:
+    """The reference arm: the reference's CPU algorithm (the oracle port:
+    the reference binary is built for this container's x86 host and its
+    sources do not travel) on every host core as independent processes,
+    one oracle per core, each step a bounded sample of the workload's group
+    with the step's share of same-event pairs.  The timed steps add up to
+    at least 10 s of sampling."""
+    import multiprocessing as mp
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    nproc = os.cpu_count() or 1
     p = workload_params(args.workload)
-    groups = make_workload(args.workload, max_groups=1)
-    nthreads = os.cpu_count() or 1
-    steps = []
-    for k in range(args.warmup + args.steps):
-        r = cpu_baseline(groups[0], p, nthreads=nthreads, target_s=4.0)
-        if k >= args.warmup:
-            steps.append(r)
-    v = statistics.median(s["value"] for s in steps)
+    group = make_workload(args.workload, max_groups=1)[0]
+    f = step_mix(group)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(nproc, initializer=_ref_init, initargs=(args.workload,)) as pool:
+        # one process alone: the per-core rate, and the sample size
+        pairs, dt = pool.apply(_ref_task, ((0, nproc, 4e6 * f, 4e6 * (1 - f)),))
+        pairs, dt = pool.apply(_ref_task, ((0, nproc, 4e7 * f, 4e7 * (1 - f)),))
+        per_core = pairs / dt
+        step_s = max(0.5, 10.0 / max(1, args.steps))
+        budget = per_core * step_s
+        steps = []
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_ref_task, [(w, nproc, budget * f, budget * (1 - f))
+                                       for w in range(nproc)])
+            wall = time.perf_counter() - t0
+            if k >= args.warmup:
+                steps.append((sum(r[0] for r in res), max(r[1] for r in res), wall))
+    v = sum(s[0] for s in steps) / sum(s[1] for s in steps)
+    timed = sum(s[1] for s in steps)
+    sample = ("%d processes, one oracle each, %d timed steps of %.2g s: same-event pairs of a "
+              "slice of one ~%dk-particle group and mixed pairs of its events, %.1f%% "
+              "same-event as in the GPU step; %.3g pairs per step in all, %.1f s timed"
+              % (nproc, len(steps), step_s, group[0][0].size // 1000, 100 * f,
+                 steps[-1][0], timed))
     line = {"impl": "reference", "metric": "candidate pairs binned per second (same + mixed event)",
             "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "ms_per_step": 1e3 * timed / len(steps),
             "config": {"workload": args.workload, "reference_arm": "CPU oracle port of the "
-                       "reference pair loops, all host threads"},
-            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": nthreads, "kind": "port",
-                             "sample": steps[-1]["sample"]},
+                       "reference pair loops, one process per host core"},
+            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": nproc, "kind": "port",
+                             "processes": nproc, "per_core_value": per_core,
+                             "sample": sample},
             "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -518,7 +581,7 @@ def small_leg(E, torch, dev, stream, flush, local, steps=3) -> dict:
             ms.append(e0.elapsed_time(e1))
     eng.close()
     value = total / (statistics.median(ms) * 1e-3)
-    cpu = cpu_baseline(groups[0], p, nthreads=1, target_s=3.0)
+    cpu = cpu_baseline(groups[0], p, target_s=3.0)
     return {"events": 100, "groups": len(groups), "pairs_per_step": total,
             "jobs_per_launch": len(jobs), "value": value, "unit": "pairs/s",
             "ms_per_step": statistics.median(ms), "steps": steps,
@@ -1095,9 +1158,10 @@ def main() -> None:
         pairs_all = float(pairs)
     value = pairs_all / (t_ms * 1e-3)
 
-    def time_variant(kernel, precision, nsteps, label, batch):
-        """Same workload, another kernel family / precision, same GPU."""
-        engv = E.Engine(device=local, precision=precision, kernel=kernel, **p)
+    def time_variant(kernel, precision, nsteps, label, batch, **over):
+        """Same workload, another kernel family / precision (or parameters
+        `over`), same GPU."""
+        engv = E.Engine(device=local, precision=precision, kernel=kernel, **dict(p, **over))
         engv.set_stream(stream.cuda_stream)
         ms_tot, prs = 0.0, 0
         for k in range(nsteps + 1):  # the first step warms up
@@ -1134,6 +1198,13 @@ def main() -> None:
         variants["grid-" + args.precision] = time_variant(
             E.KERNEL_SCREENED_GRID, prec, 1,
             "screened, one launch per list, no sorting or culling", False)
+        # the same workload with the q_inv histograms too
+        # (invariant_radius_flag = 1): 1-D q_inv numerator and denominator
+        # beside the 3-D ones, every tile pair kept by the cull
+        variants["batched-" + args.precision + "-qinv"] = time_variant(
+            E.KERNEL_SCREENED, prec, 2,
+            "batched persistent, with the q_inv histograms (invariant_radius_flag = 1)", True,
+            invariant_radius_flag=1)
 
     # roofline of the dominant kernel, k_persistent_same: the FP64-pipe
     # instructions it executes (ncu count per binned pair, see
@@ -1258,7 +1329,7 @@ def main() -> None:
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
-        cpu = cpu_baseline(groups[0], p, nthreads=1)
+        cpu = cpu_baseline(groups[0], p)
 
     uneven = serving = ingest = average = None
     balance = fits = precision = precision_df = None
