@@ -600,6 +600,89 @@ rapidity_shift = 0.0
 """
 
 
+DROPIN_PARAMS = """echo_level = 9
+read_in_mode = 10
+ecoOutput = 0
+analyze_flow = 0
+analyze_HBT = 1
+analyze_balance_function = 0
+analyze_ebe_yield = 0
+randomSeed = 1
+read_in_real_mixed_events = 0
+particle_monval = 211
+distinguish_isospin = 1
+resonance_weak_feed_down_flag = 0
+resonance_feed_down_flag = 0
+select_resonances_flag = 0
+net_particle_flag = 0
+flag_charge_dependence = 0
+rapidity_shift = 0.0
+readRapidityShiftFromFile = 0
+long_comoving_boost = 1
+needed_number_of_pairs = 1e18
+invariant_radius_flag = 0
+KT_min = 0.0
+KT_max = 1.0
+n_Kphi = 8
+HBTrap_min = -1.0
+HBTrap_max = 1.0
+qnpts = 41
+q_min = -0.15
+q_max = 0.15
+"""
+
+
+def dropin_leg(seed: int = 1) -> dict:
+    """The drop-in executable end to end (lib/hbt_afterburner.e: read the
+    gzip samples, bin every buffer - its same-event list and every event's
+    rotated partners in one batched call - and write the reference's
+    HBT_correlation_function files) on the small configuration (100 pi+
+    events, Poisson(500), buffers of 5000, 5 partners, 4 K_T bins) and on
+    one central buffer (100 events of Poisson(1500), ~150k particles, 10
+    partners, 8 K_T x 8 K_phi bins).  Against the oracle's restatement of
+    the reference's buffer loop and writer on one host core on the small
+    configuration (the whole run)."""
+    from hadronic_afterburner_toolkit_gb300 import synth
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    exe = os.path.join(REPO, "hadronic_afterburner_toolkit_gb300", "lib", "hbt_afterburner.e")
+    out = {}
+    cases = (("small", synth.small_pions(seed=seed), 5000, 5, 5, 0),
+             ("central_buffer", synth.central_pions(n_events=100, seed=seed), 150000, 10, 9, 1))
+    for name, ev, buf, nmix, nkt, az in cases:
+        with tempfile.TemporaryDirectory() as work:
+            res = os.path.join(work, "results")
+            os.makedirs(res)
+            synth.write_mode10(os.path.join(res, "particle_samples.gz"), ev)
+            with open(os.path.join(work, "parameters.dat"), "w") as f:
+                f.write(DROPIN_PARAMS + "event_buffer_size = %d\nn_KT = %d\nazimuthal_flag = %d\n"
+                        "hbt_mixed_partners = %d\n" % (buf, nkt, az, nmix))
+            t0 = time.perf_counter()
+            proc = subprocess.run([exe], cwd=work, capture_output=True, text=True, timeout=600)
+            wall = time.perf_counter() - t0
+            if proc.returncode != 0:
+                raise RuntimeError("drop-in failed: " + proc.stderr[-500:])
+            pairs = sum(int(l.split(":")[1]) for l in proc.stdout.splitlines()
+                        if l.startswith("[Info] number of") and "pairs:" in l)
+            files = [f for f in os.listdir(res) if f.startswith("HBT_correlation")]
+            r = {"particles": ev.n_particles, "buffers": len(synth.buffers(ev, buf)),
+                 "pairs": pairs, "wall_s": wall, "pairs_per_s": pairs / wall,
+                 "files_written": len(files)}
+            if name == "small":
+                # the oracle's buffer loop and writer, one host core
+                p = dict(workload_params("small"), n_KT=nkt)
+                orc = oracle_lib.Oracle(number_of_mixed_events=nmix, seed=1, **p)
+                t0 = time.perf_counter()
+                for a, b in synth.buffers(ev, buf):
+                    orc.process_buffer(synth.subset(ev, a, b))
+                os.makedirs(os.path.join(work, "oracle"))
+                orc.write(os.path.join(work, "oracle"))
+                cpu = time.perf_counter() - t0
+                r.update(cpu_oracle_s=cpu, cpu_cores=1, speedup_vs_cpu_core=cpu / wall)
+            out[name] = r
+    return out
+
+
 def capped_leg(E, torch, dev, dgroups, groups, p, local, uncapped_ms, cap=3e7, n_groups=3):
     """The central workload at the reference's default pair cap,
     needed_number_of_pairs = 3e7 (parameters.dat), which binds in the first
@@ -914,16 +997,23 @@ def fit_leg(n_tables: int = 256, cpu_seconds: float = 8.0) -> dict:
     return res
 
 
-def precision_leg(E, groups, p, local, other=None, n_kaon_groups: int = 3) -> dict:
-    """FP32-weight (or `other`) form against the FP64 form on the precision
-    configuration: one central pi+ group and the first K+ groups (1000 K+
-    events, Poisson(250), T = 0.30 GeV, oversample 100, 10 partners), same
-    grid and bins. Counts and denominators must be identical; for the
-    numerator (sum of cos) and the mean-q sums, per bin: the error per pair
-    |fp32w - fp64| / count, and the relative error over the bins whose sum
-    does not cancel (at least 100 pairs, |sum| at least half the count times
-    1 for cos or 0.01 GeV for q). The FP64 form is the oracle's stand-in at this size
-    (it matches the CPU oracle to 1e-12 per pair on the test cases)."""
+def precision_leg(E, groups, p, local, n_kaon_groups: int = 3) -> dict:
+    """The precision configuration against the FP64 oracle: one central pi+
+    group and the first K+ groups (1000 K+ events, Poisson(250), T = 0.30
+    GeV, oversample 100, 10 partners), same grid and bins, each binned by
+    the FP64, FP32-weight and double-float forms on the GPU and by the
+    oracle's pair loops on every host core.  Per form: counts and
+    denominators identical or not; numerator (sum of cos(q.dx)) error per
+    bin as |dnum| / count (over every bin with a pair), as |dnum| / sum of
+    |cos| and as |dnum| / |num| (both over the bins with at least 2 pairs,
+    the ones the writer prints); the mean-q sums' error per pair."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    L = oracle_lib.lib()
+    import ctypes
+    L.orc_get_abs_num.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+    nthreads = os.cpu_count() or 1
+
     def run(groups_, prec):
         eng = E.Engine(device=local, precision=prec, **p)
         for cols, mixed in groups_:
@@ -932,30 +1022,49 @@ def precision_leg(E, groups, p, local, other=None, n_kaon_groups: int = 3) -> di
         eng.close()
         return h
 
-    def errors(h64, h32):
-        out = {"counts_identical": bool(np.array_equal(h64["count"], h32["count"])),
-               "den_identical": bool(np.array_equal(h64["den"], h32["den"])),
-               "bins_with_pairs": int((h64["count"] > 0).sum())}
-        m = h64["count"] > 0
-        big = h64["count"] >= 100
-        for k, scale in (("num", 1.0), ("q_out", 0.01), ("q_side", 0.01), ("q_long", 0.01)):
-            d = np.abs(h32[k] - h64[k])
-            out[k + "_max_err_per_pair"] = float((d[m] / h64["count"][m]).max()) if m.any() else 0.0
-            # relative error where the bin's sum does not cancel: at least 100
-            # pairs and |sum| >= half the count times 1 (cos) or 0.01 GeV (q)
-            sel = big & (np.abs(h64[k]) >= 0.5 * scale * h64["count"])
-            out[k + "_max_rel_err_coherent_bins"] = (
-                float((d[sel] / np.abs(h64[k][sel])).max()) if sel.any() else 0.0)
+    def oracle(groups_):
+        orc = oracle_lib.Oracle(**p)
+        t0 = time.perf_counter()
+        for cols, mixed in groups_:
+            orc.bin_same(cols, nthreads=nthreads)
+            for l1, l2 in mixed:
+                orc.bin_mixed(l1, l2, nthreads=nthreads)
+        h = orc.hist()
+        dt = time.perf_counter() - t0
+        h["abs_num"] = np.zeros_like(h["num"])
+        L.orc_get_abs_num(orc._h, h["abs_num"].ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return h, dt
+
+    def errors(ho, hg):
+        cnt = ho["count"]
+        m, sel = cnt > 0, cnt >= 2
+        dn = np.abs(hg["num"] - ho["num"])
+        out = {"counts_identical": bool(np.array_equal(ho["count"], hg["count"])),
+               "den_identical": bool(np.array_equal(ho["den"], hg["den"])),
+               "counters_identical": bool(np.array_equal(ho["ctr_num"], hg["ctr_num"]) and
+                                          np.array_equal(ho["ctr_den"], hg["ctr_den"])),
+               "num_max_err_per_pair": float((dn[m] / cnt[m]).max()),
+               "num_max_err_per_abs_cos": float((dn[sel] / np.maximum(ho["abs_num"][sel],
+                                                                     1e-300)).max()),
+               "num_max_rel_err": float((dn[sel] / np.maximum(np.abs(ho["num"][sel]),
+                                                             1e-300)).max())}
+        for k in ("q_out", "q_side", "q_long"):
+            out[k + "_max_err_per_pair_gev"] = float(
+                (np.abs(hg[k] - ho[k])[m] / cnt[m]).max())
         return out
 
-    other = E.PRECISION_FP32W if other is None else other
-    res = {}
-    pi = groups[:1]
-    res["pi+"] = errors(run(pi, E.PRECISION_FP64), run(pi, other))
-    kg = make_workload("kaons", max_groups=n_kaon_groups)
-    res["K+"] = errors(run(kg, E.PRECISION_FP64), run(kg, other))
-    res["K+"]["groups"] = len(kg)
-    res["K+"]["particles_per_group"] = int(np.mean([g[0][0].size for g in kg]))
+    res = {"bin_selection": "per pair: bins with >= 1 pair; per |cos| sum and relative: bins "
+                            "with >= 2 pairs (the ones the reference's writer prints)",
+           "oracle": "oracle pair loops on %d host threads" % nthreads}
+    for name, gs in (("pi+", groups[:1]),
+                     ("K+", make_workload("kaons", max_groups=n_kaon_groups))):
+        ho, dt = oracle(gs)
+        r = {"groups": len(gs), "particles_per_group": int(np.mean([g[0][0].size for g in gs])),
+             "bins_with_pairs": int((ho["count"] > 0).sum()), "oracle_s": dt}
+        for label, prec in (("fp64", E.PRECISION_FP64), ("fp32w", E.PRECISION_FP32W),
+                            ("df64", E.PRECISION_DF64)):
+            r[label] = errors(ho, run(gs, prec))
+        res[name] = r
     return res
 
 
@@ -983,6 +1092,92 @@ def make_requests(n_jobs: int, seed: int = 5):
                    needed_number_of_pairs=1e18)
         reqs.append((cols, np.ascontiguousarray(ev.offsets, dtype=np.int64), prm, k + 1))
     return reqs
+
+
+def serving_stream(E, local, reqs, rate, n, precision, seed):
+    """n requests at Poisson arrivals of `rate` jobs/s through the serving
+    loop.  Each request takes one event set of the pool `reqs` (in turn)
+    with its own draw of the configuration's analysis parameters (qnpts in
+    {21, 41, 61}, q_max in [0.1, 0.3] GeV, 2-8 K_T bins).  A second thread
+    waits for the requests in order, records their latency (submit to
+    results in host memory) and releases them.  Latency percentiles are
+    taken over the steady-state window: requests that arrived between 10 %
+    and 90 % of the arrival span."""
+    import threading
+    from hadronic_afterburner_toolkit_gb300 import server
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    prms = []
+    for k in range(n):
+        qmax = float(rng.uniform(0.1, 0.3))
+        prms.append(dict(reqs[k % len(reqs)][2], qnpts=int(rng.choice([21, 41, 61])),
+                         q_min=-qmax, q_max=qmax, n_KT=int(rng.integers(2, 9)) + 1,
+                         precision=precision, kernel=E.KERNEL_SCREENED))
+    ids = [None] * n
+    lat = np.zeros(n)
+    pairs = [0]
+    submitted = threading.Event()
+    with server.Server(device=local) as srv:
+        def waiter():
+            for k in range(n):
+                while ids[k] is None:
+                    time.sleep(1e-4)
+                srv.wait(ids[k])
+                inf = srv.info(ids[k])
+                lat[k] = inf["latency_ms"]
+                pairs[0] += inf["pairs_same"] + inf["pairs_mixed"]
+                srv.release(ids[k])
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        late = 0.0
+        for k in range(n):
+            now = time.perf_counter() - t0
+            if arrivals[k] > now:
+                time.sleep(arrivals[k] - now)
+            else:
+                late = max(late, now - arrivals[k])
+            cols, off, _, sd = reqs[k % len(reqs)]
+            ids[k] = srv.submit(cols, off, prms[k], oversample=1, mixed_partners=1, seed=sd + k)
+        submitted.set()
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    span = float(arrivals[-1])
+    win = (arrivals >= 0.1 * span) & (arrivals <= 0.9 * span)
+    return {"requests": n, "rate_jobs_per_s": rate, "arrival_span_s": span, "wall_s": wall,
+            "pairs_per_s": pairs[0] / wall,
+            "offered_pairs_per_s": pairs[0] / span,
+            "p50_ms": float(np.percentile(lat[win], 50)),
+            "p99_ms": float(np.percentile(lat[win], 99)),
+            "max_ms": float(lat[win].max()), "window_requests": int(win.sum()),
+            "all_p99_ms": float(np.percentile(lat, 99)),
+            "submit_lag_max_s": late, "rounds": st["rounds"], "peak_active": st["peak_active"],
+            "peak_device_bytes": st["peak_bytes"], "gpu_busy_ms": st["gpu_busy_ms"]}
+
+
+def steady_serving_leg(E, local, n=1000, seed=7) -> dict:
+    """Serving at steady state and overloaded, each over n >= 1000
+    requests: first config 5's 200 jobs/s, which is above what the GPU
+    sustains for these requests (its throughput over the run is the
+    measured capacity), then 60 % of that capacity in jobs/s, for the FP64
+    and FP32-weight forms."""
+    reqs = make_requests(48, seed)
+    out = {"job_semantics": "each event of a request is its own same-event list (oversample "
+                            "1) with one rotated partner event; config 5's one-buffer jobs "
+                            "with nev/2+1 partners would offer ~1e12 pairs/s at 200 jobs/s, "
+                            "tens of times this GPU's capacity",
+           "event_sets": len(reqs)}
+    over = serving_stream(E, local, reqs, 200.0, n, E.PRECISION_FP64, seed)
+    out["overloaded-fp64"] = over
+    mean_pairs = over["pairs_per_s"] * over["wall_s"] / n
+    capacity = over["pairs_per_s"] / mean_pairs  # jobs/s the GPU sustained
+    out["capacity_jobs_per_s_fp64"] = capacity
+    out["mean_pairs_per_request"] = mean_pairs
+    rate = 0.6 * capacity
+    out["steady-fp64"] = serving_stream(E, local, reqs, rate, n, E.PRECISION_FP64, seed + 1)
+    out["steady-fp32w"] = serving_stream(E, local, reqs, rate, n, E.PRECISION_FP32W, seed + 1)
+    return out
 
 
 def serving_leg(E, local, n_jobs=48, rate=200.0, seed=5) -> dict:
@@ -1332,17 +1527,18 @@ def main() -> None:
         cpu = cpu_baseline(groups[0], p)
 
     uneven = serving = ingest = average = None
-    balance = fits = precision = precision_df = None
+    balance = fits = precision = None
+    dropin = None
     if not args.no_ingest and rank == 0:
         ingest = ingest_leg()
         average = average_leg()
+        dropin = dropin_leg()
     if not args.no_bf and rank == 0:
         balance = bf_leg()
     if not args.no_fit and rank == 0:
         fits = fit_leg()
     if not args.no_precision and rank == 0 and args.workload == "central":
         precision = precision_leg(E, groups, p, local)
-        precision_df = precision_leg(E, groups, p, local, other=E.PRECISION_DF64)
     small = None
     if not args.no_uneven and rank == 0 and args.workload == "central":
         small = small_leg(E, torch, dev, stream, flush, local)
@@ -1353,6 +1549,7 @@ def main() -> None:
         uneven = uneven_leg(E, torch, dev, stream, flush, local)
     if not args.no_serving:
         serving = serving_leg(E, local, n_jobs=args.serving_jobs)
+        serving["steady_state"] = steady_serving_leg(E, local)
 
     if rank == 0:
         st = eng.stats()
@@ -1393,14 +1590,14 @@ def main() -> None:
                 "cpu_baseline": cpu,
                 "small_config": small,
                 "capped": capped,
+                "dropin": dropin,
                 "uneven": uneven,
                 "serving": serving,
                 "ingest": ingest,
                 "average": average,
                 "balance_function": balance,
                 "radii_fit": fits,
-                "precision_fp32w_vs_fp64": precision,
-                "precision_df64_vs_fp64": precision_df,
+                "precision_vs_oracle": precision,
                 "stats": st}
         print(json.dumps(line))
     eng.close()
