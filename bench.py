@@ -1249,6 +1249,9 @@ def main() -> None:
                     help="skip the radii-fit leg")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the FP32-weight against FP64 error report")
+    ap.add_argument("--order-items", type=int, default=0, choices=[0, 1],
+                    help="hbt_tuning.order_items of the timed engine: same-event tile pairs "
+                         "in momentum-region order")
     ap.add_argument("--no-capped", action="store_true",
                     help="skip the central workload at the default pair cap (3e7)")
     ap.add_argument("--no-ingest", action="store_true",
@@ -1293,7 +1296,7 @@ def main() -> None:
     batched = kern == E.KERNEL_SCREENED
     if batched:
         # CUDA events around the persistent kernels (the roofline's kernel time)
-        eng.set_tuning(time_kernels=1)
+        eng.set_tuning(time_kernels=1, order_items=args.order_items)
 
     def run_group(engine, grp, batch, device=True):
         """One oversample group: its same-event pairs and every event's
@@ -1568,6 +1571,7 @@ def main() -> None:
                            "qnpts": p["qnpts"], "n_KT_bins": p["n_KT"] - 1,
                            "n_Kphi": p["n_Kphi"] if p["azimuthal_flag"] else 1,
                            "precision": args.precision, "kernel": args.kernel,
+                           "order_items": args.order_items,
                            "l2": "flushed (256 MB write) between steps",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "pairs_per_step": pairs_all / args.steps / max(world, 1),

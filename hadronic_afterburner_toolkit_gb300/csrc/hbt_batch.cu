@@ -159,6 +159,22 @@ __device__ __forceinline__ bool boxes_may_pair(const BatchJob &b, const Box &a, 
     return true;
 }
 
+// Momentum-space region of a tile pair's pairs: K = (p_1 + p_2) / 2 at the
+// boxes' centres, in K_T cells of 1/32 GeV (up to 2 GeV) and 32 azimuthal
+// sectors, above the analysis index (serving).  Items of one region update
+// the same few histogram slots.
+__device__ __forceinline__ unsigned region_key(const BatchJob &job, const Box &a, const Box &c) {
+    const double kx = 0.25 * (a.x0 + a.x1 + c.x0 + c.x1);
+    const double ky = 0.25 * (a.y0 + a.y1 + c.y0 + c.y1);
+    const double kt = sqrt(kx * kx + ky * ky);
+    const unsigned kc = kt < 2.0 ? (unsigned)(kt * 32.0) : 63u;
+    double ph = atan2(ky, kx) * (16.0 / 3.141592653589793) + 16.0;  // [0, 32]
+    const unsigned pc = ph >= 0.0 && ph < 32.0 ? (unsigned)ph : 0u;
+    // (below 0x1FFFFF, so that no key equals the unused entries' 0xffffffff)
+    const unsigned dev = job.dev < 0x1FFFFE ? (unsigned)job.dev : 0x1FFFFEu;
+    return (dev << 11) | (kc << 5) | pc;
+}
+
 // Culled queues: same-event items at items[0, same_cap), mixed-event items
 // at items[same_cap, same_cap + mixed_cap); n_items[0] / n_items[1] count them.
 __global__ void k_cull(BatchDev b) {
@@ -181,7 +197,13 @@ __global__ void k_cull(BatchDev b) {
             const Item it = Item{(unsigned)J, (unsigned)ti, (unsigned)tj};
             if (job.kind == 0) {
                 const unsigned slot = atomicAdd(b.n_items, 1u);
-                if (slot < b.same_cap) b.items[slot] = it;
+                if (slot < b.same_cap) {
+                    b.items[slot] = it;
+                    if (b.order_items) {
+                        b.item_key_in[slot] = region_key(job, A, B);
+                        b.item_pos_in[slot] = slot;
+                    }
+                }
             } else {
                 const unsigned slot = atomicAdd(b.n_items + 1, 1u);
                 if (slot < b.mixed_cap) b.items[b.same_cap + slot] = it;
@@ -207,6 +229,14 @@ cudaError_t persistent_mixed(const Device &d, const BatchDev &b, int grid, cudaS
         return mode == MODE_FAST ? persistent_mixed_qinv(d, b, grid, st) : cudaErrorNotSupported;
     if (mode == MODE_FAST) return persistent_mixed_fast(d, b, grid, st);
     return persistent_mixed_ordered(d, b, grid, st, mode);
+}
+
+size_t item_sort_temp_bytes(long long n) {
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (const unsigned *)nullptr,
+                                    (unsigned *)nullptr, (const unsigned *)nullptr,
+                                    (unsigned *)nullptr, (int)n, 0, 32);
+    return bytes;
 }
 
 size_t batch_sort_temp_bytes(long long cap) {
@@ -238,9 +268,21 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
     }
     if ((e = cudaMemsetAsync(b.n_items, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(b.item_next, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
+    if (b.order_items && b.same_cap > 0 &&
+        (e = cudaMemsetAsync(b.item_key_in, 0xff, (size_t)b.same_cap * sizeof(unsigned), st)) !=
+            cudaSuccess)
+        return e;
     if (b.total_pairs > 0) {
         k_cull<<<gs, 256, 0, st>>>(b);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (b.order_items && b.same_cap > 0) {
+        // unused entries keep the key 0xffffffff and sort behind the queue
+        size_t bytes = b.item_sort_temp_bytes;
+        e = cub::DeviceRadixSort::SortPairs(b.item_sort_temp, bytes, b.item_key_in,
+                                            b.item_key_out, b.item_pos_in, b.item_pos_out,
+                                            (int)b.same_cap, 0, 32, st);
+        if (e != cudaSuccess) return e;
     }
     // the COUNT pass bins nothing: no FP32 partials to merge
     const int prec = mode == MODE_COUNT ? 0 : d.precision;

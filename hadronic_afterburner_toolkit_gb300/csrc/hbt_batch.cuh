@@ -69,6 +69,14 @@ struct BatchDev {
     unsigned mixed_cap;   // candidate mixed-event tile pairs
     unsigned *n_items;    // [2] culled queue lengths (same, mixed)
     unsigned *item_next;  // [2] persistent-kernel cursors
+    // Same-event queue order by momentum-space region (order_items): k_cull
+    // writes each kept item's region key and position, a radix sort orders
+    // the positions by key, and the same-event kernel takes items in that
+    // order, so the CTAs running at any time update few histogram slots.
+    int order_items;
+    unsigned *item_key_in, *item_key_out, *item_pos_in, *item_pos_out;
+    void *item_sort_temp;
+    size_t item_sort_temp_bytes;
     // cell sizes of the sort key
     double p_extent, inv_cell_pt, y_extent, inv_cell_y;
     // Several analyses in one launch (the serving loop): each job's engine
@@ -80,6 +88,8 @@ struct BatchDev {
 
 int persistent_blocks_per_sm();
 size_t batch_sort_temp_bytes(long long cap);
+// Scratch bytes of the same-event queue's region sort for n items.
+size_t item_sort_temp_bytes(long long n);
 // Sort, box, cull and bin one batch.  chunk > 0 splits the FP32-weight
 // form's same-event queue into chunks of that many items with a merge of
 // the FP32 partials after each: of `d` for a one-analysis batch, of every

@@ -63,7 +63,7 @@ struct hbt_ctx {
     hbt::BatchRunner runner;
     int persistent_grid = 152 * 4;
     int sms = 152, max_blocks_per_sm = 5;
-    hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0};
+    hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0, 0};
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging
@@ -384,6 +384,7 @@ hbt::Tuning runner_tuning(const hbt_ctx *c, const hbt_tuning &t) {
     r.cell_y = t.cell_y;
     r.graph = t.use_graph != 0;
     r.time_kernels = t.time_kernels != 0;
+    r.order_items = t.order_items != 0;
     return r;
 }
 
@@ -427,7 +428,8 @@ std::vector<FastJob> fast_jobs_of(int32_t n_jobs, const hbt_job *jobs) {
 bool tuning_valid(const hbt_tuning &t) {
     return t.blocks_per_sm >= 0 && t.cell_pt >= 0.0 && t.cell_y >= 0.0 && t.merge_chunk >= 0 &&
            t.merge_chunk <= kMergeChunk && (t.use_graph == 0 || t.use_graph == 1) &&
-           (t.time_kernels == 0 || t.time_kernels == 1);
+           (t.time_kernels == 0 || t.time_kernels == 1) &&
+           (t.order_items == 0 || t.order_items == 1);
 }
 
 hbt_tuning tuning_defaults(hbt_tuning t) {

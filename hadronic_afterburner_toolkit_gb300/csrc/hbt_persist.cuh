@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(D
         __syncthreads();
         const unsigned k = item;
         if (k >= stop) break;
-        const Item it = b.items[k];
+        const Item it = b.items[b.order_items ? b.item_pos_out[k] : k];
         const BatchJob &job = b.jobs[it.job];
         const Device &dd = item_device(d, b, job, dsm);
         const BatchList &la = b.lists[job.la];

@@ -12,7 +12,7 @@ BatchRunner::~BatchRunner() {
     for (cudaEvent_t e : marks_)
         if (e) cudaEventDestroy(e);
     Buf *all[] = {&lists_, &jobs_, &offs_, &table_, &keys_, &vals_, &sort_temp_, &boxes_,
-                  &items_, &counters_, &devs_};
+                  &items_, &counters_, &devs_, &item_order_, &item_sort_temp_};
     for (Buf *b : all)
         if (b->p) cudaFree(b->p);
 }
@@ -234,6 +234,10 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
         !grow(items_, (size_t)pairs * sizeof(Item), err) ||
         !grow(counters_, 4 * sizeof(unsigned), err))
         return false;
+    if (t.order_items && same_pairs > 0 &&
+        (!grow(item_order_, (size_t)4 * same_pairs * sizeof(unsigned), err) ||
+         !grow(item_sort_temp_, item_sort_temp_bytes(same_pairs), err)))
+        return false;
     std::vector<long long> offs(list_off);
     offs.insert(offs.end(), tile_off.begin(), tile_off.end());
     offs.insert(offs.end(), pair_off.begin(), pair_off.end());
@@ -280,6 +284,16 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
     b.inv_cell_y = 1.0 / t.cell_y;
     b.devs = devs_dev;
     b.n_devs = n_devs;
+    b.order_items = t.order_items && same_pairs > 0 ? 1 : 0;
+    if (b.order_items) {
+        unsigned *o = static_cast<unsigned *>(item_order_.p);
+        b.item_key_in = o;
+        b.item_key_out = o + same_pairs;
+        b.item_pos_in = o + 2 * same_pairs;
+        b.item_pos_out = o + 3 * same_pairs;
+        b.item_sort_temp = item_sort_temp_.p;
+        b.item_sort_temp_bytes = item_sort_temp_.bytes;
+    }
     const cudaError_t e = launch(d, b, devs_host, n_devs, t, st, mode);
     if (e != cudaSuccess) {
         err = std::string("batch launch failed: ") + cudaGetErrorString(e);

@@ -33,6 +33,7 @@ struct Tuning {
     double cell_y = 0.05;    // Morton cell of rapidity
     bool graph = true;       // launch the pipeline as a CUDA graph
     bool time_kernels = false;  // record events around the persistent kernels
+    bool order_items = false;   // same-event items in momentum-region order
 };
 
 class BatchRunner {
@@ -84,6 +85,7 @@ class BatchRunner {
     cudaError_t launch(const Device &d, const BatchDev &b, const Device *devs_host, int n_devs,
                        const Tuning &t, cudaStream_t st, int mode);
     Buf lists_, jobs_, offs_, table_, keys_, vals_, sort_temp_, boxes_, items_, counters_, devs_;
+    Buf item_order_, item_sort_temp_;
     long long last_pairs_ = 0, last_same_ = 0, last_mixed_ = 0;
     cudaStream_t last_stream_ = nullptr;
     int last_reuse_ = -1;

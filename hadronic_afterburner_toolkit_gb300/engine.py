@@ -59,7 +59,8 @@ class HbtJob(ctypes.Structure):
 
 class HbtTuning(ctypes.Structure):
     _fields_ = [("blocks_per_sm", _I32), ("cell_pt", _D), ("cell_y", _D),
-                ("merge_chunk", _I32), ("use_graph", _I32), ("time_kernels", _I32)]
+                ("merge_chunk", _I32), ("use_graph", _I32), ("time_kernels", _I32),
+                ("order_items", _I32)]
 
 
 class HbtStats(ctypes.Structure):

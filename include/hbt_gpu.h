@@ -188,6 +188,11 @@ typedef struct hbt_tuning {
                                launches */
     int32_t time_kernels;   /* 1: time the persistent kernels with CUDA events
                                (hbt_stats.same_kernel_ms / mixed_kernel_ms) */
+    int32_t order_items;    /* 1: take the same-event tile pairs in the order of
+                               their momentum-space region (K_T and azimuth of
+                               the tiles' mean momentum), so that the CTAs
+                               running at any time update few histogram slots;
+                               0: in the order the cull found them */
 } hbt_tuning;
 
 hbt_status hbt_set_tuning(hbt_ctx *ctx, const hbt_tuning *t);
