@@ -53,12 +53,16 @@ def _run_oracle(p, jobs, psi=0.0):
     return orc.hist()
 
 
-@pytest.mark.parametrize("az,boost", [(0, 1), (1, 1), (0, 0), (1, 0)])
-def test_batch_matches_oracle(az, boost):
+@pytest.mark.parametrize("az,boost,order", [(0, 1, 0), (1, 1, 0), (0, 0, 0), (1, 0, 0),
+                                            (0, 1, 1), (1, 0, 1)])
+def test_batch_matches_oracle(az, boost, order):
+    """order = 1: the same-event tile pairs taken in momentum-region order
+    (hbt_tuning.order_items); the bins and counts do not depend on it."""
     from hadronic_afterburner_toolkit_gb300 import engine as E
     p = dict(BASE, azimuthal_flag=az, long_comoving_boost=boost)
     jobs = _uneven_jobs(seed=3 + az + 2 * boost)
     eng = E.Engine(**p)
+    eng.set_tuning(order_items=order)
     eng.set_psi_ref(0.7)
     eng.bin_batch(jobs)
     h = _run_oracle(p, jobs, psi=0.7)
