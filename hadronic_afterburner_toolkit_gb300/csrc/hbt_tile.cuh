@@ -168,13 +168,61 @@ __device__ __forceinline__ int screen_lcms(const Screen &S, float4 a, float4 b, 
 }
 
 // Stage B: window checks.  Returns 0 (reject), 1 (all windows certainly
-// passed), 2 (undecided).
+// passed), 2 (undecided).  The K_T and LCMS parts of screen_kt and
+// screen_lcms in one function (the forms without q_inv histograms keep it
+// whole: split, their register allocation spilled more).
 template <bool BOOST>
 __device__ __forceinline__ int screen_windows(const Screen &S, float4 a, float4 b, Q &q) {
-    const int cls = screen_kt(S, a, b, q);
-    if (cls == 0) return 0;
-    const int w = screen_lcms<BOOST>(S, a, b, q);
-    return w == 1 ? cls : w;
+    q.sx = a.x + b.x;
+    q.sy = a.y + b.y;
+    const float dx = a.x - b.x, dy = a.y - b.y;
+    q.Ax = fabsf(a.x) + fabsf(b.x);
+    q.Ay = fabsf(a.y) + fabsf(b.y);
+    q.k2 = __fmaf_rn(q.sx, q.sx, q.sy * q.sy);
+    const float AA = __fmaf_rn(q.Ax, q.Ax, q.Ay * q.Ay);
+    // |k2 - (S_x^2 + S_y^2)|
+    q.ek2 = 6.1f * U * __fmaf_rn(q.Ax, fabsf(q.sx), q.Ay * fabsf(q.sy)) + 3.1f * U * q.k2 +
+            1e-13f * AA;
+    // K_T window (reference rejects Kp2 < KT_min^2 or Kp2 > KT_max^2)
+    const float ekt = 2.0f * q.ek2 + S.kt_slack;
+    if ((S.kt_lo4 > 0.0f && q.k2 + ekt < S.kt_lo4) || q.k2 - ekt > S.kt_hi4) return 0;
+    int cls = ((S.kt_lo4 == 0.0f || q.k2 - ekt > S.kt_lo4) && q.k2 + ekt < S.kt_hi4) ? 1 : 2;
+    const float rel_k2 = __fdividef(q.ek2, q.k2) * 1.0001f;
+    if (!(q.k2 > 0.0f) || !(rel_k2 <= 0.05f)) return 2;  // |S| too small for the bounds
+    const float inv = rsqrtf(q.k2);
+    const float rel_inv = 0.53f * rel_k2 + 4.5f * U;
+    const float eN = 9.0f * U * AA;
+    const float no = __fmaf_rn(dx, q.sx, dy * q.sy);
+    const float ns = __fmaf_rn(dy, q.sx, -(dx * q.sy));
+    q.qo = no * inv;
+    q.eqo = __fmaf_rn(fabsf(no), rel_inv, eN) * inv + U * fabsf(q.qo);
+    q.qs = ns * inv;
+    q.eqs = __fmaf_rn(fabsf(ns), rel_inv, eN) * inv + U * fabsf(q.qs);
+    const float dz = a.z - b.z;
+    const float Az = fabsf(a.z) + fabsf(b.z);
+    if (BOOST) {
+        const float sE = a.w + b.w, sz = a.z + b.z, dE = a.w - b.w;
+        const float AE = fabsf(a.w) + fabsf(b.w);
+        const float m = sE - sz, p = sE + sz;
+        const float e0 = 2.01f * U * (AE + Az);
+        const float rel_m2 =
+            (__fdividef(e0 + U * fabsf(m), m) + __fdividef(e0 + U * fabsf(p), p)) * 1.0001f +
+            1.01f * U;
+        if (!(m > 0.0f) || !(p > 0.0f) || !(rel_m2 <= 0.05f)) return 2;
+        const float rl = rsqrtf(m * p);
+        const float rel_rl = 0.53f * rel_m2 + 4.5f * U;
+        const float nl = __fmaf_rn(sE, dz, -(sz * dE));
+        q.ql = nl * rl;
+        q.eql = __fmaf_rn(fabsf(nl), rel_rl, 17.0f * U * AE * Az) * rl + U * fabsf(q.ql);
+    } else {
+        q.ql = dz;
+        q.eql = 2.1f * U * Az;
+    }
+    const int wo = window_class(S, q.qo, q.eqo), ws = window_class(S, q.qs, q.eqs),
+              wl = window_class(S, q.ql, q.eql);
+    if (wo == 0 || ws == 0 || wl == 0) return 0;
+    if (wo == 2 || ws == 2 || wl == 2) return 2;
+    return cls;
 }
 
 // floor((v - base) / delta_q) when certain, else -1.
@@ -678,6 +726,47 @@ __device__ __forceinline__ void drain(T *q, int count, int lane, F &process) {
     __syncwarp();
 }
 
+// Sum of x over the lanes in `peers` (the lanes of the warp holding the
+// same key, from __match_any_sync), left in the group's lowest lane: a tree
+// over the lanes' ranks in their group, log2(group size) shuffle rounds
+// (each lane adds its next remaining peer's value, then the odd ranks drop
+// out and the ranks halve).  Called by all 32 lanes.
+__device__ __forceinline__ double sum_peers(unsigned peers, double x) {
+    const int lane = threadIdx.x & 31;
+    unsigned rest = peers & (0xfffffffeu << lane);  // peers above this lane
+    int rank = __popc(peers & ((1u << lane) - 1u));
+    while (__any_sync(0xffffffffu, rest != 0u)) {
+        const int next = __ffs(rest);  // 1-based, 0: none left
+        const double t = __shfl_sync(0xffffffffu, x, next ? next - 1 : lane);
+        if (next) x += t;
+        rest &= ~__ballot_sync(0xffffffffu, rank & 1);
+        rank >>= 1;
+    }
+    return x;
+}
+
+// One q_inv histogram update per group of lanes with the same bin (`key`,
+// 0xffffffff: no update): the q_inv histogram has only n_KT x qnpts bins,
+// which the pairs of a warp share, so per-pair atomics would queue on a few
+// addresses.  num: add q_inv and cos (numerator, same-event) or only the
+// count (denominator, mixed-event).  Called by all 32 lanes.
+__device__ __forceinline__ void qinv_update(const Device &d, unsigned key, double qv, double wv,
+                                            bool num) {
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int lane = threadIdx.x & 31;
+    const bool leader = (peers & ((1u << lane) - 1u)) == 0u && key != 0xffffffffu;
+    if (num) {
+        const double sq = sum_peers(peers, qv), sw = sum_peers(peers, wv);
+        if (leader) {
+            atomicAdd(&d.h.qi_sums[key].q, sq);
+            atomicAdd(&d.h.qi_sums[key].w, sw);
+            atomicAdd(d.h.qi_cnt + key, (unsigned long long)__popc(peers));
+        }
+    } else if (leader) {
+        atomicAdd(d.h.qi_den + key, (unsigned long long)__popc(peers));
+    }
+}
+
 // A mixed-event pair the screens left undecided: the reference chain
 // decides.  Out of line: it runs for a few pairs per thousand, and inlined
 // its registers would crowd the screen's (the kernel spilled 420 bytes).
@@ -826,286 +915,296 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
     auto *q2 = sm.queue2[w];
     int count = 0, count2 = 0;
 
-    // stage C with q_inv histograms, for 32 screened pairs: the 3-D event
-    // and the q_inv event of each pair (cos(q.dx) computed once for both)
-    auto values_q = [&](uint4 e4, bool valid) {
-        if (!valid) return;
-        const unsigned e = e4.x;
-        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
-        const bool swap = (e >> 16) & 1u;
-        bool has3 = (e >> 18) & 1u, hasq = (e >> 19) & 1u;
-        const int bin = (int)e4.y, slot = (int)(e4.z & 0xffffu), iK = (int)(e4.z >> 16);
-        const int kq = (int)e4.w;
-        double A[8], B[8];  // first and second particle of the pair
-#pragma unroll
-        for (int f = 0; f < 8; f++) {
-            const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
-            const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
-            A[f] = swap ? v : u;
-            B[f] = swap ? u : v;
-        }
-        const long long oa = sm.oi[qi], ob = sm.oj[qj];
-        const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
-        if ((e >> 17) & 1u) {
-            // undecided: the reference chain decides both events
-            if (MODE == MODE_FAST)
-                undecided_pair_ordered<false, MODE_FAST>(d, A, B, i0 + qi, j0 + qj, n, n);
-            else
-                undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
-            return;
-        }
-        if (MODE != MODE_FAST) {
-            has3 = has3 && admit<MODE>(d, slot, row, n);
-            hasq = hasq && admit<MODE>(d, d.g.n_slots + iK, row, n);
-            if (!has3 && !hasq) return;
-        }
-        const long long at = (long long)slot * d.g.q3 + bin;
-        double wq;
-        if (PREC == 1) {
-            float2 a[8], b[8];
+    // the q_inv form's stages exist only in its instantiation: a lambda that
+    // captures the queue counters by reference, even unused, would take
+    // their addresses and push them to local memory in the other forms
+    if constexpr (QINV) {
+        // stage C with q_inv histograms, for 32 screened pairs: the 3-D event
+        // and the q_inv event of each pair (cos(q.dx) computed once for both)
+        auto values_q = [&](uint4 e4, bool valid) {
+            // this lane's q_inv event, added per group of lanes at the end
+            unsigned qkey = 0xffffffffu;
+            double qsum = 0.0, qw = 0.0;
+            const unsigned e = e4.x;
+            const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+            const bool swap = (e >> 16) & 1u;
+            bool has3 = valid && ((e >> 18) & 1u), hasq = valid && ((e >> 19) & 1u);
+            const int bin = (int)e4.y, slot = (int)(e4.z & 0xffffu), iK = (int)(e4.z >> 16);
+            const int kq = (int)e4.w;
+            double A[8], B[8];  // first and second particle of the pair
 #pragma unroll
             for (int f = 0; f < 8; f++) {
-                a[f] = spi[f][qi];
-                b[f] = spj[f][qj];
+                const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+                const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+                A[f] = swap ? v : u;
+                B[f] = swap ? u : v;
             }
-            float4 v = values32_split<BOOST>(d.s, a, b);
-            if (swap) {
-                v.x = -v.x;
-                v.y = -v.y;
-                v.z = -v.z;
+            const long long oa = sm.oi[qi], ob = sm.oj[qj];
+            const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
+            if (valid && ((e >> 17) & 1u)) {
+                // undecided: the reference chain decides both events
+                if (MODE == MODE_FAST)
+                    undecided_pair_ordered<false, MODE_FAST>(d, A, B, i0 + qi, j0 + qj, n, n);
+                else
+                    undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
+                has3 = hasq = false;
             }
-            if (has3) {
-                atomicAdd(d.part + at, v);
-                atomicAdd(d.h.cnt + at, 1ull);
+            if (MODE != MODE_FAST) {
+                has3 = has3 && admit<MODE>(d, slot, row, n);
+                hasq = hasq && admit<MODE>(d, d.g.n_slots + iK, row, n);
             }
-            wq = v.w;
-        } else {
-            double vo, vs, vl;
-            if (PREC == 0) {
-                values64<BOOST>(d.g, cs, A, B, vo, vs, vl, wq);
-            } else {
+            if (has3 || hasq) {
+                const long long at = (long long)slot * d.g.q3 + bin;
+                double wq;
+                if (PREC == 1) {
+                    float2 a[8], b[8];
+#pragma unroll
+                    for (int f = 0; f < 8; f++) {
+                        a[f] = spi[f][qi];
+                        b[f] = spj[f][qj];
+                    }
+                    float4 v = values32_split<BOOST>(d.s, a, b);
+                    if (swap) {
+                        v.x = -v.x;
+                        v.y = -v.y;
+                        v.z = -v.z;
+                    }
+                    if (has3) {
+                        atomicAdd(d.part + at, v);
+                        atomicAdd(d.h.cnt + at, 1ull);
+                    }
+                    wq = v.w;
+                } else {
+                    double vo, vs, vl;
+                    if (PREC == 0) {
+                        values64<BOOST>(d.g, cs, A, B, vo, vs, vl, wq);
+                    } else {
+                        float2 a[8], b[8];
+#pragma unroll
+                        for (int f = 0; f < 8; f++) {
+                            a[f] = spi[f][qi];
+                            b[f] = spj[f][qj];
+                        }
+                        values_df<BOOST>(d.s, reinterpret_cast<const float4 *>(cs), a, b,
+                                         sm.offi, sm.offj, swap, vo, vs, vl, wq);
+                    }
+                    if (has3) {
+                        Sums *h = d.h.sums + at;
+                        atomicAdd(&h->qo, vo);
+                        atomicAdd(&h->qs, vs);
+                        atomicAdd(&h->ql, vl);
+                        atomicAdd(&h->w, wq);
+                        atomicAdd(d.h.cnt + at, 1ull);
+                    }
+                }
+                if (hasq) {
+                    // the reference's q_inv expression (FP64, same order, no
+                    // contraction): the summed value equals the oracle's
+                    const double q_x = A[0] - B[0], q_y = A[1] - B[1], q_z = A[2] - B[2];
+                    const double q_E = A[3] - B[3];
+                    qsum = sqrt(-(q_E * q_E - q_x * q_x - q_y * q_y - q_z * q_z));
+                    qw = wq;
+                    qkey = (unsigned)(iK * d.g.qnpts + kq);
+                }
+            }
+            qinv_update(d, qkey, qsum, qw, true);
+        };
+
+        // stage B with q_inv histograms: the K_T window and bin, the 3-D
+        // windows and bins, and the q_inv window and bin of each pair; a pair
+        // with any of them undecided goes to the reference chain as a whole
+        auto screen_q = [&](unsigned e, bool valid) {
+            const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+            const bool swap = (e >> 16) & 1u;
+            const float4 fa = swap ? sm.fj[qj] : sm.fi[qi], fb = swap ? sm.fi[qi] : sm.fj[qj];
+            Q s;
+            int c3 = 0, cq = 0, iK = -1, bin = 0, slot = -1, kq = 0;
+            bool und = false;
+            if (valid) {
+                const int kt = screen_kt(S, fa, fb, s);
+                if (kt != 0) {
+                    c3 = screen_lcms<BOOST>(S, fa, fb, s);
+                    cq = qinv_class(S, fa, fb, kq);
+                    if (c3 == 1 || cq == 1) {
+                        iK = kt == 1 ? kt_index(S, s) : -1;
+                        und = iK < 0;
+                    }
+                    if (c3 == 1 && !und) {
+                        int iK2 = 0;
+                        if (decide_bins(S, s, iK2, bin)) {
+                            slot = iK2;
+                            if (AZ) {
+                                const int ip = kphi_screen(S, s);
+                                slot = ip < 0 ? -1 : iK2 * d.g.n_Kphi + ip;
+                            }
+                        }
+                        und = slot < 0;
+                    }
+                    und = und || c3 == 2 || cq == 2;
+                }
+            }
+            const bool take = valid && (und || c3 == 1 || cq == 1);
+            const unsigned x = e | (und ? 1u << 17 : 0u) | (!und && c3 == 1 ? 1u << 18 : 0u) |
+                               (!und && cq == 1 ? 1u << 19 : 0u);
+            const uint4 ent = make_uint4(x, (unsigned)bin,
+                                         (unsigned)(slot < 0 ? 0 : slot) |
+                                             ((unsigned)(iK < 0 ? 0 : iK) << 16),
+                                         (unsigned)kq);
+            enqueue(q2, count2, take, ent, lane, values_q);
+        };
+
+        for (int jj = 0; jj < jend; jj++) {
+            const long long j = j0 + jj;
+            const bool swap = oa > sm.oj[jj];
+            const bool take = i < n && j > i &&
+                              (prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]) ||
+                               prefilter_qinv(S, a, sm.fj[jj]));
+            enqueue(q, count, take,
+                    (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16), lane,
+                    screen_q);
+        }
+        drain(q, count, lane, screen_q);
+        drain(q2, count2, lane, values_q);
+    } else {
+        // stage C for 32 screened pairs (all lanes of the warp in step)
+        auto values = [&](uint2 e2, bool valid) {
+            if (!valid) return;
+            const unsigned e = e2.x;
+            const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+            const bool swap = (e >> 16) & 1u;
+            const int slot = (e >> 17) & 1u ? -1 : (int)(e >> 18);
+            const int bin = (int)e2.y;
+            if (MODE != MODE_FAST) {
+                const long long oa = sm.oi[qi], ob = sm.oj[qj];
+                const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
+                if (slot < 0) {
+                    double A[8], B[8];
+#pragma unroll
+                    for (int f = 0; f < 8; f++) {
+                        const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+                        const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+                        A[f] = swap ? v : u;
+                        B[f] = swap ? u : v;
+                    }
+                    undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
+                    return;
+                }
+                if (!admit<MODE>(d, slot, row, n)) return;
+            }
+            if (PREC == 1 && slot >= 0) {
+                // the pair as stored (i, j); swapping first and second negates
+                // q_out, q_side, q_long exactly and leaves the phase unchanged
                 float2 a[8], b[8];
 #pragma unroll
                 for (int f = 0; f < 8; f++) {
                     a[f] = spi[f][qi];
                     b[f] = spj[f][qj];
                 }
-                values_df<BOOST>(d.s, reinterpret_cast<const float4 *>(cs), a, b, sm.offi,
-                                 sm.offj, swap, vo, vs, vl, wq);
+                float4 v = values32_split<BOOST>(d.s, a, b);
+                if (swap) {
+                    v.x = -v.x;
+                    v.y = -v.y;
+                    v.z = -v.z;
+                }
+                const long long at = (long long)slot * d.g.q3 + bin;
+                atomicAdd(d.part + at, v);
+                atomicAdd(d.h.cnt + at, 1ull);
+                return;
             }
-            if (has3) {
+            if (PREC == 2 && slot >= 0) {
+                float2 a[8], b[8];
+#pragma unroll
+                for (int f = 0; f < 8; f++) {
+                    a[f] = spi[f][qi];
+                    b[f] = spj[f][qj];
+                }
+                double vo, vs, vl, vw;
+                values_df<BOOST>(d.s, reinterpret_cast<const float4 *>(cs), a, b, sm.offi, sm.offj,
+                                 swap, vo, vs, vl, vw);
+                const long long at = (long long)slot * d.g.q3 + bin;
                 Sums *h = d.h.sums + at;
                 atomicAdd(&h->qo, vo);
                 atomicAdd(&h->qs, vs);
                 atomicAdd(&h->ql, vl);
-                atomicAdd(&h->w, wq);
+                atomicAdd(&h->w, vw);
                 atomicAdd(d.h.cnt + at, 1ull);
-            }
-        }
-        if (hasq) {
-            // the reference's q_inv expression (FP64, same order, no
-            // contraction): the summed value equals the oracle's exactly
-            const double q_x = A[0] - B[0], q_y = A[1] - B[1], q_z = A[2] - B[2];
-            const double q_E = A[3] - B[3];
-            const double qinv = sqrt(-(q_E * q_E - q_x * q_x - q_y * q_y - q_z * q_z));
-            const int aq = iK * d.g.qnpts + kq;
-            atomicAdd(&d.h.qi_sums[aq].q, qinv);
-            atomicAdd(&d.h.qi_sums[aq].w, wq);
-            atomicAdd(d.h.qi_cnt + aq, 1ull);
-        }
-    };
-
-    // stage B with q_inv histograms: the K_T window and bin, the 3-D
-    // windows and bins, and the q_inv window and bin of each pair; a pair
-    // with any of them undecided goes to the reference chain as a whole
-    auto screen_q = [&](unsigned e, bool valid) {
-        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
-        const bool swap = (e >> 16) & 1u;
-        const float4 fa = swap ? sm.fj[qj] : sm.fi[qi], fb = swap ? sm.fi[qi] : sm.fj[qj];
-        Q s;
-        int c3 = 0, cq = 0, iK = -1, bin = 0, slot = -1, kq = 0;
-        bool und = false;
-        if (valid) {
-            const int kt = screen_kt(S, fa, fb, s);
-            if (kt != 0) {
-                c3 = screen_lcms<BOOST>(S, fa, fb, s);
-                cq = qinv_class(S, fa, fb, kq);
-                if (c3 == 1 || cq == 1) {
-                    iK = kt == 1 ? kt_index(S, s) : -1;
-                    und = iK < 0;
-                }
-                if (c3 == 1 && !und) {
-                    int iK2 = 0;
-                    if (decide_bins(S, s, iK2, bin)) {
-                        slot = iK2;
-                        if (AZ) {
-                            const int ip = kphi_screen(S, s);
-                            slot = ip < 0 ? -1 : iK2 * d.g.n_Kphi + ip;
-                        }
-                    }
-                    und = slot < 0;
-                }
-                und = und || c3 == 2 || cq == 2;
-            }
-        }
-        const bool take = valid && (und || c3 == 1 || cq == 1);
-        const unsigned x = e | (und ? 1u << 17 : 0u) | (!und && c3 == 1 ? 1u << 18 : 0u) |
-                           (!und && cq == 1 ? 1u << 19 : 0u);
-        const uint4 ent = make_uint4(x, (unsigned)bin,
-                                     (unsigned)(slot < 0 ? 0 : slot) |
-                                         ((unsigned)(iK < 0 ? 0 : iK) << 16),
-                                     (unsigned)kq);
-        if constexpr (QINV) enqueue(q2, count2, take, ent, lane, values_q);
-    };
-
-    // stage C for 32 screened pairs (all lanes of the warp in step)
-    auto values = [&](uint2 e2, bool valid) {
-        if (!valid) return;
-        const unsigned e = e2.x;
-        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
-        const bool swap = (e >> 16) & 1u;
-        const int slot = (e >> 17) & 1u ? -1 : (int)(e >> 18);
-        const int bin = (int)e2.y;
-        if (MODE != MODE_FAST) {
-            const long long oa = sm.oi[qi], ob = sm.oj[qj];
-            const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
-            if (slot < 0) {
-                double A[8], B[8];
-#pragma unroll
-                for (int f = 0; f < 8; f++) {
-                    const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
-                    const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
-                    A[f] = swap ? v : u;
-                    B[f] = swap ? u : v;
-                }
-                undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
                 return;
             }
-            if (!admit<MODE>(d, slot, row, n)) return;
-        }
-        if (PREC == 1 && slot >= 0) {
-            // the pair as stored (i, j); swapping first and second negates
-            // q_out, q_side, q_long exactly and leaves the phase unchanged
-            float2 a[8], b[8];
+            // FP64 form, or a pair the window screen left undecided: the pair in
+            // the reference's orientation, from the FP64 tile or (FP32-weight
+            // form) the FP64 columns themselves
+            double A[8], B[8];  // first and second particle of the pair
 #pragma unroll
             for (int f = 0; f < 8; f++) {
-                a[f] = spi[f][qi];
-                b[f] = spj[f][qj];
+                const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+                const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+                A[f] = swap ? v : u;
+                B[f] = swap ? u : v;
             }
-            float4 v = values32_split<BOOST>(d.s, a, b);
-            if (swap) {
-                v.x = -v.x;
-                v.y = -v.y;
-                v.z = -v.z;
-            }
-            const long long at = (long long)slot * d.g.q3 + bin;
-            atomicAdd(d.part + at, v);
-            atomicAdd(d.h.cnt + at, 1ull);
-            return;
-        }
-        if (PREC == 2 && slot >= 0) {
-            float2 a[8], b[8];
-#pragma unroll
-            for (int f = 0; f < 8; f++) {
-                a[f] = spi[f][qi];
-                b[f] = spj[f][qj];
-            }
-            double vo, vs, vl, vw;
-            values_df<BOOST>(d.s, reinterpret_cast<const float4 *>(cs), a, b, sm.offi, sm.offj,
-                             swap, vo, vs, vl, vw);
-            const long long at = (long long)slot * d.g.q3 + bin;
-            Sums *h = d.h.sums + at;
-            atomicAdd(&h->qo, vo);
-            atomicAdd(&h->qs, vs);
-            atomicAdd(&h->ql, vl);
-            atomicAdd(&h->w, vw);
-            atomicAdd(d.h.cnt + at, 1ull);
-            return;
-        }
-        // FP64 form, or a pair the window screen left undecided: the pair in
-        // the reference's orientation, from the FP64 tile or (FP32-weight
-        // form) the FP64 columns themselves
-        double A[8], B[8];  // first and second particle of the pair
-#pragma unroll
-        for (int f = 0; f < 8; f++) {
-            const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
-            const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
-            A[f] = swap ? v : u;
-            B[f] = swap ? u : v;
-        }
-        if (PREC == 0 && slot >= 0) {
-            double vo, vs, vl, vw;
-            values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
-            const long long at = (long long)slot * d.g.q3 + bin;
-            Sums *h = d.h.sums + at;
-            atomicAdd(&h->qo, vo);
-            atomicAdd(&h->qs, vs);
-            atomicAdd(&h->ql, vl);
-            atomicAdd(&h->w, vw);
-            atomicAdd(d.h.cnt + at, 1ull);
-            return;
-        }
-        if (PREC == 1) {
-            undecided_pair32<BOOST>(d, A, B, i0 + qi, j0 + qj, n);
-            return;
-        }
-        if (PREC == 2) {
-            undecided_pair64(d, A, B, i0 + qi, j0 + qj, n);
-            return;
-        }
-        {
-            // undecided somewhere: the reference chain decides (and may hand
-            // a K_phi edge to the host)
-            const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2],
-                                                 B[3], A + 4, B + 4);
-            if (PREC != 1 || full.ev3 != 1) {
-                consume<false, MODE_FAST>(d, i0 + qi, j0 + qj, n, n, full);
-            } else {
-                const long long at = (long long)full.slot * d.g.q3 + full.bin;
-                atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
+            if (PREC == 0 && slot >= 0) {
+                double vo, vs, vl, vw;
+                values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
+                const long long at = (long long)slot * d.g.q3 + bin;
+                Sums *h = d.h.sums + at;
+                atomicAdd(&h->qo, vo);
+                atomicAdd(&h->qs, vs);
+                atomicAdd(&h->ql, vl);
+                atomicAdd(&h->w, vw);
                 atomicAdd(d.h.cnt + at, 1ull);
+                return;
             }
-        }
-    };
-
-    // stage B for 32 prefiltered pairs: window screen and bins; the pairs
-    // inside the window (or undecided) go to the second queue
-    auto screen = [&](unsigned e, bool valid) {
-        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
-        const bool swap = (e >> 16) & 1u;
-        Q s;
-        int wcls = 0;
-        if (valid)
-            wcls = swap ? screen_windows<BOOST>(S, sm.fj[qj], sm.fi[qi], s)
-                        : screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
-        int iK = 0, bin = 0, slot = -1;
-        if (wcls == 1 && decide_bins(S, s, iK, bin)) {
-            slot = iK;
-            if (AZ) {
-                const int ip = kphi_screen(S, s);
-                slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
+            if (PREC == 1) {
+                undecided_pair32<BOOST>(d, A, B, i0 + qi, j0 + qj, n);
+                return;
             }
-        }
-        if constexpr (!QINV)
-            enqueue(q2, count2, wcls != 0, bin_entry(e, slot < 0, slot < 0 ? 0 : slot, bin),
-                    lane, values);
-    };
+            if (PREC == 2) {
+                undecided_pair64(d, A, B, i0 + qi, j0 + qj, n);
+                return;
+            }
+            {
+                // undecided somewhere: the reference chain decides (and may hand
+                // a K_phi edge to the host)
+                const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2],
+                                                     B[3], A + 4, B + 4);
+                if (PREC != 1 || full.ev3 != 1) {
+                    consume<false, MODE_FAST>(d, i0 + qi, j0 + qj, n, n, full);
+                } else {
+                    const long long at = (long long)full.slot * d.g.q3 + full.bin;
+                    atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
+                    atomicAdd(d.h.cnt + at, 1ull);
+                }
+            }
+        };
 
-    for (int jj = 0; jj < jend; jj++) {
-        const long long j = j0 + jj;
-        const bool swap = oa > sm.oj[jj];
-        bool take = i < n && j > i && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
-        if (QINV) take = take || (i < n && j > i && prefilter_qinv(S, a, sm.fj[jj]));
-        const unsigned e = (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16);
-        if constexpr (QINV)
-            enqueue(q, count, take, e, lane, screen_q);
-        else
-            enqueue(q, count, take, e, lane, screen);
-    }
-    if constexpr (QINV) {
-        drain(q, count, lane, screen_q);
-        drain(q2, count2, lane, values_q);
-    } else {
+        // stage B for 32 prefiltered pairs: window screen and bins; the pairs
+        // inside the window (or undecided) go to the second queue
+        auto screen = [&](unsigned e, bool valid) {
+            const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+            const bool swap = (e >> 16) & 1u;
+            Q s;
+            int wcls = 0;
+            if (valid)
+                wcls = swap ? screen_windows<BOOST>(S, sm.fj[qj], sm.fi[qi], s)
+                            : screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+            int iK = 0, bin = 0, slot = -1;
+            if (wcls == 1 && decide_bins(S, s, iK, bin)) {
+                slot = iK;
+                if (AZ) {
+                    const int ip = kphi_screen(S, s);
+                    slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
+                }
+            }
+            enqueue(q2, count2, wcls != 0, bin_entry(e, slot < 0, slot < 0 ? 0 : slot, bin), lane,
+                    values);
+        };
+
+        for (int jj = 0; jj < jend; jj++) {
+            const long long j = j0 + jj;
+            const bool swap = oa > sm.oj[jj];
+            const bool take = i < n && j > i && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
+            enqueue(q, count, take,
+                    (unsigned)il | ((unsigned)jj << 8) | ((swap ? 1u : 0u) << 16), lane, screen);
+        }
         drain(q, count, lane, screen);
         drain(q2, count2, lane, values);
     }
@@ -1176,69 +1275,74 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
         }
     };
 
-    // with q_inv histograms: the 3-D and the q_inv denominator events
-    auto process_q = [&](unsigned e, bool valid) {
-        if (!valid) return;
-        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
-        Q s;
-        const int kt = screen_kt(S, sm.fi[qi], sm.fj[qj], s);
-        if (kt == 0) return;
-        const int c3 = screen_lcms<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
-        int kq = 0, iK = -1, bin = 0, slot = -1;
-        const int cq = qinv_class(S, sm.fi[qi], sm.fj[qj], kq);
-        bool und = false;
-        if (c3 == 1 || cq == 1) {
-            iK = kt == 1 ? kt_index(S, s) : -1;
-            und = iK < 0;
-        }
-        if (c3 == 1 && !und) {
-            int iK2 = 0;
-            if (decide_bins(S, s, iK2, bin)) {
-                slot = iK2;
-                if (AZ) {
-                    const int ip = kphi_screen(S, s);
-                    slot = ip < 0 ? -1 : iK2 * d.g.n_Kphi + ip;
+    if constexpr (QINV) {
+        // with q_inv histograms: the 3-D and the q_inv denominator events
+        auto process_q = [&](unsigned e, bool valid) {
+            const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+            unsigned qkey = 0xffffffffu;  // this lane's q_inv denominator bin
+            if (valid) {
+                Q s;
+                const int kt = screen_kt(S, sm.fi[qi], sm.fj[qj], s);
+                int c3 = 0, cq = 0, kq = 0, iK = -1, bin = 0, slot = -1;
+                if (kt != 0) {
+                    c3 = screen_lcms<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
+                    cq = qinv_class(S, sm.fi[qi], sm.fj[qj], kq);
+                }
+                bool und = false;
+                if (c3 == 1 || cq == 1) {
+                    iK = kt == 1 ? kt_index(S, s) : -1;
+                    und = iK < 0;
+                }
+                if (c3 == 1 && !und) {
+                    int iK2 = 0;
+                    if (decide_bins(S, s, iK2, bin)) {
+                        slot = iK2;
+                        if (AZ) {
+                            const int ip = kphi_screen(S, s);
+                            slot = ip < 0 ? -1 : iK2 * d.g.n_Kphi + ip;
+                        }
+                    }
+                    und = slot < 0;
+                }
+                und = und || c3 == 2 || cq == 2;
+                const long long row = orig1 ? (long long)orig1[i0 + qi] : i0 + qi;
+                const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
+                if (und) {
+                    if (MODE == MODE_FAST) {
+                        undecided_mixed_pair(d, l1, l2, i0 + qi, j0 + qj, n1, n2);
+                    } else {
+                        const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi],
+                                             l1[3][i0 + qi]};
+                        const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
+                                             l2[3][j0 + qj]};
+                        undecided_pair_ordered<true, MODE>(d, A, B, row, col, n1, n2);
+                    }
+                } else {
+                    bool h3 = c3 == 1, hq = cq == 1;
+                    if (MODE != MODE_FAST) {
+                        h3 = h3 && admit<MODE>(d, slot, row, n1);
+                        hq = hq && admit<MODE>(d, d.g.n_slots + iK, row, n1);
+                    }
+                    if (h3) atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
+                    if (hq) qkey = (unsigned)(iK * d.g.qnpts + kq);
                 }
             }
-            und = slot < 0;
-        }
-        und = und || c3 == 2 || cq == 2;
-        if (!und && c3 != 1 && cq != 1) return;
-        const long long row = orig1 ? (long long)orig1[i0 + qi] : i0 + qi;
-        const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
-        if (und) {
-            if (MODE == MODE_FAST) {
-                undecided_mixed_pair(d, l1, l2, i0 + qi, j0 + qj, n1, n2);
-            } else {
-                const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi],
-                                     l1[3][i0 + qi]};
-                const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
-                                     l2[3][j0 + qj]};
-                undecided_pair_ordered<true, MODE>(d, A, B, row, col, n1, n2);
-            }
-            return;
-        }
-        bool h3 = c3 == 1, hq = cq == 1;
-        if (MODE != MODE_FAST) {
-            h3 = h3 && admit<MODE>(d, slot, row, n1);
-            hq = hq && admit<MODE>(d, d.g.n_slots + iK, row, n1);
-        }
-        if (h3) atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
-        if (hq) atomicAdd(d.h.qi_den + iK * d.g.qnpts + kq, 1ull);
-    };
+            qinv_update(d, qkey, 0.0, 0.0, false);
+        };
 
-    for (int jj = 0; jj < jend; jj++) {
-        bool take = active && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
-        if (QINV) take = take || (active && prefilter_qinv(S, a, sm.fj[jj]));
-        if constexpr (QINV)
+        for (int jj = 0; jj < jend; jj++) {
+            const bool take = active && (prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]) ||
+                                         prefilter_qinv(S, a, sm.fj[jj]));
             enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process_q);
-        else
-            enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process);
-    }
-    if constexpr (QINV)
+        }
         drain(q, count, lane, process_q);
-    else
+    } else {
+        for (int jj = 0; jj < jend; jj++) {
+            const bool take = active && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
+            enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process);
+        }
         drain(q, count, lane, process);
+    }
 }
 
 }  // namespace tile

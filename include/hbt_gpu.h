@@ -67,9 +67,12 @@ typedef struct hbt_params {
     int32_t long_comoving_boost;    /* "long_comoving_boost" */
     double needed_number_of_pairs;  /* "needed_number_of_pairs" (pair cap) */
     int32_t precision;              /* hbt_precision */
-    /* Half-width (rad) of the zone around a K_phi bin edge inside which a
-     * pair's azimuthal bin is decided on the host with the C library's
-     * atan2 instead of the device's; 0 selects the default (1e-13). */
+    /* Half-width (rad) of the zone around a K_phi bin edge inside which the
+     * reference chain (the plain kernel, and pairs the screened kernels'
+     * FP32 test cannot decide) hands a pair's azimuthal bin to the host's
+     * C-library atan2 instead of the device's; 0 selects the default
+     * (1e-13).  The screened kernels decide the other pairs' bins in FP32
+     * with an error bound. */
     double kphi_defer_tol;
     int32_t kernel; /* hbt_kernel */
 } hbt_params;
