@@ -66,8 +66,14 @@ struct hbt_ctx {
     hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0, 0};
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
-    // input staging
-    DevBuf in;
+    // input staging, two buffers in turn: the host-to-device copy of a call
+    // runs on `copy_in` while the binning of the previous call still reads
+    // the other buffer (in_free: recorded on `stream` after that binning)
+    DevBuf in[2];
+    int in_next = 0, in_cur = -1;
+    bool in_used[2] = {false, false};
+    cudaStream_t copy_in = nullptr;
+    cudaEvent_t in_free[2] = {nullptr, nullptr};
     // readback: two FP64 arrays of the histogram size, used in turn
     DevBuf exp;
     // overlapped readback (hbt_read_hist_async): a snapshot of the six
@@ -512,13 +518,26 @@ hbt_status bin_mixed_device(hbt_ctx *c, long long n1, const double *const *l1, l
     return HBT_OK;
 }
 
-// Copies host columns into the staging buffer; returns device pointers.
+// Copies host columns into a staging buffer; returns device pointers.  The
+// copies run on the context's copy stream into the buffer the previous call
+// did not use, so they overlap that call's binning; the call returns once
+// the copies are done (the caller may then reuse its arrays).  Serving
+// contexts, whose memory comes stream-ordered from a pool, copy on their
+// own stream.
 hbt_status stage(hbt_ctx *c, const double *const *src, const long long *len, int ncols,
                  const double **dst) {
+    if (!c->copy_in && !c->pool) {
+        CU(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking));
+        for (cudaEvent_t &e : c->in_free) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    cudaStream_t cs = c->pool ? c->stream : c->copy_in;
+    const int buf = c->pool ? 0 : c->in_next;
     size_t total = 0;
     for (int f = 0; f < ncols; f++) total += (size_t)((len[f] + 31) / 32 * 32);
-    TRY(dalloc(c, c->in, total * sizeof(double)));
-    double *base = ptr<double>(c->in);
+    TRY(dalloc(c, c->in[buf], total * sizeof(double)));
+    double *base = ptr<double>(c->in[buf]);
+    // the binning that read this buffer last must be done with it
+    if (!c->pool && c->in_used[buf]) CU(cudaStreamWaitEvent(cs, c->in_free[buf], 0));
     size_t off = 0;
     for (int f = 0; f < ncols; f++) {
         dst[f] = base + off;
@@ -538,13 +557,32 @@ hbt_status stage(hbt_ctx *c, const double *const *src, const long long *len, int
             g++;
         const size_t n = (size_t)(dst[g] - dst[f]) + (size_t)len[g];
         CU(cudaMemcpyAsync(const_cast<double *>(dst[f]), src[f], n * sizeof(double),
-                           cudaMemcpyHostToDevice, c->stream));
+                           cudaMemcpyHostToDevice, cs));
         f = g + 1;
     }
-    // the caller's arrays may be reused once the copies are done
-    CU(cudaEventRecord(c->staged, c->stream));
+    // the caller's arrays may be reused once the copies are done; the
+    // binning stream starts after them
+    CU(cudaEventRecord(c->staged, cs));
     CU(cudaEventSynchronize(c->staged));
+    if (cs != c->stream) CU(cudaStreamWaitEvent(c->stream, c->staged, 0));
+    if (!c->pool) {
+        c->in_cur = buf;
+        c->in_next ^= 1;
+    }
     return HBT_OK;
+}
+
+// After the binning of the staged lists is queued on the context's stream:
+// the staging buffer is free once that work is done.
+hbt_status staged_done(hbt_ctx *c, hbt_status s) {
+    if (c->in_cur >= 0) {
+        const cudaError_t e = cudaEventRecord(c->in_free[c->in_cur], c->stream);
+        c->in_used[c->in_cur] = e == cudaSuccess;
+        c->in_cur = -1;
+        if (e != cudaSuccess && s == HBT_OK)
+            return fail(c, HBT_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+    }
+    return s;
 }
 
 }  // namespace
@@ -693,7 +731,7 @@ void hbt_destroy(hbt_ctx *c) {
     DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
-                      &c->apply_iphi, &c->in, &c->part, &c->comp, &c->exp};
+                      &c->apply_iphi, &c->in[0], &c->in[1], &c->part, &c->comp, &c->exp};
     if (c->copy) cudaStreamSynchronize(c->copy);
     for (DevBuf *b : bufs) dfree(c, *b);
     dfree(c, c->snap);
@@ -702,6 +740,10 @@ void hbt_destroy(hbt_ctx *c) {
     if (c->copy) cudaStreamDestroy(c->copy);
     if (c->flag_host) cudaFreeHost(c->flag_host);
     if (c->staged) cudaEventDestroy(c->staged);
+    if (c->copy_in) cudaStreamSynchronize(c->copy_in);
+    for (cudaEvent_t e : c->in_free)
+        if (e) cudaEventDestroy(e);
+    if (c->copy_in) cudaStreamDestroy(c->copy_in);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
 }
@@ -767,7 +809,7 @@ hbt_status hbt_bin_same(hbt_ctx *c, int64_t n, const hbt_soa8 *l) {
     const long long len[8] = {n, n, n, n, n, n, n, n};
     const double *dv[8];
     TRY(stage(c, src, len, 8, dv));
-    return bin_same_device(c, n, dv);
+    return staged_done(c, bin_same_device(c, n, dv));
 }
 
 hbt_status hbt_bin_mixed(hbt_ctx *c, int64_t n1, const hbt_soa4 *a, int64_t n2,
@@ -779,7 +821,7 @@ hbt_status hbt_bin_mixed(hbt_ctx *c, int64_t n1, const hbt_soa4 *a, int64_t n2,
     const long long len[8] = {n1, n1, n1, n1, n2, n2, n2, n2};
     const double *dv[8];
     TRY(stage(c, src, len, 8, dv));
-    return bin_mixed_device(c, n1, dv, n2, dv + 4);
+    return staged_done(c, bin_mixed_device(c, n1, dv, n2, dv + 4));
 }
 
 hbt_status hbt_bin_batch_dev(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs) {
@@ -859,7 +901,7 @@ hbt_status hbt_bin_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs) {
             for (int q = 0; q < 4; q++) *b[q] = dv[at++];
         }
     }
-    return hbt_bin_batch_dev(c, n_jobs, dj.data());
+    return staged_done(c, hbt_bin_batch_dev(c, n_jobs, dj.data()));
 }
 
 hbt_status hbt_set_tuning(hbt_ctx *c, const hbt_tuning *t) {
