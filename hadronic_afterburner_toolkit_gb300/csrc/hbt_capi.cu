@@ -6,6 +6,7 @@
 // bin edge with the C library's atan2 (as the reference does,
 // src/HBT_correlation.cpp:408-416).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -92,6 +93,15 @@ struct hbt_ctx {
     // allocation-failure injection (hbt_inject_alloc_failure): allocations
     // left to succeed before one fails; -1 = off
     int fail_after = -1;
+    // stream-ordered K_phi deferral drain (drain_deferrals_async): pinned
+    // copies of the deferral count and records, the host-decided bins
+    // ([0] = records to apply, [4 + k] = bin of record k) and their device
+    // copy; pairs decided by queued host functions
+    unsigned *count_host = nullptr;
+    hbt::Deferral *defer_host = nullptr;
+    int *apply_host = nullptr;
+    DevBuf apply_dev;
+    std::atomic<unsigned long long> deferred_async{0};
 };
 
 namespace {
@@ -213,6 +223,51 @@ hbt_status drain_deferrals(hbt_ctx *c) {
     CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
     CU(cudaStreamSynchronize(c->stream));
     c->st.deferred_kphi += n;
+    c->st.launches++;
+    return HBT_OK;
+}
+
+// Host function queued on the context's stream by drain_deferrals_async:
+// decides the copied records' K_phi bins with the C library's atan2.  Makes
+// no CUDA call.  An overflowing buffer applies nothing (the kernels raised
+// the error flag, which the reads report).
+void CUDART_CB decide_deferrals(void *arg) {
+    hbt_ctx *c = static_cast<hbt_ctx *>(arg);
+    const unsigned n = *c->count_host;
+    const unsigned m = n > kDeferCap ? 0u : n;
+    for (unsigned k = 0; k < m; k++) {
+        const hbt::Deferral &r = c->defer_host[k];
+        c->apply_host[4 + k] = host_kphi(c->d.g, r.Kx, r.Ky, r.psi);
+    }
+    c->apply_host[0] = (int)m;
+    c->deferred_async += m;
+}
+
+// drain_deferrals without waiting: the count and records are copied to
+// pinned host memory, a host function decides the bins, and the apply
+// kernel runs after it, all in the context's stream order, so the caller
+// returns while the binning before it is still running.  Serving contexts
+// (memory from a pool) take the waiting path.
+hbt_status drain_deferrals_async(hbt_ctx *c) {
+    if (!c->prm.azimuthal_flag) return HBT_OK;
+    if (c->pool) return drain_deferrals(c);
+    if (!c->count_host) {
+        CU(cudaMallocHost(&c->count_host, sizeof(unsigned)));
+        CU(cudaMallocHost(&c->defer_host, kDeferCap * sizeof(hbt::Deferral)));
+        CU(cudaMallocHost(&c->apply_host, (4 + kDeferCap) * sizeof(int)));
+    }
+    TRY(dalloc(c, c->apply_dev, (4 + kDeferCap) * sizeof(int)));
+    CU(cudaMemcpyAsync(c->count_host, c->n_defer.p, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CU(cudaMemcpyAsync(c->defer_host, c->defer.p, kDeferCap * sizeof(hbt::Deferral),
+                       cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaLaunchHostFunc(c->stream, decide_deferrals, c));
+    CU(cudaMemcpyAsync(c->apply_dev.p, c->apply_host, (4 + kDeferCap) * sizeof(int),
+                       cudaMemcpyHostToDevice, c->stream));
+    const int *dev = ptr<int>(c->apply_dev);
+    CU(hbt::launch_apply_n(c->d, ptr<hbt::Deferral>(c->defer), dev + 4, dev, (int)kDeferCap,
+                           c->stream));
+    CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
     c->st.launches++;
     return HBT_OK;
 }
@@ -739,6 +794,10 @@ void hbt_destroy(hbt_ctx *c) {
     if (c->copy_ev) cudaEventDestroy(c->copy_ev);
     if (c->copy) cudaStreamDestroy(c->copy);
     if (c->flag_host) cudaFreeHost(c->flag_host);
+    if (c->count_host) cudaFreeHost(c->count_host);
+    if (c->defer_host) cudaFreeHost(c->defer_host);
+    if (c->apply_host) cudaFreeHost(c->apply_host);
+    dfree(c, c->apply_dev);
     if (c->staged) cudaEventDestroy(c->staged);
     if (c->copy_in) cudaStreamSynchronize(c->copy_in);
     for (cudaEvent_t e : c->in_free)
@@ -779,6 +838,7 @@ hbt_status hbt_reset(hbt_ctx *c) {
     CU(cudaStreamSynchronize(c->stream));
     for (int f = 0; f < 4; f++) c->ub[f] = 0;
     memset(&c->st, 0, sizeof(c->st));
+    c->deferred_async = 0;
     return HBT_OK;
 }
 
@@ -1080,7 +1140,7 @@ hbt_status hbt_read_hist_async(hbt_ctx *c, double *num_count, double *q_out_sum,
     if (!c) return HBT_ERR_INVALID;
     CU(cudaSetDevice(c->device));
     TRY(hbt_read_hist_wait(c));  // one read in flight: the snapshot is reused
-    TRY(drain_deferrals(c));
+    TRY(drain_deferrals_async(c));
     if (!c->copy) {
         CU(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
         CU(cudaEventCreateWithFlags(&c->snap_ev, cudaEventDisableTiming));
@@ -1166,6 +1226,7 @@ hbt_status hbt_get_stats(hbt_ctx *c, hbt_stats *out) {
     u64 stats[hbt::STAT_N];
     CU(cudaMemcpy(stats, c->stats.p, sizeof(stats), cudaMemcpyDeviceToHost));
     *out = c->st;
+    out->deferred_kphi += c->deferred_async;
     out->anomalies = stats[hbt::STAT_ANOMALY];
     long long cs = 0, cm = 0, ks = 0, km = 0;
     if (c->runner.tile_counts(cs, cm, ks, km)) {

@@ -152,6 +152,9 @@ cudaError_t launch_cut(const Device &d, long long rows, int n_stream,
 // Bins n deferred records with their host-resolved K_phi bins (iphi[k]).
 cudaError_t launch_apply(const Device &d, const Deferral *rec, const int *iphi, int n,
                          cudaStream_t st);
+// The same with the record count in device memory (*count <= cap).
+cudaError_t launch_apply_n(const Device &d, const Deferral *rec, const int *iphi, const int *count,
+                           int cap, cudaStream_t st);
 cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, int n_res,
                                cudaStream_t st);
 cudaError_t launch_counters(const Device &d, unsigned long long *out, cudaStream_t st);

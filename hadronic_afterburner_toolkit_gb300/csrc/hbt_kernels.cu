@@ -189,9 +189,8 @@ __global__ void __launch_bounds__(1024) k_cut(Device d, long long rows,
 }
 
 // Bins deferred records with their host-resolved K_phi bins (fast mode).
-__global__ void k_apply(Device d, const Deferral *rec, const int *iphi, int n) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+__device__ __forceinline__ void apply_one(const Device &d, const Deferral *rec, const int *iphi,
+                                          int k) {
     const int ip = iphi[k];
     if (ip < 0) return;
     const Deferral r = rec[k];
@@ -206,6 +205,18 @@ __global__ void k_apply(Device d, const Deferral *rec, const int *iphi, int n) {
         atomicAdd(&s->w, r.cosw);
         atomicAdd(d.h.cnt + at, 1ull);
     }
+}
+
+__global__ void k_apply(Device d, const Deferral *rec, const int *iphi, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) apply_one(d, rec, iphi, k);
+}
+
+// As k_apply, with the number of records read from device memory (decided
+// by a host function queued on the same stream).
+__global__ void k_apply_n(Device d, const Deferral *rec, const int *iphi, const int *count) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < *count) apply_one(d, rec, iphi, k);
 }
 
 // Adds host-resolved deferred pairs to the per-row survivor counts.
@@ -323,6 +334,12 @@ cudaError_t launch_apply(const Device &d, const Deferral *rec, const int *iphi, 
                          cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     k_apply<<<(n + 127) / 128, 128, 0, st>>>(d, rec, iphi, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_n(const Device &d, const Deferral *rec, const int *iphi, const int *count,
+                           int cap, cudaStream_t st) {
+    k_apply_n<<<(cap + 127) / 128, 128, 0, st>>>(d, rec, iphi, count);
     return cudaGetLastError();
 }
 

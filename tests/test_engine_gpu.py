@@ -402,3 +402,40 @@ def test_qinv_edge_pairs_bit_exact(kernel):
     h = orc.hist()
     assert h["qinv_count"].sum() > 1000 and h["qinv_den"].sum() > 1000
     parity.compare(eng.hist(), h, _qscale(p))
+
+
+def test_async_readback_applies_host_decided_kphi_edges():
+    """hbt_read_hist_async decides the deferred K_phi edges in the stream's
+    order (a host function queued after the binning) without waiting for the
+    binning: with a wide deferral zone on the reference chain, many pairs
+    take that path, and the snapshot equals the oracle's binning."""
+    from hadronic_afterburner_toolkit_gb300 import engine as E
+    p = dict(FULL, kphi_defer_tol=0.05, kernel=1)
+    eng, orc = _engine(**p), _oracle(**{k: v for k, v in p.items() if k != "kernel"})
+    for x in (eng, orc):
+        x.set_psi_ref(-0.2)
+    ev = parity.lists(seed=404)
+    c = parity.cols8(ev)
+    l1 = parity.rotated4(ev, 0.0, 0, ev.offsets[2])
+    l2 = parity.rotated4(ev, 1.3, ev.offsets[2], None)
+    for x in (eng, orc):
+        x.bin_same(c)
+        x.bin_mixed(l1, l2)
+    n = int(eng.L.hbt_n_bins(eng.handle))
+    snap = [np.full(n, -1.0) for _ in range(6)]
+    eng._check(eng.L.hbt_read_hist_async(eng.handle, *[a.ctypes.data_as(E._PD) for a in snap]))
+    eng._check(eng.L.hbt_read_hist_wait(eng.handle))
+    assert eng.stats()["deferred_kphi"] > 100
+    o = orc.hist()
+    got = dict(zip(("count", "q_out", "q_side", "q_long", "num", "den"), snap))
+    for k in ("count", "den"):
+        assert np.array_equal(got[k], o[k]), k
+    for k in ("q_out", "q_side", "q_long", "num"):
+        bound = parity.RTOL * np.maximum(o["count"], 1.0) * (1.0 if k == "num" else _qscale(p))
+        assert (np.abs(got[k] - o[k]) <= bound).all(), k
+    # a second read (nothing new deferred) leaves the histograms as they are
+    again = [np.zeros(n) for _ in range(6)]
+    eng._check(eng.L.hbt_read_hist_async(eng.handle, *[a.ctypes.data_as(E._PD) for a in again]))
+    eng._check(eng.L.hbt_read_hist_wait(eng.handle))
+    for a, b in zip(again, snap):
+        np.testing.assert_array_equal(a, b)
