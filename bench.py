@@ -73,8 +73,9 @@ STAGE_OPS_MIXED = tuple(sum(c[:4]) for c in STAGE_COUNTS_MIXED)
 # profiles/k_persistent_same_fp64_central.md.
 FP64_WARP_INST_PER_BINNED_PAIR = 3549259087 / 1942004247
 # DRAM bytes (read + write) of one k_persistent_same launch on a central
-# group, FP64 form: same capture.
-CENTRAL_SAME_DRAM_BYTES = 290474240 + 1157159424
+# group, FP64 form, same-event items in momentum-region order (the default
+# hbt_tuning.order_items): profiles/k_persistent_same_fp64_central.md.
+CENTRAL_SAME_DRAM_BYTES = 176657664 + 264997632
 
 
 def workload_params(name: str) -> dict:
@@ -1249,7 +1250,7 @@ def main() -> None:
                     help="skip the radii-fit leg")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the FP32-weight against FP64 error report")
-    ap.add_argument("--order-items", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--order-items", type=int, default=1, choices=[0, 1],
                     help="hbt_tuning.order_items of the timed engine: same-event tile pairs "
                          "in momentum-region order")
     ap.add_argument("--no-capped", action="store_true",

@@ -64,7 +64,7 @@ struct hbt_ctx {
     hbt::BatchRunner runner;
     int persistent_grid = 152 * 4;
     int sms = 152, max_blocks_per_sm = 5;
-    hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0, 0};
+    hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0, 1};
     // ordered admission scratch
     DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
     // input staging, two buffers in turn: the host-to-device copy of a call
@@ -1023,7 +1023,8 @@ hbt_status hbt_autotune_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs, d
     hbt_tuning cur = c->tune;
     double cur_ms = 0.0;
     hbt_status rs = time_one(cur, cur_ms);
-    // coordinate search: sort cells, then CTAs per SM, then the merge chunk
+    // coordinate search: sort cells, then CTAs per SM, then the item order,
+    // then the merge chunk
     const double cells[][2] = {{0.01, 0.025}, {0.02, 0.05}, {0.04, 0.1}, {0.02, 0.1}, {0.04, 0.05},
                                {0.01, 0.05}};
     for (const auto &cl : cells) {
@@ -1045,6 +1046,16 @@ hbt_status hbt_autotune_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs, d
         if (cand.blocks_per_sm == cur.blocks_per_sm) continue;
         double ms = 0.0;
         rs = time_one(cand, ms);
+        if (rs == HBT_OK && ms < cur_ms) {
+            cur = cand;
+            cur_ms = ms;
+        }
+    }
+    {
+        hbt_tuning cand = cur;
+        cand.order_items = cur.order_items ? 0 : 1;
+        double ms = 0.0;
+        if (rs == HBT_OK) rs = time_one(cand, ms);
         if (rs == HBT_OK && ms < cur_ms) {
             cur = cand;
             cur_ms = ms;

@@ -191,19 +191,20 @@ typedef struct hbt_tuning {
                                launches */
     int32_t time_kernels;   /* 1: time the persistent kernels with CUDA events
                                (hbt_stats.same_kernel_ms / mixed_kernel_ms) */
-    int32_t order_items;    /* 1: take the same-event tile pairs in the order of
-                               their momentum-space region (K_T and azimuth of
-                               the tiles' mean momentum), so that the CTAs
-                               running at any time update few histogram slots;
-                               0: in the order the cull found them */
+    int32_t order_items;    /* 1 (default): take the same-event tile pairs in the
+                               order of their momentum-space region (K_T and
+                               azimuth of the tiles' mean momentum), so that the
+                               CTAs running at any time update few histogram
+                               slots (on the central workload 3.3x less DRAM
+                               traffic); 0: in the order the cull found them */
 } hbt_tuning;
 
 hbt_status hbt_set_tuning(hbt_ctx *ctx, const hbt_tuning *t);
 hbt_status hbt_get_tuning(hbt_ctx *ctx, hbt_tuning *t);
 
 /* Autotuner.  No counterpart in the reference.  Times candidate tunings
- * (sort cells, CTAs per SM, merge chunk) on up to `max_pairs` candidate
- * pairs of the batch (device arrays, jobs taken in order; 0: 2e9) with
+ * (sort cells, CTAs per SM, item order, merge chunk) on up to `max_pairs`
+ * candidate pairs of the batch (device arrays, jobs taken in order; 0: 2e9) with
  * scratch histograms, keeps the fastest for this context and returns it
  * with its time.  The context's histograms are not touched. */
 hbt_status hbt_autotune_batch(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs,
