@@ -1488,11 +1488,26 @@ def main() -> None:
     e2e = None
     if not args.no_e2e:
         eng2 = E.Engine(device=local, precision=prec, kernel=kern, **p)
+        eng2.set_tuning(order_items=args.order_items)
+        # each group's columns packed in one pinned host array in the order
+        # the batch stages them, every column a multiple of 32 doubles (the
+        # layout the drop-in's HBT_correlation builds), so a step's inputs
+        # cross in one copy
         pin = []
         for cols, mixed in groups:
-            pc = [torch.from_numpy(c).pin_memory().numpy() for c in cols]
-            pm = [([torch.from_numpy(x).pin_memory().numpy() for x in l1],
-                   [torch.from_numpy(x).pin_memory().numpy() for x in l2]) for l1, l2 in mixed]
+            seq = list(cols) + [x for l1, l2 in mixed for x in list(l1) + list(l2)]
+            sizes = [(x.size + 31) // 32 * 32 for x in seq]
+            buf = torch.empty(sum(sizes), dtype=torch.float64).pin_memory().numpy()
+            views, at = [], 0
+            for x, sz in zip(seq, sizes):
+                buf[at:at + x.size] = x
+                views.append(buf[at:at + x.size])
+                at += sz
+            pc, k = views[:8], 8
+            pm = []
+            for l1, l2 in mixed:
+                pm.append((views[k:k + 4], views[k + 4:k + 8]))
+                k += 8
             pin.append((pc, pm))
         nb = eng2.L.hbt_n_bins(eng2.handle)
         # two pinned result sets: the histograms of step k copy to the host
