@@ -445,7 +445,10 @@ hbt::Tuning runner_tuning(const hbt_ctx *c, const hbt_tuning &t) {
     r.cell_y = t.cell_y;
     r.graph = t.use_graph != 0;
     r.time_kernels = t.time_kernels != 0;
-    r.order_items = t.order_items != 0;
+    // the FP32-weight form keeps the cull's order: in region order a merge
+    // chunk's pairs crowd into fewer bins and the FP32 partials' rounding
+    // reached 3e-6 per pair on the central workload, above the form's bound
+    r.order_items = t.order_items != 0 && c->d.precision != HBT_PRECISION_FP32W;
     return r;
 }
 

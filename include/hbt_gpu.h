@@ -196,7 +196,10 @@ typedef struct hbt_tuning {
                                azimuth of the tiles' mean momentum), so that the
                                CTAs running at any time update few histogram
                                slots (on the central workload 3.3x less DRAM
-                               traffic); 0: in the order the cull found them */
+                               traffic); 0: in the order the cull found them.
+                               The FP32-weight form always takes the cull's
+                               order (its FP32 partials' bound needs the pairs of
+                               a merge chunk spread over many bins) */
 } hbt_tuning;
 
 hbt_status hbt_set_tuning(hbt_ctx *ctx, const hbt_tuning *t);
