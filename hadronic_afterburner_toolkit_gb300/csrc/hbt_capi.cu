@@ -26,7 +26,6 @@ using hbt::u64;
 
 namespace {
 
-const double kHbarC = 0.197327053;  // GeV fm (src/parameters.h:4)
 const unsigned kDeferCap = 1u << 16;
 const u64 kInf = ~0ull;
 
@@ -670,7 +669,8 @@ void grid_from_params(const hbt_params &p, Grid &g) {
     g.two_pi = 2. * M_PI;
     g.psi_ref = 0.0;
     g.kphi_tol = p.kphi_defer_tol > 0 ? p.kphi_defer_tol : 1e-13;
-    g.hbarC_inv = 1. / kHbarC;
+    g.hbarC_inv = 1. / hbt::kHbarC;
+    g.cph = make_cos_scale(g.hbarC_inv);
 }
 
 void screen_from_grid(const Grid &g, Screen &s) {
@@ -1054,7 +1054,9 @@ hbt_status hbt_autotune_batch(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs, d
             cur_ms = ms;
         }
     }
-    {
+    if (c->d.precision == HBT_PRECISION_FP32W) {
+        cur.order_items = 0;  // the FP32-weight form always runs in the cull's order
+    } else {
         hbt_tuning cand = cur;
         cand.order_items = cur.order_items ? 0 : 1;
         double ms = 0.0;

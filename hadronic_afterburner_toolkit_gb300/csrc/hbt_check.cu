@@ -1,5 +1,6 @@
-// Device evaluation of the table-driven FP64 functions and of the
-// double-float cos of the pair kernels (include/hbt_check.h).
+// Device evaluation of the table-driven FP64 functions, the refined FP64
+// reciprocal square root and the double-float cos of the pair kernels
+// (include/hbt_check.h).
 #include "../../include/hbt_check.h"
 #include "hbt_math.cuh"
 #include "hbt_tile.cuh"
@@ -19,15 +20,26 @@ __global__ void k_check_dfcos(long long n, const double *x, double *out) {
     }
 }
 
-__global__ void k_check_math(int which, long long n, const double *x, double *out) {
+__global__ void k_check_math(int which, CosScale k, long long n, const double *x, double *out) {
     __shared__ double2 cs[COS_TABLE];
     __shared__ double et[EXP_TABLE];
     fill_cos_table(cs);
     fill_exp_table(et);
     __syncthreads();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        out[i] = which == HBT_CHECK_COS ? table_cos(cs, x[i]) : table_exp(et, x[i]);
+         i += (long long)gridDim.x * blockDim.x) {
+        double v;
+        if (which == HBT_CHECK_COS || which == HBT_CHECK_COS_PHASE) {
+            v = table_cos(cs, k, x[i]);
+        } else if (which == HBT_CHECK_RSQRT) {
+            v = rsqrt_refined(x[i]);
+        } else if (which == HBT_CHECK_RSQRT_START) {
+            asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(v) : "d"(x[i]));
+        } else {
+            v = table_exp(et, x[i]);
+        }
+        out[i] = v;
+    }
 }
 
 }  // namespace
@@ -35,7 +47,7 @@ __global__ void k_check_math(int which, long long n, const double *x, double *ou
 extern "C" hbt_status hbt_check_math(int device, int32_t which, int64_t n, const double *x,
                                      double *out) {
     if (n < 0 || (n > 0 && (!x || !out)) ||
-        (which != HBT_CHECK_COS && which != HBT_CHECK_EXP && which != HBT_CHECK_DFCOS))
+        which < HBT_CHECK_COS || which > HBT_CHECK_RSQRT_START)
         return HBT_ERR_INVALID;
     if (n == 0) return HBT_OK;
     if (cudaSetDevice(device) != cudaSuccess) return HBT_ERR_CUDA;
@@ -47,7 +59,9 @@ extern "C" hbt_status hbt_check_math(int device, int32_t which, int64_t n, const
         if (which == HBT_CHECK_DFCOS)
             k_check_dfcos<<<(unsigned)blocks, 256>>>(n, d, d + n);
         else
-            k_check_math<<<(unsigned)blocks, 256>>>(which, n, d, d + n);
+            k_check_math<<<(unsigned)blocks, 256>>>(
+                which, make_cos_scale(which == HBT_CHECK_COS_PHASE ? 1.0 / hbt::kHbarC : 1.0), n,
+                d, d + n);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, d + n, n * sizeof(double), cudaMemcpyDeviceToHost);

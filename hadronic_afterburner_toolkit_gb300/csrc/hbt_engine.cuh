@@ -5,9 +5,13 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "hbt_math.cuh"
+
 namespace hbt {
 
 typedef unsigned long long u64;
+
+constexpr double kHbarC = 0.197327053;  // GeV fm (src/parameters.h:4)
 
 // Histogram geometry and the constants the reference derives in its
 // constructor (src/HBT_correlation.cpp:25-61, :253, :289-290, :342-345),
@@ -20,6 +24,7 @@ struct Grid {
     double KT_min, dKT, KT_min_sq, KT_max_sq;
     double dKphi, two_pi, psi_ref, kphi_tol;
     double hbarC_inv;
+    CosScale cph;  // table_cos constants for cos(q.dx / hbarC)
 };
 
 // Per-bin numerator sums, one 32-byte L2 sector per bin.

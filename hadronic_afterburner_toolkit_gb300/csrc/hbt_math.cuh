@@ -5,6 +5,9 @@
 // (include/hbt_check.h, tests/test_math_gpu.py).
 #pragma once
 
+#include <cmath>
+#include <cstring>
+
 // Table of cos and sin of 2 pi k / 512, k = 0..511, for table_cos, filled
 // by each CTA of the FP64-form same-event kernels.
 constexpr int COS_TABLE = 512;
@@ -16,26 +19,81 @@ __device__ __forceinline__ void fill_cos_table(double2 *cs) {
     }
 }
 
-// cos(x), table-driven (the argument reduction of P. T. P. Tang's
-// table-driven elementary functions): x = k (2 pi / 512) + d with
-// k = rint(x 512 / 2 pi) and d from a two-part split of 2 pi / 512 (the
-// leading part has 26 significant bits, so k times it is exact for
-// |k| < 2^27), |d| <= pi / 512 = 6.2e-3; then
-//   cos x = cos(2 pi k / 512) cos d - sin(2 pi k / 512) sin d
-// with cos d to d^4 and sin d to d^5 from their Taylor series (truncation
-// below 1e-16 and 1e-18).  |x| >= 2^20 (never on this path: |q.dx| / hbarC
-// is a few hundred at most) falls back to cos().
-__device__ __forceinline__ double table_cos(const double2 *cs, double x) {
-    if (!(fabs(x) < 1048576.0)) return cos(x);
-    const double kd = rint(x * 81.48733086305042);          // 512 / (2 pi)
-    double d = __fma_rn(-kd, 0.01227184641174972, x);       // leading part
-    d = __fma_rn(-kd, -1.086645907356806e-10, d);           // 2 pi / 512 - leading part
-    const int k = __double2int_rn(kd) & (COS_TABLE - 1);
+// Constants of table_cos for one scale h: it returns cos(h ph) of a phase
+// ph (h = 1 / hbarC for the pair numerators, h = 1 for a plain cos), with
+// the product h ph never rounded.  Filled on the host by make_cos_scale.
+struct CosScale {
+    double c1;       // h 512 / (2 pi): table points per unit of ph
+    double s1, s2;   // (2 pi / 512) / h = s1 + s2, s1 with 26 significant bits
+    double h;        // h, and the Taylor coefficients of cos(h d'), sin(h d')
+    double c2, c4;   //   -h^2 / 2, h^4 / 24
+    double s3, s5;   //   -h^3 / 6, h^5 / 120
+    unsigned lim_hi; // high word of L, the largest power of two with L c1 < 2^27
+};
+
+// (2 pi / 512) / h is formed in double-double arithmetic (2 pi as a
+// two-part constant, the division's remainder taken exactly with an FMA),
+// then split into s1, its leading 26 significant bits (the low 27 bits of
+// the significand cleared, so that k s1 is exact for |k| < 2^27), and the
+// rest s2: s1 + s2 holds the step to about 2^-79 relative.
+static inline CosScale make_cos_scale(double h) {
+    CosScale k;
+    const double t_hi = 6.283185307179586 / 512.0, t_lo = 2.4492935982947064e-16 / 512.0;
+    const double q1 = t_hi / h;
+    const double q2 = (std::fma(-q1, h, t_hi) + t_lo) / h;
+    unsigned long long bits;
+    std::memcpy(&bits, &q1, sizeof bits);
+    bits &= ~((1ull << 27) - 1);
+    std::memcpy(&k.s1, &bits, sizeof bits);
+    k.s2 = (q1 - k.s1) + q2;
+    k.c1 = h * (512.0 / 6.283185307179586);
+    k.h = h;
+    k.c2 = -0.5 * h * h;
+    k.c4 = h * h * h * h / 24.0;
+    k.s3 = -h * h * h / 6.0;
+    k.s5 = h * h * h * h * h / 120.0;
+    int m = 40;
+    while (m > -40 && std::ldexp(1.0, m) * k.c1 >= 134217728.0) m--;
+    k.lim_hi = (unsigned)(1023 + m) << 20;
+    return k;
+}
+
+// cos(h ph), table-driven (the argument reduction of P. T. P. Tang's
+// table-driven elementary functions, done on ph itself): ph = k s + d' with
+// s = (2 pi / 512) / h, k the integer nearest to ph c1 (the exact product,
+// rounded once by an FMA against 1.5 2^52, whose low word then holds k) and
+// d' from the two-part split of s, so that d = h d' is at most pi / 512 =
+// 6.2e-3 in magnitude; then
+//   cos(h ph) = cos(2 pi k / 512) cos d - sin(2 pi k / 512) sin d
+// with cos d to d^4 and sin d to d^5 from their Taylor series in d'
+// (truncation below 1e-16 and 1e-18).  |ph| >= L (k could reach 2^27;
+// never on the pair path, where |q.dx| / hbarC is a few hundred at most) and
+// NaN fall back to cos(h ph).
+__device__ __forceinline__ double table_cos(const double2 *cs, const CosScale &k, double ph) {
+    if (!(((unsigned)__double2hiint(ph) & 0x7fffffffu) < k.lim_hi)) return cos(k.h * ph);
+    const double t = __fma_rn(ph, k.c1, 6755399441055744.0);  // 1.5 2^52
+    const double kd = t - 6755399441055744.0;
+    double d = __fma_rn(-kd, k.s1, ph);
+    d = __fma_rn(-kd, k.s2, d);
+    const int j = __double2loint(t) & (COS_TABLE - 1);
     const double d2 = d * d;
-    const double cd = __fma_rn(d2, __fma_rn(d2, 1.0 / 24.0, -0.5), 1.0);
-    const double sd = d * __fma_rn(d2, __fma_rn(d2, 1.0 / 120.0, -1.0 / 6.0), 1.0);
-    const double2 e = cs[k];
+    const double cd = __fma_rn(d2, __fma_rn(d2, k.c4, k.c2), 1.0);
+    const double sd = d * __fma_rn(d2, __fma_rn(d2, k.s5, k.s3), k.h);
+    const double2 e = cs[j];
     return __fma_rn(e.x, cd, -(e.y * sd));
+}
+
+// 1/sqrt(x) for the pair numerators' q sums: the FP64 approximate
+// reciprocal square root (PTX rsqrt.approx.ftz.f64) refined by one
+// Newton-Raphson step carried to its second-order term: with
+// e = 1 - x y0^2, 1/sqrt(x) = y0 (1 - e)^(-1/2) = y0 (1 + e/2 + 3e^2/8 + ...),
+// so a start of relative error r leaves about 2.5 r^3 plus the rounding of
+// the last steps.  For normal x > 0; 0 gives NaN.
+__device__ __forceinline__ double rsqrt_refined(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = __fma_rn(-(x * y), y, 1.0);
+    return __fma_rn(y, e * __fma_rn(e, 0.375, 0.5), y);
 }
 
 // Table of 2^(j / 64), j = 0..63, for table_exp, filled by each CTA that

@@ -335,7 +335,9 @@ __device__ __forceinline__ int kphi_screen(const Screen &S, const Q &q) {
 }
 
 // FP64 summed values of an accepted same-event pair (algebraically the
-// reference's q_out, q_side, q_long and cos(q.dx / hbarC)).
+// reference's q_out, q_side, q_long and cos(q.dx / hbarC)); the two
+// 1/sqrt come from rsqrt_refined, the cos from table_cos of the unrounded
+// product of the phase and 1/hbarC.
 template <bool BOOST>
 __device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const double *a,
                                          const double *b, double &qo, double &qs, double &ql,
@@ -343,12 +345,12 @@ __device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const
     const double sx = a[0] + b[0], sy = a[1] + b[1];
     const double dx = a[0] - b[0], dy = a[1] - b[1];
     const double dz = a[2] - b[2], dE = a[3] - b[3];
-    const double inv = rsqrt(__fma_rn(sx, sx, sy * sy));
+    const double inv = rsqrt_refined(__fma_rn(sx, sx, sy * sy));
     qo = __fma_rn(dx, sx, dy * sy) * inv;
     qs = __fma_rn(dy, sx, -(dx * sy)) * inv;
     if (BOOST) {
         const double sE = a[3] + b[3], sz = a[2] + b[2];
-        ql = __fma_rn(sE, dz, -(sz * dE)) * rsqrt((sE - sz) * (sE + sz));
+        ql = __fma_rn(sE, dz, -(sz * dE)) * rsqrt_refined((sE - sz) * (sE + sz));
     } else {
         ql = dz;
     }
@@ -358,7 +360,7 @@ __device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const
     ph = __fma_rn(-dx, a[4] - b[4], ph);
     ph = __fma_rn(-dy, a[5] - b[5], ph);
     ph = __fma_rn(-dz, a[6] - b[6], ph);
-    w = table_cos(cs, g.hbarC_inv * ph);
+    w = table_cos(cs, g.cph, ph);
 }
 
 // Summed values of the FP32-weight form.  The momentum sums and differences

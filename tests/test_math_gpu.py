@@ -1,11 +1,14 @@
-"""The engine's table-driven FP64 functions (csrc/hbt_math.cuh), run on the
-device through hbt_check_math, against the host's libm (numpy): cos, used
-for the same-event numerators, and exp, used by the radii fits.
+"""The engine's own FP64 functions (csrc/hbt_math.cuh), run on the device
+through hbt_check_math, against the host's libm (numpy): cos, used for the
+same-event numerators, exp, used by the radii fits, and the refined
+reciprocal square root of the FP64 form's q values.
 
 Bounds: cos within 3e-16 absolute over |x| < 1000 (the phases of the pair
-kernels are a few hundred at most) and 1e-15 absolute near 2^20; exp within
-4 ulp relative over |x| < 700 and within 1e-15 relative of libm outside
-(there it calls the device's exp())."""
+kernels are a few hundred at most) and 1e-15 absolute near 2^20, at scale 1
+and at the pair kernels' scale 1/hbarC (against the product taken in long
+double); exp within 4 ulp relative over |x| < 700 and within 1e-15 relative
+of libm outside (there it calls the device's exp()); the reciprocal square
+root within 2 ulp over 1e-12 < x < 1e12."""
 import ctypes
 
 import numpy as np
@@ -85,3 +88,69 @@ def test_df_cos_against_libm():
     xf = hf.astype(np.float64) + (far - hf.astype(np.float64)).astype(np.float32).astype(np.float64)
     assert np.max(np.abs(_dev(2, far) - np.cos(xf))) < 1e-15
     np.testing.assert_array_equal(np.isnan(_dev(2, [np.nan, np.inf])), [True, True])
+
+
+HBARC = 0.197327053  # GeV fm, the pair kernels' constant
+
+
+def _two_prod(a, b):
+    """a * b = p + e exactly (Dekker's product with Veltkamp's split)."""
+    p = a * b
+
+    def split(v):
+        c = 134217729.0 * v
+        hi = c - (c - v)
+        return hi, v - hi
+    ah, al = split(a)
+    bh, bl = split(b)
+    return p, ((ah * bh - p) + ah * bl + al * bh) + al * bl
+
+
+def _cos_scaled(h, x):
+    """cos(h x) of the exact product: cos(p + e) = cos p - e sin p (e is
+    below half an ulp of p, so the next term is below 1e-20)."""
+    p, e = _two_prod(np.full_like(x, h), x)
+    return np.cos(p) - np.sin(p) * e
+
+
+def test_table_cos_at_the_pair_scale():
+    """cos(ph / hbarC) of phases ph in GeV fm, the reduction done on ph
+    itself, against libm's cos of the exact product (3.5e-16: the device's
+    3e-16 at scale 1 plus the reference's own rounding)."""
+    rng = np.random.default_rng(4)
+    h = 1.0 / HBARC
+    step = 2 * np.pi / 512 / h
+    k = np.arange(-3000, 3000)
+    x = np.concatenate([rng.uniform(-200, 200, 200000), rng.uniform(-0.5, 0.5, 50000),
+                        k * step, k * step + step / 2, np.nextafter(k * step + step / 2, 0),
+                        [0.0, -0.0, 1e-300, 5e-324, HBARC * np.pi]])
+    assert np.max(np.abs(_dev(3, x) - _cos_scaled(h, x))) < 3.5e-16
+    big = rng.uniform(-262143, 262143, 20000)  # the table's range at this scale
+    assert np.max(np.abs(_dev(3, big) - _cos_scaled(h, big))) < 1e-15
+    np.testing.assert_array_equal(np.isnan(_dev(3, [np.nan, np.inf])), [True, True])
+    # beyond it the device's cos of the rounded product h * x
+    tail = np.array([262144.0, -3e6, 1e10])
+    assert np.max(np.abs(_dev(3, tail) - np.cos(h * tail))) < 1e-15
+
+
+def test_rsqrt_refined():
+    rng = np.random.default_rng(5)
+    x = np.concatenate([np.exp(rng.uniform(np.log(1e-12), np.log(1e12), 300000)),
+                        rng.uniform(0.01, 40.0, 100000),
+                        2.0 ** np.arange(-39, 40), np.nextafter(2.0 ** np.arange(-39, 40), 0),
+                        [1.0, 4.0, 0.25, 2.0, 0.5]])
+    got = _dev(4, x)
+    want = (1 / np.sqrt(x.astype(np.longdouble))).astype(np.float64)
+    assert np.max(np.abs(got - want) / np.spacing(want)) <= 2
+
+
+def test_rsqrt_start_accuracy():
+    """The start value of rsqrt_refined, the device's approximate FP64
+    reciprocal square root: relative error below 2^-19, where the refinement's
+    truncation (2.5 r^3) stays under 0.2 ulp."""
+    rng = np.random.default_rng(6)
+    x = np.concatenate([np.exp(rng.uniform(np.log(1e-12), np.log(1e12), 300000)),
+                        2.0 ** np.arange(-39, 40), [1.0, 4.0, 0.25, 2.0, 0.5]])
+    got = _dev(5, x)
+    want = (1 / np.sqrt(x.astype(np.longdouble))).astype(np.float64)
+    assert np.max(np.abs(got / want - 1)) < 2.0 ** -19
