@@ -1,6 +1,5 @@
-// Device evaluation of the table-driven FP64 functions, the refined FP64
-// reciprocal square root and the double-float cos of the pair kernels
-// (include/hbt_check.h).
+// Device evaluation of the table-driven FP64 functions and of the
+// double-float cos of the pair kernels (include/hbt_check.h).
 #include "../../include/hbt_check.h"
 #include "hbt_math.cuh"
 #include "hbt_tile.cuh"
@@ -29,15 +28,10 @@ __global__ void k_check_math(int which, CosScale k, long long n, const double *x
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         double v;
-        if (which == HBT_CHECK_COS || which == HBT_CHECK_COS_PHASE) {
+        if (which == HBT_CHECK_COS || which == HBT_CHECK_COS_PHASE)
             v = table_cos(cs, k, x[i]);
-        } else if (which == HBT_CHECK_RSQRT) {
-            v = rsqrt_refined(x[i]);
-        } else if (which == HBT_CHECK_RSQRT_START) {
-            asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(v) : "d"(x[i]));
-        } else {
+        else
             v = table_exp(et, x[i]);
-        }
         out[i] = v;
     }
 }
@@ -47,7 +41,7 @@ __global__ void k_check_math(int which, CosScale k, long long n, const double *x
 extern "C" hbt_status hbt_check_math(int device, int32_t which, int64_t n, const double *x,
                                      double *out) {
     if (n < 0 || (n > 0 && (!x || !out)) ||
-        which < HBT_CHECK_COS || which > HBT_CHECK_RSQRT_START)
+        which < HBT_CHECK_COS || which > HBT_CHECK_COS_PHASE)
         return HBT_ERR_INVALID;
     if (n == 0) return HBT_OK;
     if (cudaSetDevice(device) != cudaSuccess) return HBT_ERR_CUDA;

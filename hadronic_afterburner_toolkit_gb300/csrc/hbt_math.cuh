@@ -83,19 +83,6 @@ __device__ __forceinline__ double table_cos(const double2 *cs, const CosScale &k
     return __fma_rn(e.x, cd, -(e.y * sd));
 }
 
-// 1/sqrt(x) for the pair numerators' q sums: the FP64 approximate
-// reciprocal square root (PTX rsqrt.approx.ftz.f64) refined by one
-// Newton-Raphson step carried to its second-order term: with
-// e = 1 - x y0^2, 1/sqrt(x) = y0 (1 - e)^(-1/2) = y0 (1 + e/2 + 3e^2/8 + ...),
-// so a start of relative error r leaves about 2.5 r^3 plus the rounding of
-// the last steps.  For normal x > 0; 0 gives NaN.
-__device__ __forceinline__ double rsqrt_refined(double x) {
-    double y;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    const double e = __fma_rn(-(x * y), y, 1.0);
-    return __fma_rn(y, e * __fma_rn(e, 0.375, 0.5), y);
-}
-
 // Table of 2^(j / 64), j = 0..63, for table_exp, filled by each CTA that
 // uses it.
 constexpr int EXP_TABLE = 64;

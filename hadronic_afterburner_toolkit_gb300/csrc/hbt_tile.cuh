@@ -334,35 +334,6 @@ __device__ __forceinline__ int kphi_screen(const Screen &S, const Q &q) {
     return (int)k;
 }
 
-// FP64 summed values of an accepted same-event pair (algebraically the
-// reference's q_out, q_side, q_long and cos(q.dx / hbarC)); the two
-// 1/sqrt come from rsqrt_refined, the cos from table_cos of the unrounded
-// product of the phase and 1/hbarC.
-template <bool BOOST>
-__device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const double *a,
-                                         const double *b, double &qo, double &qs, double &ql,
-                                         double &w) {
-    const double sx = a[0] + b[0], sy = a[1] + b[1];
-    const double dx = a[0] - b[0], dy = a[1] - b[1];
-    const double dz = a[2] - b[2], dE = a[3] - b[3];
-    const double inv = rsqrt_refined(__fma_rn(sx, sx, sy * sy));
-    qo = __fma_rn(dx, sx, dy * sy) * inv;
-    qs = __fma_rn(dy, sx, -(dx * sy)) * inv;
-    if (BOOST) {
-        const double sE = a[3] + b[3], sz = a[2] + b[2];
-        ql = __fma_rn(sE, dz, -(sz * dE)) * rsqrt_refined((sE - sz) * (sE + sz));
-    } else {
-        ql = dz;
-    }
-    // q.dx = dE dt - dx dX - dy dY - dz dZ, accumulated with fused
-    // multiply-adds (one rounding per term)
-    double ph = dE * (a[7] - b[7]);
-    ph = __fma_rn(-dx, a[4] - b[4], ph);
-    ph = __fma_rn(-dy, a[5] - b[5], ph);
-    ph = __fma_rn(-dz, a[6] - b[6], ph);
-    w = table_cos(cs, g.cph, ph);
-}
-
 // Summed values of the FP32-weight form.  The momentum sums and differences
 // are taken in FP64 (no cancellation), then q_out, q_side, q_long follow in
 // FP32 (relative error a few 1e-7).  cos: the phase is computed and reduced
@@ -417,6 +388,20 @@ __device__ __forceinline__ float4 values32(const Grid &g, const double *a, const
 struct FF {
     float h, l;
 };
+
+// Exact FP32 -> FP64 conversion of a normal FP32 value or zero through its
+// bits, on the integer pipe (the conversion instruction runs on the FP64
+// pipe): the exponent
+// rebiased by 1023 - 127 = 896, the significand moved up by 29 bits.  FP32
+// subnormals (below 1.2e-38, which the low parts of these values never
+// reach but at zero) give a signed zero; infinities and NaN are not
+// handled (the values of binned pairs are finite).
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+    const unsigned u = __float_as_uint(f), m = u & 0x7fffffffu, sign = u & 0x80000000u;
+    const bool normal = m >= 0x00800000u;
+    const unsigned hi = normal ? ((m >> 3) + (896u << 20)) | sign : sign;
+    return __hiloint2double((int)hi, normal ? (int)(m << 29) : 0);
+}
 
 __device__ __forceinline__ FF two_sum(float a, float b) {
     const float s = __fadd_rn(a, b);
@@ -626,34 +611,75 @@ __device__ __forceinline__ double df_cos(const float4 *tab, FF ph) {
     return (double)r.h + (double)r.l;
 }
 
+// hi + lo rounded once to FP64: with the conversion instructions (the
+// double-float form, whose FP64 pipe has room), or on the integer pipe (the
+// FP64 form, whose FP64 pipe is the busiest).
 __device__ __forceinline__ double ff_double(FF a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ double ff_double_bits(FF a) {
+    return f32_to_f64_bits(a.h) + f32_to_f64_bits(a.l);
+}
+
+// x as hi + lo, two FP32 values formed from its bits on the integer pipe:
+// hi is x with the significand truncated to 24 bits, lo the remaining 29
+// bits truncated to 24, so that |x - hi - lo| < 2^-46 |x| (both parts carry
+// the sign of x).  For x = 0 or 2^-100 <= |x| < 2^100 (momenta, their sums
+// and differences); a lo part below the FP32 normal range (2^-126) is
+// dropped, and magnitudes outside the range give zero.
+__device__ __forceinline__ FF f64_to_ff_bits(double x) {
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned sign = hw & 0x80000000u, ae = hw & 0x7fffffffu;
+    const bool in_range = ae - ((1023u - 100u) << 20) < (200u << 20);
+    // hi: the exponent rebiased by 1023 - 127 = 896, the top 23 explicit bits
+    const unsigned hb = __funnelshift_l(lw, ae - (896u << 20), 3) | sign;
+    // lo: the low 29 bits r, worth r 2^(E - 1075); its leading bit is bit
+    // 31 - clz(r), so the FP32 exponent field is E - 917 - clz(r)
+    const unsigned r = lw & 0x1fffffffu;
+    const int lz = __clz(r);
+    const int e = (int)(ae >> 20) - 917 - lz;
+    const unsigned lb = (r != 0u && e > 0)
+                            ? ((unsigned)e << 23) | (((r << (lz & 31)) >> 8) & 0x7fffffu) | sign
+                            : sign;
+    return in_range ? FF{__uint_as_float(hb), __uint_as_float(lb)} : FF{0.0f, 0.0f};
+}
+
+// q_out, q_side, q_long of a pair in double-float arithmetic from its
+// momentum differences dp and sums sp (px, py, pz, E; sp[2], sp[3] only
+// with the boost): q_out = (dx sx + dy sy) / |s_T|, q_side = (dy sx - dx sy)
+// / |s_T| and, with the longitudinal boost, q_long = (sE dz - sz dE) /
+// sqrt(sE^2 - sz^2) (algebraically the reference's expressions), each
+// operation in double-float: about 1e-14 relative, or 2^-45 of |dp_T| in
+// absolute terms where q_out or q_side cancels.
+template <bool BOOST>
+__device__ __forceinline__ void ff_lcms(const FF *dp, const FF *sp, FF &vo, FF &vs, FF &vl) {
+    const FF inv = ff_rsqrt(ff_add(ff_mul(sp[0], sp[0]), ff_mul(sp[1], sp[1])));
+    vo = ff_mul(ff_add(ff_mul(dp[0], sp[0]), ff_mul(dp[1], sp[1])), inv);
+    vs = ff_mul(ff_add(ff_mul(dp[1], sp[0]), ff_neg(ff_mul(dp[0], sp[1]))), inv);
+    vl = dp[2];
+    if (BOOST) {
+        const FF m2 = ff_mul(ff_add(sp[3], ff_neg(sp[2])), ff_add(sp[3], sp[2]));
+        vl = ff_mul(ff_add(ff_mul(sp[3], dp[2]), ff_neg(ff_mul(sp[2], dp[3]))), ff_rsqrt(m2));
+    }
+}
 
 // Summed values of a binned pair in the double-float form, for the pair as
 // stored (first = a from the i-tile, second = b from the j-tile): a, b are
 // the eight split columns (momenta relative to the tiles' offsets oa, ob),
 // results as FP64, q_out, q_side, q_long negated when `neg` (the pair's
-// reference orientation is (b, a)).  The same expressions as values64, each
-// operation in double-float; q_out, q_side, q_long to about 1e-15 relative,
+// reference orientation is (b, a)).  The expressions of ff_lcms and
+// values64 from the split columns, each operation in double-float; q_out, q_side, q_long to about 1e-15 relative,
 // the phase to 2^-48 of its terms.
 template <bool BOOST>
 __device__ __forceinline__ void values_df(const Screen &S, const float4 *tab, const float2 *a,
                                           const float2 *b, const float *oa, const float *ob,
                                           bool neg, double &qo, double &qs, double &ql,
                                           double &w) {
-    FF dp[4], sp[4];
+    FF dp[4], sp[4], vo, vs, vl;
 #pragma unroll
     for (int f = 0; f < 4; f++) {
         dp[f] = ff_add(ff_diff(a[f], b[f]), two_sum(oa[f], -ob[f]));
         if (f < 2 || BOOST) sp[f] = ff_add(ff_sum(a[f], b[f]), two_sum(oa[f], ob[f]));
     }
-    const FF inv = ff_rsqrt(ff_add(ff_mul(sp[0], sp[0]), ff_mul(sp[1], sp[1])));
-    FF vo = ff_mul(ff_add(ff_mul(dp[0], sp[0]), ff_mul(dp[1], sp[1])), inv);
-    FF vs = ff_mul(ff_add(ff_mul(dp[1], sp[0]), ff_neg(ff_mul(dp[0], sp[1]))), inv);
-    FF vl = dp[2];
-    if (BOOST) {
-        const FF m2 = ff_mul(ff_add(sp[3], ff_neg(sp[2])), ff_add(sp[3], sp[2]));
-        vl = ff_mul(ff_add(ff_mul(sp[3], dp[2]), ff_neg(ff_mul(sp[2], dp[3]))), ff_rsqrt(m2));
-    }
+    ff_lcms<BOOST>(dp, sp, vo, vs, vl);
     if (neg) {
         vo = ff_neg(vo);
         vs = ff_neg(vs);
@@ -667,6 +693,44 @@ __device__ __forceinline__ void values_df(const Screen &S, const float4 *tab, co
     ph = ff_add(ph, ff_neg(ff_mul(dp[1], ff_diff(a[5], b[5]))));
     ph = ff_add(ph, ff_neg(ff_mul(dp[2], ff_diff(a[6], b[6]))));
     w = df_cos(tab, ff_mul(ph, FF{S.hc_h, S.hc_l}));
+}
+
+// FP64 summed values of an accepted same-event pair (algebraically the
+// reference's q_out, q_side, q_long and cos(q.dx / hbarC)).  The momentum
+// differences and sums are FP64 (one rounding each, so that cancelling sums
+// stay exact to the last bits), and so are the phase q.dx and its cos
+// (table_cos of the unrounded product with 1/hbarC, 3e-16).  q_out, q_side
+// and the boosted q_long, which are only summed, follow in double-float on
+// the FP32 pipe (ff_lcms: about 1e-14 relative) from the FP64 sums and
+// differences split on the integer pipe, and come back as FP64 with one
+// addition each.  Of the FP64 pipe, which bounds this form, a binned pair
+// then takes 29 to 31 instructions instead of 55.
+template <bool BOOST>
+__device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const double *a,
+                                         const double *b, double &qo, double &qs, double &ql,
+                                         double &w) {
+    const double dx = a[0] - b[0], dy = a[1] - b[1];
+    const double dz = a[2] - b[2], dE = a[3] - b[3];
+    FF dp[4] = {f64_to_ff_bits(dx), f64_to_ff_bits(dy), f64_to_ff_bits(dz), f64_to_ff_bits(dE)};
+    FF sp[4];
+    sp[0] = f64_to_ff_bits(a[0] + b[0]);
+    sp[1] = f64_to_ff_bits(a[1] + b[1]);
+    if (BOOST) {
+        sp[2] = f64_to_ff_bits(a[2] + b[2]);
+        sp[3] = f64_to_ff_bits(a[3] + b[3]);
+    }
+    FF vo, vs, vl;
+    ff_lcms<BOOST>(dp, sp, vo, vs, vl);
+    qo = ff_double_bits(vo);
+    qs = ff_double_bits(vs);
+    ql = BOOST ? ff_double_bits(vl) : dz;
+    // q.dx = dE dt - dx dX - dy dY - dz dZ, accumulated with fused
+    // multiply-adds (one rounding per term)
+    double ph = dE * (a[7] - b[7]);
+    ph = __fma_rn(-dx, a[4] - b[4], ph);
+    ph = __fma_rn(-dy, a[5] - b[5], ph);
+    ph = __fma_rn(-dz, a[6] - b[6], ph);
+    w = table_cos(cs, g.cph, ph);
 }
 
 // Shared memory of one tile pair; E2 is the entry of the second same-event
@@ -1132,18 +1196,15 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                 atomicAdd(d.h.cnt + at, 1ull);
                 return;
             }
-            // FP64 form, or a pair the window screen left undecided: the pair in
-            // the reference's orientation, from the FP64 tile or (FP32-weight
-            // form) the FP64 columns themselves
-            double A[8], B[8];  // first and second particle of the pair
-#pragma unroll
-            for (int f = 0; f < 8; f++) {
-                const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
-                const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
-                A[f] = swap ? v : u;
-                B[f] = swap ? u : v;
-            }
             if (PREC == 0 && slot >= 0) {
+                // the pair in the reference's orientation, from the FP64 tile
+                double A[8], B[8];
+#pragma unroll
+                for (int f = 0; f < 8; f++) {
+                    const double u = sm.si[f][qi], v = sm.sj[f][qj];
+                    A[f] = swap ? v : u;
+                    B[f] = swap ? u : v;
+                }
                 double vo, vs, vl, vw;
                 values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
                 const long long at = (long long)slot * d.g.q3 + bin;
@@ -1154,6 +1215,17 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                 atomicAdd(&h->w, vw);
                 atomicAdd(d.h.cnt + at, 1ull);
                 return;
+            }
+            // a pair the window screen left undecided: the pair in the
+            // reference's orientation, from the FP64 tile or (FP32-weight and
+            // double-float forms) the FP64 columns themselves
+            double A[8], B[8];  // first and second particle of the pair
+#pragma unroll
+            for (int f = 0; f < 8; f++) {
+                const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+                const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+                A[f] = swap ? v : u;
+                B[f] = swap ? u : v;
             }
             if (PREC == 1) {
                 undecided_pair32<BOOST>(d, A, B, i0 + qi, j0 + qj, n);

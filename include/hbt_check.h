@@ -2,8 +2,7 @@
  * hbt_check.h - device checks of the engine's own FP64 elementary functions
  * (libhbt_gpu.so).  The pair kernels and the radii fits evaluate cos and
  * exp with table-driven implementations of their own (csrc/hbt_math.cuh,
- * and the double-float cos of csrc/hbt_tile.cuh), and the FP64 form's
- * q values with a refined approximate reciprocal square root;
+ * and the double-float cos of csrc/hbt_tile.cuh);
  * this entry point runs them on the device over caller-given arguments so
  * that tests can compare them with the host's libm.  Not part of the
  * reference's interface.
@@ -23,9 +22,6 @@ extern "C" {
                              hi = (float)x and lo = (float)(x - hi) */
 #define HBT_CHECK_COS_PHASE 3 /* table_cos with the pair kernels' scale:
                                  cos(x / hbarC), the product never rounded */
-#define HBT_CHECK_RSQRT 4 /* rsqrt_refined, the FP64 form's 1/sqrt(x) */
-#define HBT_CHECK_RSQRT_START 5 /* its start value, the device's approximate
-                                   FP64 reciprocal square root */
 
 /* out[i] = f(x[i]) on `device` for the function `which`; host arrays. */
 hbt_status hbt_check_math(int device, int32_t which, int64_t n, const double *x, double *out);

@@ -112,19 +112,17 @@ def test_missing_library_fails_loudly(tmp_path):
 
 def test_check_math_rejects_unknown_functions_without_a_device_call(lib):
     """hbt_check_math validates `which` (cos, exp, double-float cos, cos at
-    the pair scale, reciprocal square root and its start) and its arrays
-    before touching a device."""
+    the pair scale) and its arrays before touching a device."""
     L = engine.load()
     L.hbt_check_math.restype = ctypes.c_int32
     L.hbt_check_math.argtypes = [ctypes.c_int, ctypes.c_int32, ctypes.c_int64,
                                  ctypes.c_void_p, ctypes.c_void_p]
     x = (ctypes.c_double * 1)(0.5)
     out = (ctypes.c_double * 1)()
-    assert L.hbt_check_math(0, 6, 1, x, out) == 1           # HBT_ERR_INVALID
+    assert L.hbt_check_math(0, 4, 1, x, out) == 1           # HBT_ERR_INVALID
     assert L.hbt_check_math(0, -1, 1, x, out) == 1
     assert L.hbt_check_math(0, 2, 1, None, out) == 1        # missing input
     assert L.hbt_check_math(0, 2, 0, None, None) == 0       # nothing to do
     text = open(CHECK_HEADER).read()
     assert "#define HBT_CHECK_DFCOS 2" in text
-    for define in ("HBT_CHECK_COS_PHASE 3", "HBT_CHECK_RSQRT 4", "HBT_CHECK_RSQRT_START 5"):
-        assert "#define " + define in text
+    assert "#define HBT_CHECK_COS_PHASE 3" in text

@@ -1,14 +1,12 @@
 """The engine's own FP64 functions (csrc/hbt_math.cuh), run on the device
 through hbt_check_math, against the host's libm (numpy): cos, used for the
-same-event numerators, exp, used by the radii fits, and the refined
-reciprocal square root of the FP64 form's q values.
+same-event numerators, and exp, used by the radii fits.
 
 Bounds: cos within 3e-16 absolute over |x| < 1000 (the phases of the pair
 kernels are a few hundred at most) and 1e-15 absolute near 2^20, at scale 1
-and at the pair kernels' scale 1/hbarC (against the product taken in long
-double); exp within 4 ulp relative over |x| < 700 and within 1e-15 relative
-of libm outside (there it calls the device's exp()); the reciprocal square
-root within 2 ulp over 1e-12 < x < 1e12."""
+and at the pair kernels' scale 1/hbarC (against libm's cos of the exact
+product, 3.5e-16); exp within 4 ulp relative over |x| < 700 and within 1e-15 relative
+of libm outside (there it calls the device's exp())."""
 import ctypes
 
 import numpy as np
@@ -131,26 +129,3 @@ def test_table_cos_at_the_pair_scale():
     # beyond it the device's cos of the rounded product h * x
     tail = np.array([262144.0, -3e6, 1e10])
     assert np.max(np.abs(_dev(3, tail) - np.cos(h * tail))) < 1e-15
-
-
-def test_rsqrt_refined():
-    rng = np.random.default_rng(5)
-    x = np.concatenate([np.exp(rng.uniform(np.log(1e-12), np.log(1e12), 300000)),
-                        rng.uniform(0.01, 40.0, 100000),
-                        2.0 ** np.arange(-39, 40), np.nextafter(2.0 ** np.arange(-39, 40), 0),
-                        [1.0, 4.0, 0.25, 2.0, 0.5]])
-    got = _dev(4, x)
-    want = (1 / np.sqrt(x.astype(np.longdouble))).astype(np.float64)
-    assert np.max(np.abs(got - want) / np.spacing(want)) <= 2
-
-
-def test_rsqrt_start_accuracy():
-    """The start value of rsqrt_refined, the device's approximate FP64
-    reciprocal square root: relative error below 2^-19, where the refinement's
-    truncation (2.5 r^3) stays under 0.2 ulp."""
-    rng = np.random.default_rng(6)
-    x = np.concatenate([np.exp(rng.uniform(np.log(1e-12), np.log(1e12), 300000)),
-                        2.0 ** np.arange(-39, 40), [1.0, 4.0, 0.25, 2.0, 0.5]])
-    got = _dev(5, x)
-    want = (1 / np.sqrt(x.astype(np.longdouble))).astype(np.float64)
-    assert np.max(np.abs(got / want - 1)) < 2.0 ** -19
