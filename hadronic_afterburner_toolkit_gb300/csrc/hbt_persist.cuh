@@ -53,9 +53,12 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
 // spills: 167 ms per central group, against 194 ms at 5 and 234 ms at 6,
 // where its 80 registers spill in the pair loop), the FP32-weight form and
 // the mixed-event kernel at 6.
+#ifndef HBT_FP64_SAME_CTAS
+#define HBT_FP64_SAME_CTAS 5  // compile-time choice for the FP64 form (-D to measure others)
+#endif
 template <int PREC>
 struct SameCtas {
-    static constexpr int value = PREC == 1 ? 6 : (PREC == 2 ? 4 : 5);
+    static constexpr int value = PREC == 1 ? 6 : (PREC == 2 ? 4 : HBT_FP64_SAME_CTAS);
 };
 constexpr int kMixedCtas = 6;
 
