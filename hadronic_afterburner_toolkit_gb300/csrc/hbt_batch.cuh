@@ -32,6 +32,9 @@ struct BatchJob {
     // 1: the job's analysis bins q_inv histograms, whose window the 3-D
     // bounds do not cover: every tile pair is kept
     int qinv;
+    // ordered cap admission of several jobs at once: the job's first row in
+    // the admission's row order (Caps::rows_total)
+    long long row_base;
 };
 
 // Momentum-space box of a 128-particle tile.

@@ -65,7 +65,7 @@ struct hbt_ctx {
     int sms = 152, max_blocks_per_sm = 5;
     hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0, 1};
     // ordered admission scratch
-    DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi;
+    DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi, straddle_jobs;
     // input staging, two buffers in turn: the host-to-device copy of a call
     // runs on `copy_in` while the binning of the previous call still reads
     // the other buffer (in_free: recorded on `stream` after that binning)
@@ -310,6 +310,63 @@ bool caps_may_bind(const hbt_ctx *c, int mixed, u64 P) {
 hbt_status run_fast_jobs(hbt_ctx *c, std::vector<hbt::FastJob> jobs, int mode = hbt::MODE_FAST);
 bool batched_ok(const hbt_ctx *c);
 
+// After a count pass with K_phi bins: the pairs deferred to the host (K_phi
+// within kphi_defer_tol of an edge) get their bins from the C library's
+// atan2 here, are added to the row counts, and are looked up by the order
+// pass and the straddle kernel under key row * cols + column.
+hbt_status resolve_count_deferrals(hbt_ctx *c, long long rows, long long cols) {
+    if (!c->prm.azimuthal_flag) return HBT_OK;
+    unsigned n = 0;
+    TRY(read_defer_count(c, &n));
+    if (n > kDeferCap) return fail(c, HBT_ERR_DEVICE, "K_phi deferral buffer overflow");
+    if (n > 0) {
+        std::vector<hbt::Deferral> rec(n);
+        CU(cudaMemcpyAsync(rec.data(), c->defer.p, n * sizeof(hbt::Deferral),
+                           cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+        std::vector<hbt::Resolved> res(n);
+        for (unsigned k = 0; k < n; k++) {
+            res[k].key = rec[k].i * cols + rec[k].j;
+            res[k].iphi = host_kphi(c->d.g, rec[k].Kx, rec[k].Ky, rec[k].psi);
+            res[k].iK = rec[k].iK;
+        }
+        std::sort(res.begin(), res.end(),
+                  [](const hbt::Resolved &x, const hbt::Resolved &y) { return x.key < y.key; });
+        TRY(dalloc(c, c->resolved, n * sizeof(hbt::Resolved)));
+        refresh_device(c);
+        CU(cudaMemcpyAsync(c->resolved.p, res.data(), n * sizeof(hbt::Resolved),
+                           cudaMemcpyHostToDevice, c->stream));
+        c->d.caps.n_resolved = (int)n;
+        CU(hbt::launch_defer_count(c->d, rows, cols, (int)n, c->stream));
+        c->st.deferred_kphi += n;
+        c->st.launches++;
+    }
+    CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
+    return HBT_OK;
+}
+
+// Remaining admissions per stream bin of one counter family (mixed = 0:
+// numerators, 1: denominators), from the counters read back: cap - count
+// + 1 (a counter may pass the cap by one, as the reference's test is
+// `count > cap`), 0 for a full bin, unlimited for bins without a cap.
+std::vector<u64> remaining_of(const hbt_ctx *c, int mixed, const std::vector<u64> &ctr) {
+    const int ns = c->d.g.n_slots, nk = c->d.g.n_KT, nst = c->n_stream;
+    std::vector<u64> rem(nst, kInf);
+    for (int s = 0; s < ns; s++) {
+        const u64 v = ctr[(mixed ? ns : 0) + s];
+        if (v > c->cap)
+            rem[s] = 0;
+        else
+            rem[s] = (c->cap - v == kInf) ? kInf : c->cap - v + 1;
+    }
+    for (int k = 0; k < nk; k++) {
+        const u64 v = ctr[2 * ns + (mixed ? nk : 0) + k];
+        rem[ns + k] = (c->prm.invariant_radius_flag == 1) ? (v < c->cap_qinv ? c->cap_qinv - v : 0)
+                                                          : kInf;
+    }
+    return rem;
+}
+
 // Ordered admission for one launch (same-event: mixed = 0).  The two
 // passes over every pair (COUNT: survivors per stream bin and row; ORDER:
 // the rows before each bin's cut) run on the batched screened kernels when
@@ -331,20 +388,8 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
     TRY(drain_deferrals(c));
     std::vector<u64> ctr;
     TRY(read_counters(c, ctr));
-    const int ns = c->d.g.n_slots, nk = c->d.g.n_KT, nst = c->n_stream;
-    std::vector<u64> rem(nst, kInf);
-    for (int s = 0; s < ns; s++) {
-        const u64 v = ctr[(mixed ? ns : 0) + s];
-        if (v > c->cap)
-            rem[s] = 0;
-        else
-            rem[s] = (c->cap - v == kInf) ? kInf : c->cap - v + 1;
-    }
-    for (int k = 0; k < nk; k++) {
-        const u64 v = ctr[2 * ns + (mixed ? nk : 0) + k];
-        rem[ns + k] = (c->prm.invariant_radius_flag == 1) ? (v < c->cap_qinv ? c->cap_qinv - v : 0)
-                                                          : kInf;
-    }
+    const int nst = c->n_stream;
+    const std::vector<u64> rem = remaining_of(c, mixed, ctr);
     TRY(dalloc(c, c->rowcnt, (size_t)nst * rows * sizeof(unsigned)));
     TRY(dalloc(c, c->row_cut, nst * sizeof(long long)));
     TRY(dalloc(c, c->quota, nst * sizeof(u64)));
@@ -363,36 +408,7 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
             CU(hbt::launch_same(c->d, hbt::MODE_COUNT, rows, a, c->stream));
         c->st.launches++;
     }
-    // deferred K_phi bins: decided here, added to the row counts, and looked
-    // up by the admission passes
-    if (c->prm.azimuthal_flag) {
-        unsigned n = 0;
-        TRY(read_defer_count(c, &n));
-        if (n > kDeferCap) return fail(c, HBT_ERR_DEVICE, "K_phi deferral buffer overflow");
-        if (n > 0) {
-            std::vector<hbt::Deferral> rec(n);
-            CU(cudaMemcpyAsync(rec.data(), c->defer.p, n * sizeof(hbt::Deferral),
-                               cudaMemcpyDeviceToHost, c->stream));
-            CU(cudaStreamSynchronize(c->stream));
-            std::vector<hbt::Resolved> res(n);
-            for (unsigned k = 0; k < n; k++) {
-                res[k].key = rec[k].i * cols + rec[k].j;
-                res[k].iphi = host_kphi(c->d.g, rec[k].Kx, rec[k].Ky, rec[k].psi);
-                res[k].iK = rec[k].iK;
-            }
-            std::sort(res.begin(), res.end(),
-                      [](const hbt::Resolved &x, const hbt::Resolved &y) { return x.key < y.key; });
-            TRY(dalloc(c, c->resolved, n * sizeof(hbt::Resolved)));
-            refresh_device(c);
-            CU(cudaMemcpyAsync(c->resolved.p, res.data(), n * sizeof(hbt::Resolved),
-                               cudaMemcpyHostToDevice, c->stream));
-            c->d.caps.n_resolved = (int)n;
-            CU(hbt::launch_defer_count(c->d, rows, cols, (int)n, c->stream));
-            c->st.deferred_kphi += n;
-            c->st.launches++;
-        }
-        CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
-    }
+    TRY(resolve_count_deferrals(c, rows, cols));
     CU(cudaMemcpyAsync(c->remaining.p, rem.data(), nst * sizeof(u64), cudaMemcpyHostToDevice,
                        c->stream));
     CU(hbt::launch_cut(c->d, rows, nst, ptr<unsigned long long>(c->remaining), c->stream));
@@ -414,6 +430,76 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
     c->st.launches += 2;
     c->st.ordered_passes++;
     c->d.caps.n_resolved = 0;
+    return HBT_OK;
+}
+
+// Ordered admission of several mixed-event jobs at once, in the reference's
+// order (src/HBT_correlation.cpp:199-216: the events in turn, each against
+// its partners; within a job the pairs by list-1 row, then list-2 column).
+// The jobs' rows are numbered jointly (a job's first row is the number of
+// list-1 particles of the jobs before it), so that one count pass, one cut
+// per stream bin and one order pass on the batched kernels admit exactly the
+// pairs that job-by-job admission would, and each stream bin's cut row is
+// admitted pair by pair inside its own job (k_straddle_jobs).  Batched
+// kernels without q_inv histograms only (the callers check).
+hbt_status ordered_launch_mixed_jobs(hbt_ctx *c, const std::vector<hbt::FastJob> &in) {
+    std::vector<hbt::FastJob> jobs;
+    std::vector<hbt::StraddleJob> sj;
+    long long rows = 0, cols = 0;
+    for (hbt::FastJob j : in) {
+        if (j.kind != 1 || j.na < 1 || j.nb < 1) continue;
+        j.row_base = rows;
+        hbt::StraddleJob t = {};
+        for (int f = 0; f < 4; f++) {
+            t.a[f] = j.a[f];
+            t.b[f] = j.b[f];
+        }
+        t.n1 = j.na;
+        t.n2 = j.nb;
+        t.row_base = rows;
+        jobs.push_back(j);
+        sj.push_back(t);
+        rows += j.na;
+        cols = std::max(cols, j.nb);
+    }
+    if (jobs.empty()) return HBT_OK;
+    TRY(drain_deferrals(c));
+    std::vector<u64> ctr;
+    TRY(read_counters(c, ctr));
+    const int nst = c->n_stream;
+    const std::vector<u64> rem = remaining_of(c, 1, ctr);
+    TRY(dalloc(c, c->rowcnt, (size_t)nst * rows * sizeof(unsigned)));
+    TRY(dalloc(c, c->row_cut, nst * sizeof(long long)));
+    TRY(dalloc(c, c->quota, nst * sizeof(u64)));
+    TRY(dalloc(c, c->remaining, nst * sizeof(u64)));
+    TRY(dalloc(c, c->straddle_jobs, sj.size() * sizeof(hbt::StraddleJob)));
+    refresh_device(c);
+    // the joint row numbering holds for the two passes and the straddle only
+    struct JointRows {
+        hbt::Caps &caps;
+        ~JointRows() {
+            caps.rows_total = caps.cols_key = 0;
+            caps.n_resolved = 0;
+        }
+    } joint{c->d.caps};
+    c->d.caps.n_resolved = 0;
+    c->d.caps.rows_total = rows;
+    c->d.caps.cols_key = cols;
+    CU(cudaMemsetAsync(c->rowcnt.p, 0, (size_t)nst * rows * sizeof(unsigned), c->stream));
+    CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
+    CU(cudaMemcpyAsync(c->straddle_jobs.p, sj.data(), sj.size() * sizeof(hbt::StraddleJob),
+                       cudaMemcpyHostToDevice, c->stream));
+    TRY(run_fast_jobs(c, jobs, hbt::MODE_COUNT));
+    TRY(resolve_count_deferrals(c, rows, cols));
+    CU(cudaMemcpyAsync(c->remaining.p, rem.data(), nst * sizeof(u64), cudaMemcpyHostToDevice,
+                       c->stream));
+    CU(hbt::launch_cut(c->d, rows, nst, ptr<unsigned long long>(c->remaining), c->stream));
+    TRY(run_fast_jobs(c, jobs, hbt::MODE_ORDER));
+    CU(hbt::launch_jobs_straddle(c->d, ptr<hbt::StraddleJob>(c->straddle_jobs), (int)sj.size(),
+                                 rows, nst, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    c->st.launches += 2;
+    c->st.ordered_passes++;
     return HBT_OK;
 }
 
@@ -693,6 +779,7 @@ void screen_from_grid(const Grid &g, Screen &s) {
     s.psi_slack = f(slack(g.psi_ref, s.psi));
     s.two_pi = f(g.two_pi);
     s.inv_dKphi = f(1.0 / g.dKphi);
+    s.kphi_tol = std::nextafter(f(g.kphi_tol), INFINITY);
     s.qnpts = g.qnpts;
     s.n_KT = g.n_KT;
     s.n_Kphi = g.n_Kphi;
@@ -789,7 +876,8 @@ void hbt_destroy(hbt_ctx *c) {
     DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
-                      &c->apply_iphi, &c->in[0], &c->in[1], &c->part, &c->comp, &c->exp};
+                      &c->apply_iphi, &c->straddle_jobs, &c->in[0], &c->in[1], &c->part,
+                      &c->comp, &c->exp};
     if (c->copy) cudaStreamSynchronize(c->copy);
     for (DevBuf *b : bufs) dfree(c, *b);
     dfree(c, c->snap);
@@ -904,6 +992,29 @@ hbt_status hbt_bin_batch_dev(hbt_ctx *c, int32_t n_jobs, const hbt_job *jobs) {
         std::vector<u64> ctr;
         TRY(read_counters(c, ctr));
         sequential = caps_may_bind(c, 0, P_same) || caps_may_bind(c, 1, P_mixed);
+    }
+    if (sequential && batched_ok(c) && !c->d.g.qinv) {
+        // the numerator and denominator counters are separate families, so
+        // the same-event jobs (each admitted on its own, in order) and the
+        // mixed-event jobs (admitted together in their joint order) keep the
+        // reference's order for the caps
+        for (int k = 0; k < n_jobs; k++)
+            if (jobs[k].kind == 0) TRY(hbt_bin_same_dev(c, jobs[k].na, &jobs[k].a));
+        if (P_mixed > 0) {
+            std::vector<FastJob> mj;
+            for (const FastJob &f : fast_jobs_of(n_jobs, jobs))
+                if (f.kind == 1) mj.push_back(f);
+            c->st.pairs_mixed += P_mixed;
+            if (caps_may_bind(c, 1, P_mixed)) {
+                TRY(ordered_launch_mixed_jobs(c, mj));
+                std::vector<u64> ctr;
+                TRY(read_counters(c, ctr));
+            } else {
+                TRY(run_fast_jobs(c, mj));
+                c->ub[1] += P_mixed;
+            }
+        }
+        return HBT_OK;
     }
     if (sequential) {
         // one job at a time keeps the reference's order for the caps

@@ -84,6 +84,11 @@ struct Caps {
     unsigned long long *quota; // [n_stream] admissions left in the straddle row
     const Resolved *resolved;  // deferred pairs resolved on the host
     int n_resolved;
+    // admission of several mixed-event jobs in one pair of passes: a pair's
+    // row is its job's row_base plus its position in list 1, rowcnt holds
+    // rows_total rows per stream bin and deferral keys are row * cols_key +
+    // column (0: one job, its own list sizes)
+    long long rows_total, cols_key;
 };
 
 // FP32 copies of the constants used by the FP32 pair screen (hbt_fast.cu),
@@ -104,6 +109,12 @@ struct Screen {
     // q_inv prefilter (invariant_radius_flag): square of the upper window
     // bound with its slack and a margin; -1 when no q_inv >= 0 can pass
     float qi_hi2;
+    // Grid::kphi_tol rounded up: the K_phi screen leaves pairs this close to
+    // an edge (plus its error bound) to the reference chain, which hands
+    // them to the host, so that every pass that meets such a pair (the
+    // screened kernels and the pair-by-pair cut rows of cap admission)
+    // decides it the same way
+    float kphi_tol;
 };
 
 // Host: the prefilter constants of a screen whose window is filled in.
@@ -160,6 +171,15 @@ cudaError_t launch_apply(const Device &d, const Deferral *rec, const int *iphi, 
 // The same with the record count in device memory (*count <= cap).
 cudaError_t launch_apply_n(const Device &d, const Deferral *rec, const int *iphi, const int *count,
                            int cap, cudaStream_t st);
+// A mixed-event job of a multi-job ordered admission, as the straddle
+// kernel reads it: its lists in the caller's order and its first row.
+struct StraddleJob {
+    const double *a[4];
+    const double *b[4];
+    long long n1, n2, row_base;
+};
+cudaError_t launch_jobs_straddle(const Device &d, const StraddleJob *jobs, int n_jobs,
+                                 long long rows, int n_stream, cudaStream_t st);
 cudaError_t launch_defer_count(const Device &d, long long rows, long long cols, int n_res,
                                cudaStream_t st);
 cudaError_t launch_counters(const Device &d, unsigned long long *out, cudaStream_t st);

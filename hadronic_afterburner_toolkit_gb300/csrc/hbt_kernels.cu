@@ -71,24 +71,26 @@ __global__ void __launch_bounds__(TILE) k_mixed(Device d, long long n1, Cols4 l1
     }
 }
 
-// Ordered admission of one stream bin's cut row: the first `quota`
-// survivors in pair order (one warp per stream bin).
+// Ordered admission of stream bin b's cut row (row r of the list a8, whose
+// pairs run over cols particles: a8 itself after r for same-event lists,
+// b4 for mixed-event lists): the first `quota` survivors in pair order, by
+// one warp.  A deferred K_phi bin is looked up under key_row * key_cols + j.
 template <bool MIXED>
-__global__ void k_straddle(Device d, long long rows, long long cols, Cols8 a8, Cols4 b4) {
-    const int b = blockIdx.x;
-    const long long r = d.caps.row_cut[b];
-    if (r >= rows) return;
+__device__ __forceinline__ void straddle_row(const Device &d, int b, long long r,
+                                             long long key_row, long long key_cols,
+                                             long long cols, const double *const *a8,
+                                             const double *const *b4) {
     const unsigned long long quota = d.caps.quota[b];
     const int lane = threadIdx.x;
     const int ns = d.g.n_slots;
     unsigned long long admitted = 0;
-    const double apx = a8.p[0][r], apy = a8.p[1][r], apz = a8.p[2][r], aE = a8.p[3][r];
+    const double apx = a8[0][r], apy = a8[1][r], apz = a8[2][r], aE = a8[3][r];
     double ax[4] = {0, 0, 0, 0};
     if (!MIXED) {
-        ax[0] = a8.p[4][r];
-        ax[1] = a8.p[5][r];
-        ax[2] = a8.p[6][r];
-        ax[3] = a8.p[7][r];
+        ax[0] = a8[4][r];
+        ax[1] = a8[5][r];
+        ax[2] = a8[6][r];
+        ax[3] = a8[7][r];
     }
     const long long jstart = MIXED ? 0 : r + 1;
     for (long long j0 = jstart; j0 < cols && admitted < quota; j0 += 32) {
@@ -100,17 +102,14 @@ __global__ void k_straddle(Device d, long long rows, long long cols, Cols8 a8, C
         if (j < cols) {
             double bx[4] = {0, 0, 0, 0};
             if (!MIXED) {
-                bx[0] = a8.p[4][j];
-                bx[1] = a8.p[5][j];
-                bx[2] = a8.p[6][j];
-                bx[3] = a8.p[7][j];
+                bx[0] = a8[4][j];
+                bx[1] = a8[5][j];
+                bx[2] = a8[6][j];
+                bx[3] = a8[7][j];
             }
-            const double *src0 = MIXED ? b4.p[0] : a8.p[0];
-            const double *src1 = MIXED ? b4.p[1] : a8.p[1];
-            const double *src2 = MIXED ? b4.p[2] : a8.p[2];
-            const double *src3 = MIXED ? b4.p[3] : a8.p[3];
-            c = pair_chain<MIXED>(d.g, apx, apy, apz, aE, src0[j], src1[j], src2[j], src3[j],
-                                  ax, bx);
+            const double *const *src = MIXED ? b4 : a8;
+            c = pair_chain<MIXED>(d.g, apx, apy, apz, aE, src[0][j], src[1][j], src[2][j],
+                                  src[3][j], ax, bx);
             if (c.iK >= 0) {
                 if (b >= ns) {
                     has = c.qi_k >= 0 && ns + c.iK == b;
@@ -118,7 +117,7 @@ __global__ void k_straddle(Device d, long long rows, long long cols, Cols8 a8, C
                     slot = c.slot;
                     has = slot == b;
                 } else if (c.ev3 == 2) {
-                    slot = resolved_slot(d, r * cols + j, c.iK);
+                    slot = resolved_slot(d, key_row * key_cols + j, c.iK);
                     has = slot == b;
                 }
             }
@@ -141,6 +140,34 @@ __global__ void k_straddle(Device d, long long rows, long long cols, Cols8 a8, C
         }
         admitted += __popc(m);
     }
+}
+
+// One launch's cut rows, one warp per stream bin.
+template <bool MIXED>
+__global__ void k_straddle(Device d, long long rows, long long cols, Cols8 a8, Cols4 b4) {
+    const int b = blockIdx.x;
+    const long long r = d.caps.row_cut[b];
+    if (r >= rows) return;
+    straddle_row<MIXED>(d, b, r, r, cols, cols, a8.p, b4.p);
+}
+
+// The cut rows of several mixed-event jobs admitted together: a stream
+// bin's cut row r (in the jobs' joint row order) belongs to the last job
+// whose row_base is at most r.
+__global__ void k_straddle_jobs(Device d, const StraddleJob *jobs, int n_jobs, long long rows) {
+    const int b = blockIdx.x;
+    const long long r = d.caps.row_cut[b];
+    if (r >= rows) return;
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].row_base <= r)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const StraddleJob &job = jobs[lo];
+    straddle_row<true>(d, b, r - job.row_base, r, d.caps.cols_key, job.n2, job.a, job.b);
 }
 
 // Per stream bin: first row at which the running survivor count exceeds
@@ -321,6 +348,13 @@ cudaError_t launch_mixed_straddle(const Device &d, long long n1, const double *c
     Cols8 a;
     for (int f = 0; f < 8; f++) a.p[f] = f < 4 ? l1[f] : nullptr;
     k_straddle<true><<<n_stream, 32, 0, st>>>(d, n1, n2, a, cols4(l2));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_jobs_straddle(const Device &d, const StraddleJob *jobs, int n_jobs,
+                                 long long rows, int n_stream, cudaStream_t st) {
+    if (n_jobs < 1) return cudaSuccess;
+    k_straddle_jobs<<<n_stream, 32, 0, st>>>(d, jobs, n_jobs, rows);
     return cudaGetLastError();
 }
 

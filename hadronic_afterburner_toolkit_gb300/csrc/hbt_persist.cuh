@@ -48,13 +48,14 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
 }
 
 // Resident CTAs per SM (register budget 65536 / (128 x CTAs)): measured on
-// GB300, the FP64 form of the same-event kernel is fastest at 5 (its FP64
-// values need the registers), the double-float form at 4 (118 registers, no
-// spills: 167 ms per central group, against 194 ms at 5 and 234 ms at 6,
-// where its 80 registers spill in the pair loop), the FP32-weight form and
-// the mixed-event kernel at 6.
+// GB300, the FP64 form of the same-event kernel is fastest at 4 (128
+// registers, no spills: 152.7 ms per central group, against 158.8 ms at 5
+// with 96 registers and 216 ms at 6 with 80, both spilling), the
+// double-float form at 4 too (118 registers, no spills: 167 ms, against 194
+// ms at 5 and 234 ms at 6), the FP32-weight form and the mixed-event kernel
+// at 6.
 #ifndef HBT_FP64_SAME_CTAS
-#define HBT_FP64_SAME_CTAS 5  // compile-time choice for the FP64 form (-D to measure others)
+#define HBT_FP64_SAME_CTAS 4  // compile-time choice for the FP64 form (-D to measure others)
 #endif
 template <int PREC>
 struct SameCtas {
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, B
         }
         mixed_tile_pair<AZ, BOOST, MODE, QINV>(dd, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
                                          (long long)it.tj * FT, b.orig + la.off,
-                                         b.orig + lb.off);
+                                         b.orig + lb.off, job.row_base);
         __syncthreads();
     }
 }

@@ -210,6 +210,7 @@ bool BatchRunner::run_impl(const std::vector<FastJob> &jobs, const Device &d,
         b.ql_max = j.q_window * (1.0 + 1e-6) + 1e-300;
         b.boost = j.boost;
         b.qinv = j.qinv;
+        b.row_base = j.row_base;
         pair_off.push_back(pairs);
         pairs += b.n_pairs;
         bj.push_back(b);

@@ -23,6 +23,7 @@ struct FastJob {
     double q_window;     // Q = max(|lo|, |hi|) of the analysis' q window
     int boost;           // long_comoving_boost of the analysis
     int qinv;            // 1: the analysis bins q_inv histograms (no cull)
+    long long row_base;  // first row in a multi-job ordered admission (Caps::rows_total)
 };
 
 // Launch shape of a batch, chosen by hbt_set_tuning / hbt_autotune_batch.

@@ -324,7 +324,8 @@ __device__ __forceinline__ int kphi_screen(const Screen &S, const Q &q) {
                     1.0e-6f + S.psi_slack;
     float d = phi - S.psi;
     if (d < 0.0f) d += S.two_pi;
-    const float ed = 2.0f * e + 1.0e-6f;
+    // pairs within the host's deferral zone go to the reference chain too
+    const float ed = 2.0f * e + 1.0e-6f + S.kphi_tol;
     if (!(d > ed) || !(d < S.two_pi - ed)) return -2;
     const float r = d * S.inv_dKphi;
     const float er = ed * S.inv_dKphi + 4.0f * U * r;
@@ -1295,7 +1296,8 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
                                                 const double *const *l2, long long n2,
                                                 long long i0, long long j0,
                                                 const unsigned *orig1 = nullptr,
-                                                const unsigned *orig2 = nullptr) {
+                                                const unsigned *orig2 = nullptr,
+                                                long long row_base = 0) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     sm.fi[tid] = (i0 + tid < n1) ? make_float4((float)l1[0][i0 + tid], (float)l1[1][i0 + tid],
                                                (float)l1[2][i0 + tid], (float)l1[3][i0 + tid])
@@ -1314,6 +1316,10 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
     const int jend = (int)min((long long)FT, n2 - j0);
     unsigned *q = sm.queue[w];
     int count = 0;
+    // ordered admission: row stride of the survivor counts and key stride of
+    // the deferrals (several jobs admitted together, or this job alone)
+    const long long rows = d.caps.rows_total ? d.caps.rows_total : n1;
+    const long long cols = d.caps.cols_key ? d.caps.cols_key : n2;
 
     auto process = [&](unsigned e, bool valid) {
         if (!valid) return;
@@ -1330,17 +1336,17 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
             }
         }
         if (MODE != MODE_FAST) {
-            const long long row = orig1 ? (long long)orig1[i0 + qi] : i0 + qi;
+            const long long row = row_base + (orig1 ? (long long)orig1[i0 + qi] : i0 + qi);
             const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
             if (slot < 0) {
                 const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi],
                                      l1[3][i0 + qi]};
                 const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
                                      l2[3][j0 + qj]};
-                undecided_pair_ordered<true, MODE>(d, A, B, row, col, n1, n2);
+                undecided_pair_ordered<true, MODE>(d, A, B, row, col, rows, cols);
                 return;
             }
-            if (!admit<MODE>(d, slot, row, n1)) return;
+            if (!admit<MODE>(d, slot, row, rows)) return;
         }
         if (slot >= 0) {
             atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
@@ -1379,7 +1385,7 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
                     und = slot < 0;
                 }
                 und = und || c3 == 2 || cq == 2;
-                const long long row = orig1 ? (long long)orig1[i0 + qi] : i0 + qi;
+                const long long row = row_base + (orig1 ? (long long)orig1[i0 + qi] : i0 + qi);
                 const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
                 if (und) {
                     if (MODE == MODE_FAST) {
@@ -1389,13 +1395,13 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
                                              l1[3][i0 + qi]};
                         const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
                                              l2[3][j0 + qj]};
-                        undecided_pair_ordered<true, MODE>(d, A, B, row, col, n1, n2);
+                        undecided_pair_ordered<true, MODE>(d, A, B, row, col, rows, cols);
                     }
                 } else {
                     bool h3 = c3 == 1, hq = cq == 1;
                     if (MODE != MODE_FAST) {
-                        h3 = h3 && admit<MODE>(d, slot, row, n1);
-                        hq = hq && admit<MODE>(d, d.g.n_slots + iK, row, n1);
+                        h3 = h3 && admit<MODE>(d, slot, row, rows);
+                        hq = hq && admit<MODE>(d, d.g.n_slots + iK, row, rows);
                     }
                     if (h3) atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
                     if (hq) qkey = (unsigned)(iK * d.g.qnpts + kq);

@@ -72,7 +72,10 @@ typedef struct hbt_params {
      * FP32 test cannot decide) hands a pair's azimuthal bin to the host's
      * C-library atan2 instead of the device's; 0 selects the default
      * (1e-13).  The screened kernels decide the other pairs' bins in FP32
-     * with an error bound. */
+     * with an error bound.  At most 65536 pairs are handed over per launch,
+     * or per count pass of ordered cap admission (which covers all of a
+     * batch's mixed-event jobs); more raise HBT_ERR_DEVICE, which only a
+     * tolerance many orders above the default can reach. */
     double kphi_defer_tol;
     int32_t kernel; /* hbt_kernel */
 } hbt_params;

@@ -100,7 +100,30 @@ def test_batch_with_binding_caps_runs_in_reference_order():
     eng = E.Engine(**p)
     eng.bin_batch(jobs)
     h = _run_oracle(p, jobs)
-    assert (h["ctr_num"] == 31).any()
+    assert (h["ctr_num"] == 31).any() and (h["ctr_den"] == 31).any()
+    parity.compare(eng.hist(), h, _qscale(p))
+
+
+def test_batch_mixed_jobs_admitted_together():
+    """Binding caps on a batch of many mixed-event jobs: their pairs are
+    admitted together in the jobs' joint row order (one count pass, one cut
+    per slot and one order pass; each slot's cut row inside its own job),
+    with K_phi edges within a wide deferral tolerance (1e-3 rad: thousands of
+    pairs, within the 65536 a count pass may hand over) decided on the host.
+    Equal to the oracle binning the jobs one by one in the reference's
+    order."""
+    from hadronic_afterburner_toolkit_gb300 import engine as E
+    p = dict(BASE, azimuthal_flag=1, needed_number_of_pairs=40)
+    jobs = _uneven_jobs(seed=51, n_groups=3)
+    eng = E.Engine(kphi_defer_tol=1e-3, **p)
+    eng.set_psi_ref(0.4)
+    eng.bin_batch(jobs)
+    h = _run_oracle(p, jobs, psi=0.4)
+    assert (h["ctr_den"] == 41).any() and (h["ctr_den"] < 41).any()
+    st = eng.stats()
+    assert st["deferred_kphi"] > 0
+    # one admission for all mixed jobs, at most one per same-event job
+    assert st["ordered_passes"] <= 1 + sum(1 for j in jobs if j[0] == "same")
     parity.compare(eng.hist(), h, _qscale(p))
 
 

@@ -115,9 +115,10 @@ def test_binding_caps_admit_pairs_in_reference_order(az):
 
 @pytest.mark.parametrize("kernel", [0, 1])
 def test_kphi_edge_pairs_decided_on_host(kernel):
-    """A wide deferral zone sends many pairs of the reference chain through
-    the host atan2 path (the screened kernels decide a K_phi bin in FP32
-    when its error bound allows and hand the rest to the chain); bins must
+    """A wide deferral zone sends many pairs through the host atan2 path
+    (the screened kernels decide a K_phi bin in FP32 when its error bound
+    allows and the pair lies outside the zone, and hand the rest to the
+    reference chain, which defers the pairs inside the zone); bins must
     equal the oracle's exactly either way."""
     p = dict(FULL, kphi_defer_tol=0.05, kernel=kernel)
     eng, orc = _engine(**p), _oracle(**{k: v for k, v in p.items() if k != "kernel"})
@@ -132,8 +133,7 @@ def test_kphi_edge_pairs_decided_on_host(kernel):
     eng.bin_mixed(l1, l2)
     orc.bin_mixed(l1, l2)
     h = eng.hist()
-    if kernel == 1:
-        assert eng.stats()["deferred_kphi"] > 100
+    assert eng.stats()["deferred_kphi"] > 100
     parity.compare(h, orc.hist(), _qscale(p))
 
 

@@ -298,9 +298,10 @@ def test_small_configuration_with_a_binding_cap(small_run, azimuthal):
     which binds in the busiest K_T (x K_phi) slots within the first buffers:
     pairs are admitted in the reference's order (src/HBT_correlation.cpp
     :400-406, :651-655) through the batched kernels' count and order passes
-    plus the pair-by-pair cut row, one job at a time.  Counts, denominators
-    and counters identical to the oracle's buffer loop; K_phi edges decided
-    on the host take part in the order."""
+    plus the pair-by-pair cut row: each buffer's same-event job alone, its
+    mixed-event jobs together in their joint row order.  Counts,
+    denominators and counters identical to the oracle's buffer loop; K_phi
+    edges decided on the host take part in the order."""
     ev, bufs, _, jobs = small_run
     p = dict(SMALL, needed_number_of_pairs=1e6, azimuthal_flag=azimuthal, n_Kphi=4)
     orc = oracle_lib.Oracle(number_of_mixed_events=5, seed=1, **p)
