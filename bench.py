@@ -1376,9 +1376,14 @@ def main() -> None:
             if k > 0:
                 ms_tot += e0.elapsed_time(e1)
                 prs += group_pairs(groups[g])
+        st = engv.stats()
         engv.close()
-        return {"kernel": label, "value": prs / (ms_tot * 1e-3),
-                "ms_per_step": ms_tot / nsteps, "steps": nsteps}
+        out = {"kernel": label, "value": prs / (ms_tot * 1e-3),
+               "ms_per_step": ms_tot / nsteps, "steps": nsteps}
+        if batch and kernel == E.KERNEL_SCREENED:
+            # tile pairs of the last launch the cull kept, of the candidates
+            out["tiles_same_kept"] = [st["tiles_same_kept"], st["tiles_same"]]
+        return out
 
     # the plain form (FP64 reference chain on every pair, one call per list)
     # and the other forms, on the same GPU
@@ -1399,7 +1404,7 @@ def main() -> None:
             "screened, one launch per list, no sorting or culling", False)
         # the same workload with the q_inv histograms too
         # (invariant_radius_flag = 1): 1-D q_inv numerator and denominator
-        # beside the 3-D ones, every tile pair kept by the cull
+        # beside the 3-D ones, tile pairs kept for either window
         variants["batched-" + args.precision + "-qinv"] = time_variant(
             E.KERNEL_SCREENED, prec, 2,
             "batched persistent, with the q_inv histograms (invariant_radius_flag = 1)", True,

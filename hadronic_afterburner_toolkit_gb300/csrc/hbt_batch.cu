@@ -102,7 +102,7 @@ __global__ void k_boxes(BatchDev b) {
     const long long t = warp - l.tile_off;
     const long long s0 = l.off + t * FT, s1 = min(l.off + (t + 1) * FT, l.off + l.n);
     double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300, Y0 = 1e300, Y1 = -1e300, m0 = 1e300;
-    double z0 = 1e300, z1 = -1e300;
+    double z0 = 1e300, z1 = -1e300, mm0 = 1e300, mm1 = -1e300;
     for (long long s = s0 + lane; s < s1; s += 32) {
         const double px = b.table[s], py = b.table[b.cap + s];
         const double pz = b.table[2 * b.cap + s], E = b.table[3 * b.cap + s];
@@ -122,6 +122,14 @@ __global__ void k_boxes(BatchDev b) {
             Y1 = 1e300;
         }
         m0 = fmin(m0, m2 > 0.0 ? sqrt(m2) : 0.0);
+        const double mm = m2 - (px * px + py * py);
+        if (mm == mm) {
+            mm0 = fmin(mm0, mm);
+            mm1 = fmax(mm1, mm);
+        } else {
+            mm0 = -1e300;  // never treated as one mass
+            mm1 = 1e300;
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         x0 = fmin(x0, __shfl_xor_sync(0xffffffffu, x0, o));
@@ -133,30 +141,43 @@ __global__ void k_boxes(BatchDev b) {
         m0 = fmin(m0, __shfl_xor_sync(0xffffffffu, m0, o));
         z0 = fmin(z0, __shfl_xor_sync(0xffffffffu, z0, o));
         z1 = fmax(z1, __shfl_xor_sync(0xffffffffu, z1, o));
+        mm0 = fmin(mm0, __shfl_xor_sync(0xffffffffu, mm0, o));
+        mm1 = fmax(mm1, __shfl_xor_sync(0xffffffffu, mm1, o));
     }
-    if (lane == 0) b.boxes[warp] = Box{x0, x1, y0, y1, Y0, Y1, m0, z0, z1};
+    if (lane == 0) b.boxes[warp] = Box{x0, x1, y0, y1, Y0, Y1, m0, z0, z1, mm0, mm1};
 }
 
 // Can a pair with one particle in box a and one in box b pass the windows?
+// The 3-D windows bound q_x^2 + q_y^2 and |q_long|; the LCMS q_long of two
+// particles with transverse masses m_1, m_2 and rapidity gap dy is
+// 2 m_1 m_2 sinh(dy) / sqrt(m_1^2 + m_2^2 + 2 m_1 m_2 cosh(dy)), which
+// grows with dy, m_1 and m_2, so the boxes' smallest m_T and gap bound it
+// from below.  With q_inv histograms a pair may also pass the q_inv window:
+// for two particles of one mass q.K = 0, so in the LCMS
+// q_inv^2 = q_out^2 (1 - beta_T^2) + q_side^2 + q_long^2 >= q_long^2, and
+// only the q_long bound culls (tiles whose masses differ keep every pair).
 __device__ __forceinline__ bool boxes_may_pair(const BatchJob &b, const Box &a, const Box &c) {
-    if (b.qinv) return true;
+    const double gY = fmax(0.0, fmax(a.Y0 - c.Y1, c.Y0 - a.Y1));
+    double qlong_lcms = 0.0;  // lower bound of |q_long| in the LCMS
+    if (gY > 0.0) {
+        const double m1 = a.m0, m2 = c.m0;
+        qlong_lcms = 2.0 * m1 * m2 * sinh(gY) /
+                     sqrt(m1 * m1 + m2 * m2 + 2.0 * m1 * m2 * cosh(gY));
+    }
     const double gx = fmax(0.0, fmax(a.x0 - c.x1, c.x0 - a.x1));
     const double gy = fmax(0.0, fmax(a.y0 - c.y1, c.y0 - a.y1));
-    if (gx * gx + gy * gy > b.qt2_max) return false;
+    bool pass3 = !(gx * gx + gy * gy > b.qt2_max);
     if (b.boost) {
-        const double gY = fmax(0.0, fmax(a.Y0 - c.Y1, c.Y0 - a.Y1));
-        if (gY > 0.0) {
-            const double m1 = a.m0, m2 = c.m0;
-            const double f = 2.0 * m1 * m2 * sinh(gY) /
-                             sqrt(m1 * m1 + m2 * m2 + 2.0 * m1 * m2 * cosh(gY));
-            if (f > b.ql_max) return false;
-        }
+        pass3 = pass3 && !(qlong_lcms > b.ql_max);
     } else {
         // q_long = q_z
         const double gz = fmax(0.0, fmax(a.z0 - c.z1, c.z0 - a.z1));
-        if (gz > b.ql_max) return false;
+        pass3 = pass3 && !(gz > b.ql_max);
     }
-    return true;
+    if (pass3 || !b.qinv) return pass3;
+    const double lo = fmin(a.mm0, c.mm0), hi = fmax(a.mm1, c.mm1);
+    if (!(hi - lo <= 1e-9 * fabs(hi))) return true;
+    return !(qlong_lcms > b.ql_max);
 }
 
 // Momentum-space region of a tile pair's pairs: K = (p_1 + p_2) / 2 at the

@@ -29,8 +29,9 @@ struct BatchJob {
     double qt2_max;
     double ql_max;
     int boost;
-    // 1: the job's analysis bins q_inv histograms, whose window the 3-D
-    // bounds do not cover: every tile pair is kept
+    // 1: the job's analysis bins q_inv histograms: a tile pair is also kept
+    // when its pairs may fall in the q_inv window (the LCMS q_long bound,
+    // for tiles of one particle mass)
     int qinv;
     // ordered cap admission of several jobs at once: the job's first row in
     // the admission's row order (Caps::rows_total)
@@ -43,6 +44,7 @@ struct Box {
     double Y0, Y1;          // rapidity range
     double m0;              // smallest m_T = sqrt(E^2 - p_z^2)
     double z0, z1;          // p_z range
+    double mm0, mm1;        // range of the mass squared E^2 - |p|^2
 };
 
 struct Item {

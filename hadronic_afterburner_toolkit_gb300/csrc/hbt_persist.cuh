@@ -49,8 +49,9 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
 
 // Resident CTAs per SM (register budget 65536 / (128 x CTAs)): measured on
 // GB300, the FP64 form of the same-event kernel is fastest at 4 (128
-// registers, no spills: 152.7 ms per central group, against 158.8 ms at 5
-// with 96 registers and 216 ms at 6 with 80, both spilling), the
+// registers, no spills: 152.7 ms per central group, against 173.6 ms at 3
+// with 164 registers, 158.8 ms at 5 with 96 and 216 ms at 6 with 80, the
+// last two spilling), the
 // double-float form at 4 too (118 registers, no spills: 167 ms, against 194
 // ms at 5 and 234 ms at 6), the FP32-weight form and the mixed-event kernel
 // at 6.
