@@ -18,9 +18,11 @@
 //                2 m_T1 m_T2 cosh(y1 - y2)),
 //     which grows with m_T1, m_T2 and |y1 - y2|, so its smallest value over
 //     two tiles bounds |q_long| from below; without the boost q_long = q_z.
-//     Each bound carries a 1e-6 relative margin for rounding;
+//     With q_inv histograms the LCMS q_long bound alone also keeps a tile
+//     pair (boxes_may_pair).  Each bound carries a 1e-6 relative margin for
+//     rounding;
 //  4. k_persistent_same / k_persistent_mixed (hbt_persist.cuh): persistent
-//     CTAs (5 per SM) pull (job, i-tile, j-tile) items from the culled
+//     CTAs (4 to 6 per SM) pull (job, i-tile, j-tile) items from the culled
 //     same-event and mixed-event queues and run the screened tile-pair
 //     bodies of hbt_tile.cuh.  The FP32-weight form runs the same-event
 //     queue in chunks and merges the FP32 partials between them.
