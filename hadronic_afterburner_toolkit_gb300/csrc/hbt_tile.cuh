@@ -752,6 +752,10 @@ struct TileSmemT {
     // swap, undecided, 3-D event, q_inv event) bits, y = q bin, z = slot |
     // K_T bin << 16, w = q_inv bin
     E2 queue2[FT / 32][QCAP];
+    // pairs the screen left undecided, (i, j, swap) bits: the reference
+    // chain runs on them 32 at a time (inline, a warp would run it for the
+    // one or two lanes holding such a pair)
+    unsigned queue3[FT / 32][QCAP];
     unsigned oi[FT], oj[FT];  // original list positions (pair orientation)
     float offi[4], offj[4];   // double-float form: the tiles' momentum offsets
 };
@@ -862,7 +866,7 @@ __device__ __noinline__ void undecided_pair32(const Device &d, const double *A, 
     }
 }
 
-// A same-event pair of the double-float form that the screens left
+// A same-event pair of the FP64 or double-float form that the screens left
 // undecided: the reference chain decides and bins it with FP64 values.  Out
 // of line, so that the chain's registers do not spill in the pair loop.
 static __device__ __noinline__ void undecided_pair64(const Device &d, const double *A,
@@ -1133,32 +1137,48 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
         drain(q, count, lane, screen_q);
         drain(q2, count2, lane, values_q);
     } else {
-        // stage C for 32 screened pairs (all lanes of the warp in step)
-        auto values = [&](uint2 e2, bool valid) {
+        unsigned *q3 = sm.queue3[w];
+        int count3 = 0;
+        // stage D for 32 pairs the screen left undecided: the reference chain
+        // decides them (and may hand a K_phi edge to the host), from the FP64
+        // tile or (FP32-weight and double-float forms) the FP64 columns
+        auto chains = [&](unsigned e, bool valid) {
             if (!valid) return;
-            const unsigned e = e2.x;
             const int qi = e & 0xff, qj = (e >> 8) & 0xff;
             const bool swap = (e >> 16) & 1u;
-            const int slot = (e >> 17) & 1u ? -1 : (int)(e >> 18);
-            const int bin = (int)e2.y;
+            double A[8], B[8];  // first and second particle of the pair
+#pragma unroll
+            for (int f = 0; f < 8; f++) {
+                const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+                const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+                A[f] = swap ? v : u;
+                B[f] = swap ? u : v;
+            }
             if (MODE != MODE_FAST) {
                 const long long oa = sm.oi[qi], ob = sm.oj[qj];
                 const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
-                if (slot < 0) {
-                    double A[8], B[8];
-#pragma unroll
-                    for (int f = 0; f < 8; f++) {
-                        const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
-                        const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
-                        A[f] = swap ? v : u;
-                        B[f] = swap ? u : v;
-                    }
-                    undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
-                    return;
-                }
+                undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
+                return;
+            }
+            if (PREC == 1)
+                undecided_pair32<BOOST>(d, A, B, i0 + qi, j0 + qj, n);
+            else
+                undecided_pair64(d, A, B, i0 + qi, j0 + qj, n);
+        };
+
+        // stage C for one decided pair: its values into its bin
+        auto decided = [&](uint2 e2) {
+            const unsigned e = e2.x;
+            const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+            const bool swap = (e >> 16) & 1u;
+            const int slot = (int)(e >> 18);
+            const int bin = (int)e2.y;
+            if (MODE != MODE_FAST) {
+                const long long oa = sm.oi[qi], ob = sm.oj[qj];
+                const long long row = oa < ob ? oa : ob;
                 if (!admit<MODE>(d, slot, row, n)) return;
             }
-            if (PREC == 1 && slot >= 0) {
+            if (PREC == 1) {
                 // the pair as stored (i, j); swapping first and second negates
                 // q_out, q_side, q_long exactly and leaves the phase unchanged
                 float2 a[8], b[8];
@@ -1178,26 +1198,17 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                 atomicAdd(d.h.cnt + at, 1ull);
                 return;
             }
-            if (PREC == 2 && slot >= 0) {
+            double vo, vs, vl, vw;
+            if (PREC == 2) {
                 float2 a[8], b[8];
 #pragma unroll
                 for (int f = 0; f < 8; f++) {
                     a[f] = spi[f][qi];
                     b[f] = spj[f][qj];
                 }
-                double vo, vs, vl, vw;
                 values_df<BOOST>(d.s, reinterpret_cast<const float4 *>(cs), a, b, sm.offi, sm.offj,
                                  swap, vo, vs, vl, vw);
-                const long long at = (long long)slot * d.g.q3 + bin;
-                Sums *h = d.h.sums + at;
-                atomicAdd(&h->qo, vo);
-                atomicAdd(&h->qs, vs);
-                atomicAdd(&h->ql, vl);
-                atomicAdd(&h->w, vw);
-                atomicAdd(d.h.cnt + at, 1ull);
-                return;
-            }
-            if (PREC == 0 && slot >= 0) {
+            } else {
                 // the pair in the reference's orientation, from the FP64 tile
                 double A[8], B[8];
 #pragma unroll
@@ -1206,49 +1217,24 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                     A[f] = swap ? v : u;
                     B[f] = swap ? u : v;
                 }
-                double vo, vs, vl, vw;
                 values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
-                const long long at = (long long)slot * d.g.q3 + bin;
-                Sums *h = d.h.sums + at;
-                atomicAdd(&h->qo, vo);
-                atomicAdd(&h->qs, vs);
-                atomicAdd(&h->ql, vl);
-                atomicAdd(&h->w, vw);
-                atomicAdd(d.h.cnt + at, 1ull);
-                return;
             }
-            // a pair the window screen left undecided: the pair in the
-            // reference's orientation, from the FP64 tile or (FP32-weight and
-            // double-float forms) the FP64 columns themselves
-            double A[8], B[8];  // first and second particle of the pair
-#pragma unroll
-            for (int f = 0; f < 8; f++) {
-                const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
-                const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
-                A[f] = swap ? v : u;
-                B[f] = swap ? u : v;
-            }
-            if (PREC == 1) {
-                undecided_pair32<BOOST>(d, A, B, i0 + qi, j0 + qj, n);
-                return;
-            }
-            if (PREC == 2) {
-                undecided_pair64(d, A, B, i0 + qi, j0 + qj, n);
-                return;
-            }
-            {
-                // undecided somewhere: the reference chain decides (and may hand
-                // a K_phi edge to the host)
-                const Chain full = pair_chain<false>(d.g, A[0], A[1], A[2], A[3], B[0], B[1], B[2],
-                                                     B[3], A + 4, B + 4);
-                if (PREC != 1 || full.ev3 != 1) {
-                    consume<false, MODE_FAST>(d, i0 + qi, j0 + qj, n, n, full);
-                } else {
-                    const long long at = (long long)full.slot * d.g.q3 + full.bin;
-                    atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
-                    atomicAdd(d.h.cnt + at, 1ull);
-                }
-            }
+            const long long at = (long long)slot * d.g.q3 + bin;
+            Sums *h = d.h.sums + at;
+            atomicAdd(&h->qo, vo);
+            atomicAdd(&h->qs, vs);
+            atomicAdd(&h->ql, vl);
+            atomicAdd(&h->w, vw);
+            atomicAdd(d.h.cnt + at, 1ull);
+        };
+
+        // stage C for 32 screened pairs (all lanes of the warp in step): the
+        // decided pairs' values, then the undecided ones to stage D's queue
+        // (last, so that stage D runs with nothing of stage C live)
+        auto values = [&](uint2 e2, bool valid) {
+            const bool undecided = valid && ((e2.x >> 17) & 1u);
+            if (valid && !undecided) decided(e2);
+            enqueue(q3, count3, undecided, e2.x & 0x1ffffu, lane, chains);
         };
 
         // stage B for 32 prefiltered pairs: window screen and bins; the pairs
@@ -1282,6 +1268,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
         }
         drain(q, count, lane, screen);
         drain(q2, count2, lane, values);
+        drain(q3, count3, lane, chains);
     }
 }
 
@@ -1321,12 +1308,30 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
     const long long rows = d.caps.rows_total ? d.caps.rows_total : n1;
     const long long cols = d.caps.cols_key ? d.caps.cols_key : n2;
 
-    auto process = [&](unsigned e, bool valid) {
+    // pairs the screen left undecided, 32 at a time: the reference chain
+    // decides (inline, a warp would run it for one or two lanes)
+    unsigned *q3 = sm.queue3[w];
+    int count3 = 0;
+    auto chains = [&](unsigned e, bool valid) {
         if (!valid) return;
+        const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+        if (MODE != MODE_FAST) {
+            const long long row = row_base + (orig1 ? (long long)orig1[i0 + qi] : i0 + qi);
+            const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
+            const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi], l1[3][i0 + qi]};
+            const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj], l2[3][j0 + qj]};
+            undecided_pair_ordered<true, MODE>(d, A, B, row, col, rows, cols);
+        } else {
+            undecided_mixed_pair(d, l1, l2, i0 + qi, j0 + qj, n1, n2);
+        }
+    };
+
+    // one screened pair: its denominator bin, or undecided (true)
+    auto screened = [&](unsigned e) -> bool {
         const int qi = e & 0xff, qj = (e >> 8) & 0xff;
         Q s;
         const int wcls = screen_windows<BOOST>(S, sm.fi[qi], sm.fj[qj], s);
-        if (wcls == 0) return;
+        if (wcls == 0) return false;
         int iK = 0, bin = 0, slot = -1;
         if (wcls == 1 && decide_bins(S, s, iK, bin)) {
             slot = iK;
@@ -1335,24 +1340,19 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
                 slot = ip < 0 ? -1 : iK * d.g.n_Kphi + ip;
             }
         }
+        if (slot < 0) return true;
         if (MODE != MODE_FAST) {
             const long long row = row_base + (orig1 ? (long long)orig1[i0 + qi] : i0 + qi);
-            const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
-            if (slot < 0) {
-                const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi],
-                                     l1[3][i0 + qi]};
-                const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
-                                     l2[3][j0 + qj]};
-                undecided_pair_ordered<true, MODE>(d, A, B, row, col, rows, cols);
-                return;
-            }
-            if (!admit<MODE>(d, slot, row, rows)) return;
+            if (!admit<MODE>(d, slot, row, rows)) return false;
         }
-        if (slot >= 0) {
-            atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
-        } else {
-            undecided_mixed_pair(d, l1, l2, i0 + qi, j0 + qj, n1, n2);
-        }
+        atomicAdd(d.h.den + (long long)slot * d.g.q3 + bin, 1ull);
+        return false;
+    };
+
+    // 32 prefiltered pairs (all lanes of the warp in step)
+    auto process = [&](unsigned e, bool valid) {
+        const bool undecided = valid && screened(e);
+        enqueue(q3, count3, undecided, e, lane, chains);
     };
 
     if constexpr (QINV) {
@@ -1422,6 +1422,7 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
             enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process);
         }
         drain(q, count, lane, process);
+        drain(q3, count3, lane, chains);
     }
 }
 
