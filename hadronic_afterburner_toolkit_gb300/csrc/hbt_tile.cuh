@@ -992,6 +992,30 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
     if constexpr (QINV) {
         // stage C with q_inv histograms, for 32 screened pairs: the 3-D event
         // and the q_inv event of each pair (cos(q.dx) computed once for both)
+        unsigned *q3 = sm.queue3[w];
+        int count3 = 0;
+        // the pairs left undecided, 32 at a time: the reference chain
+        // decides both events
+        auto chains_q = [&](unsigned e, bool valid) {
+            if (!valid) return;
+            const int qi = e & 0xff, qj = (e >> 8) & 0xff;
+            const bool swap = (e >> 16) & 1u;
+            double A[8], B[8];  // first and second particle of the pair
+#pragma unroll
+            for (int f = 0; f < 8; f++) {
+                const double u = PREC == 0 ? sm.si[f][qi] : c[f][i0 + qi];
+                const double v = PREC == 0 ? sm.sj[f][qj] : c[f][j0 + qj];
+                A[f] = swap ? v : u;
+                B[f] = swap ? u : v;
+            }
+            if (MODE == MODE_FAST) {
+                undecided_pair_ordered<false, MODE_FAST>(d, A, B, i0 + qi, j0 + qj, n, n);
+            } else {
+                const long long oa = sm.oi[qi], ob = sm.oj[qj];
+                const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
+                undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
+            }
+        };
         auto values_q = [&](uint4 e4, bool valid) {
             // this lane's q_inv event, added per group of lanes at the end
             unsigned qkey = 0xffffffffu;
@@ -1011,15 +1035,10 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                 B[f] = swap ? u : v;
             }
             const long long oa = sm.oi[qi], ob = sm.oj[qj];
-            const long long row = oa < ob ? oa : ob, col = oa < ob ? ob : oa;
-            if (valid && ((e >> 17) & 1u)) {
-                // undecided: the reference chain decides both events
-                if (MODE == MODE_FAST)
-                    undecided_pair_ordered<false, MODE_FAST>(d, A, B, i0 + qi, j0 + qj, n, n);
-                else
-                    undecided_pair_ordered<false, MODE>(d, A, B, row, col, n, n);
-                has3 = hasq = false;
-            }
+            const long long row = oa < ob ? oa : ob;
+            // undecided: both events wait for the reference chain (stage D)
+            const bool undecided = valid && ((e >> 17) & 1u);
+            if (undecided) has3 = hasq = false;
             if (MODE != MODE_FAST) {
                 has3 = has3 && admit<MODE>(d, slot, row, n);
                 hasq = hasq && admit<MODE>(d, d.g.n_slots + iK, row, n);
@@ -1079,6 +1098,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                 }
             }
             qinv_update(d, qkey, qsum, qw, true);
+            enqueue(q3, count3, undecided, e & 0x1ffffu, lane, chains_q);
         };
 
         // stage B with q_inv histograms: the K_T window and bin, the 3-D
@@ -1136,6 +1156,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
         }
         drain(q, count, lane, screen_q);
         drain(q2, count2, lane, values_q);
+        drain(q3, count3, lane, chains_q);
     } else {
         unsigned *q3 = sm.queue3[w];
         int count3 = 0;
@@ -1360,6 +1381,7 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
         auto process_q = [&](unsigned e, bool valid) {
             const int qi = e & 0xff, qj = (e >> 8) & 0xff;
             unsigned qkey = 0xffffffffu;  // this lane's q_inv denominator bin
+            bool undecided = false;       // both events wait for the chain
             if (valid) {
                 Q s;
                 const int kt = screen_kt(S, sm.fi[qi], sm.fj[qj], s);
@@ -1386,18 +1408,8 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
                 }
                 und = und || c3 == 2 || cq == 2;
                 const long long row = row_base + (orig1 ? (long long)orig1[i0 + qi] : i0 + qi);
-                const long long col = orig2 ? (long long)orig2[j0 + qj] : j0 + qj;
-                if (und) {
-                    if (MODE == MODE_FAST) {
-                        undecided_mixed_pair(d, l1, l2, i0 + qi, j0 + qj, n1, n2);
-                    } else {
-                        const double A[4] = {l1[0][i0 + qi], l1[1][i0 + qi], l1[2][i0 + qi],
-                                             l1[3][i0 + qi]};
-                        const double B[4] = {l2[0][j0 + qj], l2[1][j0 + qj], l2[2][j0 + qj],
-                                             l2[3][j0 + qj]};
-                        undecided_pair_ordered<true, MODE>(d, A, B, row, col, rows, cols);
-                    }
-                } else {
+                undecided = und;
+                if (!und) {
                     bool h3 = c3 == 1, hq = cq == 1;
                     if (MODE != MODE_FAST) {
                         h3 = h3 && admit<MODE>(d, slot, row, rows);
@@ -1408,6 +1420,7 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
                 }
             }
             qinv_update(d, qkey, 0.0, 0.0, false);
+            enqueue(q3, count3, undecided, e, lane, chains);
         };
 
         for (int jj = 0; jj < jend; jj++) {
@@ -1416,6 +1429,7 @@ __device__ __forceinline__ void mixed_tile_pair(const Device &d, SM &sm,
             enqueue(q, count, take, (unsigned)il | ((unsigned)jj << 8), lane, process_q);
         }
         drain(q, count, lane, process_q);
+        drain(q3, count3, lane, chains);
     } else {
         for (int jj = 0; jj < jend; jj++) {
             const bool take = active && prefilter<BOOST>(S, a, ga, sm.fj[jj], sm.gj[jj]);
