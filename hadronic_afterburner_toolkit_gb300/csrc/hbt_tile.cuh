@@ -704,22 +704,24 @@ __device__ __forceinline__ void values_df(const Screen &S, const float4 *tab, co
 // and the boosted q_long, which are only summed, follow in double-float on
 // the FP32 pipe (ff_lcms: about 1e-14 relative) from the FP64 sums and
 // differences split on the integer pipe, and come back as FP64 with one
-// addition each.  Of the FP64 pipe, which bounds this form, a binned pair
-// then takes 29 to 31 instructions instead of 55.
+// addition each.  The longitudinal sums sz = p_z1 + p_z2 and sE = E_1 + E_2
+// (used with the boost only) come in as double-float sums of the particles'
+// split values (2^-47 of the sum: sE does not cancel, and sz enters q_long
+// through sz dE and M_T^2 = (sE - sz)(sE + sz), where its absolute error
+// stays below 1e-14 GeV).  Of the FP64 pipe, which bounds this form, a
+// binned pair then takes 27 to 29 instructions instead of 55.
 template <bool BOOST>
 __device__ __forceinline__ void values64(const Grid &g, const double2 *cs, const double *a,
-                                         const double *b, double &qo, double &qs, double &ql,
-                                         double &w) {
+                                         const double *b, FF sz, FF sE, double &qo, double &qs,
+                                         double &ql, double &w) {
     const double dx = a[0] - b[0], dy = a[1] - b[1];
     const double dz = a[2] - b[2], dE = a[3] - b[3];
     FF dp[4] = {f64_to_ff_bits(dx), f64_to_ff_bits(dy), f64_to_ff_bits(dz), f64_to_ff_bits(dE)};
     FF sp[4];
     sp[0] = f64_to_ff_bits(a[0] + b[0]);
     sp[1] = f64_to_ff_bits(a[1] + b[1]);
-    if (BOOST) {
-        sp[2] = f64_to_ff_bits(a[2] + b[2]);
-        sp[3] = f64_to_ff_bits(a[3] + b[3]);
-    }
+    sp[2] = sz;
+    sp[3] = sE;
     FF vo, vs, vl;
     ff_lcms<BOOST>(dp, sp, vo, vs, vl);
     qo = ff_double_bits(vo);
@@ -746,6 +748,9 @@ struct TileSmemT {
     float4 fj[FT];     // FP32 momenta of the j-tile
     float2 gi[FT];     // (|px| + |py|, |pz|) of the i-tile (prefilter)
     float2 gj[FT];
+    // FP64 form: FP32 low parts of p_z and E (their high parts are fi, fj's
+    // z and w), for the longitudinal sums in double-float
+    float2 li[FT], lj[FT];
     unsigned queue[FT / 32][QCAP];
     // same-event pairs that passed the window screen: x = (i, j, swap,
     // undecided, slot) bits, y = q bin (bin_entry); with q_inv, x = (i, j,
@@ -936,6 +941,12 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                                  (float)sm.si[3][tid]);
         sm.fj[tid] = make_float4((float)sm.sj[0][tid], (float)sm.sj[1][tid], (float)sm.sj[2][tid],
                                  (float)sm.sj[3][tid]);
+        if (BOOST) {
+            sm.li[tid] = make_float2((float)(sm.si[2][tid] - (double)sm.fi[tid].z),
+                                     (float)(sm.si[3][tid] - (double)sm.fi[tid].w));
+            sm.lj[tid] = make_float2((float)(sm.sj[2][tid] - (double)sm.fj[tid].z),
+                                     (float)(sm.sj[3][tid] - (double)sm.fj[tid].w));
+        }
     } else if (PREC == 1) {
         for (int f = 0; f < 8; f++) {
             spi[f][tid] = split((i0 + tid < n) ? c[f][i0 + tid] : 0.0);
@@ -1067,7 +1078,14 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                 } else {
                     double vo, vs, vl;
                     if (PREC == 0) {
-                        values64<BOOST>(d.g, cs, A, B, vo, vs, vl, wq);
+                        FF sz = {0.0f, 0.0f}, sE = {0.0f, 0.0f};
+                        if (BOOST) {
+                            const float4 fa = sm.fi[qi], fb = sm.fj[qj];
+                            const float2 la = sm.li[qi], lb = sm.lj[qj];
+                            sz = ff_sum(make_float2(fa.z, la.x), make_float2(fb.z, lb.x));
+                            sE = ff_sum(make_float2(fa.w, la.y), make_float2(fb.w, lb.y));
+                        }
+                        values64<BOOST>(d.g, cs, A, B, sz, sE, vo, vs, vl, wq);
                     } else {
                         float2 a[8], b[8];
 #pragma unroll
@@ -1238,7 +1256,14 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                     A[f] = swap ? v : u;
                     B[f] = swap ? u : v;
                 }
-                values64<BOOST>(d.g, cs, A, B, vo, vs, vl, vw);
+                FF sz = {0.0f, 0.0f}, sE = {0.0f, 0.0f};
+                if (BOOST) {
+                    const float4 fa = sm.fi[qi], fb = sm.fj[qj];
+                    const float2 la = sm.li[qi], lb = sm.lj[qj];
+                    sz = ff_sum(make_float2(fa.z, la.x), make_float2(fb.z, lb.x));
+                    sE = ff_sum(make_float2(fa.w, la.y), make_float2(fb.w, lb.y));
+                }
+                values64<BOOST>(d.g, cs, A, B, sz, sE, vo, vs, vl, vw);
             }
             const long long at = (long long)slot * d.g.q3 + bin;
             Sums *h = d.h.sums + at;
