@@ -1249,12 +1249,14 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                                  swap, vo, vs, vl, vw);
             } else {
                 // the pair in the reference's orientation, from the FP64 tile
+                // (the two rows chosen once, then read column by column)
+                const double *ra = swap ? &sm.sj[0][qj] : &sm.si[0][qi];
+                const double *rb = swap ? &sm.si[0][qi] : &sm.sj[0][qj];
                 double A[8], B[8];
 #pragma unroll
                 for (int f = 0; f < 8; f++) {
-                    const double u = sm.si[f][qi], v = sm.sj[f][qj];
-                    A[f] = swap ? v : u;
-                    B[f] = swap ? u : v;
+                    A[f] = ra[f * FT];
+                    B[f] = rb[f * FT];
                 }
                 FF sz = {0.0f, 0.0f}, sE = {0.0f, 0.0f};
                 if (BOOST) {
