@@ -170,9 +170,12 @@ typedef struct hbt_job {
  * (job, i-tile, j-tile) items - the pair loops of many
  * combine_and_bin_particle_pairs / _mixed_events calls at once
  * (src/HBT_correlation.cpp:282-461, :554-689).  The result equals calling
- * hbt_bin_same / hbt_bin_mixed for each job in order; when a pair cap could
- * bind, the jobs are run one by one to keep the reference's admission
- * order.  hbt_bin_batch takes host arrays, hbt_bin_batch_dev device arrays. */
+ * hbt_bin_same / hbt_bin_mixed for each job in order.  When a pair cap could
+ * bind, the reference's admission order is kept: the same-event jobs are
+ * admitted one by one, the mixed-event jobs together in their joint order
+ * (one count and one order pass over all of them; the numerator and
+ * denominator caps are separate, so the two kinds do not interact).
+ * hbt_bin_batch takes host arrays, hbt_bin_batch_dev device arrays. */
 hbt_status hbt_bin_batch(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs);
 hbt_status hbt_bin_batch_dev(hbt_ctx *ctx, int32_t n_jobs, const hbt_job *jobs);
 
