@@ -24,9 +24,12 @@
 //     work of stage C again runs on 32 pairs at a time.
 //  C. Histogram update.  Mixed pairs add 1 to their denominator bin.
 //     Same-event pairs add q_out, q_side, q_long and cos(q.dx / hbarC):
-//       FP64 form  - FP64 values from algebraically identical expressions
-//                    (q_out = (q_x S_x + q_y S_y) / |S|, ...) and a
-//                    table-driven FP64 cos (table_cos, hbt_math.cuh);
+//       FP64 form  - the phase q.dx and its cos in FP64 (table_cos,
+//                    hbt_math.cuh, of the unrounded product with 1/hbarC);
+//                    q_out, q_side, q_long from algebraically identical
+//                    expressions (q_out = (q_x S_x + q_y S_y) / |S|, ...) in
+//                    double-float on the FP32 pipe, from the FP64 sums and
+//                    differences (values64);
 //       FP32W form - each FP64 column split once per tile into hi + lo
 //                    FP32 parts; differences and the phase in double-float
 //                    arithmetic on the FP32 pipe, q values in FP32, cos by
@@ -39,6 +42,8 @@
 //     and position difference, so it negates q_out, q_side, q_long exactly
 //     (IEEE rounding is symmetric in sign) and leaves the phase and its cos
 //     unchanged.
+//  D. Pairs left undecided in B go to a third per-warp queue; the reference
+//     chain runs on them 32 at a time.
 //
 // Error analysis (u = 2^-24).  Inputs are FP64 values v rounded once to
 // FP32: |v32 - v| <= u|v|.  For s = a +- b in FP32, |s - S| <= 2.01 u A with

@@ -139,6 +139,32 @@ def test_batch_fp32w_counts_exact():
     assert worst["num"] < 1e-6
 
 
+def test_batch_counts_do_not_depend_on_the_schedule():
+    """The histogram updates are atomic and every pair is visited once, so
+    counts, denominators and counters come out the same whatever the number
+    of persistent CTAs, the sort cells or the item order (the sums agree to
+    rounding: their order changes)."""
+    from hadronic_afterburner_toolkit_gb300 import engine as E
+    p = dict(BASE, azimuthal_flag=1)
+    jobs = _uneven_jobs(seed=61, n_groups=3)
+    ref = None
+    for bps, cell, order in ((0, 0.02, 1), (1, 0.02, 0), (2, 0.01, 1), (3, 0.04, 0),
+                             (5, 0.02, 1), (8, 0.01, 0)):
+        eng = E.Engine(**p)
+        eng.set_tuning(blocks_per_sm=bps, cell_pt=cell, order_items=order)
+        eng.set_psi_ref(0.25)
+        eng.bin_batch(jobs)
+        h = eng.hist()
+        eng.close()
+        if ref is None:
+            ref = h
+            continue
+        for k in ("count", "den", "ctr_num", "ctr_den"):
+            assert np.array_equal(h[k], ref[k]), (k, bps, cell, order)
+        for k in ("q_out", "q_side", "q_long", "num"):
+            np.testing.assert_allclose(h[k], ref[k], rtol=0, atol=1e-12 * (ref["count"].max() + 1))
+
+
 def test_batch_device_resident():
     torch = pytest.importorskip("torch")
     from hadronic_afterburner_toolkit_gb300 import engine as E
