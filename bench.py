@@ -689,9 +689,11 @@ def capped_leg(E, torch, dev, dgroups, groups, p, local, uncapped_ms, cap=3e7, n
     needed_number_of_pairs = 3e7 (parameters.dat), which binds in the first
     group: every job runs the two passes of ordered cap admission (count
     survivors per row, admit the rows before each slot's cut) on the batched
-    kernels, and the cut rows pair by pair, one job at a time in the
-    reference's order.  Later groups find most slots full.  Device-resident
-    inputs, CUDA events around each group."""
+    kernels, and the cut rows pair by pair in the reference's order: the
+    same-event job alone, the group's mixed-event jobs together in their
+    joint row order.  Later groups find the busiest slots full; the passes'
+    tile cull skips tile pairs whose pairs can reach only full slots.
+    Device-resident inputs, CUDA events around each group."""
     eng = E.Engine(device=local, **dict(p, needed_number_of_pairs=cap))
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
@@ -716,8 +718,9 @@ def capped_leg(E, torch, dev, dgroups, groups, p, local, uncapped_ms, cap=3e7, n
             "first_group_vs_uncapped": ms[0] / uncapped_ms,
             "slots_at_cap": int((ctr["num"] > cap).sum()),
             "ordered_passes": st["ordered_passes"],
-            "path": "count and order passes on the batched screened kernels, cut rows "
-                    "by the pair-order kernel, jobs one at a time"}
+            "path": "count and order passes on the batched screened kernels (tile pairs "
+                    "reaching only full slots skipped), cut rows by the pair-order kernel; "
+                    "same-event job alone, mixed-event jobs together"}
 
 
 def ingest_leg(n_events: int = 200, seed: int = 3) -> dict:

@@ -198,9 +198,67 @@ __device__ __forceinline__ unsigned region_key(const BatchJob &job, const Box &a
     return (dev << 11) | (kc << 5) | pc;
 }
 
+// Ordered cap admission: the 3-D slots already at their cap (of the pass's
+// counter family) and the grid constants that map a tile pair to the slots
+// its pairs can reach.  full == nullptr: no slot test.
+struct SlotCull {
+    const unsigned char *full;
+    double KT_min, dKT, KT_min_sq, KT_max_sq, psi, dKphi, two_pi;
+    int n_KT, n_Kphi, az;
+};
+
+// Can the pairs of boxes a and c reach only slots already at their cap?
+// K = (p_1 + p_2) / 2 lies in the rectangle of the boxes' mean p_x, p_y
+// ranges: its K_T range (nearest and farthest points) gives the K_T bins the
+// reference can assign (K_perp^2 in [KT_min^2, KT_max^2], src/HBT_correlation.cpp
+// :323-366), its angle range the K_phi bins (:408-422), each widened by a
+// margin far above rounding.  A rectangle that holds the origin is never
+// skipped (its pairs may have K_perp = 0, counted as anomalies).  Admission
+// admits nothing more in a full slot, so such a tile pair needs neither the
+// count nor the order pass.
+__device__ bool slots_all_full(const SlotCull &sc, const Box &a, const Box &c) {
+    const double x0 = 0.5 * (a.x0 + c.x0), x1 = 0.5 * (a.x1 + c.x1);
+    const double y0 = 0.5 * (a.y0 + c.y0), y1 = 0.5 * (a.y1 + c.y1);
+    if (x0 <= 0.0 && x1 >= 0.0 && y0 <= 0.0 && y1 >= 0.0) return false;
+    const double nx = x0 > 0.0 ? x0 : (x1 < 0.0 ? x1 : 0.0);
+    const double ny = y0 > 0.0 ? y0 : (y1 < 0.0 ? y1 : 0.0);
+    const double fx = fmax(fabs(x0), fabs(x1)), fy = fmax(fabs(y0), fabs(y1));
+    const double k2lo = (nx * nx + ny * ny) * (1.0 - 1e-9), k2hi = (fx * fx + fy * fy) * (1.0 + 1e-9);
+    if (k2hi < sc.KT_min_sq || k2lo > sc.KT_max_sq) return true;  // no pair in the K_T window
+    const double klo = sqrt(fmax(k2lo, sc.KT_min_sq)), khi = sqrt(fmin(k2hi, sc.KT_max_sq));
+    const int i0 = max(0, (int)floor((klo - sc.KT_min) / sc.dKT - 1e-6));
+    const int i1 = min(sc.n_KT - 1, (int)floor((khi - sc.KT_min) / sc.dKT + 1e-6));
+    if (!sc.az) {
+        for (int k = i0; k <= i1; k++)
+            if (!sc.full[k]) return false;
+        return true;
+    }
+    // the angle range around the centre's direction (under pi: the
+    // rectangle does not hold the origin), as bins modulo n_Kphi
+    const double cth = atan2(0.5 * (y0 + y1), 0.5 * (x0 + x1));
+    const double cx[4] = {x0, x1, x0, x1}, cy[4] = {y0, y0, y1, y1};
+    double lo = 0.0, hi = 0.0;
+    for (int q = 0; q < 4; q++) {
+        const double da = remainder(atan2(cy[q], cx[q]) - cth, sc.two_pi);
+        lo = fmin(lo, da);
+        hi = fmax(hi, da);
+    }
+    double u = cth + lo - 1e-6 - sc.psi;
+    u -= sc.two_pi * floor(u / sc.two_pi);
+    const int p0 = (int)floor(u / sc.dKphi);
+    const int p1 = (int)floor((u + hi - lo + 2e-6) / sc.dKphi);
+    const int np = min(sc.n_Kphi, p1 - p0 + 1);
+    for (int k = i0; k <= i1; k++)
+        for (int t = 0; t < np; t++) {
+            const int ip = ((p0 + t) % sc.n_Kphi + sc.n_Kphi) % sc.n_Kphi;  // u may round below 0
+            if (!sc.full[k * sc.n_Kphi + ip]) return false;
+        }
+    return true;
+}
+
 // Culled queues: same-event items at items[0, same_cap), mixed-event items
 // at items[same_cap, same_cap + mixed_cap); n_items[0] / n_items[1] count them.
-__global__ void k_cull(BatchDev b) {
+__global__ void k_cull(BatchDev b, SlotCull sc) {
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < b.total_pairs;
          p += (long long)gridDim.x * blockDim.x) {
         const int J = find_range(b.pair_off, b.n_jobs, p);
@@ -216,7 +274,7 @@ __global__ void k_cull(BatchDev b) {
         }
         const Box &A = b.boxes[b.lists[job.la].tile_off + ti];
         const Box &B = b.boxes[b.lists[job.lb].tile_off + tj];
-        if (boxes_may_pair(job, A, B)) {
+        if (boxes_may_pair(job, A, B) && !(sc.full && !job.qinv && slots_all_full(sc, A, B))) {
             const Item it = Item{(unsigned)J, (unsigned)ti, (unsigned)tj};
             if (job.kind == 0) {
                 const unsigned slot = atomicAdd(b.n_items, 1u);
@@ -296,7 +354,21 @@ cudaError_t run_batch(const Device &d, const BatchDev &b, int grid, unsigned chu
             cudaSuccess)
         return e;
     if (b.total_pairs > 0) {
-        k_cull<<<gs, 256, 0, st>>>(b);
+        SlotCull sc = {};
+        if (mode != MODE_FAST && d.caps.slot_full && !b.devs) {
+            sc.full = d.caps.slot_full;
+            sc.KT_min = d.g.KT_min;
+            sc.dKT = d.g.dKT;
+            sc.KT_min_sq = d.g.KT_min_sq;
+            sc.KT_max_sq = d.g.KT_max_sq;
+            sc.psi = d.g.psi_ref;
+            sc.dKphi = d.g.dKphi;
+            sc.two_pi = d.g.two_pi;
+            sc.n_KT = d.g.n_KT;
+            sc.n_Kphi = d.g.n_Kphi;
+            sc.az = d.g.azimuthal;
+        }
+        k_cull<<<gs, 256, 0, st>>>(b, sc);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (b.order_items && b.same_cap > 0) {

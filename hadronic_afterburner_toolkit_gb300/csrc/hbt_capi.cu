@@ -65,7 +65,8 @@ struct hbt_ctx {
     int sms = 152, max_blocks_per_sm = 5;
     hbt_tuning tune = {0, 0.02, 0.05, kMergeChunk, 1, 0, 1};
     // ordered admission scratch
-    DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi, straddle_jobs;
+    DevBuf rowcnt, row_cut, quota, remaining, resolved, counters, apply_iphi, straddle_jobs,
+        slot_full;
     // input staging, two buffers in turn: the host-to-device copy of a call
     // runs on `copy_in` while the binning of the previous call still reads
     // the other buffer (in_free: recorded on `stream` after that binning)
@@ -367,6 +368,31 @@ std::vector<u64> remaining_of(const hbt_ctx *c, int mixed, const std::vector<u64
     return rem;
 }
 
+// Uploads which 3-D slots have no admission left (rem[s] == 0) for the
+// batched passes' cull (Caps::slot_full); the caller clears it afterwards.
+hbt_status set_slot_full(hbt_ctx *c, const std::vector<u64> &rem) {
+    const int ns = c->d.g.n_slots;
+    std::vector<unsigned char> full(ns);
+    bool any = false;
+    for (int s = 0; s < ns; s++) {
+        full[s] = rem[s] == 0 ? 1 : 0;
+        any = any || full[s];
+    }
+    if (!any) return HBT_OK;
+    TRY(dalloc(c, c->slot_full, ns));
+    CU(cudaMemcpyAsync(c->slot_full.p, full.data(), ns, cudaMemcpyHostToDevice, c->stream));
+    // the copy reads the host vector before it goes out of scope
+    CU(cudaStreamSynchronize(c->stream));
+    c->d.caps.slot_full = ptr<unsigned char>(c->slot_full);
+    return HBT_OK;
+}
+
+// Clears Caps::slot_full when an ordered pass ends, on every return path.
+struct SlotFullScope {
+    hbt::Caps &caps;
+    ~SlotFullScope() { caps.slot_full = nullptr; }
+};
+
 // Ordered admission for one launch (same-event: mixed = 0).  The two
 // passes over every pair (COUNT: survivors per stream bin and row; ORDER:
 // the rows before each bin's cut) run on the batched screened kernels when
@@ -395,6 +421,9 @@ hbt_status ordered_launch(hbt_ctx *c, int mixed, long long rows, long long cols,
     TRY(dalloc(c, c->quota, nst * sizeof(u64)));
     TRY(dalloc(c, c->remaining, nst * sizeof(u64)));
     refresh_device(c);
+    // the batched passes skip tile pairs that reach only full slots
+    SlotFullScope slot_scope{c->d.caps};
+    if (batched) TRY(set_slot_full(c, rem));
     c->d.caps.n_resolved = 0;
     CU(cudaMemsetAsync(c->rowcnt.p, 0, (size_t)nst * rows * sizeof(unsigned), c->stream));
     CU(cudaMemsetAsync(c->n_defer.p, 0, sizeof(unsigned), c->stream));
@@ -482,6 +511,8 @@ hbt_status ordered_launch_mixed_jobs(hbt_ctx *c, const std::vector<hbt::FastJob>
             caps.n_resolved = 0;
         }
     } joint{c->d.caps};
+    SlotFullScope slot_scope{c->d.caps};
+    TRY(set_slot_full(c, rem));
     c->d.caps.n_resolved = 0;
     c->d.caps.rows_total = rows;
     c->d.caps.cols_key = cols;
@@ -876,8 +907,8 @@ void hbt_destroy(hbt_ctx *c) {
     DevBuf *bufs[] = {&c->sums,   &c->cnt,     &c->den,       &c->qi_sums,  &c->qi_cnt,
                       &c->qi_den, &c->stats,   &c->defer,     &c->n_defer,  &c->rowcnt,
                       &c->row_cut, &c->quota,  &c->remaining, &c->resolved, &c->counters,
-                      &c->apply_iphi, &c->straddle_jobs, &c->in[0], &c->in[1], &c->part,
-                      &c->comp, &c->exp};
+                      &c->apply_iphi, &c->straddle_jobs, &c->slot_full, &c->in[0], &c->in[1],
+                      &c->part, &c->comp, &c->exp};
     if (c->copy) cudaStreamSynchronize(c->copy);
     for (DevBuf *b : bufs) dfree(c, *b);
     dfree(c, c->snap);

@@ -89,6 +89,10 @@ struct Caps {
     // rows_total rows per stream bin and deferral keys are row * cols_key +
     // column (0: one job, its own list sizes)
     long long rows_total, cols_key;
+    // the 3-D slots already at their cap in the pass's counter family
+    // (n_slots bytes), so that the batched passes skip tile pairs that can
+    // reach no other slot; nullptr: none
+    const unsigned char *slot_full;
 };
 
 // FP32 copies of the constants used by the FP32 pair screen (hbt_fast.cu),
