@@ -127,6 +127,34 @@ def test_batch_mixed_jobs_admitted_together():
     parity.compare(eng.hist(), h, _qscale(p))
 
 
+def test_batch_cap_passes_skip_tile_pairs_of_full_slots():
+    """Once the busiest slots are past the cap, the count and order passes
+    skip the tile pairs whose pairs can reach only those slots: fewer tile
+    pairs kept than an uncapped launch of the same job keeps, with counts
+    and counters equal to the oracle's."""
+    from hadronic_afterburner_toolkit_gb300 import engine as E
+    from hadronic_afterburner_toolkit_gb300 import synth
+    p0 = dict(BASE, azimuthal_flag=1)
+    a = parity.cols8(synth.generate(1, np.array([3000]), seed=71))
+    b = parity.cols8(synth.generate(1, np.array([3000]), seed=72))
+    first = _run_oracle(p0, [("same", a)], psi=0.3)["ctr_num"]
+    cap = float(np.median(first[first > 0]))
+    p = dict(p0, needed_number_of_pairs=cap)
+    jobs = [("same", a), ("same", b)]
+    eng = E.Engine(**p)
+    eng.set_psi_ref(0.3)
+    eng.bin_batch(jobs[:1])
+    eng.bin_batch(jobs[1:])
+    kept = eng.stats()["tiles_same_kept"]
+    free = E.Engine(**p0)
+    free.set_psi_ref(0.3)
+    free.bin_batch(jobs[1:])
+    assert 0 < kept < free.stats()["tiles_same_kept"]
+    h = _run_oracle(p, jobs, psi=0.3)
+    assert (h["ctr_num"] > cap).any() and (h["ctr_num"] <= cap).any()
+    parity.compare(eng.hist(), h, _qscale(p))
+
+
 def test_batch_fp32w_counts_exact():
     from hadronic_afterburner_toolkit_gb300 import engine as E
     p = dict(BASE, azimuthal_flag=1)
