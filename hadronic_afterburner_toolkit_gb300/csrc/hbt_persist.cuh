@@ -47,20 +47,28 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
     return dsm;
 }
 
-// Resident CTAs per SM (register budget 65536 / (128 x CTAs)): measured on
-// GB300, the FP64 form of the same-event kernel is fastest at 4 (128
-// registers, no spills: 152.7 ms per central group, against 173.6 ms at 3
-// with 164 registers, 158.8 ms at 5 with 96 and 216 ms at 6 with 80, the
-// last two spilling), the
-// double-float form at 4 too (118 registers, no spills: 167 ms, against 194
-// ms at 5 and 234 ms at 6), the FP32-weight form and the mixed-event kernel
-// at 6.
+// Resident CTAs per SM (register budget 65536 / (128 x CTAs); shared
+// memory allows 5 of the FP64 and double-float forms' 38.4 KB): measured on
+// GB300, the FP64 form of the same-event kernel is fastest at 5 (96
+// registers, no spills: 141.0 ms kernel per central group against 144.6 ms
+// at 4 with 124 registers; at 3, 164 registers, it took 173.6 ms), the
+// double-float form at 4 (118 registers, no spills: 150.9 ms kernel, against
+// 152.9 ms at 5 with 96 registers), the FP32-weight form at 6 (80
+// registers: 107.0 ms, against 109.1 ms at 5) and the mixed-event kernel at
+// 6 (12.6 ms, against 13.0 ms at 5).
 #ifndef HBT_FP64_SAME_CTAS
-#define HBT_FP64_SAME_CTAS 4  // compile-time choice for the FP64 form (-D to measure others)
+#define HBT_FP64_SAME_CTAS 5  // compile-time choice for the FP64 form (-D to measure others)
+#endif
+#ifndef HBT_DF64_SAME_CTAS
+#define HBT_DF64_SAME_CTAS 4  // the same for the double-float form
+#endif
+#ifndef HBT_FP32W_SAME_CTAS
+#define HBT_FP32W_SAME_CTAS 6  // and for the FP32-weight form
 #endif
 template <int PREC>
 struct SameCtas {
-    static constexpr int value = PREC == 1 ? 6 : (PREC == 2 ? 4 : HBT_FP64_SAME_CTAS);
+    static constexpr int value =
+        PREC == 1 ? HBT_FP32W_SAME_CTAS : (PREC == 2 ? HBT_DF64_SAME_CTAS : HBT_FP64_SAME_CTAS);
 };
 constexpr int kMixedCtas = 6;
 
