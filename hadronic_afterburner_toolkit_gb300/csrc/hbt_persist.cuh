@@ -70,7 +70,10 @@ struct SameCtas {
     static constexpr int value =
         PREC == 1 ? HBT_FP32W_SAME_CTAS : (PREC == 2 ? HBT_DF64_SAME_CTAS : HBT_FP64_SAME_CTAS);
 };
-constexpr int kMixedCtas = 6;
+#ifndef HBT_MIXED_CTAS
+#define HBT_MIXED_CTAS 6  // the mixed-event kernel's
+#endif
+constexpr int kMixedCtas = HBT_MIXED_CTAS;
 
 // Same-event items [base, min(end, queued)) pulled by persistent CTAs.
 // MODE: fast binning, or one pass of ordered cap admission.
