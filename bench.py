@@ -71,11 +71,11 @@ STAGE_OPS_MIXED = tuple(sum(c[:4]) for c in STAGE_COUNTS_MIXED)
 # form, all of the kernel's FP64 work (values, undecided pairs, tile loads)
 # divided by the pairs it bins: measured on one central group launch,
 # profiles/k_persistent_same_fp64_central.md.
-FP64_WARP_INST_PER_BINNED_PAIR = 1899463329 / 1942004247
+FP64_WARP_INST_PER_BINNED_PAIR = 1899528993 / 1942004247
 # DRAM bytes (read + write) of one k_persistent_same launch on a central
 # group, FP64 form, same-event items in momentum-region order (the default
 # hbt_tuning.order_items): profiles/k_persistent_same_fp64_central.md.
-CENTRAL_SAME_DRAM_BYTES = 181989888 + 289923584
+CENTRAL_SAME_DRAM_BYTES = 190039040 + 338685440
 
 
 def workload_params(name: str) -> dict:
