@@ -54,8 +54,9 @@ __device__ __forceinline__ const Device &item_device(const Device &d, const Batc
 // at 4 with 124 registers; at 3, 164 registers, it took 173.6 ms), the
 // double-float form at 4 (118 registers, no spills: 150.9 ms kernel, against
 // 152.9 ms at 5 with 96 registers), the FP32-weight form at 6 (80
-// registers: 107.0 ms, against 109.1 ms at 5) and the mixed-event kernel at
-// 6 (12.6 ms, against 13.0 ms at 5).
+// registers: 107.0 ms, against 109.1 ms at 5 and 127.8 ms at 7 with 72) and
+// the mixed-event kernel at 6 (12.6 ms, against 13.0 ms at 5 and 18.3 ms at
+// 7).
 #ifndef HBT_FP64_SAME_CTAS
 #define HBT_FP64_SAME_CTAS 5  // compile-time choice for the FP64 form (-D to measure others)
 #endif
