@@ -34,17 +34,19 @@ namespace persist {
 
 using namespace tile;
 
-// Engine descriptor of an item: the launch's own, or (serving many
-// analyses) the job's entry of b.devs copied into shared memory.
-__device__ __forceinline__ const Device &item_device(const Device &d, const BatchDev &b,
-                                                    const BatchJob &job, Device &dsm) {
-    if (!b.devs) return d;
+// Serving many analyses in one launch (MANY): the job's engine descriptor,
+// its entry of b.devs, copied into shared memory.  A launch of one analysis
+// reads the descriptor from its kernel parameter instead: its fields are
+// then constant-bank operands, where a reference that may point to either
+// the parameter or shared memory made every field a generic load (the
+// same-event kernel took 141 ms per central group that way, 121 ms
+// without).
+__device__ __forceinline__ void load_device(const BatchDev &b, const BatchJob &job, Device &dsm) {
     const int *src = reinterpret_cast<const int *>(b.devs + job.dev);
     int *dst = reinterpret_cast<int *>(&dsm);
     for (int k = threadIdx.x; k < (int)(sizeof(Device) / sizeof(int)); k += blockDim.x)
         dst[k] = src[k];
     __syncthreads();
-    return dsm;
 }
 
 // Resident CTAs per SM (register budget 65536 / (128 x CTAs); shared
@@ -77,12 +79,12 @@ struct SameCtas {
 constexpr int kMixedCtas = HBT_MIXED_CTAS;
 
 // Same-event items [base, min(end, queued)) pulled by persistent CTAs.
-// MODE: fast binning, or one pass of ordered cap admission.
-template <bool AZ, bool BOOST, int PREC, int MODE, bool QINV>
+// MODE: fast binning, or one pass of ordered cap admission; MANY: the items
+// of many analyses (b.devs), fast binning only.
+template <bool AZ, bool BOOST, int PREC, int MODE, bool QINV, bool MANY>
 __global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(Device d, BatchDev b, unsigned base,
                                                            unsigned end) {
     __shared__ SmemFor<QINV> sm;
-    __shared__ Device dsm;
     __shared__ unsigned item;
     __shared__ double2 cs[COS_TABLE];
     if (PREC == 0) fill_cos_table(cs);
@@ -95,22 +97,29 @@ __global__ void __launch_bounds__(FT, SameCtas<PREC>::value) k_persistent_same(D
         if (k >= stop) break;
         const Item it = b.items[b.order_items ? b.item_pos_out[k] : k];
         const BatchJob &job = b.jobs[it.job];
-        const Device &dd = item_device(d, b, job, dsm);
         const BatchList &la = b.lists[job.la];
         const double *c[8];
 #pragma unroll
         for (int f = 0; f < 8; f++) c[f] = b.table + (long long)f * b.cap + la.off;
-        same_tile_pair<AZ, BOOST, PREC, MODE, QINV>(dd, sm, cs, c, b.orig + la.off, la.n,
-                                              (long long)it.ti * FT, (long long)it.tj * FT);
+        if constexpr (MANY) {
+            __shared__ Device dsm;
+            load_device(b, job, dsm);
+            same_tile_pair<AZ, BOOST, PREC, MODE, QINV>(dsm, sm, cs, c, b.orig + la.off, la.n,
+                                                        (long long)it.ti * FT,
+                                                        (long long)it.tj * FT);
+        } else {
+            same_tile_pair<AZ, BOOST, PREC, MODE, QINV>(d, sm, cs, c, b.orig + la.off, la.n,
+                                                        (long long)it.ti * FT,
+                                                        (long long)it.tj * FT);
+        }
         __syncthreads();
     }
 }
 
 // Mixed-event items, all in one launch.
-template <bool AZ, bool BOOST, int MODE, bool QINV>
+template <bool AZ, bool BOOST, int MODE, bool QINV, bool MANY>
 __global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, BatchDev b) {
     __shared__ TileSmem sm;
-    __shared__ Device dsm;
     __shared__ unsigned item;
     const unsigned stop = min(b.n_items[1], b.mixed_cap);
     for (;;) {
@@ -120,7 +129,6 @@ __global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, B
         if (k >= stop) break;
         const Item it = b.items[b.same_cap + k];
         const BatchJob &job = b.jobs[it.job];
-        const Device &dd = item_device(d, b, job, dsm);
         const BatchList &la = b.lists[job.la], &lb = b.lists[job.lb];
         const double *c1[4], *c2[4];
 #pragma unroll
@@ -128,9 +136,19 @@ __global__ void __launch_bounds__(FT, kMixedCtas) k_persistent_mixed(Device d, B
             c1[f] = b.table + (long long)f * b.cap + la.off;
             c2[f] = b.table + (long long)f * b.cap + lb.off;
         }
-        mixed_tile_pair<AZ, BOOST, MODE, QINV>(dd, sm, c1, la.n, c2, lb.n, (long long)it.ti * FT,
-                                         (long long)it.tj * FT, b.orig + la.off,
-                                         b.orig + lb.off, job.row_base);
+        if constexpr (MANY) {
+            __shared__ Device dsm;
+            load_device(b, job, dsm);
+            mixed_tile_pair<AZ, BOOST, MODE, QINV>(dsm, sm, c1, la.n, c2, lb.n,
+                                                   (long long)it.ti * FT, (long long)it.tj * FT,
+                                                   b.orig + la.off, b.orig + lb.off,
+                                                   job.row_base);
+        } else {
+            mixed_tile_pair<AZ, BOOST, MODE, QINV>(d, sm, c1, la.n, c2, lb.n,
+                                                   (long long)it.ti * FT, (long long)it.tj * FT,
+                                                   b.orig + la.off, b.orig + lb.off,
+                                                   job.row_base);
+        }
         __syncthreads();
     }
 }
@@ -156,18 +174,36 @@ int persistent_grid(K kernel, int grid) {
     return sm_count() * nb;
 }
 
+// The kernel for one analysis, or (b.devs, fast binning only) for many.
 template <bool AZ, bool BOOST, int PREC, int MODE, bool QINV>
 cudaError_t launch_same_items(const Device &d, const BatchDev &b, unsigned base, unsigned end,
                               int grid, cudaStream_t st) {
-    grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC, MODE, QINV>, grid);
-    k_persistent_same<AZ, BOOST, PREC, MODE, QINV><<<grid, FT, 0, st>>>(d, b, base, end);
+    if (b.devs) {
+        if constexpr (MODE == MODE_FAST) {
+            grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC, MODE, QINV, true>, grid);
+            k_persistent_same<AZ, BOOST, PREC, MODE, QINV, true><<<grid, FT, 0, st>>>(d, b, base,
+                                                                                     end);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    grid = persistent_grid(k_persistent_same<AZ, BOOST, PREC, MODE, QINV, false>, grid);
+    k_persistent_same<AZ, BOOST, PREC, MODE, QINV, false><<<grid, FT, 0, st>>>(d, b, base, end);
     return cudaGetLastError();
 }
 
 template <bool AZ, bool BOOST, int MODE, bool QINV>
 cudaError_t launch_mixed_items(const Device &d, const BatchDev &b, int grid, cudaStream_t st) {
-    grid = persistent_grid(k_persistent_mixed<AZ, BOOST, MODE, QINV>, grid);
-    k_persistent_mixed<AZ, BOOST, MODE, QINV><<<grid, FT, 0, st>>>(d, b);
+    if (b.devs) {
+        if constexpr (MODE == MODE_FAST) {
+            grid = persistent_grid(k_persistent_mixed<AZ, BOOST, MODE, QINV, true>, grid);
+            k_persistent_mixed<AZ, BOOST, MODE, QINV, true><<<grid, FT, 0, st>>>(d, b);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    grid = persistent_grid(k_persistent_mixed<AZ, BOOST, MODE, QINV, false>, grid);
+    k_persistent_mixed<AZ, BOOST, MODE, QINV, false><<<grid, FT, 0, st>>>(d, b);
     return cudaGetLastError();
 }
 

@@ -18,7 +18,7 @@ cudaError_t persistent_mixed_fast(const Device &d, const BatchDev &b, int grid, 
 int persistent_blocks_per_sm() {
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, k_persistent_same<true, true, 0, MODE_FAST, false>, FT, 0) != cudaSuccess)
+            &nb, k_persistent_same<true, true, 0, MODE_FAST, false, false>, FT, 0) != cudaSuccess)
         return 4;
     return nb > 0 ? nb : 1;
 }
