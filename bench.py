@@ -75,7 +75,7 @@ FP64_WARP_INST_PER_BINNED_PAIR = 1899528993 / 1942004247
 # DRAM bytes (read + write) of one k_persistent_same launch on a central
 # group, FP64 form, same-event items in momentum-region order (the default
 # hbt_tuning.order_items): profiles/k_persistent_same_fp64_central.md.
-CENTRAL_SAME_DRAM_BYTES = 190039040 + 338685440
+CENTRAL_SAME_DRAM_BYTES = 187360768 + 331953920
 
 
 def workload_params(name: str) -> dict:
