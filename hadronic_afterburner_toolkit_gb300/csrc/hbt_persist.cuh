@@ -54,16 +54,16 @@ __device__ __forceinline__ void load_device(const BatchDev &b, const BatchJob &j
 // GB300, the FP64 form of the same-event kernel is fastest at 5 (96
 // registers, no spills: 141.0 ms kernel per central group against 144.6 ms
 // at 4 with 124 registers; at 3, 164 registers, it took 173.6 ms), the
-// double-float form at 4 (118 registers, no spills: 150.9 ms kernel, against
-// 152.9 ms at 5 with 96 registers), the FP32-weight form at 6 (80
-// registers: 107.0 ms, against 109.1 ms at 5 and 127.8 ms at 7 with 72) and
-// the mixed-event kernel at 6 (12.6 ms, against 13.0 ms at 5 and 18.3 ms at
-// 7).
+// double-float form at 5 too (96 registers: 119.8 ms kernel against 123.1
+// ms at 4 with 128, with the descriptor read from the kernel parameter), the
+// FP32-weight form at 6 (80 registers: 94.0 ms, against 97.4 ms at 5 and,
+// before the descriptor change, 127.8 ms at 7 with 72) and the mixed-event
+// kernel at 6 (12.6 ms, against 13.0 ms at 5 and 18.3 ms at 7).
 #ifndef HBT_FP64_SAME_CTAS
 #define HBT_FP64_SAME_CTAS 5  // compile-time choice for the FP64 form (-D to measure others)
 #endif
 #ifndef HBT_DF64_SAME_CTAS
-#define HBT_DF64_SAME_CTAS 4  // the same for the double-float form
+#define HBT_DF64_SAME_CTAS 5  // the same for the double-float form
 #endif
 #ifndef HBT_FP32W_SAME_CTAS
 #define HBT_FP32W_SAME_CTAS 6  // and for the FP32-weight form
