@@ -1471,7 +1471,8 @@ def main() -> None:
                                                  "sqrt_gops", "cos_gops", "atomic_gops_l2",
                                                  "atomic_gops_256mb")},
                 # the reference's per-pair chain on every pair at these rates
-                # (SURVEY-style stage counts x measured survival): the time an
+                # (operation counts per stage of the chain x the measured
+                # fraction of pairs reaching that stage): the time an
                 # implementation of the plain chain cannot beat
                 "reference_chain": {
                     "stage_counts_same": STAGE_COUNTS_SAME,

@@ -7,7 +7,7 @@
 * ``lib/libhbt_host.so`` and ``lib/hbt_afterburner.e`` - the C++ drop-in host
   side (parameter reader, event reader, HBT_correlation driver, writer),
   when its sources are present;
-* ``oracle/liboracle.so`` - the CPU checker used by the tests.
+* ``oracle/liboracle.so`` - the CPU oracle the tests compare against.
 
 The pair-binning translation unit is compiled with ``--fmad=false`` so that
 no FP64 multiply-add is contracted: every bin-deciding operation rounds as

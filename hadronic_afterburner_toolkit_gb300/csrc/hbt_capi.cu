@@ -39,10 +39,12 @@ struct DevBuf {
 // FP32-weight form: same-event tile pairs (at most 128 x 128 pairs each)
 // between two merges of the FP32 partials into the FP64 bins, and the
 // largest value a tuning may set.  The partials' rounding grows with the
-// pairs a bin takes between merges: on the central workload the worst
-// numerator error per pair is 6e-7 with 8192 (1e-6 to 2e-6 with 16384),
-// inside the form's 1e-6 bound.
-constexpr int kMergeChunk = 8192;
+// pairs a bin takes between merges (about linearly: the cos terms a busy
+// bin takes are alike, so their roundings add up rather than cancel): on
+// the central workload the worst numerator error per pair reached 1.05e-6
+// with 8192 (the work items' queue order, and so each chunk's items, vary
+// from run to run), above the form's 1e-6 bound; 4096 halves it.
+constexpr int kMergeChunk = 4096;
 
 struct hbt_ctx {
     hbt_params prm;

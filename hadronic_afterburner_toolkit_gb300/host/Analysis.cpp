@@ -41,7 +41,7 @@ void Analysis::InitializeAnalysis() {
 void Analysis::PerformAnalysis() {
     InitializeAnalysis();
     if (paraRdr_.getVal("analyze_flow") != 0)
-        std::cout << "[Warning] analyze_flow: the flow analysis is not part of this build; "
+        std::cout << "[Warning] analyze_flow: the flow analysis is not part of this library; "
                      "skipped" << std::endl;
     if (paraRdr_.getVal("analyze_HBT") == 1) {
         std::cout << "[Info] Analyze HBT ..." << std::endl;
@@ -56,7 +56,7 @@ void Analysis::PerformAnalysis() {
         particle_list_.reset();
     }
     if (paraRdr_.getVal("analyze_ebe_yield") == 1)
-        std::cout << "[Warning] analyze_ebe_yield: not part of this build; skipped" << std::endl;
+        std::cout << "[Warning] analyze_ebe_yield: not part of this library; skipped" << std::endl;
 }
 
 // src/Analysis.cpp:817-835

@@ -2,7 +2,7 @@
 // reference's Analysis class, src/Analysis.{h,cpp}: parameter dictionary,
 // RNG seeding and the buffer loops of Analysis::HBTAnalysis and
 // Analysis::BalanceFunctionAnalysis, src/Analysis.cpp:817-874).  The flow
-// and yield analyses are not part of this build and are skipped with a
+// and yield analyses are not part of this library and are skipped with a
 // warning.
 #pragma once
 

@@ -31,7 +31,7 @@ particleSamples::particleSamples(ParameterReader &paraRdr, std::string path,
     }
     if (paraRdr_.getVal("resonance_feed_down_flag") == 1 ||
         paraRdr_.getVal("resonance_weak_feed_down_flag") == 1)
-        throw std::runtime_error("particleSamples: resonance decays are not part of this build");
+        throw std::runtime_error("particleSamples: resonance decays are not part of this library");
 
     std::string file, file_mixed;
     bool gz = false;
@@ -45,7 +45,7 @@ particleSamples::particleSamples(ParameterReader &paraRdr, std::string path,
     } else {
         throw std::runtime_error("particleSamples: read_in_mode " +
                                  std::to_string(read_in_mode_) +
-                                 " is not supported by this build (0 and 10 are)");
+                                 " is not supported by this library (0 and 10 are)");
     }
     const bool fast =
         !paraRdr_.exist("hbt_fast_reader") || paraRdr_.getVal("hbt_fast_reader") != 0;

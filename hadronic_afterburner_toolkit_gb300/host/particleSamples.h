@@ -13,7 +13,7 @@
 //    baryon sign, strangeness sign) looked up in EOS/pdg.dat;
 //  - the balance-function species lists (:1300-1330, :1370-1460, :538-551).
 // Other reader modes (UrQMD, JAM, SMASH, iSS binary) and resonance decays
-// are not part of this build; asking for them throws.
+// are not part of this library; asking for them throws.
 #pragma once
 
 #include <cstdio>

@@ -8,7 +8,7 @@
  * pT, phi_p, rap_y, rap_eta of boostParticles, src/particleSamples.cpp
  * :442-468, and the per-species lists of filter_particles, :1300-1330 and
  * :1370-1460, plain Monte-Carlo numbers only).  Used by the tests as the
- * checker of the GPU balance-function kernel and by the benchmark as the
+ * oracle of the GPU balance-function kernel and by the benchmark as the
  * timed CPU baseline; nothing in the product links or calls it.
  *
  * Parity pin: driven over tests/golden_bf/, its output files are

@@ -1,7 +1,7 @@
 """CPU restatement of the reference's HBT radii fit
-(ebe_scripts/fit_HBT_radii.py) for one correlation table - TEST AND
-BASELINE INFRASTRUCTURE ONLY (the checker of the GPU fits and the timed CPU
-baseline of the benchmark's fit leg; the product is hbt_fit_radii).
+(ebe_scripts/fit_HBT_radii.py) for one correlation table - TEST
+INFRASTRUCTURE ONLY (the oracle of the GPU fits and the timed CPU
+comparison of the benchmark's fit leg; the product is hbt_fit_radii).
 
 Per table (an eight-column array, :60-67): nan_to_num, columns 0-2 as
 q_out, q_side, q_long, column 6 as C and column 7 + 1e-15 as its error;

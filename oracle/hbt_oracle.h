@@ -3,7 +3,7 @@
  *
  * A plain, sequential restatement of the reference's HBT correlation
  * algorithm (src/HBT_correlation.cpp in chunshen1987/hadronic_afterburner_toolkit),
- * used by the test-suite as the checker of the GPU engine and by the
+ * used by the test-suite as the oracle of the GPU engine and by the
  * benchmark as the timed CPU baseline.  Nothing in the product links or
  * calls this library.
  *

@@ -1,6 +1,6 @@
 """ctypes access to the CPU oracle (oracle/liboracle.so) for the tests.
 
-Test infrastructure: the oracle is the checker, never the thing measured.
+Test infrastructure: the oracle is what results are compared against, never the thing measured.
 Also parses the golden inputs (mode-10 gzip text and OSCAR text) into CSR
 event tables, applies the species filter and splits buffers with the
 reader's rule, and replays whole golden cases through the oracle.
