@@ -39,12 +39,13 @@ struct DevBuf {
 // FP32-weight form: same-event tile pairs (at most 128 x 128 pairs each)
 // between two merges of the FP32 partials into the FP64 bins, and the
 // largest value a tuning may set.  The partials' rounding grows with the
-// pairs a bin takes between merges (about linearly: the cos terms a busy
-// bin takes are alike, so their roundings add up rather than cancel): on
-// the central workload the worst numerator error per pair reached 1.05e-6
-// with 8192 (the work items' queue order, and so each chunk's items, vary
-// from run to run), above the form's 1e-6 bound; 4096 halves it.
-constexpr int kMergeChunk = 4096;
+// pairs a partial bin takes between merges (about linearly: the cos terms
+// a busy bin takes are alike, so their roundings add up rather than
+// cancel).  On the central workload, with one partial array, the worst
+// numerator error per pair reached 1.05e-6 with 8192 (the work items' queue
+// order, and so each chunk's items, vary from run to run), above the
+// form's 1e-6 bound; the two partial arrays (partials_of) halve it.
+constexpr int kMergeChunk = 8192;
 
 struct hbt_ctx {
     hbt_params prm;
@@ -174,6 +175,8 @@ void refresh_device(hbt_ctx *c) {
     c->d.caps.quota = ptr<unsigned long long>(c->quota);
     c->d.caps.resolved = ptr<hbt::Resolved>(c->resolved);
     c->d.part = ptr<float4>(c->part);
+    // the second partial array follows the first (same length)
+    c->d.part_b = c->d.part ? c->d.part + (size_t)c->d.g.n_slots * c->d.g.q3 : nullptr;
     c->d.comp = ptr<hbt::Sums>(c->comp);
 }
 
@@ -889,7 +892,7 @@ hbt_status ctx_create(const hbt_params *p, int device, cudaMemPool_t pool, hbt_c
         (s = dalloc(c, c->defer, kDeferCap * sizeof(hbt::Deferral))) != HBT_OK ||
         (s = dalloc(c, c->n_defer, sizeof(unsigned))) != HBT_OK ||
         (p->precision == HBT_PRECISION_FP32W &&
-         ((s = dalloc(c, c->part, nb * sizeof(float4))) != HBT_OK ||
+         ((s = dalloc(c, c->part, 2 * nb * sizeof(float4))) != HBT_OK ||
           (s = dalloc(c, c->comp, nb * sizeof(hbt::Sums))) != HBT_OK)))
         return s;
     refresh_device(c);
@@ -1432,7 +1435,7 @@ size_t ctx_device_bytes(const hbt_params &p) {
     // bins, counts, the readback buffers, the q_inv bins, the deferrals
     size_t bytes = nb * (sizeof(Sums) + 2 * sizeof(u64) + 2 * sizeof(double)) +
                    nq * (sizeof(QiSums) + 2 * sizeof(u64)) + kDeferCap * sizeof(Deferral) + 4096;
-    if (p.precision == HBT_PRECISION_FP32W) bytes += nb * (sizeof(float4) + sizeof(Sums));
+    if (p.precision == HBT_PRECISION_FP32W) bytes += nb * (2 * sizeof(float4) + sizeof(Sums));
     return bytes;
 }
 

@@ -147,15 +147,28 @@ struct Device {
     unsigned defer_cap;
     Caps caps;
     // FP32-weight form: FP32 partial sums per bin {q_out, q_side, q_long,
-    // cos}, merged into h.sums with the Kahan compensation terms `comp`
+    // cos}, merged into h.sums with the Kahan compensation terms `comp`.
+    // Two arrays: pairs of even warps add to `part`, of odd warps to
+    // `part_b`, so each partial bin takes about half of a bin's pairs
+    // between two merges (partials_of below).
     int precision;                 // hbt_precision
     float4 *part;
+    float4 *part_b;
     Sums *comp;
     long long merge_chunk_blocks;  // same-event CTAs between two merges
     long long block_offset;        // first triangular tile pair of a launch chunk
 };
 
 enum Mode { MODE_FAST = 0, MODE_COUNT = 1, MODE_ORDER = 2 };
+
+// The FP32 partial array the calling warp adds to: odd warps of a CTA use
+// the second one.  The rounding of an FP32 partial grows with the pairs it
+// takes between merges (a busy bin's cos terms are alike, so their
+// roundings add up), and two arrays halve that count without merging more
+// often.
+__device__ __forceinline__ float4 *partials_of(const Device &d) {
+    return (threadIdx.x & 32) ? d.part_b : d.part;
+}
 
 // Launchers (hbt_kernels.cu).
 cudaError_t launch_same(const Device &d, int mode, long long n, const double *const *c8,

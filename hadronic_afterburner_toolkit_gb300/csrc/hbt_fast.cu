@@ -43,11 +43,16 @@ __global__ void __launch_bounds__(256) k_merge_partials(Device d, long long nbin
     if (n_items && chunk_base >= *n_items) return;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nbins;
          k += (long long)gridDim.x * blockDim.x) {
-        const float4 p = d.part[k];
-        if (p.x == 0.0f && p.y == 0.0f && p.z == 0.0f && p.w == 0.0f) continue;
+        const float4 p = d.part[k], r = d.part_b[k];
+        if (p.x == 0.0f && p.y == 0.0f && p.z == 0.0f && p.w == 0.0f && r.x == 0.0f &&
+            r.y == 0.0f && r.z == 0.0f && r.w == 0.0f)
+            continue;
         Sums s = d.h.sums[k];
         Sums c = d.comp[k];
-        const double in[4] = {(double)p.x, (double)p.y, (double)p.z, (double)p.w};
+        // the two partials' sum in FP64 (exact unless their exponents differ
+        // by more than 28)
+        const double in[4] = {(double)p.x + (double)r.x, (double)p.y + (double)r.y,
+                              (double)p.z + (double)r.z, (double)p.w + (double)r.w};
         double *sv[4] = {&s.qo, &s.qs, &s.ql, &s.w};
         double *cv[4] = {&c.qo, &c.qs, &c.ql, &c.w};
 #pragma unroll
@@ -60,6 +65,7 @@ __global__ void __launch_bounds__(256) k_merge_partials(Device d, long long nbin
         d.h.sums[k] = s;
         d.comp[k] = c;
         d.part[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        d.part_b[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 

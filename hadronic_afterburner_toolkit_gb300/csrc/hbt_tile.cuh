@@ -871,7 +871,7 @@ __device__ __noinline__ void undecided_pair32(const Device &d, const double *A, 
         consume<false, MODE_FAST>(d, i, j, n, n, full);
     } else {
         const long long at = (long long)full.slot * d.g.q3 + full.bin;
-        atomicAdd(d.part + at, values32<BOOST>(d.g, A, B));
+        atomicAdd(partials_of(d) + at, values32<BOOST>(d.g, A, B));
         atomicAdd(d.h.cnt + at, 1ull);
     }
 }
@@ -1076,7 +1076,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                         v.z = -v.z;
                     }
                     if (has3) {
-                        atomicAdd(d.part + at, v);
+                        atomicAdd(partials_of(d) + at, v);
                         atomicAdd(d.h.cnt + at, 1ull);
                     }
                     wq = v.w;
@@ -1238,7 +1238,7 @@ __device__ __forceinline__ void same_tile_pair(const Device &d, SmemFor<QINV> &s
                     v.z = -v.z;
                 }
                 const long long at = (long long)slot * d.g.q3 + bin;
-                atomicAdd(d.part + at, v);
+                atomicAdd(partials_of(d) + at, v);
                 atomicAdd(d.h.cnt + at, 1ull);
                 return;
             }

@@ -189,7 +189,7 @@ typedef struct hbt_tuning {
     double cell_pt;         /* sort cell of p_x and p_y in GeV (0: 0.02) */
     double cell_y;          /* sort cell of rapidity (0: 0.05) */
     int32_t merge_chunk;    /* FP32-weight form: same-event tile pairs between two
-                               merges of the partials, <= 4096 (0: 4096; the
+                               merges of the partials, <= 8192 (0: 8192; the
                                bound keeps the numerator within 1e-6 per pair) */
     int32_t use_graph;      /* 1: launch the sort-cull-bin pipeline as a CUDA graph,
                                captured when a batch of the same shape comes twice in

@@ -7,7 +7,8 @@ summed values change precision: q_out / q_side / q_long are the FP32 screen
 values (relative error < 1e-6) and cos(q.dx / hbarC) is evaluated in FP32
 after an FP64 phase and range reduction (absolute error < 2e-7).  They are
 accumulated into FP32 partial bins, merged into the FP64 bins with Kahan
-compensation every 4096 same-event tile pairs.  Stated per-bin bound checked here:
+compensation every 8192 same-event tile pairs (pairs of even and odd
+warps in two partial arrays).  Stated per-bin bound checked here:
 |sum - oracle| <= 1e-5 * count * scale (scale = max|q| of the window, or 1
 for the cos numerator).
 """
