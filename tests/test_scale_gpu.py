@@ -14,7 +14,10 @@ reference's files) on the same inputs:
   of Poisson(1500)), 8 K_T x 8 K_phi bins with psi_ref from the event
   plane, 10 partners - against the oracle's multi-threaded pair loops;
 * the precision configuration on that group and on three K+ groups: the
-  FP32-weight and double-float forms against the same oracle.
+  FP32-weight and double-float forms against the same oracle;
+* three ~50k-particle groups of the uneven-multiplicity configuration in
+  one batched call, FP64 and (autotuned, replayed as a CUDA graph)
+  FP32-weight forms.
 
 The reference path these cover is src/HBT_correlation.cpp:177-218 (driver),
 :291-461 (same-event loop) and :563-689 (mixed-event loop).  Partners and
@@ -354,3 +357,64 @@ def test_central_group_with_qinv_and_kphi(central_group):
     h, st = engine_hist(p, jobs, psi)
     assert o["qinv_count"].sum() > 1e9
     parity.compare(h, o, q_scale=0.15)
+
+
+UNEVEN = dict(qnpts=41, q_min=-0.15, q_max=0.15, n_KT=5, KT_min=0.0, KT_max=1.0, n_Kphi=8,
+              azimuthal_flag=0, invariant_radius_flag=0, long_comoving_boost=1,
+              needed_number_of_pairs=1e18)
+
+
+@pytest.fixture(scope="module")
+def uneven_groups(host):
+    """The first three ~50k-particle groups of the uneven-multiplicity
+    workload (4096 pi+ events, multiplicities log-uniform in [20, 3000],
+    sigma_xy = 1.2 N^(1/3) fm), 10 rotated partners per event."""
+    ev = synth.uneven_pions(seed=3)
+    bufs = synth.buffers(ev, 50000)[:3]
+    plans = mixed_plan(host, 1, [b - a for a, b in bufs], 10)
+    jobs = []
+    for (a, b), (partners, angles) in zip(bufs, plans):
+        jobs += buffer_jobs(synth.subset(ev, a, b), partners, angles)
+    return jobs, oracle_mt(UNEVEN, jobs)
+
+
+def _device_jobs(jobs):
+    torch = pytest.importorskip("torch")
+
+    def dev(cols):
+        return [torch.from_numpy(np.ascontiguousarray(c)).cuda() for c in cols]
+    return [("same", dev(j[1])) if j[0] == "same" else ("mixed", dev(j[1]), dev(j[2]))
+            for j in jobs]
+
+
+def test_uneven_configuration_groups_in_one_batched_call(uneven_groups):
+    """Three groups of the uneven-multiplicity configuration at full size
+    (41^3 grid, 4 K_T bins) with every same-event and mixed-event list of
+    them in one batched call, as the benchmark runs it: the FP64 form against
+    the oracle (counts identical, sums within parity.RTOL); then the
+    FP32-weight form, autotuned and launched twice from device arrays (the
+    second launch replays the captured CUDA graph): counts exactly twice the
+    oracle's, the numerator within 1e-6 and the q sums within 1e-5 x 0.15 GeV
+    per pair."""
+    jobs, o = uneven_groups
+    assert o["pairs_same"] > 1e9 and o["count"].sum() > 1e8
+    h, st = engine_hist(UNEVEN, jobs)
+    parity.compare(h, o, q_scale=0.15)
+    assert st["anomalies"] == o["anomalies"]
+
+    djobs = _device_jobs(jobs)
+    eng = engine.Engine(device=0, precision=engine.PRECISION_FP32W, **UNEVEN)
+    eng.autotune(djobs)
+    eng.set_tuning(use_graph=1)
+    eng.bin_batch(djobs, device=True)
+    eng.bin_batch(djobs, device=True)
+    h = eng.hist()
+    st = eng.stats()
+    eng.close()
+    assert st["graph_replays"] + st["graph_captures"] >= 1
+    o2 = {k: 2 * np.asarray(o[k]) for k in ("count", "den", "ctr_num", "ctr_den", "num",
+                                            "abs_num", "q_out", "q_side", "q_long")}
+    for k in ("count", "den", "ctr_num", "ctr_den"):
+        assert np.array_equal(np.asarray(h[k]), o2[k]), k
+    e = _precision_errors(h, o2)
+    assert e["num_per_pair"] <= 1e-6 and e["q_per_pair"] <= 1e-5 * 0.15, e
