@@ -75,10 +75,13 @@ unsigned long long current_context_id() {
     std::call_once(once, [] {
         void *p = nullptr, *q = nullptr;
         cudaDriverEntryPointQueryResult r1, r2;
-        if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &p, cudaEnableDefault, &r1) ==
-                cudaSuccess &&
+        // the two entry points as CUDA 12.0 defined them (cuCtxGetId first
+        // appeared there)
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                             &r1) == cudaSuccess &&
             r1 == cudaDriverEntryPointSuccess &&
-            cudaGetDriverEntryPoint("cuCtxGetId", &q, cudaEnableDefault, &r2) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2) ==
+                cudaSuccess &&
             r2 == cudaDriverEntryPointSuccess) {
             cur = reinterpret_cast<GetCurrent>(p);
             id = reinterpret_cast<GetId>(q);
