@@ -163,16 +163,18 @@ def build_oracle() -> str:
 
 def build_reference(ref_root: str | None = None) -> str | None:
     """Compile the unmodified reference into oracle/_ref when a checkout of
-    it is named (``ref_root``, else the environment variable
-    HBT_REFERENCE_ROOT) and its sources are there."""
-    ref_root = ref_root or os.environ.get("HBT_REFERENCE_ROOT")
-    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src")):
+    it is found: ``ref_root``, else the one oracle/Makefile finds (the
+    environment variable HBT_REFERENCE_ROOT, else where the checkout is
+    mounted on the development machine).  None when there is none."""
+    target = ["ref", "REF=" + ref_root] if ref_root else ["ref-if-present"]
+    if ref_root and not os.path.isdir(os.path.join(ref_root, "src")):
         return None
     try:
-        _run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + ref_root])
+        _run(["make", "-s", "-C", os.path.join(REPO, "oracle")] + target)
     except RuntimeError:
         return None
-    return os.path.join(REPO, "oracle", "_ref", "hadronic_afterburner_tools.e")
+    exe = os.path.join(REPO, "oracle", "_ref", "hadronic_afterburner_tools.e")
+    return exe if os.path.exists(exe) else None
 
 
 def build_all(force: bool = False, verbose: bool = False) -> None:

@@ -147,8 +147,10 @@ def param_text(p: dict) -> str:
     return "\n".join(lines) + "\n"
 
 
-def run_case(name: str, case: dict, ref_root: str) -> None:
-    out_dir = os.path.join(HERE, name)
+def run_case(name: str, case: dict, ref_root: str, out_root: str = HERE) -> None:
+    """Runs the reference binary on one case and writes the case's files
+    into out_root/name (tests/golden/<name> for the committed fixtures)."""
+    out_dir = os.path.join(out_root, name)
     os.makedirs(out_dir, exist_ok=True)
     params = dict(BASE_PARAMS)
     params.update(case["params"])

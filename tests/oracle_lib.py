@@ -259,9 +259,25 @@ def filter_species(ev, monval: int):
     return synth.Events(off, *[getattr(ev, f)[keep] for f in fields])
 
 
-def golden_case(name: str):
-    """(params, events, mixed_events_or_None) of one golden case."""
-    d = os.path.join(GOLDEN, name)
+def reference_checkout() -> str:
+    """The reference checkout on this machine, if any: HBT_REFERENCE_ROOT,
+    else the one the oracle's build recipe (oracle/Makefile) finds; "" when
+    there is none."""
+    env = os.environ.get("HBT_REFERENCE_ROOT", "")
+    if env:
+        return env
+    try:
+        out = subprocess.run(["make", "-s", "-C", ORACLE_DIR, "print-ref"],
+                             capture_output=True, text=True, timeout=60)
+    except (OSError, subprocess.SubprocessError):
+        return ""
+    return out.stdout.strip() if out.returncode == 0 else ""
+
+
+def golden_case(name: str, root: str = GOLDEN):
+    """(params, events, mixed_events_or_None) of one golden case (a folder
+    of root holding parameters.dat and the input files)."""
+    d = os.path.join(root, name)
     prm = read_params(os.path.join(d, "parameters.dat"))
     if int(prm["read_in_mode"]) == 10:
         ev = read_mode10(os.path.join(d, "particle_samples.gz"))
@@ -298,9 +314,9 @@ def buffer_ranges(mult, event_buffer_size):
     return out
 
 
-def run_golden_case_through_oracle(name: str, out_dir: str) -> Oracle:
+def run_golden_case_through_oracle(name: str, out_dir: str, root: str = GOLDEN) -> Oracle:
     from hadronic_afterburner_toolkit_gb300 import synth
-    prm, ev, mixed = golden_case(name)
+    prm, ev, mixed = golden_case(name, root)
     shift = prm.get("rapidity_shift", 0.0)
     if shift != 0.0:
         rapidity_shift(ev, shift)

@@ -22,13 +22,14 @@ import os
 import numpy as np
 import pytest
 
+import oracle_lib
 from hadronic_afterburner_toolkit_gb300 import build
 
 # the reference checkout whose unit-test fixtures are read in place
-REF = os.environ.get("HBT_REFERENCE_ROOT", "")
+REF = oracle_lib.reference_checkout()
 UNIT = os.path.join(REF, "unit_tests") if REF else ""
 pytestmark = pytest.mark.skipif(not UNIT or not os.path.isdir(UNIT),
-                                reason="set HBT_REFERENCE_ROOT to a reference checkout")
+                                reason="no reference checkout (HBT_REFERENCE_ROOT)")
 
 
 @pytest.fixture(scope="module")
