@@ -35,8 +35,9 @@
 //                    arithmetic on the FP32 pipe, q values in FP32, cos by
 //                    quadrant reduction and FP32 Taylor polynomials
 //                    (values32_split); added with one float4 vector atomic
-//                    into FP32 partial bins that are merged into the FP64
-//                    bins with Kahan compensation.
+//                    into FP32 partial bins (two arrays, even and odd warps:
+//                    partials_of) that are merged into the FP64 bins with
+//                    Kahan compensation.
 //     In the FP32-weight form a pair is evaluated as stored (i, j) and
 //     oriented afterwards: swapping first and second negates every momentum
 //     and position difference, so it negates q_out, q_side, q_long exactly
