@@ -147,35 +147,83 @@ def param_text(p: dict) -> str:
     return "\n".join(lines) + "\n"
 
 
-def run_case(name: str, case: dict, ref_root: str, out_root: str = HERE) -> None:
-    """Runs the reference binary on one case and writes the case's files
-    into out_root/name (tests/golden/<name> for the committed fixtures)."""
+def random_case(k: int) -> dict:
+    """Case k of a seeded sweep of parameter sets and inputs: grid size (odd
+    and even), symmetric or asymmetric window (one without q = 0), K_T edges
+    and range, boost, K_phi bins, q_inv histograms, a cap that binds or not,
+    buffer size (down to one event), rapidity window and shift, the mixing
+    seed."""
+    rng = np.random.default_rng(4000 + k)
+    q_max = round(float(rng.uniform(0.06, 0.3)), 4)
+    q_min = -q_max if rng.random() < 0.6 else round(float(rng.uniform(-q_max, 0.02)), 4)
+    kt_min = round(float(rng.choice([0.0, rng.uniform(0.0, 0.3)])), 4)
+    params = {
+        "qnpts": int(rng.choice([4, 5, 7, 8, 11, 15])),
+        "q_min": q_min, "q_max": q_max,
+        "n_KT": int(rng.integers(2, 7)),
+        "KT_min": kt_min, "KT_max": round(kt_min + float(rng.uniform(0.3, 1.2)), 4),
+        "long_comoving_boost": int(rng.integers(0, 2)),
+        "azimuthal_flag": int(rng.integers(0, 2)),
+        "n_Kphi": int(rng.integers(2, 7)),
+        "invariant_radius_flag": int(rng.integers(0, 2)),
+        "needed_number_of_pairs": int(rng.choice([20, 300, 30000000])),
+        "event_buffer_size": int(rng.choice([1, 50, 120, 400])),
+        "HBTrap_min": round(-float(rng.uniform(0.4, 1.2)), 4),
+        "HBTrap_max": round(float(rng.uniform(0.4, 1.2)), 4),
+        "rapidity_shift": round(float(rng.choice([0.0, rng.uniform(-0.3, 0.3)])), 4),
+        "randomSeed": int(rng.integers(1, 10000)),
+    }
+    n_events = int(rng.integers(8, 30))
+    mu = float(rng.uniform(15.0, 70.0))
+    return dict(events=lambda: _events_basic(seed=5000 + k, n_events=n_events, mu=mu),
+                params=params)
+
+
+def write_case(name: str, case: dict, out_root: str = HERE) -> str:
+    """Writes one case's parameters.dat and input files into out_root/name
+    (no run); returns that folder."""
     out_dir = os.path.join(out_root, name)
     os.makedirs(out_dir, exist_ok=True)
     params = dict(BASE_PARAMS)
     params.update(case["params"])
     ev = case["events"]()
     mixed = case["mixed"]() if "mixed" in case else None
-    mode = params["read_in_mode"]
+    if params["read_in_mode"] == 10:
+        inputs = {"particle_samples.gz": ev}
+        if mixed is not None:
+            inputs["particle_samples_mixed_event.gz"] = mixed
+        for fn, e in inputs.items():
+            synth.write_mode10(os.path.join(out_dir, fn), e)
+    else:
+        inputs = {"OSCAR.DAT": ev}
+        if mixed is not None:
+            inputs["OSCAR_mixed_event.DAT"] = mixed
+        for fn, e in inputs.items():
+            synth.write_oscar(os.path.join(out_dir, fn), e)
+    with open(os.path.join(out_dir, "parameters.dat"), "w") as f:
+        f.write(param_text(params))
+    return out_dir
+
+
+def input_files(case_dir: str) -> list:
+    """The input files of a case folder (what goes into results/)."""
+    return sorted(fn for fn in os.listdir(case_dir)
+                  if (fn.endswith(".gz") and fn != "outputs.tar.gz") or fn.endswith(".DAT"))
+
+
+def run_case(name: str, case: dict, ref_root: str, out_root: str = HERE) -> None:
+    """Runs the reference binary on one case and writes the case's files
+    into out_root/name (tests/golden/<name> for the committed fixtures)."""
+    out_dir = write_case(name, case, out_root)
+    inputs = input_files(out_dir)
 
     with tempfile.TemporaryDirectory() as tmp:
         res = os.path.join(tmp, "results")
         os.makedirs(res)
         os.symlink(os.path.join(ref_root, "EOS"), os.path.join(tmp, "EOS"))
-        if mode == 10:
-            inputs = {"particle_samples.gz": ev}
-            if mixed is not None:
-                inputs["particle_samples_mixed_event.gz"] = mixed
-            for fn, e in inputs.items():
-                synth.write_mode10(os.path.join(res, fn), e)
-        else:
-            inputs = {"OSCAR.DAT": ev}
-            if mixed is not None:
-                inputs["OSCAR_mixed_event.DAT"] = mixed
-            for fn, e in inputs.items():
-                synth.write_oscar(os.path.join(res, fn), e)
-        with open(os.path.join(tmp, "parameters.dat"), "w") as f:
-            f.write(param_text(params))
+        for fn in inputs:
+            shutil.copy(os.path.join(out_dir, fn), res)
+        shutil.copy(os.path.join(out_dir, "parameters.dat"), tmp)
         proc = subprocess.run([REF_BIN], cwd=tmp, capture_output=True, text=True)
         if proc.returncode != 0:
             raise RuntimeError("reference failed on %s:\n%s" % (name, proc.stdout[-2000:]))
@@ -184,9 +232,6 @@ def run_case(name: str, case: dict, ref_root: str, out_root: str = HERE) -> None
         pairs = [re.sub(r"\x1b\[[0-9;]*m", "", p).strip() for p in pairs]
         with open(os.path.join(out_dir, "pairs.txt"), "w") as f:
             f.write("\n".join(pairs) + "\n")
-        for fn in inputs:
-            shutil.copy(os.path.join(res, fn), os.path.join(out_dir, fn))
-        shutil.copy(os.path.join(tmp, "parameters.dat"), out_dir)
         outs = sorted(fn for fn in os.listdir(res) if fn.startswith("HBT_correlation"))
         with tarfile.open(os.path.join(out_dir, "outputs.tar.gz"), "w:gz") as tar:
             for fn in outs:

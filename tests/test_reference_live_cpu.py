@@ -9,9 +9,11 @@ sources).  Then:
   committed ones (the fixtures are the reference's own outputs);
 * two cases that are not among the fixtures (K_phi bins with q_inv
   histograms and binding caps; no longitudinal boost with a rapidity shift,
-  K_T and rapidity cuts and an asymmetric q grid) run through the reference
-  binary and through the oracle: every output file byte-identical (x86-64;
-  to the printed precision elsewhere) and the same logged pair totals.
+  K_T and rapidity cuts and an asymmetric q grid), and a seeded sweep of 24
+  random parameter sets (make_golden.random_case), run through the
+  reference binary and through the oracle: every output file byte-identical
+  (x86-64; to the printed precision elsewhere) and the same logged pair
+  totals.
 
 Skipped where there is no reference checkout (the GPU machine).
 """
@@ -91,3 +93,22 @@ def test_oracle_matches_reference_on_a_new_case(name, tmp_path):
     if cap is not None:
         # the cap binds: some slot's counter ran one past it
         assert (np.asarray(h["ctr_num"]) == cap + 1).any()
+
+
+@pytest.mark.parametrize("k", range(24))
+def test_oracle_matches_reference_on_random_parameter_sets(k, tmp_path):
+    """A seeded sweep of parameter sets through the reference binary and
+    the oracle: byte-identical files and the same pair totals."""
+    name = "sweep%02d" % k
+    make_golden.run_case(name, make_golden.random_case(k), REF_ROOT, out_root=str(tmp_path))
+    case_dir = os.path.join(str(tmp_path), name)
+    want = _outputs(case_dir)
+    out_dir = os.path.join(str(tmp_path), "oracle_out")
+    os.makedirs(out_dir)
+    orc = oracle_lib.run_golden_case_through_oracle(name, out_dir, root=str(tmp_path))
+    got = {f: open(os.path.join(out_dir, f), "rb").read() for f in os.listdir(out_dir)}
+    assert sorted(got) == sorted(want) and want
+    for f in want:
+        parity.same_output_file(got[f], want[f], f)
+    h = orc.hist()
+    assert (h["pairs_same"], h["pairs_mixed"]) == _pair_totals(case_dir)
