@@ -179,6 +179,25 @@ def random_case(k: int) -> dict:
                 params=params)
 
 
+def random_oscar_case(k: int) -> dict:
+    """Case k of a seeded sweep over the OSCAR reader (read_in_mode 0):
+    events holding pi+, pi- and K+ in shuffled order, the analysed species
+    drawn among them, a separate real mixed-event file or not, and the
+    parameters of random_case."""
+    rng = np.random.default_rng(6000 + k)
+    case = random_case(1000 + k)
+    params = dict(case["params"])
+    params["read_in_mode"] = 0
+    params["particle_monval"] = int(rng.choice([211, -211, 321]))
+    real_mixed = bool(rng.integers(0, 2))
+    params["read_in_real_mixed_events"] = int(real_mixed)
+    params["event_buffer_size"] = int(rng.choice([1, 40, 100, 300]))
+    out = dict(events=lambda: _events_mixed_species(7000 + k), params=params)
+    if real_mixed:
+        out["mixed"] = lambda: _events_mixed_species(8000 + k)
+    return out
+
+
 def write_case(name: str, case: dict, out_root: str = HERE) -> str:
     """Writes one case's parameters.dat and input files into out_root/name
     (no run); returns that folder."""

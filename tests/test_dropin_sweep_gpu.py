@@ -5,7 +5,9 @@ make_golden.random_case(k) draws case k: grid size (odd and even),
 symmetric or asymmetric q window (one without q = 0), K_T edges and range,
 longitudinal boost, K_phi bins, q_inv histograms, a pair cap that binds or
 not, buffer size (down to one event per buffer), rapidity window and shift,
-the mixing seed.  On the CPU the same 24 cases run through the reference
+the mixing seed; and 8 cases on the OSCAR reader with mixed species, a
+random analysed species and, in some, a real mixed-event file
+(random_oscar_case).  On the CPU the same cases run through the reference
 binary and the oracle with byte-identical output files
 (tests/test_reference_live_cpu.py); here lib/hbt_afterburner.e (reader,
 HBT_correlation, the batched GPU kernels, writer) runs each case and every
@@ -44,11 +46,13 @@ def _logged_totals(stdout):
     return same, mixed
 
 
-@pytest.mark.parametrize("k", range(24))
-def test_dropin_matches_oracle_on_random_parameter_sets(k, tmp_path):
+@pytest.mark.parametrize("kind,k", [("mode10", k) for k in range(24)] +
+                         [("oscar", k) for k in range(8)])
+def test_dropin_matches_oracle_on_random_parameter_sets(kind, k, tmp_path):
     from test_dropin_gpu import compare_files
-    name = "sweep%02d" % k
-    case_dir = make_golden.write_case(name, make_golden.random_case(k), str(tmp_path))
+    name = "sweep_%s_%02d" % (kind, k)
+    case = make_golden.random_case(k) if kind == "mode10" else make_golden.random_oscar_case(k)
+    case_dir = make_golden.write_case(name, case, str(tmp_path))
     work = os.path.join(str(tmp_path), "work")
     res = os.path.join(work, "results")
     os.makedirs(res)

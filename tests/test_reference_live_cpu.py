@@ -10,7 +10,8 @@ sources).  Then:
 * two cases that are not among the fixtures (K_phi bins with q_inv
   histograms and binding caps; no longitudinal boost with a rapidity shift,
   K_T and rapidity cuts and an asymmetric q grid), and a seeded sweep of 24
-  random parameter sets (make_golden.random_case), run through the
+  random parameter sets (make_golden.random_case) plus 8 on the OSCAR
+  reader with mixed species (random_oscar_case), run through the
   reference binary and through the oracle: every output file byte-identical
   (x86-64; to the printed precision elsewhere) and the same logged pair
   totals.
@@ -95,12 +96,16 @@ def test_oracle_matches_reference_on_a_new_case(name, tmp_path):
         assert (np.asarray(h["ctr_num"]) == cap + 1).any()
 
 
-@pytest.mark.parametrize("k", range(24))
-def test_oracle_matches_reference_on_random_parameter_sets(k, tmp_path):
+@pytest.mark.parametrize("kind,k", [("mode10", k) for k in range(24)] +
+                         [("oscar", k) for k in range(8)])
+def test_oracle_matches_reference_on_random_parameter_sets(kind, k, tmp_path):
     """A seeded sweep of parameter sets through the reference binary and
-    the oracle: byte-identical files and the same pair totals."""
-    name = "sweep%02d" % k
-    make_golden.run_case(name, make_golden.random_case(k), REF_ROOT, out_root=str(tmp_path))
+    the oracle: byte-identical files and the same pair totals.  "oscar":
+    the OSCAR reader with mixed species and, in some cases, a real
+    mixed-event file."""
+    name = "sweep_%s_%02d" % (kind, k)
+    case = make_golden.random_case(k) if kind == "mode10" else make_golden.random_oscar_case(k)
+    make_golden.run_case(name, case, REF_ROOT, out_root=str(tmp_path))
     case_dir = os.path.join(str(tmp_path), name)
     want = _outputs(case_dir)
     out_dir = os.path.join(str(tmp_path), "oracle_out")
