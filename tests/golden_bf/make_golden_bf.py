@@ -61,8 +61,40 @@ CASES = {
 }
 
 
-def run_case(name, case, ref_root):
-    out_dir = os.path.join(HERE, name)
+def random_case(k: int) -> dict:
+    """Case k of a seeded sweep: the alpha / beta species among pi+-, K+-
+    (alpha == beta included), rapidity or pseudorapidity, the Delta y grid
+    (odd and even Bnpts) and range, the p_T window, a rapidity shift, the
+    buffer size, mode-10 or OSCAR input with or without a real mixed-event
+    file, the mixing seed."""
+    rng = np.random.default_rng(9000 + k)
+    species = [211, -211, 321, -321]
+    params = {
+        "particle_alpha": int(rng.choice(species)),
+        "particle_beta": int(rng.choice(species)),
+        "rap_type": int(rng.integers(0, 2)),
+        "Bnpts": int(rng.choice([6, 9, 11, 20, 21, 41])),
+        "Brap_max": round(float(rng.uniform(0.4, 2.0)), 4),
+        "BpT_min": round(float(rng.choice([0.0, rng.uniform(0.0, 0.4)])), 4),
+        "BpT_max": round(float(rng.uniform(1.0, 3.0)), 4),
+        "rapidity_shift": round(float(rng.choice([0.0, rng.uniform(-0.3, 0.3)])), 4),
+        "event_buffer_size": int(rng.choice([1, 80, 150, 400])),
+        "read_in_mode": int(rng.choice([10, 0])),
+        "randomSeed": int(rng.integers(1, 10000)),
+    }
+    real_mixed = bool(rng.integers(0, 2))
+    params["read_in_real_mixed_events"] = int(real_mixed)
+    n_events = int(rng.integers(5, 14))
+    case = dict(events=lambda: species_mix(9500 + 10 * k, n_events), params=params)
+    if real_mixed:
+        case["mixed"] = lambda: species_mix(9700 + 10 * k, n_events + 1)
+    return case
+
+
+def run_case(name, case, ref_root, out_root=HERE):
+    """Runs the reference binary on one case and writes the case's files
+    into out_root/name (tests/golden_bf/<name> for the committed fixtures)."""
+    out_dir = os.path.join(out_root, name)
     os.makedirs(out_dir, exist_ok=True)
     params = dict(BF_PARAMS)
     params.update(case["params"])

@@ -419,8 +419,8 @@ class BfOracle:
         assert _bf_lib().orc_bf_write(self._h, path.encode()) == 0
 
 
-def bf_golden_case(name: str):
-    d = os.path.join(GOLDEN_BF, name)
+def bf_golden_case(name: str, root: str = GOLDEN_BF):
+    d = os.path.join(root, name)
     prm = read_params(os.path.join(d, "parameters.dat"))
     if int(prm["read_in_mode"]) == 10:
         ev = read_mode10(os.path.join(d, "particle_samples.gz"))
@@ -440,9 +440,10 @@ def bf_params_from(prm: dict) -> dict:
                 seed=int(prm["randomseed"]))
 
 
-def run_bf_golden_case_through_oracle(name: str, out_dir: str) -> BfOracle:
+def run_bf_golden_case_through_oracle(name: str, out_dir: str,
+                                      root: str = GOLDEN_BF) -> BfOracle:
     from hadronic_afterburner_toolkit_gb300 import synth
-    prm, ev, mixed = bf_golden_case(name)
+    prm, ev, mixed = bf_golden_case(name, root)
     shift = prm.get("rapidity_shift", 0.0)
     size = int(prm["event_buffer_size"])
     orc = BfOracle(**bf_params_from(prm))

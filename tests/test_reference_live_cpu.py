@@ -14,7 +14,13 @@ sources).  Then:
   reader with mixed species (random_oscar_case), run through the
   reference binary and through the oracle: every output file byte-identical
   (x86-64; to the printed precision elsewhere) and the same logged pair
-  totals.
+  totals;
+* the balance-function path likewise: every committed balance-function
+  fixture regenerated, and a seeded sweep of 16 random balance-function
+  parameter sets (make_golden_bf.random_case: species pairs, rapidity or
+  pseudorapidity, Delta y grids, p_T windows, shifts, buffer sizes, both
+  readers, real mixed events) through the reference and the balance-function
+  oracle, byte-identical.
 
 Skipped where there is no reference checkout (the GPU machine).
 """
@@ -29,7 +35,9 @@ import oracle_lib
 import parity
 
 sys.path.insert(0, os.path.join(oracle_lib.REPO, "tests", "golden"))
+sys.path.insert(0, os.path.join(oracle_lib.REPO, "tests", "golden_bf"))
 import make_golden  # noqa: E402
+import make_golden_bf  # noqa: E402
 
 REF_ROOT = oracle_lib.reference_checkout()
 pytestmark = [
@@ -117,3 +125,29 @@ def test_oracle_matches_reference_on_random_parameter_sets(kind, k, tmp_path):
         parity.same_output_file(got[f], want[f], f)
     h = orc.hist()
     assert (h["pairs_same"], h["pairs_mixed"]) == _pair_totals(case_dir)
+
+
+def _bf_outputs(case_dir):
+    return _outputs(case_dir)
+
+
+@pytest.mark.parametrize("name", sorted(make_golden_bf.CASES))
+def test_committed_bf_fixture_is_the_reference_output(name, tmp_path):
+    make_golden_bf.run_case(name, make_golden_bf.CASES[name], REF_ROOT, out_root=str(tmp_path))
+    assert (_bf_outputs(os.path.join(str(tmp_path), name))
+            == _bf_outputs(os.path.join(oracle_lib.GOLDEN_BF, name)))
+
+
+@pytest.mark.parametrize("k", range(16))
+def test_bf_oracle_matches_reference_on_random_parameter_sets(k, tmp_path):
+    name = "bfsweep%02d" % k
+    make_golden_bf.run_case(name, make_golden_bf.random_case(k), REF_ROOT,
+                            out_root=str(tmp_path))
+    want = _bf_outputs(os.path.join(str(tmp_path), name))
+    out_dir = os.path.join(str(tmp_path), "oracle_out")
+    os.makedirs(out_dir)
+    oracle_lib.run_bf_golden_case_through_oracle(name, out_dir, root=str(tmp_path))
+    got = {f: open(os.path.join(out_dir, f), "rb").read() for f in os.listdir(out_dir)}
+    assert sorted(got) == sorted(want) and len(want) == 3
+    for f in want:
+        parity.same_output_file(got[f], want[f], f)
