@@ -75,17 +75,29 @@ def _stub_h5py(db):
     return mod
 
 
-def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HBT_REFERENCE_ROOT")
-    if not ref:
-        raise SystemExit("usage: %s <reference checkout> (or set HBT_REFERENCE_ROOT)" % sys.argv[0])
+def reference_fits(ref: str, db: dict):
+    """Runs the unmodified reference script on database `db` (through the
+    h5py stand-in) and returns (header, {event: {K_T cut: rows}}).  The
+    interpreter state it touches (sys.modules["h5py"], sys.argv,
+    builtins.string_) is restored afterwards."""
     script = os.path.join(ref, "ebe_scripts", "fit_HBT_radii.py")
-    db = tables.database()
     h5 = _stub_h5py(db)
+    saved = (sys.modules.get("h5py"), list(sys.argv), getattr(builtins, "string_", None))
     sys.modules["h5py"] = h5
     builtins.string_ = np.bytes_
     sys.argv = [script, "database.h5"]
-    runpy.run_path(script, run_name="__main__")
+    try:
+        runpy.run_path(script, run_name="__main__")
+    finally:
+        if saved[0] is None:
+            sys.modules.pop("h5py", None)
+        else:
+            sys.modules["h5py"] = saved[0]
+        sys.argv = saved[1]
+        if saved[2] is None:
+            del builtins.string_
+        else:
+            builtins.string_ = saved[2]
     out = {}
     for ev, grp in h5.last_file.groups.items():
         out[ev] = {}
@@ -93,6 +105,14 @@ def main():
             ds = grp.items["HBT_radii_KT_%s.dat" % cut]
             out[ev][cut] = [[float(x) for x in row] for row in ds.data]
         header = grp.items["HBT_radii_KT_%s.dat" % tables.KT_CUTS[0]].attrs["header"]
+    return header, out
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HBT_REFERENCE_ROOT")
+    if not ref:
+        raise SystemExit("usage: %s <reference checkout> (or set HBT_REFERENCE_ROOT)" % sys.argv[0])
+    header, out = reference_fits(ref, tables.database())
     with open(os.path.join(HERE, "expected.json"), "w") as f:
         json.dump({"header": header.decode(), "fits": out}, f, indent=1)
         f.write("\n")

@@ -100,3 +100,24 @@ def database():
             out[ev]["HBT_correlation_function_KT_%s.dat" % cut] = make_table(
                 seed * 10 + k, p, blank_every=7 if k == 3 else 0)
     return out
+
+
+def random_database(seed: int, n_events: int = 2) -> dict:
+    """A database in the fixture's layout with source parameters, noise,
+    grid size and empty bins drawn from a seeded generator (the live
+    comparison with the reference script uses it)."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for e in range(n_events):
+        ev = "event_%d" % (e + 1)
+        out[ev] = {}
+        nq = int(rng.choice([15, 21, 25]))
+        for k, cut in enumerate(KT_CUTS):
+            p = (float(rng.uniform(0.3, 0.8)), float(rng.uniform(2.5, 8.5)),
+                 float(rng.uniform(2.5, 8.0)), float(rng.uniform(2.0, 9.0)),
+                 float(rng.uniform(0.0, 2.0)), float(rng.uniform(0.0, 1.6)))
+            out[ev]["HBT_correlation_function_KT_%s.dat" % cut] = make_table(
+                int(rng.integers(1, 1 << 30)), p, nq=nq,
+                noise=float(rng.uniform(0.01, 0.06)),
+                blank_every=int(rng.choice([0, 0, 5, 9])))
+    return out
