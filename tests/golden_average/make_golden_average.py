@@ -24,12 +24,11 @@ def row5(v):
     return "%18.8e    %.8e    %.8e    %.8e    %.8e" % tuple(v)
 
 
-def main(ref):
-    script = os.path.join(ref, "ebe_scripts", "average_event_HBT_correlation_function.py")
-    rng = np.random.default_rng(2024)
-    tmp = tempfile.mkdtemp()
-    work = os.path.join(tmp, "work")
-    n_ev, q = 5, 5
+def write_work(work, seed=2024, n_ev=5, q=5):
+    """A working folder of n_ev UrQMD* event folders, each holding two 3-D
+    files, one compact (eco) file and one q_inv file on a q^3 (q) grid;
+    bins below 40 pairs carry a zero numerator, one q_inv row a NaN."""
+    rng = np.random.default_rng(seed)
     grid = np.linspace(-0.1, 0.1, q)
     for ev in range(n_ev):
         res = os.path.join(work, "UrQMDev_%d" % ev, "UrQMD_results")
@@ -57,8 +56,20 @@ def main(ref):
             for k in range(q):
                 qm = "-nan" if (ev == 2 and k == 0) else "%.8e" % rng.uniform(0, 0.1)
                 f.write("%18s    %.8e    %.8e\n" % (qm, rng.normal(50, 5), rng.normal(45, 5)))
-    avg = os.path.join(tmp, "avg")
+
+
+def run_script(ref, work, avg):
+    """The reference's averaging script on `work`, writing into `avg`."""
+    script = os.path.join(ref, "ebe_scripts", "average_event_HBT_correlation_function.py")
     subprocess.run([sys.executable, script, work, avg], check=True, capture_output=True)
+
+
+def main(ref):
+    tmp = tempfile.mkdtemp()
+    work = os.path.join(tmp, "work")
+    write_work(work)
+    avg = os.path.join(tmp, "avg")
+    run_script(ref, work, avg)
     out = os.path.join(HERE, "case.tar.gz")
     with tarfile.open(out, "w:gz") as tar:
         tar.add(work, arcname="work")

@@ -78,3 +78,57 @@ def test_ragged_or_missing_inputs_fail(case, tmp_path):
     assert L.hbt_host_average_events(str(work).encode(), str(tmp_path / "o").encode(), 0) == -1
     assert L.hbt_host_average_events(str(tmp_path / "none").encode(),
                                      str(tmp_path / "o2").encode(), 0) == -1
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("seed,n_ev,q", [(7, 3, 4), (8, 9, 7), (9, 2, 9), (10, 12, 5)])
+def test_average_matches_reference_script_live(seed, n_ev, q, tmp_path):
+    """Where the reference checkout is on this machine: random working
+    folders (event count, grid size, pair counts, empty bins and, from three
+    events on, a NaN q_inv row drawn from a seed) through the reference's
+    averaging script and through the library call and the CLI."""
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden_average"))
+    import make_golden_average
+    import oracle_lib
+    ref = oracle_lib.reference_checkout()
+    if not ref or not os.path.exists(os.path.join(
+            ref, "ebe_scripts", "average_event_HBT_correlation_function.py")):
+        pytest.skip("no reference checkout")
+    work, want = str(tmp_path / "work"), str(tmp_path / "want")
+    make_golden_average.write_work(work, seed=seed, n_ev=n_ev, q=q)
+    make_golden_average.run_script(ref, work, want)
+    L = ctypes.CDLL(build.build_host())
+    L.hbt_host_average_events.restype = ctypes.c_int
+    L.hbt_host_average_events.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32]
+    assert L.hbt_host_average_events(work.encode(), str(tmp_path / "lib").encode(), 0) == 4
+    _check(str(tmp_path / "lib"), want)
+    exe = os.path.join(os.path.dirname(build.build_host()), "hbt_average.e")
+    proc = subprocess.run([exe, work, str(tmp_path / "cli")], capture_output=True, text=True,
+                          timeout=120)
+    assert proc.returncode == 0, proc.stderr
+    _check(str(tmp_path / "cli"), want)
+
+
+@pytest.mark.slow
+def test_committed_average_fixture_is_the_reference_output(case, tmp_path):
+    """Where the reference checkout is on this machine: the fixture's inputs
+    come from make_golden_average.write_work (byte for byte) and the
+    reference script still writes its averages for them."""
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden_average"))
+    import make_golden_average
+    import oracle_lib
+    ref = oracle_lib.reference_checkout()
+    if not ref or not os.path.exists(os.path.join(
+            ref, "ebe_scripts", "average_event_HBT_correlation_function.py")):
+        pytest.skip("no reference checkout")
+    work, want = str(tmp_path / "work"), str(tmp_path / "want")
+    make_golden_average.write_work(work)
+    for root, _, files in os.walk(os.path.join(case, "work")):
+        for f in files:
+            rel = os.path.relpath(os.path.join(root, f), os.path.join(case, "work"))
+            assert (open(os.path.join(work, rel), "rb").read()
+                    == open(os.path.join(root, f), "rb").read()), rel
+    make_golden_average.run_script(ref, work, want)
+    _check(want, os.path.join(case, "avg"))

@@ -57,6 +57,9 @@ def test_committed_fit_fixture_is_the_reference_output():
             _compare(fits[ev][cut], expected["fits"][ev][cut], (ev, cut))
 
 
+# some random tables make both the script's and the oracle's model overflow
+# in exp while the fit wanders; both warn the same way
+@pytest.mark.filterwarnings("ignore::RuntimeWarning")
 @pytest.mark.parametrize("seed", range(4))
 def test_fit_oracle_matches_reference_script_on_random_databases(seed):
     import fit_radii
