@@ -58,8 +58,10 @@ def test_committed_fit_fixture_is_the_reference_output():
 
 
 # some random tables make both the script's and the oracle's model overflow
-# in exp while the fit wanders; both warn the same way
+# in exp while the fit wanders, or leave a covariance that cannot be
+# estimated (infinite errors); both warn the same way and store the same rows
 @pytest.mark.filterwarnings("ignore::RuntimeWarning")
+@pytest.mark.filterwarnings("ignore::scipy.optimize.OptimizeWarning")
 @pytest.mark.parametrize("seed", range(4))
 def test_fit_oracle_matches_reference_script_on_random_databases(seed):
     import fit_radii
