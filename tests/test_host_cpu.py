@@ -35,8 +35,8 @@ def host():
     return L
 
 
-def _stage(name, tmp):
-    src = os.path.join(oracle_lib.GOLDEN, name)
+def _stage(name, tmp, root=oracle_lib.GOLDEN):
+    src = os.path.join(root, name)
     res = os.path.join(tmp, "results")
     os.makedirs(res, exist_ok=True)
     for fn in os.listdir(src):
@@ -47,15 +47,23 @@ def _stage(name, tmp):
 
 @pytest.mark.parametrize("name", CASES)
 def test_reader_buffers_match_reference_rule(host, name, tmp_path):
-    pfile, res = _stage(name, str(tmp_path))
-    cap = 256
+    _check_buffers(host, name, str(tmp_path), oracle_lib.GOLDEN)
+
+
+def _check_buffers(host, name, tmp, root):
+    """The reader's buffers (events and particles of the analysed species,
+    same-event and mixed-event) against the reference's buffering rule as
+    the oracle restates it (whole events until the count reaches
+    event_buffer_size)."""
+    pfile, res = _stage(name, tmp, root)
+    cap = 4096
     nev = (ctypes.c_int32 * cap)()
     npart = (ctypes.c_int64 * cap)()
     mnev = (ctypes.c_int32 * cap)()
     mpart = (ctypes.c_int64 * cap)()
     nb = host.hbt_host_scan_buffers(pfile.encode(), res.encode(), cap, nev, npart, mnev, mpart)
     assert nb > 0
-    prm, ev, mixed = oracle_lib.golden_case(name)
+    prm, ev, mixed = oracle_lib.golden_case(name, root)
     size = int(prm["event_buffer_size"])
     mon = int(prm["particle_monval"])
     want = oracle_lib.buffer_ranges(ev.multiplicities(), size)
@@ -78,7 +86,11 @@ def test_reader_buffers_match_reference_rule(host, name, tmp_path):
 @pytest.mark.parametrize("name", CASES)
 def test_writer_reproduces_reference_files(host, name, tmp_path):
     """Oracle histograms written by the drop-in writer == reference files."""
-    orc = oracle_lib.run_golden_case_through_oracle(name, str(tmp_path))
+    _check_writer(host, name, tmp_path, oracle_lib.GOLDEN)
+
+
+def _check_writer(host, name, tmp_path, root):
+    orc = oracle_lib.run_golden_case_through_oracle(name, str(tmp_path), root)
     h = orc.hist()
     out = tmp_path / "w"
     out.mkdir()
@@ -87,7 +99,7 @@ def test_writer_reproduces_reference_files(host, name, tmp_path):
                           KT_min=p["KT_min"], KT_max=p["KT_max"], n_Kphi=p["n_Kphi"],
                           azimuthal_flag=p["azimuthal_flag"],
                           invariant_radius_flag=p["invariant_radius_flag"])
-    prm, _, _ = oracle_lib.golden_case(name)
+    prm, _, _ = oracle_lib.golden_case(name, root)
     arrs = [np.ascontiguousarray(h[k]) for k in
             ("count", "q_out", "q_side", "q_long", "num", "den",
              "qinv_sum", "qinv_num", "qinv_count", "qinv_den")]
@@ -97,12 +109,53 @@ def test_writer_reproduces_reference_files(host, name, tmp_path):
                              *[a.ctypes.data_as(_PD) for a in arrs],
                              *[c.ctypes.data_as(_PU) for c in ctr])
     assert rc == 0
-    with tarfile.open(os.path.join(oracle_lib.GOLDEN, name, "outputs.tar.gz")) as tar:
+    with tarfile.open(os.path.join(root, name, "outputs.tar.gz")) as tar:
         want = {m.name: tar.extractfile(m).read() for m in tar.getmembers()}
     got = {f: open(os.path.join(out, f), "rb").read() for f in os.listdir(out)}
     assert sorted(got) == sorted(want)
     for f in want:
         parity.same_output_file(got[f], want[f], f)
+
+
+SWEEP = [("mode10", k) for k in range(24)] + [("oscar", k) for k in range(8)]
+
+
+def _sweep_case(kind, k):
+    import sys
+    sys.path.insert(0, os.path.join(oracle_lib.REPO, "tests", "golden"))
+    import make_golden
+    case = make_golden.random_case(k) if kind == "mode10" else make_golden.random_oscar_case(k)
+    return make_golden, case
+
+
+@pytest.mark.parametrize("kind,k", SWEEP)
+def test_reader_buffers_on_random_parameter_sets(host, kind, k, tmp_path):
+    """The buffering check on the random cases of make_golden (buffer sizes
+    from one event to 400 particles, species filters, real mixed-event
+    files)."""
+    mg, case = _sweep_case(kind, k)
+    root = str(tmp_path / "cases")
+    mg.write_case("c", case, root)
+    _check_buffers(host, "c", str(tmp_path), root)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("kind,k", SWEEP)
+def test_writer_on_random_parameter_sets(host, kind, k, tmp_path):
+    """Where the reference checkout is on this machine: the writer, fed the
+    oracle's histograms of a random case, reproduces the files the
+    reference binary writes for it (grid sizes, K_T edges in the file names,
+    K_phi and q_inv files)."""
+    mg, case = _sweep_case(kind, k)
+    ref = oracle_lib.reference_checkout()
+    if not ref or not os.path.exists(mg.REF_BIN):
+        pytest.skip("no reference checkout or no oracle/_ref binary")
+    root = str(tmp_path / "cases")
+    import contextlib
+    import io
+    with contextlib.redirect_stdout(io.StringIO()):
+        mg.run_case("c", case, ref, out_root=root)
+    _check_writer(host, "c", tmp_path, root)
 
 
 # ------------------------------------------------------------------ readers
