@@ -432,3 +432,18 @@ def test_readers_reject_a_truncated_gzip_file(host, fast, tmp_path):
             assert nb > 0
         else:
             assert nb == -1, cut
+
+
+@pytest.mark.parametrize("kind,k", SWEEP)
+def test_block_reader_equals_line_reader_on_random_parameter_sets(host, kind, k, tmp_path):
+    """The block reader against the line reader on the random cases' inputs
+    and buffer sizes (both readers, species filters, real mixed-event
+    files): bit-identical particles, buffer by buffer."""
+    mg, case = _sweep_case(kind, k)
+    root = str(tmp_path / "cases")
+    mg.write_case("c", case, root)
+    pfile, res = _stage("c", str(tmp_path), root)
+    n0, d0 = _digests(host, pfile, res, ["hbt_fast_reader=0"])
+    assert n0 > 0
+    n1, d1 = _digests(host, pfile, res, ["hbt_fast_reader=1", "hbt_reader_threads=3"])
+    assert (n1, d1) == (n0, d0)
